@@ -1,0 +1,312 @@
+"""Benchmark: Metropolis site-attempts/s, plain FCC 64^3 binary cluster expansion.
+
+Workload (one "step" = one Metropolis pass over every site of every chain): binary FCC
+cluster expansion (empty, point, pairs 1-4NN, 3 smallest triplets, NN tetrahedron;
+occupation basis; ECI N(0, 0.03 eV)/size^2 from seed 1), 64^3 primitive-cell supercell
+(262,144 sites), 50 % B placed by a seeded shuffle, semi-grand canonical at 8
+temperatures linspace(300, 2000, 8) K, mu = 0.  The 8 chains are independent; with
+N GPUs every rank runs its own 8 chains (weak scaling, no collective).
+
+value   device throughput of the sweep kernel: attempts / sum of CUDA-event kernel times,
+        inputs resident in HBM, L2 flushed between launches (outside the events).
+e2e     the same job through the public C-ABI with host buffers: create the batch
+        (H2D of occupations and parameters), run the passes returning per-pass samples to
+        the host (D2H), read the final occupations (D2H); wall clock.
+--impl reference: the reference's CPU path (random-site SGC Metropolis, mt19937_64,
+        FP64 cluster-expansion dE; the oracle restatement) on all host cores, one chain
+        per process, each step a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L = 64
+N_CHAINS = 8
+BYTES_PER_ATTEMPT = 56  # (1 own read + 54 neighbour reads + 1 write) x int8
+METRIC = "Metropolis site-attempts/s (FCC 64^3 CE)"
+WORKLOAD = "fcc64_binary_ce_sgc_8T"
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_inputs(rank: int):
+    from casmcode_monte_gb300 import clex
+
+    eci = clex.make_eci("fcc_binary", 1)
+    rng = np.random.default_rng(1000 + rank)
+    n = L**3
+    occ = np.stack([clex.random_occupation(2, n, rng) for _ in range(N_CHAINS)])
+    T = np.linspace(300.0, 2000.0, N_CHAINS)
+    mu = np.zeros((N_CHAINS, 1))
+    seeds = (np.arange(N_CHAINS, dtype=np.uint64) + np.uint64(1 + 1000 * rank)) * np.uint64(0x9E3779B97F4A7C15 % (2**63))
+    return eci, occ, T, mu, seeds
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def flush_l2(buf):
+    import torch
+
+    buf.add_(1)  # writes 256 MB, larger than the 129 MB L2
+
+
+def cpu_baseline_sample(seconds_target: float = 10.0) -> dict:
+    """The oracle's random-site reference loop on one host core, one 64^3 chain."""
+    from casmcode_monte_gb300 import clex
+    from tests import oracle_lib
+
+    eci, occ, T, mu, seeds = make_inputs(0)
+    orc = oracle_lib.OracleCE((L, L, L), 2, eci)
+    o = occ[0].astype(np.int32)
+    # calibrate then run a bounded sample
+    _, _, t = orc.random_site_run(o, float(T[3]), mu[3], 7, 20000)
+    rate = 20000 / max(t, 1e-9)
+    n = int(min(max(rate * seconds_target, 1e5), 5e8))
+    _, _, t = orc.random_site_run(o, float(T[3]), mu[3], 8, n)
+    return {"value": n / t, "unit": "site-attempts/s", "cores": 1, "kind": "port",
+            "sample": f"{n} random-site attempts on one 64^3 chain at T={T[3]:.0f} K (oracle restatement, g++ -O2)"}
+
+
+def _ref_worker(args):
+    chain, n_steps = args
+    from tests import oracle_lib
+
+    eci, occ, T, mu, seeds = make_inputs(0)
+    orc = oracle_lib.OracleCE((L, L, L), 2, eci)
+    _, _, t = orc.random_site_run(occ[chain].astype(np.int32), float(T[chain]), mu[chain], 100 + chain, n_steps)
+    return n_steps, t
+
+
+def run_reference(args) -> None:
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n_proc = min(cores, N_CHAINS)
+    steps_per_chain = int(args.ref_steps_per_sample)
+    ctx = mp.get_context("spawn")
+    vals = []
+    with ctx.Pool(n_proc) as pool:
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_ref_worker, [(c % N_CHAINS, steps_per_chain) for c in range(n_proc)])
+            wall = time.perf_counter() - t0
+            if i >= args.warmup:
+                vals.append(sum(r[0] for r in res) / wall)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "site-attempts/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "supercell": [L, L, L], "chains": N_CHAINS,
+                       "sample_steps_per_process": steps_per_chain, "processes": n_proc},
+            "cpu_baseline": {"value": value, "unit": "site-attempts/s", "cores": n_proc, "kind": "port",
+                             "sample": f"{steps_per_chain} random-site attempts per process, {n_proc} processes"},
+            "e2e": {"value": value, "unit": "site-attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import torch
+
+    rank, world, local = _env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from casmcode_monte_gb300 import clex
+
+    eci, occ, T, mu, seeds = make_inputs(rank)
+    model = clex.ClexModel("fcc_binary", eci)
+    batch = clex.ChainBatch(model, (L, L, L), occ, T, mu, seeds, ctas_per_chain=args.ctas_per_chain)
+    attempts_per_step = N_CHAINS * L**3
+    ppl = max(1, int(args.passes_per_launch))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    # warmup
+    left = args.warmup
+    while left > 0:
+        n = min(ppl, left)
+        batch.run(n, want_output=False)
+        left -= n
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    kernel_ms = 0.0
+    launches = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    left = args.steps
+    while left > 0:
+        n = min(ppl, left)
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        batch.run(n, want_output=False)
+        kernel_ms += batch.last_kernel_ms()
+        launches += 1
+        left -= n
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([kernel_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        kernel_ms = float(t.item())
+        dist.barrier()
+    value = attempts_per_step * args.steps * world / (kernel_ms * 1e-3)
+
+    # ---- e2e through the C-ABI with host buffers
+    e2e_ms = []
+    h2d = occ.nbytes + T.nbytes + mu.nbytes + seeds.nbytes
+    d2h_per_step = N_CHAINS * (model.n_classes + 2) * 8
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        b2 = clex.ChainBatch(model, (L, L, L), occ, T, mu, seeds, ctas_per_chain=args.ctas_per_chain)
+        corr0 = b2.corr()
+        left = args.steps
+        chunks = []
+        while left > 0:
+            n = min(ppl, left)
+            chunks.append(b2.run(n))
+            left -= n
+        final = b2.occupation()
+        torch.cuda.synchronize()
+        e2e_ms.append((time.perf_counter() - t1) * 1e3)
+        b2.close()
+    e2e_value = attempts_per_step * args.steps * world / (min(e2e_ms) * 1e-3)
+    samples = clex.accumulate(model, corr0, np.concatenate(chunks, axis=0), mu, L**3)
+
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        peak_src = "measured"
+    per_launch_attempts = attempts_per_step * ppl
+    achieved = BYTES_PER_ATTEMPT * attempts_per_step * args.steps / (kernel_ms * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "ce_sweep_fcc64_binary_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        traffic = tj["dram_bytes_per_pass"] * ppl
+    if rank == 0:
+        cpu = cpu_baseline_sample(args.cpu_seconds) if args.cpu_seconds > 0 else None
+        line = {
+            "metric": METRIC, "value": value, "unit": "site-attempts/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "i8/i32+f32 (f64 exact decisions)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "supercell": [L, L, L], "chains_per_gpu": N_CHAINS,
+                       "temperatures_K": T.tolist(), "passes_per_launch": ppl,
+                       "ctas_per_chain": batch.ctas_per_chain, "colors": batch.n_colors,
+                       "threads_per_cta": batch.threads, "l2": "flushed between launches (256 MB write)",
+                       "attempts_per_step": attempts_per_step},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                         "bytes_per_attempt": BYTES_PER_ATTEMPT, "attempts_per_launch": per_launch_attempts},
+            "e2e": {"value": e2e_value, "unit": "site-attempts/s", "h2d_bytes_per_step": h2d / args.steps,
+                    "d2h_bytes_per_step": d2h_per_step + occ.nbytes / args.steps, "ms": min(e2e_ms)},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "wall_s_timed": wall,
+            "check": {"mean_potential_energy_last_pass_eV": samples.potential_energy[-1].tolist(),
+                      "acceptance_last_pass": (samples.n_accept[-1] / L**3).tolist()},
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--passes-per-launch", type=int, default=100)
+    ap.add_argument("--ctas-per-chain", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-steps-per-sample", type=float, default=2e6)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

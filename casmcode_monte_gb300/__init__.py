@@ -1,0 +1,215 @@
+"""GB300-native lattice Metropolis Monte Carlo with libcasm-monte's API.
+
+Module layout mirrors ``libcasm.monte`` (python/libcasm/monte/__init__.py:3-8):
+
+* ``casmcode_monte_gb300``            MethodLog, RandomNumberEngine, RandomNumberGenerator, ValueMap
+* ``casmcode_monte_gb300.sampling``   samplers, completion/equilibration/convergence checks
+* ``casmcode_monte_gb300.methods``    metropolis_acceptance, basic_occupation_metropolis
+* ``casmcode_monte_gb300.events``     Conversions, OccCandidate/OccSwap/OccEvent/OccLocation
+* ``casmcode_monte_gb300.ising_cpp``  the 2-D Ising model
+* ``casmcode_monte_gb300.ising_cpp.semigrand_canonical``  SGC calculator (GPU serial replay)
+* ``casmcode_monte_gb300.clex``       FCC cluster-expansion model and GPU coloured sweeps
+
+The Metropolis loops run in ``libmontegpu.so`` (hand-written sm_103a kernels behind the
+C-ABI in ``include/montegpu.h``); there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+import json
+import os
+import sys
+import time
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+
+__version__ = "1.0.0"
+
+
+class RandomNumberEngine:
+    """A pseudo-random number engine, std::mt19937_64 (monte.cpp:469-513).
+
+    The default constructor seeds from std::random_device, as the reference does.
+    """
+
+    def __init__(self):
+        h = C.c_void_p()
+        _lib.check(_lib.lib().mg_engine_create(1, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.mg_engine_destroy(h)
+            self._h = None
+
+    def seed(self, value: int) -> None:
+        _lib.check(_lib.lib().mg_engine_seed(self._h, C.c_uint64(int(value) & (2**64 - 1))))
+
+    def seed_seq(self, values: list[int]) -> None:
+        a = np.ascontiguousarray(np.asarray(values, dtype=np.uint64))
+        _lib.check(_lib.lib().mg_engine_seed_seq(self._h, _lib.ptr(a, C.c_uint64), a.size))
+
+    def dump(self) -> str:
+        buf = C.create_string_buffer(16384)
+        _lib.check(_lib.lib().mg_engine_dump(self._h, buf, len(buf)))
+        return buf.value.decode()
+
+    def load(self, state: str) -> None:
+        _lib.check(_lib.lib().mg_engine_load(self._h, state.encode()))
+
+    def __copy__(self):
+        e = RandomNumberEngine()
+        e.load(self.dump())
+        return e
+
+    def __deepcopy__(self, memo):
+        return self.__copy__()
+
+
+class RandomNumberGenerator:
+    """Uniform integers/reals from a shared RandomNumberEngine (RandomNumberGenerator.hh:15-42)."""
+
+    def __init__(self, engine: Optional[RandomNumberEngine] = None):
+        self.engine = engine if engine is not None else RandomNumberEngine()
+
+    def random_int(self, maximum_value: int) -> int:
+        """Uniformly distributed integer in [0, maximum_value]."""
+        out = C.c_uint64()
+        _lib.check(_lib.lib().mg_engine_random_int(self.engine._h, C.c_uint64(int(maximum_value)), C.byref(out)))
+        return int(out.value)
+
+    def random_real(self, maximum_value: float) -> float:
+        """Uniformly distributed float in [0, maximum_value)."""
+        out = C.c_double()
+        _lib.check(_lib.lib().mg_engine_random_real(self.engine._h, float(maximum_value), C.byref(out)))
+        return float(out.value)
+
+
+class ValueMap:
+    """Named boolean, scalar, vector and matrix values (ValueMap.hh:14-19)."""
+
+    def __init__(self, data: Optional[dict] = None):
+        self.boolean_values: dict[str, bool] = {}
+        self.scalar_values: dict[str, float] = {}
+        self.vector_values: dict[str, np.ndarray] = {}
+        self.matrix_values: dict[str, np.ndarray] = {}
+        if data is not None:
+            v = ValueMap.from_dict(data)
+            self.__dict__.update(v.__dict__)
+
+    @staticmethod
+    def from_dict(data: dict) -> "ValueMap":
+        v = ValueMap()
+        for k, x in data.items():
+            if isinstance(x, bool):
+                v.boolean_values[k] = x
+            elif isinstance(x, (int, float)):
+                v.scalar_values[k] = float(x)
+            elif isinstance(x, str):
+                raise ValueError(f"Error reading ValueMap from dict: unsupported type for '{k}'")
+            else:
+                a = np.asarray(x, dtype=float)
+                if a.ndim == 1:
+                    v.vector_values[k] = a
+                elif a.ndim == 2:
+                    v.matrix_values[k] = a
+                else:
+                    raise ValueError(f"Error reading ValueMap from dict: unsupported shape for '{k}'")
+        return v
+
+    def to_dict(self) -> dict:
+        d: dict = {}
+        d.update(self.boolean_values)
+        d.update(self.scalar_values)
+        d.update({k: v.tolist() for k, v in self.vector_values.items()})
+        d.update({k: v.tolist() for k, v in self.matrix_values.items()})
+        return d
+
+    def is_mismatched(self, other: "ValueMap") -> bool:
+        for a, b in ((self.boolean_values, other.boolean_values), (self.scalar_values, other.scalar_values),
+                     (self.vector_values, other.vector_values), (self.matrix_values, other.matrix_values)):
+            if set(a) != set(b):
+                return True
+        for k in self.vector_values:
+            if self.vector_values[k].shape != other.vector_values[k].shape:
+                return True
+        for k in self.matrix_values:
+            if self.matrix_values[k].shape != other.matrix_values[k].shape:
+                return True
+        return False
+
+    def make_incremented_values(self, increment: "ValueMap", n_increment: float) -> "ValueMap":
+        v = copy.deepcopy(self)
+        for k, x in increment.scalar_values.items():
+            v.scalar_values[k] = v.scalar_values.get(k, 0.0) + x * n_increment
+        for k, x in increment.vector_values.items():
+            v.vector_values[k] = v.vector_values.get(k, 0 * x) + x * n_increment
+        for k, x in increment.matrix_values.items():
+            v.matrix_values[k] = v.matrix_values.get(k, 0 * x) + x * n_increment
+        return v
+
+    def __copy__(self):
+        return copy.deepcopy(self)
+
+    def __deepcopy__(self, memo):
+        v = ValueMap()
+        v.boolean_values = dict(self.boolean_values)
+        v.scalar_values = dict(self.scalar_values)
+        v.vector_values = {k: np.array(x) for k, x in self.vector_values.items()}
+        v.matrix_values = {k: np.array(x) for k, x in self.matrix_values.items()}
+        return v
+
+
+class MethodLog:
+    """Status logger with a clock and laps (MethodLog.hh:13-38; monte.cpp:111-384)."""
+
+    def __init__(self, logfile_path: Optional[str] = None, log_frequency: Optional[float] = None):
+        self._logfile_path = logfile_path
+        self._log_frequency = log_frequency
+        self._t0 = time.perf_counter()
+        self._lap = self._t0
+
+    def logfile_path(self) -> Optional[str]:
+        return self._logfile_path
+
+    def log_frequency(self) -> Optional[float]:
+        return self._log_frequency
+
+    def restart_clock(self) -> None:
+        self._t0 = time.perf_counter()
+
+    def begin_lap(self) -> None:
+        self._lap = time.perf_counter()
+
+    def time_s(self) -> float:
+        return time.perf_counter() - self._t0
+
+    def lap_time(self) -> float:
+        return time.perf_counter() - self._lap
+
+    def reset(self) -> None:
+        """Truncate the log file (status files are rewritten on each update)."""
+        if self._logfile_path:
+            os.makedirs(os.path.dirname(os.path.abspath(self._logfile_path)) or ".", exist_ok=True)
+            open(self._logfile_path, "w").close()
+
+    def reset_to_stdout(self) -> None:
+        self._logfile_path = None
+
+    def print(self, text: str) -> None:
+        if self._logfile_path:
+            with open(self._logfile_path, "a") as f:
+                f.write(text)
+        else:
+            sys.stdout.write(text)
+
+    def write_json(self, data) -> None:
+        self.print(json.dumps(data, indent=2) + "\n")
+
+
+__all__ = ["MethodLog", "RandomNumberEngine", "RandomNumberGenerator", "ValueMap"]

@@ -1,0 +1,235 @@
+"""FCC cluster-expansion Hamiltonians and GPU coloured-sweep chain batches.
+
+The reference plugs a cluster expansion into its semi-grand canonical potential
+(include/casm/monte/ising_cpp/basic_semigrand_canonical.hh:104-199: a system provides
+``formation_energy_f_type`` and ``param_composition_f_type``); the evaluator itself lives
+in the external libcasm-clexulator.  This package provides, for the FCC lattice:
+
+* ``ClexModel``: basis set ("fcc_binary" occupation basis or "fcc_ternary" Chebyshev
+  basis; see ``clex.orbits``) + one ECI per symmetrised cluster function;
+* ``make_eci``: seeded ECIs N(0, sigma) / max(size, 1)^2;
+* ``ChainBatch``: many chains (same supercell) resident on the GPU, advanced by
+  graph-coloured Metropolis passes (Philox4x32-10 random numbers keyed per chain);
+* ``SemiGrandCanonicalRun``: per-pass samples (formation/potential energy per unit cell,
+  parametric composition) derived exactly from the integer correlation sums.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from .. import _lib
+
+KB = 8.6173303e-05  # eV/K (libcasm-global)
+_GEN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "csrc", "generated")
+BASIS_KINDS = {"fcc_binary": 0, "fcc_ternary": 1}
+
+
+def basis_description(kind: str) -> dict:
+    """Classes, features and site basis of a generated basis set (JSON written by codegen)."""
+    if kind not in BASIS_KINDS:
+        raise ValueError(f"Error: unknown basis set '{kind}' (expected one of {sorted(BASIS_KINDS)})")
+    with open(os.path.join(_GEN, f"{kind}.json")) as f:
+        return json.load(f)
+
+
+def make_eci(kind: str, seed: int, sigma: float = 0.03) -> np.ndarray:
+    """ECI per class: N(0, sigma) scaled by 1 / max(cluster size, 1)^2 (numpy PCG64 stream)."""
+    d = basis_description(kind)
+    rng = np.random.default_rng(seed)
+    v = rng.normal(0.0, sigma, size=len(d["classes"]))
+    sizes = np.array([max(c["size"], 1) for c in d["classes"]], dtype=float)
+    return v / sizes**2
+
+
+class ClexModel:
+    """A cluster-expansion formation energy on the FCC lattice (handle to mg_ce_model)."""
+
+    def __init__(self, kind: str, eci: Sequence[float]):
+        self.kind = kind
+        self.desc = basis_description(kind)
+        self.eci = np.ascontiguousarray(np.asarray(eci, dtype=np.float64))
+        h = C.c_void_p()
+        _lib.check(_lib.lib().mg_ce_model_create(BASIS_KINDS[kind], _lib.ptr(self.eci, C.c_double),
+                                                 self.eci.size, C.byref(h)))
+        self._h = h
+        self.n_classes = len(self.desc["classes"])
+        self.n_species = self.desc["basis"]["n_species"]
+        self.multiplicity = np.array([c["multiplicity"] for c in self.desc["classes"]], dtype=np.int64)
+        self.scale = np.array([c["scale"] for c in self.desc["classes"]], dtype=np.float64)
+        # E_f per supercell = sum_f w_f * IntCorr_f
+        self.class_weight = (self.eci / self.multiplicity) * self.scale
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.mg_ce_model_destroy(h)
+            self._h = None
+
+    def formation_per_supercell(self, int_corr: np.ndarray) -> np.ndarray:
+        """E_f from integer correlation sums [..., n_classes] (sum over classes in order)."""
+        ic = np.asarray(int_corr, dtype=np.float64)
+        e = np.zeros(ic.shape[:-1])
+        for f in range(self.n_classes):
+            e = e + self.class_weight[f] * ic[..., f]
+        return e
+
+    def n_x(self, int_corr: np.ndarray, n_sites: int) -> np.ndarray:
+        """N * parametric composition from the point correlation sums.
+
+        binary (occupation basis): n_B = sum psi = IntCorr[point];
+        ternary (Chebyshev): sum s = n_C - n_A, sum t = N - 3 n_B.
+        """
+        ic = np.asarray(int_corr, dtype=np.int64)
+        if self.n_species == 2:
+            return ic[..., 1:2].astype(np.float64)
+        ss, st = ic[..., 1], ic[..., 2]
+        nB = (n_sites - st) // 3
+        nC = (n_sites - nB + ss) // 2
+        return np.stack([nB, nC], axis=-1).astype(np.float64)
+
+
+class ChainBatch:
+    """Chains of one L0 x L1 x L2 supercell resident on the GPU (handle to mg_ce_batch).
+
+    occ: [n_chains, N] occupant indices (l = i + L0*(j + L1*k)); temperature [n_chains];
+    mu [n_chains, n_species-1]; seeds [n_chains] (Philox keys).
+    """
+
+    def __init__(self, model: ClexModel, shape: Sequence[int], occ, temperature, mu, seeds,
+                 chain_ids=None, precision: str = "fp64", ctas_per_chain: int = 0):
+        self.model = model
+        self.shape = tuple(int(x) for x in shape)
+        L0, L1, L2 = self.shape
+        self.n_sites = L0 * L1 * L2
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int8).reshape(-1, self.n_sites))
+        self.n_chains = occ.shape[0]
+        T = np.ascontiguousarray(np.asarray(temperature, dtype=np.float64).reshape(self.n_chains))
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64).reshape(self.n_chains, model.n_species - 1))
+        seeds = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(self.n_chains))
+        ids = None
+        if chain_ids is not None:
+            ids = np.ascontiguousarray(np.asarray(chain_ids, dtype=np.uint32).reshape(self.n_chains))
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.temperature, self.mu, self.seeds = T, mu, seeds
+        self.precision = precision
+        h = C.c_void_p()
+        _lib.check(_lib.lib().mg_ce_batch_create(
+            model._h, L0, L1, L2, self.n_chains, _lib.ptr(T, C.c_double), _lib.ptr(mu, C.c_double),
+            _lib.ptr(seeds, C.c_uint64), _lib.ptr(ids, C.c_uint32) if ids is not None else None,
+            _lib.ptr(occ, C.c_int8), 0 if precision == "fp64" else 1, int(ctas_per_chain), C.byref(h)))
+        self._h = h
+        S, nc, nt, sm = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+        _lib.check(_lib.lib().mg_ce_batch_info(h, C.byref(S), C.byref(nc), C.byref(nt), C.byref(sm)))
+        self.ctas_per_chain, self.n_colors, self.threads, self.smem_bytes = S.value, nc.value, nt.value, sm.value
+        self.pass_count = 0
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.mg_ce_batch_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def n_slots(self) -> int:
+        return self.model.n_classes + 2
+
+    def run(self, n_passes: int, want_output: bool = True) -> Optional[np.ndarray]:
+        """Advance every chain by n_passes; returns [n_passes, n_chains, n_classes+2] int64."""
+        out = None
+        if want_output:
+            out = np.zeros((n_passes, self.n_chains, self.n_slots), dtype=np.int64)
+        _lib.check(_lib.lib().mg_ce_batch_run(self._h, int(n_passes),
+                                              _lib.ptr(out, C.c_longlong) if out is not None else None))
+        self.pass_count += n_passes
+        return out
+
+    def last_kernel_ms(self) -> float:
+        ms = C.c_float()
+        _lib.check(_lib.lib().mg_ce_batch_last_kernel_ms(self._h, C.byref(ms)))
+        return float(ms.value)
+
+    def occupation(self) -> np.ndarray:
+        occ = np.zeros((self.n_chains, self.n_sites), dtype=np.int8)
+        _lib.check(_lib.lib().mg_ce_batch_get_occ(self._h, _lib.ptr(occ, C.c_int8)))
+        return occ
+
+    def set_occupation(self, occ) -> None:
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int8).reshape(self.n_chains, self.n_sites))
+        _lib.check(_lib.lib().mg_ce_batch_set_occ(self._h, _lib.ptr(occ, C.c_int8)))
+
+    def corr(self) -> np.ndarray:
+        """Integer correlation sums [n_chains, n_classes] recomputed from the occupation."""
+        out = np.zeros((self.n_chains, self.model.n_classes), dtype=np.int64)
+        _lib.check(_lib.lib().mg_ce_batch_corr(self._h, _lib.ptr(out, C.c_longlong)))
+        return out
+
+    def colors(self) -> np.ndarray:
+        out = np.zeros(self.n_sites, dtype=np.int32)
+        _lib.check(_lib.lib().mg_ce_batch_colors(self._h, _lib.ptr(out, C.c_int32)))
+        return out
+
+    def delta_e(self, chain, sites, new_occ) -> np.ndarray:
+        """FP64 dE_sgc for proposals (chain, site, new occupant) on the current state."""
+        chain = np.ascontiguousarray(np.asarray(chain, dtype=np.int32).reshape(-1))
+        sites = np.ascontiguousarray(np.asarray(sites, dtype=np.int64).reshape(-1))
+        new_occ = np.ascontiguousarray(np.asarray(new_occ, dtype=np.int8).reshape(-1))
+        out = np.zeros(sites.size, dtype=np.float64)
+        _lib.check(_lib.lib().mg_ce_batch_delta_e(self._h, _lib.ptr(chain, C.c_int32), _lib.ptr(sites, C.c_longlong),
+                                                  _lib.ptr(new_occ, C.c_int8), sites.size, _lib.ptr(out, C.c_double)))
+        return out
+
+
+@dataclass
+class SweepSamples:
+    """Per-pass observables of a batch run (arrays [n_passes, n_chains])."""
+
+    int_corr: np.ndarray          # [n_passes, n_chains, n_classes] after each pass
+    formation_energy: np.ndarray  # per unit cell
+    potential_energy: np.ndarray  # per unit cell
+    param_composition: np.ndarray  # [n_passes, n_chains, n_species-1]
+    n_accept: np.ndarray
+    n_exact: np.ndarray
+    n_flipped: np.ndarray
+
+
+def accumulate(model: ClexModel, corr0: np.ndarray, out: np.ndarray, mu: np.ndarray, n_sites: int) -> SweepSamples:
+    """Cumulative integer correlations and the observables for each pass.
+
+    corr0: [n_chains, n_classes] before the passes; out: ChainBatch.run output.
+    """
+    nc = model.n_classes
+    d = out[:, :, :nc].copy()
+    d[:, :, 0] = 0
+    ic = corr0[None, :, :] + np.cumsum(d, axis=0)
+    ef = model.formation_per_supercell(ic)
+    nx = model.n_x(ic, n_sites)
+    pe = ef.copy()
+    for i in range(model.n_species - 1):
+        pe = pe - mu[None, :, i] * nx[..., i]
+    return SweepSamples(ic, ef / n_sites, pe / n_sites, nx / n_sites, out[:, :, 0], out[:, :, nc], out[:, :, nc + 1])
+
+
+def random_occupation(n_species: int, n_sites: int, rng: np.random.Generator,
+                      composition: Optional[Sequence[float]] = None) -> np.ndarray:
+    """Occupation with exact species counts (rounded composition) placed by a seeded shuffle."""
+    if composition is None:
+        composition = [1.0 / n_species] * n_species
+    counts = [int(round(c * n_sites)) for c in composition]
+    counts[-1] = n_sites - sum(counts[:-1])
+    occ = np.concatenate([np.full(c, s, dtype=np.int8) for s, c in enumerate(counts)])
+    rng.shuffle(occ)
+    return occ
+
+
+__all__ = ["ClexModel", "ChainBatch", "SweepSamples", "accumulate", "basis_description", "make_eci",
+           "random_occupation", "KB"]

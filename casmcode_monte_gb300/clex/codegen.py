@@ -1,0 +1,197 @@
+"""Generate CUDA feature functions and a JSON description for an FCC basis set.
+
+CASM generates one C++ "Clexulator" per basis set (``ZrO_Clexulator.cc`` in the
+reference's test data is such a file).  Here the same idea targets the GPU sweep: the
+cluster geometry is compiled into straight-line integer code so that every neighbour load
+uses a constant offset and every product is an integer multiply-add.
+
+Generated for each basis set ``<name>``:
+
+* ``csrc/generated/<name>.cuh``: ``features(ld, F)`` (the local sums F[k] of
+  ``orbits.local_features``) and ``anchored(ld, C)`` (per-site contributions to the
+  integer correlation sums of every class), both templated on a loader ``ld(di,dj,dk)``
+  that returns the occupant code stored for the neighbour at primitive offset
+  (di,dj,dk).  Binary stores ``occ`` (0/1), ternary stores ``s = occ-1`` (-1/0/1).
+* ``csrc/generated/<name>.json``: classes (size, multiplicity, decoration multiset,
+  squared pair distances, scale C_f), features (class, basis index at the site, bound
+  on |F|) and the site basis, read by the host code at run time.
+
+Run ``python -m casmcode_monte_gb300.clex.codegen`` to regenerate (the outputs are
+committed).
+"""
+from __future__ import annotations
+
+import json
+import os
+
+from . import orbits as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GEN_DIR = os.path.join(os.path.dirname(HERE), "csrc", "generated")
+
+
+def _psi_expr(basis: O.SiteBasis, b: int, var: str) -> str:
+    """C expression of integer psi_b from the stored code ``var``."""
+    if basis.name == "occupation":
+        assert b == 0
+        return var  # stored value is occ in {0,1}
+    if basis.name == "chebyshev":
+        return var if b == 0 else f"t_{var}"
+    raise ValueError(basis.name)
+
+
+def _var(off) -> str:
+    return "v_" + "_".join(("m" + str(-x)) if x < 0 else str(x) for x in off)
+
+
+def generate(kind: str) -> tuple[str, dict]:
+    bs = O.make_basis_set(kind)
+    basis = bs.basis
+    offs = bs.neighbour_offsets()
+    need_t = basis.name == "chebyshev"
+    lines = []
+    ns = kind
+    lines.append("// Generated by casmcode_monte_gb300/clex/codegen.py -- do not edit.")
+    lines.append(f"// Basis set '{kind}': {len(bs.classes)} classes, {bs.n_features} local features,")
+    lines.append(f"// {len(offs)} neighbour offsets (FCC 1-4NN pairs, 3 smallest triplets, NN tetrahedron).")
+    lines.append("#pragma once")
+    lines.append("#include <cstdint>")
+    lines.append(f"namespace mg {{ namespace {ns} {{")
+    lines.append(f"constexpr int NSPECIES = {basis.n_species};")
+    lines.append(f"constexpr int NFUNC = {basis.n_functions};")
+    lines.append(f"constexpr int NCLASS = {len(bs.classes)};")
+    lines.append(f"constexpr int NFEAT = {bs.n_features};")
+    lines.append(f"constexpr int NOFF = {len(offs)};")
+    lines.append(f"constexpr int HALO = {max(max(abs(c) for c in o) for o in offs)};")
+    # feature -> class, basis index tables
+    lines.append("__host__ __device__ constexpr int feat_class(int k) {")
+    lines.append("  constexpr int t[NFEAT] = {" + ", ".join(str(f.class_index) for f in bs.features) + "};")
+    lines.append("  return t[k];")
+    lines.append("}")
+    lines.append("__host__ __device__ constexpr int feat_b(int k) {")
+    lines.append("  constexpr int t[NFEAT] = {" + ", ".join(str(f.b_site) for f in bs.features) + "};")
+    lines.append("  return t[k];")
+    lines.append("}")
+    # psi tables
+    for b in range(basis.n_functions):
+        lines.append(f"__host__ __device__ constexpr int psi{b}(int o) {{")
+        lines.append("  constexpr int t[NSPECIES] = {" + ", ".join(str(x) for x in basis.psi[b]) + "};")
+        lines.append("  return t[o];")
+        lines.append("}")
+    # psi(b, o) for a runtime occupant index, written arithmetically (no table lookups)
+    if basis.name == "occupation":
+        lines.append("__host__ __device__ __forceinline__ constexpr int psi(int b, int o) { return o; }")
+    else:
+        lines.append("__host__ __device__ __forceinline__ constexpr int psi(int b, int o) {")
+        lines.append("  return b == 0 ? o - 1 : (o == 1 ? -2 : 1);")
+        lines.append("}")
+    # stored code from occupant index
+    if basis.name == "occupation":
+        lines.append("__host__ __device__ constexpr int8_t code_of_occ(int o) { return (int8_t)o; }")
+        lines.append("__host__ __device__ constexpr int occ_of_code(int c) { return c; }")
+    else:
+        lines.append("__host__ __device__ constexpr int8_t code_of_occ(int o) { return (int8_t)(o - 1); }")
+        lines.append("__host__ __device__ constexpr int occ_of_code(int c) { return c + 1; }")
+
+    def emit_loads(offsets, indent="  "):
+        out = []
+        for o in offsets:
+            v = _var(o)
+            out.append(f"{indent}const int {v} = ld({o[0]}, {o[1]}, {o[2]});")
+            if need_t:
+                out.append(f"{indent}const int t_{v} = 3 * {v} * {v} - 2;")
+        return out
+
+    # features
+    lines.append("// F[k] = sum over decorated clusters (class feat_class(k), basis feat_b(k) at the")
+    lines.append("// changing site) of the product of the other sites' integer psi values.")
+    lines.append("template <class Loader>")
+    lines.append("__device__ __forceinline__ void features(const Loader& ld, int (&F)[NFEAT]) {")
+    lines += emit_loads(offs)
+    for k, f in enumerate(bs.features):
+        terms = []
+        for t in f.terms:
+            if len(t) == 0:
+                terms.append("1")
+            else:
+                terms.append(" * ".join(_psi_expr(basis, b, _var(o)) for o, b in t))
+        lines.append(f"  F[{k}] = " + " + ".join(terms) + ";")
+    lines.append("}")
+
+    # anchored correlations
+    anc_offs = sorted({o for cls in bs.anchored for t in cls for o, _ in t})
+    lines.append("// C[f] += sum over decorated clusters of class f anchored at this site (its")
+    lines.append("// lexicographically smallest member) of the product of integer psi values.")
+    lines.append("template <class Loader>")
+    lines.append("__device__ __forceinline__ void anchored(const Loader& ld, long long (&C)[NCLASS]) {")
+    lines += emit_loads(anc_offs)
+    for ci, cls in enumerate(bs.anchored):
+        terms = []
+        for t in cls:
+            if len(t) == 0:
+                terms.append("1")
+            else:
+                terms.append(" * ".join(_psi_expr(basis, b, _var(o)) for o, b in t))
+        lines.append(f"  C[{ci}] += (long long)(" + " + ".join(terms) + ");")
+    lines.append("}")
+    lines.append("}}  // namespace")
+    src = "\n".join(lines) + "\n"
+
+    desc = {
+        "name": kind,
+        "basis": {"name": basis.name, "n_species": basis.n_species, "psi": basis.psi,
+                  "scale": basis.scale},
+        "classes": [
+            {
+                "orbit": c.orbit_index,
+                "size": c.size,
+                "d2": list(c.d2),
+                "multiplicity": c.multiplicity,
+                "decoration": list(c.decoration_multiset()),
+                "scale": bs.class_scale(i),
+            }
+            for i, c in enumerate(bs.classes)
+        ],
+        "features": [
+            {"class": f.class_index, "b": f.b_site, "n_terms": len(f.terms),
+             "max_abs": bs.max_abs_feature(k)}
+            for k, f in enumerate(bs.features)
+        ],
+        "neighbour_offsets": [list(o) for o in offs],
+        "halo": max(max(abs(c) for c in o) for o in offs),
+    }
+    return src, desc
+
+
+def class_tables(descs: dict) -> str:
+    """Host tables (multiplicity, scale, |F| bounds, neighbour offsets) as C++ source."""
+    out = ["// Generated by casmcode_monte_gb300/clex/codegen.py -- do not edit."]
+    for kind, cname in (("fcc_binary", "FccBinary"), ("fcc_ternary", "FccTernary")):
+        d = descs[kind]
+        rows = ", ".join("{%dL, %r}" % (c["multiplicity"], c["scale"]) for c in d["classes"])
+        out.append(f"const mg::ClassInfo k{cname}Classes[] = {{{rows}}};")
+        fm = ", ".join(str(f["max_abs"]) + "L" for f in d["features"])
+        out.append(f"const long k{cname}FeatMax[] = {{{fm}}};")
+        offs = ", ".join(f"{o[0]}, {o[1]}, {o[2]}" for o in d["neighbour_offsets"])
+        out.append(f"const int k{cname}Offsets[] = {{{offs}}};")
+        out.append(f"const int k{cname}NOffsets = {len(d['neighbour_offsets'])};")
+    return "\n".join(out) + "\n"
+
+
+def main():
+    os.makedirs(GEN_DIR, exist_ok=True)
+    descs = {}
+    for kind in ("fcc_binary", "fcc_ternary"):
+        src, desc = generate(kind)
+        descs[kind] = desc
+        with open(os.path.join(GEN_DIR, f"{kind}.cuh"), "w") as f:
+            f.write(src)
+        with open(os.path.join(GEN_DIR, f"{kind}.json"), "w") as f:
+            json.dump(desc, f, indent=1)
+        print(kind, len(src), "bytes")
+    with open(os.path.join(GEN_DIR, "fcc_class_tables.inc"), "w") as f:
+        f.write(class_tables(descs))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,385 @@
+// Graph-coloured semi-grand canonical Metropolis sweep over FCC cluster-expansion
+// Hamiltonians (device code, templated on a generated basis set).
+//
+// Correspondence with the reference loop (basic_occupation_metropolis.hh:381-421 and
+// metropolis.hh:26-35): every site is proposed once per pass (colour by colour, so
+// that same-colour sites share no cluster and are updated concurrently); the change
+// of semi-grand canonical energy is dE = dE_f - mu.(N dx) (basic_semigrand_canonical.hh:
+// 178-192); a proposal is accepted if dE < 0 or u < exp(-beta dE).  Random numbers are
+// Philox4x32-10 keyed by the chain's seed with counter (site, pass, chain, tag), so a
+// trajectory is a pure function of (seed, chain, initial state) independent of the
+// thread mapping.
+//
+// Layout: a chain is owned by a cluster of S CTAs; CTA r holds planes
+// [r*nk, (r+1)*nk) of the L0 x L1 x L2 supercell (l = i + L0*(j + L1*k)) plus a
+// HALO-plane border in k and a HALO-column border in i and j, as int8 codes in shared
+// memory (padded index (i+2) + PX*((j+2) + PY*(k_local+2))).  Neighbour loads are
+// constant offsets from the site's padded index.  An accepted flip writes the site and
+// its periodic copies (own padding and, through distributed shared memory, the halo
+// planes of the neighbouring CTAs).  Phases are separated by cluster barriers
+// (release/acquire).
+//
+// Energies: the generated feature function yields integer local sums F[k]; the FP32
+// fast path computes dE32 = sum_b dpsi_b * (sum_k w32[k] F[k]) - dmu.  A proposal whose
+// FP32 decision could differ from the FP64 one (|dE32| within the rounding bound, or u
+// within the relative bound of exp(-beta dE)) is re-decided exactly in FP64.  Accepted
+// changes of the integer correlation sums are accumulated exactly (int32 per thread per
+// pass, int64 per chain per pass), so per-pass energies carry no drift.
+#pragma once
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mg_common.cuh"
+
+namespace mg {
+
+namespace cg = cooperative_groups;
+
+constexpr int CE_MAX_SPECIES = 3;
+
+struct CeChainParams {
+  double beta;
+  float beta_log2e;
+  float dtol;  // bound on |dE32 - dE64|
+  float eps;   // relative bound on the fast-path acceptance probability
+  uint32_t key0, key1;
+  uint32_t chain_id;
+  double dmu64[CE_MAX_SPECIES * CE_MAX_SPECIES];  // mu . N dx for o -> o2
+  float dmu32[CE_MAX_SPECIES * CE_MAX_SPECIES];
+};
+
+template <int NFEAT>
+struct CeWeights {
+  float w32[NFEAT];
+  double w64[NFEAT];
+};
+
+struct CeGeometry {
+  int L0, L1, L2;
+  int S;   // CTAs per chain
+  int nk;  // planes per CTA
+  int PX, PY, PZ;
+  int n_colors;
+  const int* color_start;    // [S][n_colors + 1]
+  const uint32_t* entries;   // padded index | flags << 24
+  const uint32_t* site_l;    // global linear site index per entry
+};
+
+// slot layout of the per-pass outputs: 0 = accepted proposals, f = change of the
+// integer correlation sum of class f (1..NCLASS-1), NCLASS = proposals re-decided in
+// FP64, NCLASS+1 = FP32 decisions that differ from FP64 (FP32 mode only)
+template <int NCLASS>
+struct CeSlots {
+  static constexpr int N = NCLASS + 2;
+};
+
+template <int NFEAT>
+struct CeSweepArgs {
+  CeGeometry g;
+  CeWeights<NFEAT> w;
+  const CeChainParams* cp;  // [chain]
+  int8_t* occ;              // [chain][N] occupant indices
+  long long pass0;
+  int n_passes;
+  int n_chains;
+  int precision;   // 0: FP64 decisions; 1: FP32 decisions (flips counted)
+  long long* out;  // [n_passes][n_chains][NSLOT]
+};
+
+struct SmemLoader {
+  const int8_t* p;
+  int PX, PXY;
+  __device__ __forceinline__ int operator()(int di, int dj, int dk) const {
+    return p[di + dj * PX + dk * PXY];
+  }
+};
+
+__device__ __forceinline__ float fast_exp2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <class B, int NT>
+__global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__ CeSweepArgs<B::NFEAT> A) {
+  constexpr int NF = B::NFEAT;
+  constexpr int NC = B::NCLASS;
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<NC>::N;
+  extern __shared__ __align__(16) int8_t s[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+
+  const CeGeometry& g = A.g;
+  const int S = g.S;
+  const int chain = blockIdx.x / S;
+  int rank = 0;
+  cg::cluster_group cluster = cg::this_cluster();
+  if (S > 1) rank = (int)cluster.block_rank();
+  auto barrier = [&]() {
+    if (S > 1)
+      cluster.sync();
+    else
+      __syncthreads();
+  };
+
+  const int PX = g.PX, PY = g.PY, PZ = g.PZ, PXY = PX * PY;
+  const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+  const int nk = g.nk;
+  const long long N = (long long)L0 * L1 * L2;
+  const int k0 = rank * nk;
+  int8_t* gocc = A.occ + (size_t)chain * N;
+
+  // ---- load slab + borders
+  for (int idx = threadIdx.x; idx < PXY * PZ; idx += NT) {
+    const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
+    int i = ip - B::HALO, j = jp - B::HALO, k = k0 + kp - B::HALO;
+    i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+    j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+    k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+    s[idx] = B::code_of_occ(gocc[i + (long long)L0 * (j + (long long)L1 * k)]);
+  }
+  if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+
+  int8_t* s_prev = s;
+  int8_t* s_next = s;
+  if (S > 1) {
+    s_prev = cluster.map_shared_rank(s, (unsigned)((rank + S - 1) % S));
+    s_next = cluster.map_shared_rank(s, (unsigned)((rank + 1) % S));
+  }
+  const CeChainParams* cpg = A.cp + chain;
+  if (threadIdx.x < NS * NS) {
+    dmu32_sm[threadIdx.x] = cpg->dmu32[threadIdx.x];
+    dmu64_sm[threadIdx.x] = cpg->dmu64[threadIdx.x];
+  }
+  const double beta = cpg->beta;
+  const float beta_log2e = cpg->beta_log2e, dtol = cpg->dtol, eps = cpg->eps;
+  const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+  const int* cstart = g.color_start + rank * (g.n_colors + 1);
+  const int dI = L0, dJ = L1 * PX, dK = nk * PXY;
+  const int lane = threadIdx.x & 31;
+  barrier();
+
+  int acc[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+
+#pragma unroll 1
+  for (int pass = 0; pass < A.n_passes; ++pass) {
+    const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
+#pragma unroll 1
+    for (int c = 0; c < g.n_colors; ++c) {
+      const int e_end = cstart[c + 1];
+#pragma unroll 1
+      for (int e = cstart[c] + threadIdx.x; e < e_end; e += NT) {
+        const uint32_t ent = g.entries[e];
+        const uint32_t l = g.site_l[e];
+        const int pidx = (int)(ent & 0xFFFFFFu);
+        const uint32_t flags = ent >> 24;
+        const int8_t* p = s + pidx;
+        const int o = B::occ_of_code(*p);
+        const U32x4 x = philox4x32_10(U32x4{l, pass_g, chain_id, SWEEP_TAG}, key0, key1);
+        int o2;
+        if (NS == 2)
+          o2 = 1 - o;
+        else
+          o2 = (o + 1 + (int)(x.y >> 31)) % 3;
+        int F[NF];
+        B::features(SmemLoader{p, PX, PXY}, F);
+        int dpsi[B::NFUNC];
+#pragma unroll
+        for (int b = 0; b < B::NFUNC; ++b) dpsi[b] = B::psi(b, o2) - B::psi(b, o);
+        float G[B::NFUNC];
+#pragma unroll
+        for (int b = 0; b < B::NFUNC; ++b) G[b] = 0.f;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) G[B::feat_b(k)] = fmaf(A.w.w32[k], (float)F[k], G[B::feat_b(k)]);
+        float dE32 = -dmu32_sm[o * NS + o2];
+#pragma unroll
+        for (int b = 0; b < B::NFUNC; ++b) dE32 = fmaf((float)dpsi[b], G[b], dE32);
+
+        const float u32 = __uint2float_rn(x.x) * 2.3283064365386963e-10f;
+        bool amb = false, acc32;
+        if (dE32 < -dtol) {
+          acc32 = true;
+        } else {
+          const float P = fast_exp2(-dE32 * beta_log2e);
+          acc32 = (dE32 < 0.f) || (u32 < P);
+          if (dE32 <= dtol || x.x == 0u)
+            amb = true;
+          else if (!(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps)))
+            amb = true;
+        }
+        bool accept = acc32;
+        if (amb) {
+          // exact FP64 decision: dE64 = sum_b dpsi_b * (sum_k w64[k] F[k]) - dmu
+          double G64[B::NFUNC];
+#pragma unroll
+          for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
+#pragma unroll
+          for (int k = 0; k < NF; ++k)
+            G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(A.w.w64[k], (double)F[k]));
+          double dE = 0.0;
+#pragma unroll
+          for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
+          dE = __dsub_rn(dE, dmu64_sm[o * NS + o2]);
+          bool acc64;
+          if (dE < 0.0) {
+            acc64 = true;
+          } else {
+            const double u = __dmul_rn((double)x.x, 2.3283064365386962890625e-10);
+            acc64 = u < exp(__dmul_rn(-dE, beta));
+          }
+          acc[NC] += 1;
+          if (A.precision == 0) {
+            accept = acc64;
+          } else if (acc64 != acc32) {
+            acc[NC + 1] += 1;
+          }
+        }
+        if (accept) {
+          const int8_t c2 = B::code_of_occ(o2);
+          const int oi = (flags & 1u) ? dI : ((flags & 2u) ? -dI : 0);
+          const int oj = (flags & 4u) ? dJ : ((flags & 8u) ? -dJ : 0);
+          s[pidx] = c2;
+          if (oi) s[pidx + oi] = c2;
+          if (oj) s[pidx + oj] = c2;
+          if (oi && oj) s[pidx + oi + oj] = c2;
+          if (flags & 16u) {
+            int8_t* r = s_prev + pidx + dK;
+            r[0] = c2;
+            if (oi) r[oi] = c2;
+            if (oj) r[oj] = c2;
+            if (oi && oj) r[oi + oj] = c2;
+          }
+          if (flags & 32u) {
+            int8_t* r = s_next + pidx - dK;
+            r[0] = c2;
+            if (oi) r[oi] = c2;
+            if (oj) r[oj] = c2;
+            if (oi && oj) r[oi + oj] = c2;
+          }
+          acc[0] += 1;
+#pragma unroll
+          for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += dpsi[B::feat_b(k)] * F[k];
+        }
+      }
+      barrier();
+      if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+        // flush the previous pass (all warps added to it before this barrier)
+        int* buf = acc_sm[(pass - 1) & 1];
+        const int v = buf[threadIdx.x];
+        buf[threadIdx.x] = 0;
+        if (v)
+          atomicAdd(reinterpret_cast<unsigned long long*>(
+                        A.out + ((size_t)(pass - 1) * A.n_chains + chain) * NSLOT + threadIdx.x),
+                    (unsigned long long)(long long)v);
+      }
+    }
+    // per-warp reduction of this pass's accumulators into shared memory
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) {
+      const int v = warp_sum(acc[q]);
+      if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+      acc[q] = 0;
+    }
+  }
+  barrier();
+  if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+    const int pl = A.n_passes - 1;
+    int* buf = acc_sm[pl & 1];
+    const int v = buf[threadIdx.x];
+    if (v)
+      atomicAdd(reinterpret_cast<unsigned long long*>(A.out + ((size_t)pl * A.n_chains + chain) * NSLOT + threadIdx.x),
+                (unsigned long long)(long long)v);
+  }
+  // ---- write back own planes
+  for (int idx = threadIdx.x; idx < L0 * L1 * nk; idx += NT) {
+    const int i = idx % L0, j = (idx / L0) % L1, kl = idx / (L0 * L1);
+    const int pidx = (i + B::HALO) + PX * ((j + B::HALO) + PY * (kl + B::HALO));
+    gocc[i + (long long)L0 * (j + (long long)L1 * (k0 + kl))] = (int8_t)B::occ_of_code(s[pidx]);
+  }
+  barrier();
+}
+
+// ---- global-memory evaluation (per-proposal dE and full correlation sums)
+
+struct GlobalLoader {
+  const int8_t* occ;  // occupant indices of one chain
+  int i, j, k, L0, L1, L2;
+  int (*code)(int);
+  __device__ __forceinline__ int idx(int di, int dj, int dk) const {
+    int a = i + di, b = j + dj, c = k + dk;
+    a = (a < 0) ? a + L0 : (a >= L0 ? a - L0 : a);
+    b = (b < 0) ? b + L1 : (b >= L1 ? b - L1 : b);
+    c = (c < 0) ? c + L2 : (c >= L2 ? c - L2 : c);
+    return a + L0 * (b + L1 * c);
+  }
+};
+
+template <class B>
+struct GlobalCodeLoader {
+  GlobalLoader g;
+  __device__ __forceinline__ int operator()(int di, int dj, int dk) const {
+    return B::code_of_occ(g.occ[g.idx(di, dj, dk)]);
+  }
+};
+
+template <class B>
+__global__ void ce_delta_e_kernel(CeWeights<B::NFEAT> w, const int8_t* occ, int L0, int L1, int L2,
+                                  const CeChainParams* cp, const int* chain, const long long* sites,
+                                  const int8_t* new_occ, long long n, double* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  constexpr int NS = B::NSPECIES;
+  const long long N = (long long)L0 * L1 * L2;
+  const int c = chain[t];
+  const int8_t* o8 = occ + (size_t)c * N;
+  const long long l = sites[t];
+  const int i = (int)(l % L0), j = (int)((l / L0) % L1), k = (int)(l / ((long long)L0 * L1));
+  GlobalCodeLoader<B> ld{GlobalLoader{o8, i, j, k, L0, L1, L2, nullptr}};
+  int F[B::NFEAT];
+  B::features(ld, F);
+  const int o = o8[l], o2 = new_occ[t];
+  double G64[B::NFUNC];
+  for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
+  for (int k2 = 0; k2 < B::NFEAT; ++k2)
+    G64[B::feat_b(k2)] = __dadd_rn(G64[B::feat_b(k2)], __dmul_rn(w.w64[k2], (double)F[k2]));
+  double dE = 0.0;
+  for (int b = 0; b < B::NFUNC; ++b)
+    dE = __dadd_rn(dE, __dmul_rn((double)(B::psi(b, o2) - B::psi(b, o)), G64[b]));
+  out[t] = __dsub_rn(dE, cp[c].dmu64[o * NS + o2]);
+}
+
+template <class B>
+__global__ void ce_corr_kernel(const int8_t* occ, int L0, int L1, int L2, int n_chains, long long* out) {
+  // grid: (blocks per chain, chains); out[chain][NCLASS]
+  constexpr int NC = B::NCLASS;
+  const int c = blockIdx.y;
+  const long long N = (long long)L0 * L1 * L2;
+  const int8_t* o8 = occ + (size_t)c * N;
+  long long C[NC];
+  for (int f = 0; f < NC; ++f) C[f] = 0;
+  for (long long l = (long long)blockIdx.x * blockDim.x + threadIdx.x; l < N; l += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(l % L0), j = (int)((l / L0) % L1), k = (int)(l / ((long long)L0 * L1));
+    GlobalCodeLoader<B> ld{GlobalLoader{o8, i, j, k, L0, L1, L2, nullptr}};
+    B::anchored(ld, C);
+  }
+  for (int f = 0; f < NC; ++f) {
+    long long v = C[f];
+    for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o2);
+    if ((threadIdx.x & 31) == 0 && v)
+      atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)c * NC + f), (unsigned long long)v);
+  }
+}
+
+}  // namespace mg

@@ -1,0 +1,143 @@
+/*
+ * montegpu.h -- C-ABI of the GB300 lattice Metropolis library (libmontegpu.so).
+ *
+ * Plain C types only: opaque handles, pointers and sizes.  Every function returns an
+ * int status (MG_OK = 0); on failure mg_last_error() returns a message in the style of
+ * the reference's std::runtime_error texts ("Error in ...").  No function throws across
+ * the ABI.  Caller-owned buffers are copied; the library owns its handles.  A handle
+ * must not be used from two host threads at once (the reference's own event
+ * proposal helpers are non-reentrant too: function-local statics in
+ * include/casm/monte/events/OccEventProposal.hh:127,279).
+ *
+ * Which reference interface each group replaces (paths within libcasm-monte):
+ *   - RandomNumberEngine / RandomNumberGenerator:
+ *       include/casm/monte/RandomNumberGenerator.hh:15-42, definitions.hh:17,
+ *       python/src/monte.cpp:469-545 (seed, seed_seq, dump, load, random_int, random_real)
+ *   - Ising serial replay: the main loop of
+ *       include/casm/monte/methods/basic_occupation_metropolis.hh:354-425 as driven by
+ *       include/casm/monte/ising_cpp/basic_semigrand_canonical.hh:416-470 (run), with the
+ *       model of include/casm/monte/ising_cpp/model.hh:164-436
+ *   - CE batch: the semi-grand canonical potential slot
+ *       (basic_semigrand_canonical.hh:104-199, occ_delta_per_supercell) filled by a
+ *       cluster-expansion formation energy, and the per-step loop of
+ *       include/casm/monte/methods/occupation_metropolis.hh:114-150, run as coloured sweeps
+ *   - statistics: src/casm/monte/checks/EquilibrationCheck.cc:50-162,
+ *       src/casm/monte/BasicStatistics.cc:24-188, include/casm/monte/misc/math.hh:62-72
+ */
+#ifndef MONTEGPU_H
+#define MONTEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MG_OK 0
+#define MG_ERR_INVALID 1 /* invalid argument (reference: std::runtime_error) */
+#define MG_ERR_CUDA 2    /* CUDA runtime error */
+#define MG_ERR_DEVICE 4  /* a kernel reported an error status */
+
+/* ---- library ---- */
+const char* mg_last_error(void); /* thread-local message of the last failure */
+int mg_version(void);            /* 100 * major + minor */
+int mg_device_count(int* n);
+int mg_device_sm_count(int* n);
+
+/* ---- mt19937_64 engine (RandomNumberEngine; monte.cpp:469-513) ---- */
+typedef struct mg_engine mg_engine;
+/* seed_from_device != 0: seed from std::random_device (RandomNumberGenerator.hh:20-28) */
+int mg_engine_create(int seed_from_device, mg_engine** out);
+int mg_engine_destroy(mg_engine* e);
+int mg_engine_seed(mg_engine* e, uint64_t value);
+int mg_engine_seed_seq(mg_engine* e, const uint64_t* values, size_t n);
+/* state as text in the std::mersenne_twister_engine stream format */
+int mg_engine_dump(const mg_engine* e, char* buf, size_t len);
+int mg_engine_load(mg_engine* e, const char* state);
+/* RandomNumberGenerator::random_int (uniform_int_distribution, [0, max]) */
+int mg_engine_random_int(mg_engine* e, uint64_t max, uint64_t* out);
+/* RandomNumberGenerator::random_real (uniform_real_distribution, [0, max)) */
+int mg_engine_random_real(mg_engine* e, double max, double* out);
+
+/* ---- 2-D Ising semi-grand canonical serial replay (bit-exact with the reference) ----
+ * n_chains independent chains of rows x cols sites (column-major, l = rows*j + i,
+ * values +1/-1); per chain J, temperature [K], exchange potential mu and an mt19937_64
+ * engine state (text).  use_nlist selects which reference formation-energy summation
+ * (model.hh:259-290) the samples reproduce. */
+typedef struct mg_ising_replay mg_ising_replay;
+int mg_ising_replay_create(int rows, int cols, int n_chains, int use_nlist, const double* J,
+                           const double* temperature, const double* mu, const int32_t* occ,
+                           const char* const* engine_states, mg_ising_replay** out);
+/* Run n_passes passes (each rows*cols steps).  After every pass whose running count is a
+ * multiple of sample_period one sample is written per chain:
+ * samples_out[chain][max_samples][2 + rows + cols] = {sum s, sum over bonds s_a s_b,
+ * row dot products (rows), column dot products (cols)} (dots only when use_nlist == 0). */
+int mg_ising_replay_run(mg_ising_replay* h, int n_passes, int sample_period,
+                        long long* samples_out, int max_samples, int* n_samples_out);
+/* occupation [n_chains][N], engine states (buffers of state_len bytes each), counters */
+int mg_ising_replay_get_state(mg_ising_replay* h, int32_t* occ, char** engine_states,
+                              size_t state_len, unsigned long long* n_accept,
+                              unsigned long long* n_reject);
+int mg_ising_replay_last_kernel_ms(mg_ising_replay* h, float* ms);
+int mg_ising_replay_destroy(mg_ising_replay* h);
+
+/* ---- FCC cluster expansion: model and coloured-sweep chain batch ----
+ * basis_kind 0: binary occupation basis (species A,B); 1: ternary Chebyshev basis (A,B,C).
+ * eci[n_classes]: one ECI per symmetrised cluster function in the library's class order
+ * (empty, point, pairs 1-4NN, triplets, NN tetrahedron; decorated classes for ternary). */
+typedef struct mg_ce_model mg_ce_model;
+int mg_ce_model_create(int basis_kind, const double* eci, int n_eci, mg_ce_model** out);
+int mg_ce_model_info(const mg_ce_model* m, int* n_classes, int* n_features, int* n_species);
+/* per-class multiplicity (clusters per primitive cell) and scale prod(a_b) */
+int mg_ce_model_classes(const mg_ce_model* m, long* multiplicity, double* scale);
+int mg_ce_model_destroy(mg_ce_model* m);
+
+typedef struct mg_ce_batch mg_ce_batch;
+/* n_chains chains of an L0 x L1 x L2 primitive-cell supercell (l = i + L0*(j + L1*k)),
+ * occ[n_chains][N] occupant indices, temperature[n_chains] (K),
+ * mu[n_chains][n_species-1] exchange potentials conjugate to x_i = n(species i+1)/N,
+ * seeds[n_chains] (Philox keys), chain_ids (Philox counter word, NULL = 0..n-1).
+ * precision 0: FP64 acceptance decisions; 1: FP32 decisions (disagreements counted).
+ * ctas_per_chain 0 = choose automatically. */
+int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chains,
+                       const double* temperature, const double* mu, const uint64_t* seeds,
+                       const uint32_t* chain_ids, const int8_t* occ, int precision,
+                       int ctas_per_chain, mg_ce_batch** out);
+/* launch geometry: CTAs per chain, colours, threads per CTA, dynamic shared bytes */
+int mg_ce_batch_info(const mg_ce_batch* b, int* ctas_per_chain, int* n_colors, int* threads,
+                     size_t* smem_bytes);
+int mg_ce_batch_colors(const mg_ce_batch* b, int32_t* color /* [N] */);
+/* Run n_passes passes.  out (host, may be NULL) receives [n_passes][n_chains][n_classes+2]
+ * int64: slot 0 accepted proposals, slot f (1..n_classes-1) change of the integer
+ * correlation sum of class f, slot n_classes proposals re-decided in FP64, slot
+ * n_classes+1 FP32 decisions that differ from FP64. */
+int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out);
+/* device time of the sweep kernel(s) of the last run, from CUDA events on the batch's
+ * stream */
+int mg_ce_batch_last_kernel_ms(const mg_ce_batch* b, float* ms);
+int mg_ce_batch_get_occ(mg_ce_batch* b, int8_t* occ);
+int mg_ce_batch_set_occ(mg_ce_batch* b, const int8_t* occ);
+/* full recompute of the integer correlation sums [n_chains][n_classes] */
+int mg_ce_batch_corr(mg_ce_batch* b, long long* out);
+/* per-proposal FP64 dE (formation + semi-grand canonical term) on the current state */
+int mg_ce_batch_delta_e(mg_ce_batch* b, const int32_t* chain, const long long* sites,
+                        const int8_t* new_occ, long long n, double* out);
+int mg_ce_batch_destroy(mg_ce_batch* b);
+
+/* ---- statistics (host numerics shared with the device convergence kernel) ---- */
+/* _default_equilibration_check (EquilibrationCheck.cc:50-117) */
+int mg_equilibration_check(const double* obs, long n, double prec, int* is_equilibrated,
+                           long* n_samples_for_equilibration);
+/* BasicStatisticsCalculator (BasicStatistics.cc:114-188); nw = 0 for unweighted */
+int mg_basic_statistics(const double* obs, long n, const double* w, long nw, double confidence,
+                        long method, long n_resamples, double* mean,
+                        double* calculated_precision);
+int mg_autocorrelation_factor(const double* obs, long n, double increment, double* out);
+double mg_approx_erf_inv(double x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MONTEGPU_H */

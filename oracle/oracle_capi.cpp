@@ -1,0 +1,312 @@
+// ORACLE (test infrastructure only): C entry points over the CPU restatement, loaded
+// with ctypes by tests/, __graft_entry__.smoke() and bench.py's CPU baseline.  Never
+// part of the product path.
+#include <chrono>
+#include <cstring>
+#include <random>
+#include <sstream>
+#include <string>
+
+#include "oracle_ce.hh"
+
+using namespace oracle;
+
+namespace {
+
+std::string g_engine_state;
+
+void load_engine(std::mt19937_64& e, const char* state) {
+  std::stringstream ss(state);
+  ss >> e;
+}
+
+}  // namespace
+
+extern "C" {
+
+struct OrcCCParams {
+  int has_min_count, has_min_sample, has_max_count, has_max_sample;
+  long min_count, min_sample, max_count, max_sample;
+  int log_spacing;
+  long check_begin, check_period;
+  double check_base, check_shift;
+  long check_period_max;
+  double confidence;
+  // requested precision for up to 4 sampler components (sampler index into the run's
+  // sampler names, component index)
+  int n_req;
+  int req_sampler[4];
+  int req_component[4];
+  int req_abs_flag[4];
+  double req_abs[4];
+  int req_rel_flag[4];
+  double req_rel[4];
+};
+
+struct OrcRunOut {
+  long n_pass;
+  long long n_accept, n_reject;
+  long n_samples;
+  int is_complete, all_equilibrated, all_converged;
+  long n_checks;
+  long N_samples_for_all_to_equilibrate;
+  long N_samples_for_statistics;
+  double mean[4];
+  double calculated_precision[4];
+  int is_converged[4];
+};
+
+// the 10000th output of a default-constructed std::mt19937_64 ([rand.predef])
+unsigned long long orc_mt19937_64_10000th() {
+  std::mt19937_64 e;
+  e.discard(9999);
+  return e();
+}
+
+// Draws from the reference's RandomNumberGenerator: kind 0 = random_int(max_i),
+// kind 1 = random_real(max_r); engine state in/out as text (operator<< format).
+int orc_rng_draws(const char* state_in, int kind, long max_i, double max_r, long n, long* out_i,
+                  double* out_r, char* state_out, long state_len) {
+  std::mt19937_64 e;
+  load_engine(e, state_in);
+  RNG rng{&e};
+  for (long i = 0; i < n; ++i) {
+    if (kind == 0)
+      out_i[i] = rng.random_int(max_i);
+    else
+      out_r[i] = rng.random_real(max_r);
+  }
+  std::stringstream ss;
+  ss << e;
+  std::string s = ss.str();
+  if ((long)s.size() + 1 > state_len) return -1;
+  std::memcpy(state_out, s.c_str(), s.size() + 1);
+  return 0;
+}
+
+int orc_engine_seed(unsigned long long seed, char* state_out, long state_len) {
+  std::mt19937_64 e(seed);
+  std::stringstream ss;
+  ss << e;
+  std::string s = ss.str();
+  if ((long)s.size() + 1 > state_len) return -1;
+  std::memcpy(state_out, s.c_str(), s.size() + 1);
+  return 0;
+}
+
+// Ising semi-grand canonical run with the reference's semantics.  samplers are
+// "formation_energy"(0), "param_composition"(1), "potential_energy"(2) (map order).
+int orc_ising_run(long rows, long cols, double J, int use_nlist, double T, double mu, int* occ,
+                  const OrcCCParams* p, int sample_period, const char* engine_state,
+                  double* samples_out, long max_samples, OrcRunOut* out, char* state_out,
+                  long state_len) {
+  try {
+    IsingModel m;
+    m.rows = rows;
+    m.cols = cols;
+    m.J = J;
+    m.use_nlist = use_nlist != 0;
+    m.occ.assign(occ, occ + rows * cols);
+    CompletionCheckParams ccp;
+    if (p->has_min_count) ccp.cutoff_params.min_count = p->min_count;
+    if (p->has_min_sample) ccp.cutoff_params.min_sample = p->min_sample;
+    if (p->has_max_count) ccp.cutoff_params.max_count = p->max_count;
+    if (p->has_max_sample) ccp.cutoff_params.max_sample = p->max_sample;
+    ccp.log_spacing = p->log_spacing != 0;
+    ccp.check_begin = p->check_begin;
+    ccp.check_period = p->check_period;
+    ccp.check_base = p->check_base;
+    ccp.check_shift = p->check_shift;
+    ccp.check_period_max = p->check_period_max;
+    ccp.calc_statistics.confidence = p->confidence;
+    const char* names[3] = {"formation_energy", "param_composition", "potential_energy"};
+    std::vector<SamplerComponent> keys;
+    for (int r = 0; r < p->n_req; ++r) {
+      SamplerComponent k{names[p->req_sampler[r]], p->req_component[r]};
+      RequestedPrecision rp;
+      rp.abs_convergence_is_required = p->req_abs_flag[r] != 0;
+      rp.abs_precision = p->req_abs[r];
+      rp.rel_convergence_is_required = p->req_rel_flag[r] != 0;
+      rp.rel_precision = p->req_rel[r];
+      ccp.requested_precision[k] = rp;
+      keys.push_back(k);
+    }
+    std::mt19937_64 e;
+    load_engine(e, engine_state);
+    IsingRunResult R = run_ising_sgc(m, T, mu, ccp, sample_period, e);
+    std::memcpy(occ, m.occ.data(), sizeof(int) * m.occ.size());
+    long ns = get_n_samples(R.samplers);
+    out->n_samples = ns;
+    for (int s = 0; s < 3; ++s) {
+      const auto& col = R.samplers.at(names[s]).cols[0];
+      for (long i = 0; i < ns && i < max_samples; ++i) samples_out[s * max_samples + i] = col[i];
+    }
+    out->n_pass = R.n_pass;
+    out->n_accept = R.n_accept;
+    out->n_reject = R.n_reject;
+    out->is_complete = R.results.is_complete;
+    out->all_equilibrated = R.results.equilibration_check_results.all_equilibrated;
+    out->all_converged = R.results.convergence_check_results.all_converged;
+    out->n_checks = R.n_checks;
+    out->N_samples_for_all_to_equilibrate =
+        R.results.equilibration_check_results.N_samples_for_all_to_equilibrate;
+    out->N_samples_for_statistics = R.results.convergence_check_results.N_samples_for_statistics;
+    for (size_t r = 0; r < keys.size(); ++r) {
+      auto& ir = R.results.convergence_check_results.individual_results;
+      auto it = ir.find(keys[r]);
+      if (it != ir.end()) {
+        out->mean[r] = it->second.stats.mean;
+        out->calculated_precision[r] = it->second.stats.calculated_precision;
+        out->is_converged[r] = it->second.is_converged;
+      } else {
+        out->mean[r] = 0.0;
+        out->calculated_precision[r] = -1.0;
+        out->is_converged[r] = 0;
+      }
+    }
+    std::stringstream ss;
+    ss << e;
+    std::string s = ss.str();
+    if ((long)s.size() + 1 > state_len) return -1;
+    std::memcpy(state_out, s.c_str(), s.size() + 1);
+    return 0;
+  } catch (std::exception&) {
+    return -2;
+  }
+}
+
+// Ising ΔE / energies for known-answer checks
+double orc_ising_delta(long rows, long cols, double J, int use_nlist, const int* occ, long l,
+                       int new_occ, double mu) {
+  IsingModel m{rows, cols, J, use_nlist != 0, std::vector<int>(occ, occ + rows * cols), {}, {}};
+  if (m.use_nlist) m.build_nlist();
+  double dEf = m.delta_formation(l, new_occ);
+  double Ndx = 0.0;
+  Ndx += (new_occ - m.occ[l]) / 2.0;
+  return dEf - mu * Ndx;
+}
+double orc_ising_formation(long rows, long cols, double J, int use_nlist, const int* occ) {
+  IsingModel m{rows, cols, J, use_nlist != 0, std::vector<int>(occ, occ + rows * cols), {}, {}};
+  if (m.use_nlist) m.build_nlist();
+  return m.formation_per_supercell();
+}
+
+// statistics
+void orc_equilibration_check(const double* obs, long n, double prec, int* is_eq, long* n_eq) {
+  auto r = default_equilibration_check_raw(obs, n, prec);
+  *is_eq = r.is_equilibrated;
+  *n_eq = r.N_samples_for_equilibration;
+}
+void orc_basic_statistics(const double* obs, long n, const double* w, long nw, double confidence,
+                          long method, long n_resamples, double* mean, double* prec) {
+  BasicStatisticsCalculator c;
+  c.confidence = confidence;
+  c.method = method;
+  c.n_resamples = n_resamples;
+  auto s = c(obs, n, w, nw);
+  *mean = s.mean;
+  *prec = s.calculated_precision;
+}
+double orc_autocorrelation_factor(const double* obs, long n, double increment) {
+  return autocorrelation_factor(obs, n, increment);
+}
+double orc_approx_erf_inv(double x) { return approx_erf_inv(x); }
+
+void orc_philox4x32_10(const unsigned int* ctr, const unsigned int* key, unsigned int* out) {
+  auto r = philox4x32_10({ctr[0], ctr[1], ctr[2], ctr[3]}, {key[0], key[1]});
+  for (int i = 0; i < 4; ++i) out[i] = r[i];
+}
+
+// ---- cluster expansion ----
+void* orc_ce_create(long L0, long L1, long L2, int n_species, const double* V, int n_classes) {
+  try {
+    auto* S = new CESupercell();
+    S->L0 = L0;
+    S->L1 = L1;
+    S->L2 = L2;
+    S->basis = make_oracle_basis(n_species);
+    S->build();
+    if ((int)S->classes.size() != n_classes) {
+      delete S;
+      return nullptr;
+    }
+    S->V.assign(V, V + n_classes);
+    return S;
+  } catch (std::exception&) {
+    return nullptr;
+  }
+}
+void orc_ce_destroy(void* h) { delete static_cast<CESupercell*>(h); }
+int orc_ce_n_classes_for(int n_species) {
+  return (int)enumerate_classes(make_oracle_basis(n_species)).size();
+}
+// class info: size, multiplicity, decoration multiset packed as base-4 digits
+void orc_ce_class_info(int n_species, int* sizes, long* mults, long* decor_code) {
+  auto cls = enumerate_classes(make_oracle_basis(n_species));
+  for (size_t c = 0; c < cls.size(); ++c) {
+    sizes[c] = cls[c].size;
+    mults[c] = cls[c].multiplicity;
+    long code = 0;
+    for (int b : cls[c].decoration) code = code * 4 + (b + 1);
+    decor_code[c] = code;
+  }
+}
+double orc_ce_delta_e(void* h, const int* occ, long l, int new_occ, const double* mu, int n_mu) {
+  auto* S = static_cast<CESupercell*>(h);
+  std::vector<double> m(mu, mu + n_mu);
+  return S->delta_formation(occ, l, new_occ) - S->mu_dot_Ndx(m, occ[l], new_occ);
+}
+double orc_ce_formation(void* h, const int* occ) {
+  return static_cast<CESupercell*>(h)->formation_per_supercell(occ);
+}
+void orc_ce_int_corr(void* h, const int* occ, long long* out) {
+  auto C = static_cast<CESupercell*>(h)->int_corr(occ);
+  for (size_t i = 0; i < C.size(); ++i) out[i] = C[i];
+}
+int orc_ce_colored_sweep(void* h, int* occ, double T, const double* mu, int n_mu,
+                         unsigned long long seed, unsigned int chain, const int* color,
+                         int n_colors, long pass0, long n_passes, long long* corr_out,
+                         long long* nacc_out) {
+  auto* S = static_cast<CESupercell*>(h);
+  std::vector<double> m(mu, mu + n_mu);
+  std::vector<int> col(color, color + S->n());
+  auto R = colored_sweep(*S, occ, T, m, seed, chain, col, n_colors, pass0, n_passes);
+  long nc = (long)S->classes.size();
+  for (long p = 0; p < n_passes; ++p) {
+    for (long c = 0; c < nc; ++c) corr_out[p * nc + c] = R.corr[p][c];
+    nacc_out[p] = R.n_accept[p];
+  }
+  return 0;
+}
+
+// The reference's random-site semi-grand canonical loop (basic_semigrand_canonical.hh:
+// 308-320 proposal, basic_occupation_metropolis.hh:381-404 accept/apply) with the
+// clexulator-style CE potential; used as the timed CPU baseline.  Binary: o -> 1-o;
+// ternary: the other two species with equal probability (the SGC swap distribution of
+// OccEventProposal.hh:260-336).  Returns accepted steps; *seconds = wall time.
+long long orc_ce_random_site_run(void* h, int* occ, double T, const double* mu, int n_mu,
+                                 unsigned long long seed, long long n_steps, double* seconds) {
+  auto* S = static_cast<CESupercell*>(h);
+  std::vector<double> m(mu, mu + n_mu);
+  std::mt19937_64 e(seed);
+  RNG rng{&e};
+  double beta = 1.0 / (KB * T);
+  long max_l = S->n() - 1;
+  long long nacc = 0;
+  auto t0 = std::chrono::steady_clock::now();
+  for (long long s = 0; s < n_steps; ++s) {
+    long l = rng.random_int(max_l);
+    int o = occ[l];
+    int o2 = (S->basis.n_species == 2) ? 1 - o : (o + 1 + (int)rng.random_int(1L)) % 3;
+    double dE = S->delta_formation(occ, l, o2) - S->mu_dot_Ndx(m, o, o2);
+    if (metropolis_acceptance(dE, beta, rng)) {
+      occ[l] = o2;
+      ++nacc;
+    }
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  *seconds = std::chrono::duration<double>(t1 - t0).count();
+  return nacc;
+}
+
+}  // extern "C"

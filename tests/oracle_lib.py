@@ -1,0 +1,182 @@
+"""ctypes access to the CPU oracle (oracle/build/liboracle.so) -- test infrastructure only."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PATH = os.path.join(ROOT, "oracle", "build", "liboracle.so")
+
+_lib = None
+
+
+class OrcCCParams(C.Structure):
+    _fields_ = [
+        ("has_min_count", C.c_int), ("has_min_sample", C.c_int), ("has_max_count", C.c_int),
+        ("has_max_sample", C.c_int), ("min_count", C.c_long), ("min_sample", C.c_long),
+        ("max_count", C.c_long), ("max_sample", C.c_long), ("log_spacing", C.c_int),
+        ("check_begin", C.c_long), ("check_period", C.c_long), ("check_base", C.c_double),
+        ("check_shift", C.c_double), ("check_period_max", C.c_long), ("confidence", C.c_double),
+        ("n_req", C.c_int), ("req_sampler", C.c_int * 4), ("req_component", C.c_int * 4),
+        ("req_abs_flag", C.c_int * 4), ("req_abs", C.c_double * 4), ("req_rel_flag", C.c_int * 4),
+        ("req_rel", C.c_double * 4),
+    ]
+
+
+class OrcRunOut(C.Structure):
+    _fields_ = [
+        ("n_pass", C.c_long), ("n_accept", C.c_longlong), ("n_reject", C.c_longlong), ("n_samples", C.c_long),
+        ("is_complete", C.c_int), ("all_equilibrated", C.c_int), ("all_converged", C.c_int),
+        ("n_checks", C.c_long), ("N_samples_for_all_to_equilibrate", C.c_long),
+        ("N_samples_for_statistics", C.c_long), ("mean", C.c_double * 4),
+        ("calculated_precision", C.c_double * 4), ("is_converged", C.c_int * 4),
+    ]
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(PATH):
+            subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True, capture_output=True)
+        L = C.CDLL(PATH)
+        dp, lp, ip = C.POINTER(C.c_double), C.POINTER(C.c_long), C.POINTER(C.c_int)
+        L.orc_mt19937_64_10000th.restype = C.c_ulonglong
+        L.orc_rng_draws.argtypes = [C.c_char_p, C.c_int, C.c_long, C.c_double, C.c_long, lp, dp, C.c_char_p, C.c_long]
+        L.orc_engine_seed.argtypes = [C.c_ulonglong, C.c_char_p, C.c_long]
+        L.orc_ising_run.argtypes = [C.c_long, C.c_long, C.c_double, C.c_int, C.c_double, C.c_double, ip,
+                                    C.POINTER(OrcCCParams), C.c_int, C.c_char_p, dp, C.c_long,
+                                    C.POINTER(OrcRunOut), C.c_char_p, C.c_long]
+        L.orc_ising_delta.argtypes = [C.c_long, C.c_long, C.c_double, C.c_int, ip, C.c_long, C.c_int, C.c_double]
+        L.orc_ising_formation.argtypes = [C.c_long, C.c_long, C.c_double, C.c_int, ip]
+        L.orc_equilibration_check.argtypes = [dp, C.c_long, C.c_double, ip, lp]
+        L.orc_basic_statistics.argtypes = [dp, C.c_long, dp, C.c_long, C.c_double, C.c_long, C.c_long, dp, dp]
+        L.orc_autocorrelation_factor.argtypes = [dp, C.c_long, C.c_double]
+        L.orc_approx_erf_inv.argtypes = [C.c_double]
+        L.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint), C.POINTER(C.c_uint), C.POINTER(C.c_uint)]
+        L.orc_ce_n_classes_for.argtypes = [C.c_int]
+        L.orc_ce_class_info.argtypes = [C.c_int, ip, lp, lp]
+        L.orc_ising_delta.restype = C.c_double
+        L.orc_ising_formation.restype = C.c_double
+        L.orc_autocorrelation_factor.restype = C.c_double
+        L.orc_approx_erf_inv.restype = C.c_double
+        L.orc_ce_create.restype = C.c_void_p
+        L.orc_ce_create.argtypes = [C.c_long, C.c_long, C.c_long, C.c_int, C.POINTER(C.c_double), C.c_int]
+        L.orc_ce_destroy.argtypes = [C.c_void_p]
+        L.orc_ce_delta_e.restype = C.c_double
+        L.orc_ce_delta_e.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_long, C.c_int, C.POINTER(C.c_double), C.c_int]
+        L.orc_ce_formation.restype = C.c_double
+        L.orc_ce_formation.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+        L.orc_ce_int_corr.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
+        L.orc_ce_colored_sweep.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int,
+                                           C.c_ulonglong, C.c_uint, C.POINTER(C.c_int), C.c_int, C.c_long, C.c_long,
+                                           C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        L.orc_ce_random_site_run.restype = C.c_longlong
+        L.orc_ce_random_site_run.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int,
+                                             C.c_ulonglong, C.c_longlong, C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def engine_state(seed: int) -> str:
+    L = load()
+    buf = C.create_string_buffer(16384)
+    assert L.orc_engine_seed(seed, buf, len(buf)) == 0
+    return buf.value.decode()
+
+
+def make_cc_params(min_sample=None, max_sample=None, min_count=None, max_count=None, check_begin=100,
+                   check_period=100, log_spacing=False, reqs=(), confidence=0.95):
+    """reqs: list of (sampler index (0 formation, 1 param_composition, 2 potential), abs)."""
+    P = OrcCCParams()
+    P.has_min_sample = int(min_sample is not None)
+    P.min_sample = min_sample or 0
+    P.has_max_sample = int(max_sample is not None)
+    P.max_sample = max_sample or 0
+    P.has_min_count = int(min_count is not None)
+    P.min_count = min_count or 0
+    P.has_max_count = int(max_count is not None)
+    P.max_count = max_count or 0
+    P.log_spacing = int(log_spacing)
+    P.check_begin, P.check_period = check_begin, check_period
+    P.check_base, P.check_shift, P.check_period_max = 10.0, 2.0, 10000
+    P.confidence = confidence
+    P.n_req = len(reqs)
+    for i, (s, a) in enumerate(reqs):
+        P.req_sampler[i] = s
+        P.req_component[i] = 0
+        P.req_abs_flag[i] = 1
+        P.req_abs[i] = a
+    return P
+
+
+def ising_run(rows, cols, J, use_nlist, T, mu, occ, params, sample_period, seed_state, max_samples=200000):
+    L = load()
+    occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
+    samples = np.zeros((3, max_samples), dtype=np.float64)
+    out = OrcRunOut()
+    st = C.create_string_buffer(16384)
+    rc = L.orc_ising_run(rows, cols, J, int(use_nlist), T,
+                         mu, p(occ, C.c_int), C.byref(params), sample_period,
+                         seed_state.encode(), p(samples, C.c_double), max_samples, C.byref(out), st,
+                         len(st))
+    assert rc == 0, rc
+    n = out.n_samples
+    return {"occ": occ, "formation_energy": samples[0, :n].copy(), "param_composition": samples[1, :n].copy(),
+            "potential_energy": samples[2, :n].copy(), "out": out, "engine": st.value.decode()}
+
+
+class OracleCE:
+    """Oracle cluster-expansion supercell."""
+
+    def __init__(self, L, n_species, eci):
+        self.L = L
+        self.n = L[0] * L[1] * L[2]
+        self.n_species = n_species
+        self.eci = np.ascontiguousarray(np.asarray(eci, dtype=np.float64))
+        lib = load()
+        self.h = lib.orc_ce_create(L[0], L[1], L[2], n_species, p(self.eci, C.c_double), self.eci.size)
+        assert self.h, "oracle CE construction failed (class count mismatch?)"
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().orc_ce_destroy(self.h)
+            self.h = None
+
+    def delta_e(self, occ, l, new, mu):
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32))
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64))
+        return load().orc_ce_delta_e(self.h, p(occ, C.c_int), l, new, p(mu, C.c_double), mu.size)
+
+    def formation(self, occ):
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32))
+        return load().orc_ce_formation(self.h, p(occ, C.c_int))
+
+    def int_corr(self, occ, n_classes):
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32))
+        out = np.zeros(n_classes, dtype=np.int64)
+        load().orc_ce_int_corr(self.h, p(occ, C.c_int), p(out, C.c_longlong))
+        return out
+
+    def colored_sweep(self, occ, T, mu, seed, chain, colors, n_colors, pass0, n_passes, n_classes):
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64))
+        colors = np.ascontiguousarray(np.asarray(colors, dtype=np.int32))
+        corr = np.zeros((n_passes, n_classes), dtype=np.int64)
+        nacc = np.zeros(n_passes, dtype=np.int64)
+        load().orc_ce_colored_sweep(self.h, p(occ, C.c_int), T, p(mu, C.c_double), mu.size, C.c_ulonglong(seed),
+                                    C.c_uint(chain), p(colors, C.c_int), n_colors, pass0, n_passes,
+                                    p(corr, C.c_longlong), p(nacc, C.c_longlong))
+        return occ, corr, nacc
+
+    def random_site_run(self, occ, T, mu, seed, n_steps):
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64))
+        secs = C.c_double()
+        nacc = load().orc_ce_random_site_run(self.h, p(occ, C.c_int), T, p(mu, C.c_double), mu.size,
+                                             C.c_ulonglong(seed), C.c_longlong(n_steps), C.byref(secs))
+        return occ, nacc, secs.value
