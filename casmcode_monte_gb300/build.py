@@ -20,7 +20,10 @@ OBJDIR = os.path.join(LIBDIR, "obj")
 LIBNAME = "libmontegpu.so"
 SOURCES = ["mg_api.cu", "ising_replay.cu", "ce_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code keeps a*b+c unfused (-ffp-contract=off) so results match the reference's
+# un-contracted FP64 arithmetic on aarch64 as on x86-64
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
 
 

@@ -72,7 +72,7 @@ struct mg_ce_batch {
   const mg_ce_model* model = nullptr;
   int L0 = 0, L1 = 0, L2 = 0, n_chains = 0, precision = 0;
   long long N = 0;
-  int S = 1, nk = 0, PX = 0, PY = 0, PZ = 0, n_colors = 0, threads = 0;
+  int S = 1, PX = 0, PY = 0, PZ = 0, n_colors = 0, threads = 0;
   size_t smem = 0;
   long long pass = 0;
   std::vector<int32_t> color;
@@ -221,7 +221,6 @@ int launch_sweep(mg_ce_batch* bt, int n_passes, long long pass0) {
   A.g.L1 = bt->L1;
   A.g.L2 = bt->L2;
   A.g.S = bt->S;
-  A.g.nk = bt->nk;
   A.g.PX = bt->PX;
   A.g.PY = bt->PY;
   A.g.PZ = bt->PZ;
@@ -403,10 +402,11 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   int max_smem = 0;
   cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t smem_budget = (size_t)max_smem - 1024;  // static accumulators
-  // candidate CTAs per chain: divisors of L2 with >= halo planes each, <= 16
+  // candidate CTAs per chain: every CTA keeps >= halo planes; the largest slab fits
+  auto slab_smem = [&](int S) { return (size_t)b->PX * b->PY * ((L2 + S - 1) / S + 2 * halo); };
   std::vector<int> cands;
   for (int S = 1; S <= 16; ++S)
-    if (L2 % S == 0 && L2 / S >= halo && (size_t)b->PX * b->PY * (L2 / S + 2 * halo) <= smem_budget) cands.push_back(S);
+    if (L2 / S >= halo && slab_smem(S) <= smem_budget) cands.push_back(S);
   if (cands.empty()) {
     set_error("Error in mg_ce_batch_create: supercell slab does not fit in shared memory for any CTA count");
     delete b;
@@ -415,42 +415,38 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   int S = 0;
   if (ctas_per_chain > 0) {
     if (std::find(cands.begin(), cands.end(), ctas_per_chain) == cands.end()) {
-      set_error("Error in mg_ce_batch_create: ctas_per_chain must divide L2, leave >= 2 planes per CTA and fit in shared memory");
+      set_error("Error in mg_ce_batch_create: ctas_per_chain must leave >= 2 planes per CTA and fit in shared memory");
       delete b;
       return MG_ERR_INVALID;
     }
     S = ctas_per_chain;
   } else {
-    // fewest CTAs per chain that still covers the SMs (all clusters co-resident)
-    S = cands.back();
+    // minimise waves(S) / S, waves = ceil(n_chains / co-resident chains); ties -> fewer CTAs
+    double best = 1e300;
     for (int s : cands) {
-      if ((long long)s * n_chains >= sms) {
-        S = s;
-        break;
-      }
-    }
-    // do not exceed co-residency
-    while (true) {
-      const size_t smem = (size_t)b->PX * b->PY * (L2 / S + 2 * halo);
       int n_active = 0;
-      int rc = (m->kind == 0) ? max_active_clusters<mg::FccBinary, mg::NT_BINARY>(b, S, smem, &n_active)
-                              : max_active_clusters<mg::FccTernary, mg::NT_TERNARY>(b, S, smem, &n_active);
+      int rc = (m->kind == 0) ? max_active_clusters<mg::FccBinary, mg::NT_BINARY>(b, s, slab_smem(s), &n_active)
+                              : max_active_clusters<mg::FccTernary, mg::NT_TERNARY>(b, s, slab_smem(s), &n_active);
       if (rc != MG_OK) {
         delete b;
         return rc;
       }
-      if (n_active >= n_chains || S == cands.front()) break;
-      // fewer clusters fit than chains: try the next smaller S (more passes of waves are fine)
-      auto it = std::find(cands.begin(), cands.end(), S);
-      if (it == cands.begin()) break;
-      --it;
-      S = *it;
-      if (n_active * S >= sms) break;
+      if (n_active < 1) continue;
+      const double waves = (double)((n_chains + n_active - 1) / n_active);
+      const double cost = waves / s;
+      if (cost < best * (1.0 - 1e-9)) {
+        best = cost;
+        S = s;
+      }
+    }
+    if (S == 0) {
+      set_error("Error in mg_ce_batch_create: no launchable CTA count for this supercell");
+      delete b;
+      return MG_ERR_INVALID;
     }
   }
   b->S = S;
-  b->nk = L2 / S;
-  b->PZ = b->nk + 2 * halo;
+  b->PZ = (L2 + S - 1) / S + 2 * halo;
   b->smem = (size_t)b->PX * b->PY * b->PZ;
 
   // colouring and per-slab, per-colour site lists in bank-interleaved order
@@ -461,13 +457,15 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   entries.reserve(N);
   site.reserve(N);
   for (int r = 0; r < S; ++r) {
+    const int nk = L2 / S + (r < L2 % S ? 1 : 0);
+    const int k0 = r * (L2 / S) + std::min(r, L2 % S);
     for (int c = 0; c < b->n_colors; ++c) {
       cstart[(size_t)r * (b->n_colors + 1) + c] = (int)entries.size();
       std::vector<std::vector<std::pair<uint32_t, uint32_t>>> bank(32);
-      for (int kl = 0; kl < b->nk; ++kl)
+      for (int kl = 0; kl < nk; ++kl)
         for (int j = 0; j < L1; ++j)
           for (int i = 0; i < L0; ++i) {
-            const int k = r * b->nk + kl;
+            const int k = k0 + kl;
             const long long l = i + (long long)L0 * (j + (long long)L1 * k);
             if (b->color[l] != c) continue;
             const uint32_t pidx = (uint32_t)((i + halo) + b->PX * ((j + halo) + b->PY * (kl + halo)));
@@ -477,7 +475,7 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
             if (j < halo) flags |= 4;
             else if (j >= L1 - halo) flags |= 8;
             if (kl < halo) flags |= 16;
-            if (kl >= b->nk - halo) flags |= 32;
+            if (kl >= nk - halo) flags |= 32;
             bank[(pidx >> 2) & 31].push_back({pidx | (flags << 24), (uint32_t)l});
           }
       bool more = true;
@@ -731,6 +729,21 @@ int mg_ce_batch_delta_e(mg_ce_batch* b, const int32_t* chain, const long long* s
 int mg_ce_batch_destroy(mg_ce_batch* b) {
   free_batch(b);
   return MG_OK;
+}
+
+int mg_ce_max_active_chains(const mg_ce_model* m, int L0, int L1, int L2, int ctas_per_chain,
+                            int* n_chains) {
+  if (!m || !n_chains || L0 < 4 || L1 < 4 || L2 < 4 || ctas_per_chain < 1 || ctas_per_chain > 16 ||
+      L2 / ctas_per_chain < 2) {
+    set_error("Error in mg_ce_max_active_chains: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  mg_ce_batch tmp;
+  tmp.n_chains = 1;
+  const size_t smem = (size_t)(L0 + 4) * (L1 + 4) * ((L2 + ctas_per_chain - 1) / ctas_per_chain + 4);
+  int rc = (m->kind == 0) ? max_active_clusters<mg::FccBinary, mg::NT_BINARY>(&tmp, ctas_per_chain, smem, n_chains)
+                          : max_active_clusters<mg::FccTernary, mg::NT_TERNARY>(&tmp, ctas_per_chain, smem, n_chains);
+  return rc;
 }
 
 }  // extern "C"

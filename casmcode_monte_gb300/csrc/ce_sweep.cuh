@@ -11,7 +11,7 @@
 // thread mapping.
 //
 // Layout: a chain is owned by a cluster of S CTAs; CTA r holds planes
-// [r*nk, (r+1)*nk) of the L0 x L1 x L2 supercell (l = i + L0*(j + L1*k)) plus a
+// [k0(r), k0(r) + nk(r)) of the L0 x L1 x L2 supercell (l = i + L0*(j + L1*k)) plus a
 // HALO-plane border in k and a HALO-column border in i and j, as int8 codes in shared
 // memory (padded index (i+2) + PX*((j+2) + PY*(k_local+2))).  Neighbour loads are
 // constant offsets from the site's padded index.  An accepted flip writes the site and
@@ -58,9 +58,8 @@ struct CeWeights {
 
 struct CeGeometry {
   int L0, L1, L2;
-  int S;   // CTAs per chain
-  int nk;  // planes per CTA
-  int PX, PY, PZ;
+  int S;  // CTAs per chain; CTA r owns nk(r) = L2/S (+1 for r < L2%S) planes
+  int PX, PY, PZ;  // padded dims; PZ = max planes per CTA + 2 * HALO
   int n_colors;
   const int* color_start;    // [S][n_colors + 1]
   const uint32_t* entries;   // padded index | flags << 24
@@ -134,13 +133,16 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
 
   const int PX = g.PX, PY = g.PY, PZ = g.PZ, PXY = PX * PY;
   const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
-  const int nk = g.nk;
+  const int nkq = L2 / S, nkr = L2 % S;
+  const int nk = nkq + (rank < nkr ? 1 : 0);
+  const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+  const int rprev = (rank + S - 1) % S;
+  const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
   const long long N = (long long)L0 * L1 * L2;
-  const int k0 = rank * nk;
   int8_t* gocc = A.occ + (size_t)chain * N;
 
   // ---- load slab + borders
-  for (int idx = threadIdx.x; idx < PXY * PZ; idx += NT) {
+  for (int idx = threadIdx.x; idx < PXY * (nk + 2 * B::HALO); idx += NT) {
     const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
     int i = ip - B::HALO, j = jp - B::HALO, k = k0 + kp - B::HALO;
     i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
@@ -165,7 +167,11 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
   const float beta_log2e = cpg->beta_log2e, dtol = cpg->dtol, eps = cpg->eps;
   const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
   const int* cstart = g.color_start + rank * (g.n_colors + 1);
-  const int dI = L0, dJ = L1 * PX, dK = nk * PXY;
+  // periodic copies: +-L0 in i, +-L1 rows in j; a plane kl < HALO is also the upper
+  // halo of the previous CTA (at kl + nk_prev + HALO), a plane kl >= nk - HALO the
+  // lower halo of the next CTA (at kl - nk + HALO)
+  const int dI = L0, dJ = L1 * PX, dKp = nk_prev * PXY, dKn = nk * PXY;
+  (void)PZ;
   const int lane = threadIdx.x & 31;
   barrier();
 
@@ -179,10 +185,20 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
 #pragma unroll 1
     for (int c = 0; c < g.n_colors; ++c) {
       const int e_end = cstart[c + 1];
+      int e = cstart[c] + threadIdx.x;
+      uint32_t ent_next = 0u, l_next = 0u;
+      if (e < e_end) {
+        ent_next = __ldg(g.entries + e);
+        l_next = __ldg(g.site_l + e);
+      }
 #pragma unroll 1
-      for (int e = cstart[c] + threadIdx.x; e < e_end; e += NT) {
-        const uint32_t ent = g.entries[e];
-        const uint32_t l = g.site_l[e];
+      for (; e < e_end; e += NT) {
+        const uint32_t ent = ent_next;
+        const uint32_t l = l_next;
+        if (e + NT < e_end) {  // prefetch the next site of this colour
+          ent_next = __ldg(g.entries + e + NT);
+          l_next = __ldg(g.site_l + e + NT);
+        }
         const int pidx = (int)(ent & 0xFFFFFFu);
         const uint32_t flags = ent >> 24;
         const int8_t* p = s + pidx;
@@ -255,14 +271,14 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
           if (oj) s[pidx + oj] = c2;
           if (oi && oj) s[pidx + oi + oj] = c2;
           if (flags & 16u) {
-            int8_t* r = s_prev + pidx + dK;
+            int8_t* r = s_prev + pidx + dKp;
             r[0] = c2;
             if (oi) r[oi] = c2;
             if (oj) r[oj] = c2;
             if (oi && oj) r[oi + oj] = c2;
           }
           if (flags & 32u) {
-            int8_t* r = s_next + pidx - dK;
+            int8_t* r = s_next + pidx - dKn;
             r[0] = c2;
             if (oi) r[oi] = c2;
             if (oj) r[oj] = c2;

@@ -124,6 +124,10 @@ int mg_ce_batch_corr(mg_ce_batch* b, long long* out);
 int mg_ce_batch_delta_e(mg_ce_batch* b, const int32_t* chain, const long long* sites,
                         const int8_t* new_occ, long long n, double* out);
 int mg_ce_batch_destroy(mg_ce_batch* b);
+/* how many chains of this supercell can sweep concurrently with ctas_per_chain CTAs each
+ * (cudaOccupancyMaxActiveClusters on the sweep kernel); used by the autotuner */
+int mg_ce_max_active_chains(const mg_ce_model* m, int L0, int L1, int L2, int ctas_per_chain,
+                            int* n_chains);
 
 /* ---- statistics (host numerics shared with the device convergence kernel) ---- */
 /* _default_equilibration_check (EquilibrationCheck.cc:50-117) */

@@ -67,7 +67,10 @@ def test_int_corr_and_energy_match_oracle(gpu_lib, kind):
 
 @pytest.mark.parametrize("kind,L,S", [("fcc_binary", (8, 8, 8), 1), ("fcc_binary", (8, 8, 8), 2),
                                       ("fcc_binary", (12, 8, 16), 4), ("fcc_binary", (16, 16, 16), 8),
-                                      ("fcc_ternary", (8, 8, 8), 1), ("fcc_ternary", (8, 12, 8), 4)])
+                                      ("fcc_binary", (8, 8, 10), 3), ("fcc_binary", (12, 8, 13), 5),
+                                      ("fcc_binary", (16, 16, 32), 13),
+                                      ("fcc_ternary", (8, 8, 8), 1), ("fcc_ternary", (8, 12, 8), 4),
+                                      ("fcc_ternary", (8, 8, 9), 4)])
 def test_colored_sweep_bit_exact(gpu_lib, kind, L, S):
     n_chains = 3
     model, occ, T, mu = _setup(kind, L, n_chains, seed=5)
