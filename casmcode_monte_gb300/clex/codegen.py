@@ -40,6 +40,16 @@ def _psi_expr(basis: O.SiteBasis, b: int, var: str) -> str:
     raise ValueError(basis.name)
 
 
+def _sum_expr(terms: list, n_acc: int = 4) -> str:
+    """Sum of terms as n_acc interleaved partial sums, so that the products form
+    independent multiply-add chains (instruction-level parallelism)."""
+    if len(terms) <= n_acc:
+        return " + ".join(terms)
+    groups = [terms[i::n_acc] for i in range(n_acc)]
+    parts = ["(" + " + ".join(g) + ")" for g in groups]
+    return "(" + parts[0] + " + " + parts[1] + ") + (" + parts[2] + " + " + parts[3] + ")"
+
+
 def _var(off) -> str:
     return "v_" + "_".join(("m" + str(-x)) if x < 0 else str(x) for x in off)
 
@@ -115,7 +125,7 @@ def generate(kind: str) -> tuple[str, dict]:
                 terms.append("1")
             else:
                 terms.append(" * ".join(_psi_expr(basis, b, _var(o)) for o, b in t))
-        lines.append(f"  F[{k}] = " + " + ".join(terms) + ";")
+        lines.append(f"  F[{k}] = " + _sum_expr(terms) + ";")
     lines.append("}")
 
     # anchored correlations
@@ -132,7 +142,7 @@ def generate(kind: str) -> tuple[str, dict]:
                 terms.append("1")
             else:
                 terms.append(" * ".join(_psi_expr(basis, b, _var(o)) for o, b in t))
-        lines.append(f"  C[{ci}] += (long long)(" + " + ".join(terms) + ");")
+        lines.append(f"  C[{ci}] += (long long)(" + _sum_expr(terms) + ");")
     lines.append("}")
     lines.append("}}  // namespace")
     src = "\n".join(lines) + "\n"

@@ -84,14 +84,14 @@ __device__ __forceinline__ void features(const Loader& ld, int (&F)[NFEAT]) {
   const int v_2_0_m1 = ld(2, 0, -1);
   const int v_2_0_0 = ld(2, 0, 0);
   F[0] = 1;
-  F[1] = v_m1_0_0 + v_m1_0_1 + v_m1_1_0 + v_0_m1_0 + v_0_m1_1 + v_0_0_m1 + v_0_0_1 + v_0_1_m1 + v_0_1_0 + v_1_m1_0 + v_1_0_m1 + v_1_0_0;
-  F[2] = v_m1_m1_1 + v_m1_1_m1 + v_m1_1_1 + v_1_m1_m1 + v_1_m1_1 + v_1_1_m1;
-  F[3] = v_m2_0_1 + v_m2_1_0 + v_m2_1_1 + v_m1_m1_0 + v_m1_m1_2 + v_m1_0_m1 + v_m1_0_2 + v_m1_2_m1 + v_m1_2_0 + v_0_m2_1 + v_0_m1_m1 + v_0_m1_2 + v_0_1_m2 + v_0_1_1 + v_0_2_m1 + v_1_m2_0 + v_1_m2_1 + v_1_0_m2 + v_1_0_1 + v_1_1_m2 + v_1_1_0 + v_2_m1_m1 + v_2_m1_0 + v_2_0_m1;
-  F[4] = v_m2_0_0 + v_m2_0_2 + v_m2_2_0 + v_0_m2_0 + v_0_m2_2 + v_0_0_m2 + v_0_0_2 + v_0_2_m2 + v_0_2_0 + v_2_m2_0 + v_2_0_m2 + v_2_0_0;
-  F[5] = v_m1_0_0 * v_m1_0_1 + v_m1_0_0 * v_m1_1_0 + v_m1_0_0 * v_0_m1_0 + v_m1_0_0 * v_0_0_m1 + v_m1_0_1 * v_m1_1_0 + v_m1_0_1 * v_0_m1_1 + v_m1_0_1 * v_0_0_1 + v_m1_1_0 * v_0_1_m1 + v_m1_1_0 * v_0_1_0 + v_0_m1_0 * v_0_m1_1 + v_0_m1_0 * v_0_0_m1 + v_0_m1_0 * v_1_m1_0 + v_0_m1_1 * v_0_0_1 + v_0_m1_1 * v_1_m1_0 + v_0_0_m1 * v_0_1_m1 + v_0_0_m1 * v_1_0_m1 + v_0_0_1 * v_0_1_0 + v_0_0_1 * v_1_0_0 + v_0_1_m1 * v_0_1_0 + v_0_1_m1 * v_1_0_m1 + v_0_1_0 * v_1_0_0 + v_1_m1_0 * v_1_0_m1 + v_1_m1_0 * v_1_0_0 + v_1_0_m1 * v_1_0_0;
-  F[6] = v_m1_m1_1 * v_m1_0_0 + v_m1_m1_1 * v_m1_0_1 + v_m1_m1_1 * v_0_m1_0 + v_m1_m1_1 * v_0_m1_1 + v_m1_0_0 * v_m1_1_m1 + v_m1_0_0 * v_0_m1_1 + v_m1_0_0 * v_0_1_m1 + v_m1_0_1 * v_m1_1_1 + v_m1_0_1 * v_0_m1_0 + v_m1_0_1 * v_0_1_0 + v_m1_1_m1 * v_m1_1_0 + v_m1_1_m1 * v_0_0_m1 + v_m1_1_m1 * v_0_1_m1 + v_m1_1_0 * v_m1_1_1 + v_m1_1_0 * v_0_0_m1 + v_m1_1_0 * v_0_0_1 + v_m1_1_1 * v_0_0_1 + v_m1_1_1 * v_0_1_0 + v_0_m1_0 * v_1_m1_m1 + v_0_m1_0 * v_1_0_m1 + v_0_m1_1 * v_1_m1_1 + v_0_m1_1 * v_1_0_0 + v_0_0_m1 * v_1_m1_m1 + v_0_0_m1 * v_1_m1_0 + v_0_0_1 * v_1_m1_0 + v_0_0_1 * v_1_m1_1 + v_0_1_m1 * v_1_0_0 + v_0_1_m1 * v_1_1_m1 + v_0_1_0 * v_1_0_m1 + v_0_1_0 * v_1_1_m1 + v_1_m1_m1 * v_1_m1_0 + v_1_m1_m1 * v_1_0_m1 + v_1_m1_0 * v_1_m1_1 + v_1_m1_1 * v_1_0_0 + v_1_0_m1 * v_1_1_m1 + v_1_0_0 * v_1_1_m1;
-  F[7] = v_m2_0_1 * v_m1_0_0 + v_m2_0_1 * v_m1_0_1 + v_m2_1_0 * v_m1_0_0 + v_m2_1_0 * v_m1_1_0 + v_m2_1_1 * v_m1_0_1 + v_m2_1_1 * v_m1_1_0 + v_m1_m1_0 * v_m1_0_0 + v_m1_m1_0 * v_0_m1_0 + v_m1_m1_2 * v_m1_0_1 + v_m1_m1_2 * v_0_m1_1 + v_m1_0_m1 * v_m1_0_0 + v_m1_0_m1 * v_0_0_m1 + v_m1_0_0 * v_0_0_1 + v_m1_0_0 * v_0_1_0 + v_m1_0_0 * v_1_m1_0 + v_m1_0_0 * v_1_0_m1 + v_m1_0_1 * v_m1_0_2 + v_m1_0_1 * v_0_0_m1 + v_m1_0_1 * v_0_1_m1 + v_m1_0_1 * v_1_m1_0 + v_m1_0_1 * v_1_0_0 + v_m1_0_2 * v_0_0_1 + v_m1_1_0 * v_m1_2_m1 + v_m1_1_0 * v_m1_2_0 + v_m1_1_0 * v_0_m1_0 + v_m1_1_0 * v_0_m1_1 + v_m1_1_0 * v_1_0_m1 + v_m1_1_0 * v_1_0_0 + v_m1_2_m1 * v_0_1_m1 + v_m1_2_0 * v_0_1_0 + v_0_m2_1 * v_0_m1_0 + v_0_m2_1 * v_0_m1_1 + v_0_m1_m1 * v_0_m1_0 + v_0_m1_m1 * v_0_0_m1 + v_0_m1_0 * v_0_0_1 + v_0_m1_0 * v_0_1_m1 + v_0_m1_0 * v_1_m2_0 + v_0_m1_0 * v_1_0_0 + v_0_m1_1 * v_0_m1_2 + v_0_m1_1 * v_0_0_m1 + v_0_m1_1 * v_0_1_0 + v_0_m1_1 * v_1_m2_1 + v_0_m1_1 * v_1_0_m1 + v_0_m1_2 * v_0_0_1 + v_0_0_m1 * v_0_1_m2 + v_0_0_m1 * v_0_1_0 + v_0_0_m1 * v_1_0_m2 + v_0_0_m1 * v_1_0_0 + v_0_0_1 * v_0_1_m1 + v_0_0_1 * v_0_1_1 + v_0_0_1 * v_1_0_m1 + v_0_0_1 * v_1_0_1 + v_0_1_m2 * v_0_1_m1 + v_0_1_m1 * v_0_2_m1 + v_0_1_m1 * v_1_m1_0 + v_0_1_m1 * v_1_1_m2 + v_0_1_0 * v_0_1_1 + v_0_1_0 * v_0_2_m1 + v_0_1_0 * v_1_m1_0 + v_0_1_0 * v_1_1_0 + v_1_m2_0 * v_1_m1_0 + v_1_m2_1 * v_1_m1_0 + v_1_m1_0 * v_2_m1_m1 + v_1_m1_0 * v_2_m1_0 + v_1_0_m2 * v_1_0_m1 + v_1_0_m1 * v_1_1_m2 + v_1_0_m1 * v_2_m1_m1 + v_1_0_m1 * v_2_0_m1 + v_1_0_0 * v_1_0_1 + v_1_0_0 * v_1_1_0 + v_1_0_0 * v_2_m1_0 + v_1_0_0 * v_2_0_m1;
-  F[8] = v_m1_0_0 * v_m1_0_1 * v_m1_1_0 + v_m1_0_0 * v_0_m1_0 * v_0_0_m1 + v_m1_0_1 * v_0_m1_1 * v_0_0_1 + v_m1_1_0 * v_0_1_m1 * v_0_1_0 + v_0_m1_0 * v_0_m1_1 * v_1_m1_0 + v_0_0_m1 * v_0_1_m1 * v_1_0_m1 + v_0_0_1 * v_0_1_0 * v_1_0_0 + v_1_m1_0 * v_1_0_m1 * v_1_0_0;
+  F[1] = ((v_m1_0_0 + v_0_m1_1 + v_0_1_0) + (v_m1_0_1 + v_0_0_m1 + v_1_m1_0)) + ((v_m1_1_0 + v_0_0_1 + v_1_0_m1) + (v_0_m1_0 + v_0_1_m1 + v_1_0_0));
+  F[2] = ((v_m1_m1_1 + v_1_m1_1) + (v_m1_1_m1 + v_1_1_m1)) + ((v_m1_1_1) + (v_1_m1_m1));
+  F[3] = ((v_m2_0_1 + v_m1_m1_2 + v_m1_2_0 + v_0_1_m2 + v_1_m2_1 + v_1_1_0) + (v_m2_1_0 + v_m1_0_m1 + v_0_m2_1 + v_0_1_1 + v_1_0_m2 + v_2_m1_m1)) + ((v_m2_1_1 + v_m1_0_2 + v_0_m1_m1 + v_0_2_m1 + v_1_0_1 + v_2_m1_0) + (v_m1_m1_0 + v_m1_2_m1 + v_0_m1_2 + v_1_m2_0 + v_1_1_m2 + v_2_0_m1));
+  F[4] = ((v_m2_0_0 + v_0_m2_2 + v_0_2_0) + (v_m2_0_2 + v_0_0_m2 + v_2_m2_0)) + ((v_m2_2_0 + v_0_0_2 + v_2_0_m2) + (v_0_m2_0 + v_0_2_m2 + v_2_0_0));
+  F[5] = ((v_m1_0_0 * v_m1_0_1 + v_m1_0_1 * v_m1_1_0 + v_m1_1_0 * v_0_1_0 + v_0_m1_1 * v_0_0_1 + v_0_0_1 * v_0_1_0 + v_0_1_0 * v_1_0_0) + (v_m1_0_0 * v_m1_1_0 + v_m1_0_1 * v_0_m1_1 + v_0_m1_0 * v_0_m1_1 + v_0_m1_1 * v_1_m1_0 + v_0_0_1 * v_1_0_0 + v_1_m1_0 * v_1_0_m1)) + ((v_m1_0_0 * v_0_m1_0 + v_m1_0_1 * v_0_0_1 + v_0_m1_0 * v_0_0_m1 + v_0_0_m1 * v_0_1_m1 + v_0_1_m1 * v_0_1_0 + v_1_m1_0 * v_1_0_0) + (v_m1_0_0 * v_0_0_m1 + v_m1_1_0 * v_0_1_m1 + v_0_m1_0 * v_1_m1_0 + v_0_0_m1 * v_1_0_m1 + v_0_1_m1 * v_1_0_m1 + v_1_0_m1 * v_1_0_0));
+  F[6] = ((v_m1_m1_1 * v_m1_0_0 + v_m1_0_0 * v_m1_1_m1 + v_m1_0_1 * v_0_m1_0 + v_m1_1_m1 * v_0_1_m1 + v_m1_1_1 * v_0_0_1 + v_0_m1_1 * v_1_m1_1 + v_0_0_1 * v_1_m1_0 + v_0_1_0 * v_1_0_m1 + v_1_m1_0 * v_1_m1_1) + (v_m1_m1_1 * v_m1_0_1 + v_m1_0_0 * v_0_m1_1 + v_m1_0_1 * v_0_1_0 + v_m1_1_0 * v_m1_1_1 + v_m1_1_1 * v_0_1_0 + v_0_m1_1 * v_1_0_0 + v_0_0_1 * v_1_m1_1 + v_0_1_0 * v_1_1_m1 + v_1_m1_1 * v_1_0_0)) + ((v_m1_m1_1 * v_0_m1_0 + v_m1_0_0 * v_0_1_m1 + v_m1_1_m1 * v_m1_1_0 + v_m1_1_0 * v_0_0_m1 + v_0_m1_0 * v_1_m1_m1 + v_0_0_m1 * v_1_m1_m1 + v_0_1_m1 * v_1_0_0 + v_1_m1_m1 * v_1_m1_0 + v_1_0_m1 * v_1_1_m1) + (v_m1_m1_1 * v_0_m1_1 + v_m1_0_1 * v_m1_1_1 + v_m1_1_m1 * v_0_0_m1 + v_m1_1_0 * v_0_0_1 + v_0_m1_0 * v_1_0_m1 + v_0_0_m1 * v_1_m1_0 + v_0_1_m1 * v_1_1_m1 + v_1_m1_m1 * v_1_0_m1 + v_1_0_0 * v_1_1_m1));
+  F[7] = ((v_m2_0_1 * v_m1_0_0 + v_m2_1_1 * v_m1_0_1 + v_m1_m1_2 * v_m1_0_1 + v_m1_0_0 * v_0_0_1 + v_m1_0_1 * v_m1_0_2 + v_m1_0_1 * v_1_0_0 + v_m1_1_0 * v_0_m1_0 + v_m1_2_m1 * v_0_1_m1 + v_0_m1_m1 * v_0_m1_0 + v_0_m1_0 * v_1_m2_0 + v_0_m1_1 * v_0_1_0 + v_0_0_m1 * v_0_1_m2 + v_0_0_1 * v_0_1_m1 + v_0_1_m2 * v_0_1_m1 + v_0_1_0 * v_0_1_1 + v_1_m2_0 * v_1_m1_0 + v_1_0_m2 * v_1_0_m1 + v_1_0_0 * v_1_0_1) + (v_m2_0_1 * v_m1_0_1 + v_m2_1_1 * v_m1_1_0 + v_m1_m1_2 * v_0_m1_1 + v_m1_0_0 * v_0_1_0 + v_m1_0_1 * v_0_0_m1 + v_m1_0_2 * v_0_0_1 + v_m1_1_0 * v_0_m1_1 + v_m1_2_0 * v_0_1_0 + v_0_m1_m1 * v_0_0_m1 + v_0_m1_0 * v_1_0_0 + v_0_m1_1 * v_1_m2_1 + v_0_0_m1 * v_0_1_0 + v_0_0_1 * v_0_1_1 + v_0_1_m1 * v_0_2_m1 + v_0_1_0 * v_0_2_m1 + v_1_m2_1 * v_1_m1_0 + v_1_0_m1 * v_1_1_m2 + v_1_0_0 * v_1_1_0)) + ((v_m2_1_0 * v_m1_0_0 + v_m1_m1_0 * v_m1_0_0 + v_m1_0_m1 * v_m1_0_0 + v_m1_0_0 * v_1_m1_0 + v_m1_0_1 * v_0_1_m1 + v_m1_1_0 * v_m1_2_m1 + v_m1_1_0 * v_1_0_m1 + v_0_m2_1 * v_0_m1_0 + v_0_m1_0 * v_0_0_1 + v_0_m1_1 * v_0_m1_2 + v_0_m1_1 * v_1_0_m1 + v_0_0_m1 * v_1_0_m2 + v_0_0_1 * v_1_0_m1 + v_0_1_m1 * v_1_m1_0 + v_0_1_0 * v_1_m1_0 + v_1_m1_0 * v_2_m1_m1 + v_1_0_m1 * v_2_m1_m1 + v_1_0_0 * v_2_m1_0) + (v_m2_1_0 * v_m1_1_0 + v_m1_m1_0 * v_0_m1_0 + v_m1_0_m1 * v_0_0_m1 + v_m1_0_0 * v_1_0_m1 + v_m1_0_1 * v_1_m1_0 + v_m1_1_0 * v_m1_2_0 + v_m1_1_0 * v_1_0_0 + v_0_m2_1 * v_0_m1_1 + v_0_m1_0 * v_0_1_m1 + v_0_m1_1 * v_0_0_m1 + v_0_m1_2 * v_0_0_1 + v_0_0_m1 * v_1_0_0 + v_0_0_1 * v_1_0_1 + v_0_1_m1 * v_1_1_m2 + v_0_1_0 * v_1_1_0 + v_1_m1_0 * v_2_m1_0 + v_1_0_m1 * v_2_0_m1 + v_1_0_0 * v_2_0_m1));
+  F[8] = ((v_m1_0_0 * v_m1_0_1 * v_m1_1_0 + v_0_m1_0 * v_0_m1_1 * v_1_m1_0) + (v_m1_0_0 * v_0_m1_0 * v_0_0_m1 + v_0_0_m1 * v_0_1_m1 * v_1_0_m1)) + ((v_m1_0_1 * v_0_m1_1 * v_0_0_1 + v_0_0_1 * v_0_1_0 * v_1_0_0) + (v_m1_1_0 * v_0_1_m1 * v_0_1_0 + v_1_m1_0 * v_1_0_m1 * v_1_0_0));
 }
 // C[f] += sum over decorated clusters of class f anchored at this site (its
 // lexicographically smallest member) of the product of integer psi values.
@@ -127,13 +127,13 @@ __device__ __forceinline__ void anchored(const Loader& ld, long long (&C)[NCLASS
   const int v_2_0_0 = ld(2, 0, 0);
   C[0] += (long long)(1);
   C[1] += (long long)(v_0_0_0);
-  C[2] += (long long)(v_m1_0_1 * v_0_0_0 + v_m1_1_0 * v_0_0_0 + v_0_m1_1 * v_0_0_0 + v_0_0_0 * v_0_0_1 + v_0_0_0 * v_0_1_0 + v_0_0_0 * v_1_0_0);
+  C[2] += (long long)(((v_m1_0_1 * v_0_0_0 + v_0_0_0 * v_0_1_0) + (v_m1_1_0 * v_0_0_0 + v_0_0_0 * v_1_0_0)) + ((v_0_m1_1 * v_0_0_0) + (v_0_0_0 * v_0_0_1)));
   C[3] += (long long)(v_m1_1_1 * v_0_0_0 + v_0_0_0 * v_1_m1_1 + v_0_0_0 * v_1_1_m1);
-  C[4] += (long long)(v_m2_0_1 * v_0_0_0 + v_m2_1_0 * v_0_0_0 + v_m2_1_1 * v_0_0_0 + v_m1_m1_2 * v_0_0_0 + v_m1_0_2 * v_0_0_0 + v_m1_2_m1 * v_0_0_0 + v_m1_2_0 * v_0_0_0 + v_0_m1_2 * v_0_0_0 + v_0_0_0 * v_0_1_1 + v_0_0_0 * v_0_2_m1 + v_0_0_0 * v_1_0_1 + v_0_0_0 * v_1_1_0);
-  C[5] += (long long)(v_m2_0_2 * v_0_0_0 + v_m2_2_0 * v_0_0_0 + v_0_m2_2 * v_0_0_0 + v_0_0_0 * v_0_0_2 + v_0_0_0 * v_0_2_0 + v_0_0_0 * v_2_0_0);
-  C[6] += (long long)(v_m1_0_1 * v_m1_1_0 * v_0_0_0 + v_m1_0_1 * v_0_m1_1 * v_0_0_0 + v_m1_0_1 * v_0_0_0 * v_0_0_1 + v_m1_1_0 * v_0_0_0 * v_0_1_0 + v_0_m1_1 * v_0_0_0 * v_0_0_1 + v_0_0_0 * v_0_0_1 * v_0_1_0 + v_0_0_0 * v_0_0_1 * v_1_0_0 + v_0_0_0 * v_0_1_0 * v_1_0_0);
-  C[7] += (long long)(v_m1_0_1 * v_m1_1_1 * v_0_0_0 + v_m1_0_1 * v_0_0_0 * v_0_1_0 + v_m1_1_0 * v_m1_1_1 * v_0_0_0 + v_m1_1_0 * v_0_0_0 * v_0_0_1 + v_m1_1_1 * v_0_0_0 * v_0_0_1 + v_m1_1_1 * v_0_0_0 * v_0_1_0 + v_0_m1_1 * v_0_0_0 * v_1_m1_1 + v_0_m1_1 * v_0_0_0 * v_1_0_0 + v_0_0_0 * v_0_0_1 * v_1_m1_1 + v_0_0_0 * v_0_1_0 * v_1_1_m1 + v_0_0_0 * v_1_m1_1 * v_1_0_0 + v_0_0_0 * v_1_0_0 * v_1_1_m1);
-  C[8] += (long long)(v_m2_0_1 * v_m1_0_1 * v_0_0_0 + v_m2_1_0 * v_m1_1_0 * v_0_0_0 + v_m2_1_1 * v_m1_0_1 * v_0_0_0 + v_m2_1_1 * v_m1_1_0 * v_0_0_0 + v_m1_m1_2 * v_m1_0_1 * v_0_0_0 + v_m1_m1_2 * v_0_m1_1 * v_0_0_0 + v_m1_0_1 * v_m1_0_2 * v_0_0_0 + v_m1_0_1 * v_0_0_0 * v_1_0_0 + v_m1_0_2 * v_0_0_0 * v_0_0_1 + v_m1_1_0 * v_m1_2_m1 * v_0_0_0 + v_m1_1_0 * v_m1_2_0 * v_0_0_0 + v_m1_1_0 * v_0_m1_1 * v_0_0_0 + v_m1_1_0 * v_0_0_0 * v_1_0_0 + v_m1_2_0 * v_0_0_0 * v_0_1_0 + v_0_m1_1 * v_0_m1_2 * v_0_0_0 + v_0_m1_1 * v_0_0_0 * v_0_1_0 + v_0_m1_2 * v_0_0_0 * v_0_0_1 + v_0_0_0 * v_0_0_1 * v_0_1_1 + v_0_0_0 * v_0_0_1 * v_1_0_1 + v_0_0_0 * v_0_1_0 * v_0_1_1 + v_0_0_0 * v_0_1_0 * v_0_2_m1 + v_0_0_0 * v_0_1_0 * v_1_1_0 + v_0_0_0 * v_1_0_0 * v_1_0_1 + v_0_0_0 * v_1_0_0 * v_1_1_0);
+  C[4] += (long long)(((v_m2_0_1 * v_0_0_0 + v_m1_0_2 * v_0_0_0 + v_0_0_0 * v_0_1_1) + (v_m2_1_0 * v_0_0_0 + v_m1_2_m1 * v_0_0_0 + v_0_0_0 * v_0_2_m1)) + ((v_m2_1_1 * v_0_0_0 + v_m1_2_0 * v_0_0_0 + v_0_0_0 * v_1_0_1) + (v_m1_m1_2 * v_0_0_0 + v_0_m1_2 * v_0_0_0 + v_0_0_0 * v_1_1_0)));
+  C[5] += (long long)(((v_m2_0_2 * v_0_0_0 + v_0_0_0 * v_0_2_0) + (v_m2_2_0 * v_0_0_0 + v_0_0_0 * v_2_0_0)) + ((v_0_m2_2 * v_0_0_0) + (v_0_0_0 * v_0_0_2)));
+  C[6] += (long long)(((v_m1_0_1 * v_m1_1_0 * v_0_0_0 + v_0_m1_1 * v_0_0_0 * v_0_0_1) + (v_m1_0_1 * v_0_m1_1 * v_0_0_0 + v_0_0_0 * v_0_0_1 * v_0_1_0)) + ((v_m1_0_1 * v_0_0_0 * v_0_0_1 + v_0_0_0 * v_0_0_1 * v_1_0_0) + (v_m1_1_0 * v_0_0_0 * v_0_1_0 + v_0_0_0 * v_0_1_0 * v_1_0_0)));
+  C[7] += (long long)(((v_m1_0_1 * v_m1_1_1 * v_0_0_0 + v_m1_1_1 * v_0_0_0 * v_0_0_1 + v_0_0_0 * v_0_0_1 * v_1_m1_1) + (v_m1_0_1 * v_0_0_0 * v_0_1_0 + v_m1_1_1 * v_0_0_0 * v_0_1_0 + v_0_0_0 * v_0_1_0 * v_1_1_m1)) + ((v_m1_1_0 * v_m1_1_1 * v_0_0_0 + v_0_m1_1 * v_0_0_0 * v_1_m1_1 + v_0_0_0 * v_1_m1_1 * v_1_0_0) + (v_m1_1_0 * v_0_0_0 * v_0_0_1 + v_0_m1_1 * v_0_0_0 * v_1_0_0 + v_0_0_0 * v_1_0_0 * v_1_1_m1)));
+  C[8] += (long long)(((v_m2_0_1 * v_m1_0_1 * v_0_0_0 + v_m1_m1_2 * v_m1_0_1 * v_0_0_0 + v_m1_0_2 * v_0_0_0 * v_0_0_1 + v_m1_1_0 * v_0_0_0 * v_1_0_0 + v_0_m1_2 * v_0_0_0 * v_0_0_1 + v_0_0_0 * v_0_1_0 * v_0_2_m1) + (v_m2_1_0 * v_m1_1_0 * v_0_0_0 + v_m1_m1_2 * v_0_m1_1 * v_0_0_0 + v_m1_1_0 * v_m1_2_m1 * v_0_0_0 + v_m1_2_0 * v_0_0_0 * v_0_1_0 + v_0_0_0 * v_0_0_1 * v_0_1_1 + v_0_0_0 * v_0_1_0 * v_1_1_0)) + ((v_m2_1_1 * v_m1_0_1 * v_0_0_0 + v_m1_0_1 * v_m1_0_2 * v_0_0_0 + v_m1_1_0 * v_m1_2_0 * v_0_0_0 + v_0_m1_1 * v_0_m1_2 * v_0_0_0 + v_0_0_0 * v_0_0_1 * v_1_0_1 + v_0_0_0 * v_1_0_0 * v_1_0_1) + (v_m2_1_1 * v_m1_1_0 * v_0_0_0 + v_m1_0_1 * v_0_0_0 * v_1_0_0 + v_m1_1_0 * v_0_m1_1 * v_0_0_0 + v_0_m1_1 * v_0_0_0 * v_0_1_0 + v_0_0_0 * v_0_1_0 * v_0_1_1 + v_0_0_0 * v_1_0_0 * v_1_1_0)));
   C[9] += (long long)(v_m1_0_1 * v_0_m1_1 * v_0_0_0 * v_0_0_1 + v_0_0_0 * v_0_0_1 * v_0_1_0 * v_1_0_0);
 }
 }}  // namespace
