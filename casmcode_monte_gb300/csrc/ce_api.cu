@@ -10,63 +10,8 @@
 #include <vector>
 
 #include "../../include/montegpu.h"
-#include "ce_sweep.cuh"
-#include "generated/fcc_binary.cuh"
-#include "generated/fcc_ternary.cuh"
+#include "ce_host.cuh"
 #include "mg_common.cuh"
-
-namespace mg {
-
-// Adapters from the generated namespaces to the kernel's basis interface.
-#define MG_BASIS_ADAPTER(NAME, NS_)                                                       \
-  struct NAME {                                                                          \
-    static constexpr int NSPECIES = NS_::NSPECIES;                                       \
-    static constexpr int NFUNC = NS_::NFUNC;                                             \
-    static constexpr int NCLASS = NS_::NCLASS;                                           \
-    static constexpr int NFEAT = NS_::NFEAT;                                             \
-    static constexpr int HALO = NS_::HALO;                                               \
-    __host__ __device__ static constexpr int feat_class(int k) { return NS_::feat_class(k); } \
-    __host__ __device__ static constexpr int feat_b(int k) { return NS_::feat_b(k); }     \
-    __host__ __device__ static constexpr int psi(int b, int o) { return NS_::psi(b, o); } \
-    __host__ __device__ static constexpr int8_t code_of_occ(int o) { return NS_::code_of_occ(o); } \
-    __host__ __device__ static constexpr int occ_of_code(int c) { return NS_::occ_of_code(c); } \
-    template <class L>                                                                   \
-    __device__ static __forceinline__ void features(const L& ld, int (&F)[NFEAT]) {      \
-      NS_::features(ld, F);                                                              \
-    }                                                                                    \
-    template <class L>                                                                   \
-    __device__ static __forceinline__ void anchored(const L& ld, long long (&C)[NCLASS]) { \
-      NS_::anchored(ld, C);                                                              \
-    }                                                                                    \
-  };
-
-MG_BASIS_ADAPTER(FccBinary, fcc_binary)
-MG_BASIS_ADAPTER(FccTernary, fcc_ternary)
-#undef MG_BASIS_ADAPTER
-
-constexpr int NT_BINARY = 512;
-constexpr int NT_TERNARY = 256;
-
-// squared pair distances etc. are not needed on the host; multiplicities and the
-// decoration scales are derived here from the same generated tables' class counts.
-struct ClassInfo {
-  long multiplicity;
-  double scale;
-};
-
-}  // namespace mg
-
-struct mg_ce_model {
-  int kind = 0;  // 0 binary, 1 ternary
-  int n_species = 2, n_func = 1, n_classes = 0, n_features = 0;
-  std::vector<double> eci;
-  std::vector<long> mult;
-  std::vector<double> scale;
-  std::vector<int> feat_class, feat_b;
-  std::vector<long> feat_max;  // bound on |F_k|
-  std::vector<double> w64;
-  std::vector<float> w32;
-};
 
 struct mg_ce_batch {
   const mg_ce_model* model = nullptr;
@@ -92,10 +37,7 @@ struct mg_ce_batch {
 namespace {
 
 using mg::set_error;
-
-// Class multiplicity and scale (product of site-function scales over the decoration),
-// from the generated JSON-equivalent tables compiled below.
-#include "generated/fcc_class_tables.inc"
+using namespace mg::host;
 
 bool make_model(int kind, const double* eci, int n, mg_ce_model* m, std::string& err) {
   m->kind = kind;
@@ -105,22 +47,22 @@ bool make_model(int kind, const double* eci, int n, mg_ce_model* m, std::string&
     m->n_func = mg::FccBinary::NFUNC;
     m->n_classes = mg::FccBinary::NCLASS;
     m->n_features = mg::FccBinary::NFEAT;
-    info = kFccBinaryClasses;
+    info = mg::host::kFccBinaryClasses;
     for (int k = 0; k < m->n_features; ++k) {
       m->feat_class.push_back(mg::FccBinary::feat_class(k));
       m->feat_b.push_back(mg::FccBinary::feat_b(k));
-      m->feat_max.push_back(kFccBinaryFeatMax[k]);
+      m->feat_max.push_back(mg::host::kFccBinaryFeatMax[k]);
     }
   } else if (kind == 1) {
     m->n_species = mg::FccTernary::NSPECIES;
     m->n_func = mg::FccTernary::NFUNC;
     m->n_classes = mg::FccTernary::NCLASS;
     m->n_features = mg::FccTernary::NFEAT;
-    info = kFccTernaryClasses;
+    info = mg::host::kFccTernaryClasses;
     for (int k = 0; k < m->n_features; ++k) {
       m->feat_class.push_back(mg::FccTernary::feat_class(k));
       m->feat_b.push_back(mg::FccTernary::feat_b(k));
-      m->feat_max.push_back(kFccTernaryFeatMax[k]);
+      m->feat_max.push_back(mg::host::kFccTernaryFeatMax[k]);
     }
   } else {
     err = "Error in mg_ce_model_create: unknown basis_kind";
@@ -145,61 +87,6 @@ bool make_model(int kind, const double* eci, int n, mg_ce_model* m, std::string&
   return true;
 }
 
-int dpsi_max(int kind, int b) {
-  if (kind == 0) return 1;
-  return b == 0 ? 2 : 3;
-}
-
-// Linear colouring colour = (a*i + b*j + c*k) mod m, valid when a*L0, b*L1, c*L2 are
-// multiples of m and no neighbour offset maps to 0 mod m; else greedy colouring of the
-// periodic conflict graph in lexicographic site order.
-std::vector<int32_t> make_coloring(int L0, int L1, int L2, const std::vector<std::array<int, 3>>& offs,
-                                   int& n_colors) {
-  const long long N = (long long)L0 * L1 * L2;
-  std::vector<int32_t> col(N, -1);
-  for (int m = 2; m <= 32; ++m) {
-    for (int a = 0; a < m; ++a)
-      for (int b = 0; b < m; ++b)
-        for (int c = 0; c < m; ++c) {
-          if ((1LL * a * L0) % m || (1LL * b * L1) % m || (1LL * c * L2) % m) continue;
-          bool ok = true;
-          for (auto& o : offs) {
-            long long v = (1LL * a * o[0] + 1LL * b * o[1] + 1LL * c * o[2]) % m;
-            if (v < 0) v += m;
-            if (v == 0) {
-              ok = false;
-              break;
-            }
-          }
-          if (!ok) continue;
-          for (int k = 0; k < L2; ++k)
-            for (int j = 0; j < L1; ++j)
-              for (int i = 0; i < L0; ++i)
-                col[i + (long long)L0 * (j + (long long)L1 * k)] = (int32_t)((1LL * a * i + 1LL * b * j + 1LL * c * k) % m);
-          n_colors = m;
-          return col;
-        }
-  }
-  // greedy
-  n_colors = 0;
-  std::vector<char> used;
-  for (int k = 0; k < L2; ++k)
-    for (int j = 0; j < L1; ++j)
-      for (int i = 0; i < L0; ++i) {
-        used.assign(64, 0);
-        for (auto& o : offs) {
-          int a = ((i + o[0]) % L0 + L0) % L0, b = ((j + o[1]) % L1 + L1) % L1, c = ((k + o[2]) % L2 + L2) % L2;
-          const int32_t cc = col[a + (long long)L0 * (b + (long long)L1 * c)];
-          if (cc >= 0 && cc < 64) used[cc] = 1;
-        }
-        int cc = 0;
-        while (used[cc]) ++cc;
-        col[i + (long long)L0 * (j + (long long)L1 * k)] = cc;
-        n_colors = std::max(n_colors, cc + 1);
-      }
-  return col;
-}
-
 void free_batch(mg_ce_batch* b) {
   if (!b) return;
   cudaFree(b->docc);
@@ -212,92 +99,6 @@ void free_batch(mg_ce_batch* b) {
   if (b->ev1) cudaEventDestroy(b->ev1);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
-}
-
-template <class B, int NT>
-int launch_sweep(mg_ce_batch* bt, int n_passes, long long pass0) {
-  mg::CeSweepArgs<B::NFEAT> A;
-  A.g.L0 = bt->L0;
-  A.g.L1 = bt->L1;
-  A.g.L2 = bt->L2;
-  A.g.S = bt->S;
-  A.g.PX = bt->PX;
-  A.g.PY = bt->PY;
-  A.g.PZ = bt->PZ;
-  A.g.n_colors = bt->n_colors;
-  A.g.color_start = bt->dcstart;
-  A.g.entries = bt->dentries;
-  A.g.site_l = bt->dsite;
-  for (int k = 0; k < B::NFEAT; ++k) {
-    A.w.w32[k] = bt->model->w32[k];
-    A.w.w64[k] = bt->model->w64[k];
-  }
-  A.cp = bt->dcp;
-  A.occ = bt->docc;
-  A.pass0 = pass0;
-  A.n_passes = n_passes;
-  A.n_chains = bt->n_chains;
-  A.precision = bt->precision;
-  A.out = bt->dout;
-  auto kern = mg::ce_sweep_kernel<B, NT>;
-  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem));
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(bt->n_chains * bt->S), 1, 1);
-  cfg.blockDim = dim3(NT, 1, 1);
-  cfg.dynamicSmemBytes = bt->smem;
-  cfg.stream = bt->stream;
-  cudaLaunchAttribute attr[1];
-  if (bt->S > 1) {
-    if (bt->S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = (unsigned)bt->S;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-  }
-  MG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
-  MG_CUDA_TRY(cudaGetLastError());
-  return MG_OK;
-}
-
-template <class B, int NT>
-int max_active_clusters(mg_ce_batch* bt, int S, size_t smem, int* out) {
-  auto kern = mg::ce_sweep_kernel<B, NT>;
-  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-  if (S == 1) {
-    int nb = 0;
-    MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, NT, smem));
-    int dev = 0, sms = 0;
-    MG_CUDA_TRY(cudaGetDevice(&dev));
-    MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    *out = nb * sms;
-    return MG_OK;
-  }
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(bt->n_chains * S), 1, 1);
-  cfg.blockDim = dim3(NT, 1, 1);
-  cfg.dynamicSmemBytes = smem;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = (unsigned)S;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  int n = 0;
-  MG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, (void*)kern, &cfg));
-  *out = n;
-  return MG_OK;
-}
-
-std::vector<std::array<int, 3>> neighbour_offsets(int kind) {
-  std::vector<std::array<int, 3>> offs;
-  const int* t = kind == 0 ? kFccBinaryOffsets : kFccTernaryOffsets;
-  const int n = kind == 0 ? kFccBinaryNOffsets : kFccTernaryNOffsets;
-  for (int i = 0; i < n; ++i) offs.push_back({t[3 * i], t[3 * i + 1], t[3 * i + 2]});
-  return offs;
 }
 
 }  // namespace
@@ -392,144 +193,34 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   b->PY = L1 + 2 * halo;
   b->threads = m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY;
 
-  int dev = 0, sms = 0;
-  cudaError_t ce;
-  if ((ce = cudaGetDevice(&dev)) != cudaSuccess || (ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) {
-    set_error(std::string("CUDA error in mg_ce_batch_create: ") + cudaGetErrorString(ce));
-    delete b;
-    return MG_ERR_CUDA;
-  }
-  int max_smem = 0;
-  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t smem_budget = (size_t)max_smem - 1024;  // static accumulators
-  // candidate CTAs per chain: every CTA keeps >= halo planes; the largest slab fits
-  auto slab_smem = [&](int S) { return (size_t)b->PX * b->PY * ((L2 + S - 1) / S + 2 * halo); };
-  std::vector<int> cands;
-  for (int S = 1; S <= 16; ++S)
-    if (L2 / S >= halo && slab_smem(S) <= smem_budget) cands.push_back(S);
-  if (cands.empty()) {
-    set_error("Error in mg_ce_batch_create: supercell slab does not fit in shared memory for any CTA count");
-    delete b;
-    return MG_ERR_INVALID;
-  }
   int S = 0;
-  if (ctas_per_chain > 0) {
-    if (std::find(cands.begin(), cands.end(), ctas_per_chain) == cands.end()) {
-      set_error("Error in mg_ce_batch_create: ctas_per_chain must leave >= 2 planes per CTA and fit in shared memory");
-      delete b;
-      return MG_ERR_INVALID;
-    }
-    S = ctas_per_chain;
-  } else {
-    // minimise waves(S) / S, waves = ceil(n_chains / co-resident chains); ties -> fewer CTAs
-    double best = 1e300;
-    for (int s : cands) {
-      int n_active = 0;
-      int rc = (m->kind == 0) ? max_active_clusters<mg::FccBinary, mg::NT_BINARY>(b, s, slab_smem(s), &n_active)
-                              : max_active_clusters<mg::FccTernary, mg::NT_TERNARY>(b, s, slab_smem(s), &n_active);
-      if (rc != MG_OK) {
-        delete b;
-        return rc;
-      }
-      if (n_active < 1) continue;
-      const double waves = (double)((n_chains + n_active - 1) / n_active);
-      const double cost = waves / s;
-      if (cost < best * (1.0 - 1e-9)) {
-        best = cost;
-        S = s;
-      }
-    }
-    if (S == 0) {
-      set_error("Error in mg_ce_batch_create: no launchable CTA count for this supercell");
-      delete b;
-      return MG_ERR_INVALID;
-    }
+  int rc = choose_ctas(m->kind, L0, L1, L2, n_chains, ctas_per_chain, &S);
+  if (rc != MG_OK) {
+    delete b;
+    return rc;
   }
   b->S = S;
   b->PZ = (L2 + S - 1) / S + 2 * halo;
-  b->smem = (size_t)b->PX * b->PY * b->PZ;
+  b->smem = slab_smem(L0, L1, L2, S);
 
-  // colouring and per-slab, per-colour site lists in bank-interleaved order
-  auto offs = neighbour_offsets(m->kind);
-  b->color = make_coloring(L0, L1, L2, offs, b->n_colors);
-  std::vector<int> cstart((size_t)S * (b->n_colors + 1), 0);
-  std::vector<uint32_t> entries, site;
-  entries.reserve(N);
-  site.reserve(N);
-  for (int r = 0; r < S; ++r) {
-    const int nk = L2 / S + (r < L2 % S ? 1 : 0);
-    const int k0 = r * (L2 / S) + std::min(r, L2 % S);
-    for (int c = 0; c < b->n_colors; ++c) {
-      cstart[(size_t)r * (b->n_colors + 1) + c] = (int)entries.size();
-      std::vector<std::vector<std::pair<uint32_t, uint32_t>>> bank(32);
-      for (int kl = 0; kl < nk; ++kl)
-        for (int j = 0; j < L1; ++j)
-          for (int i = 0; i < L0; ++i) {
-            const int k = k0 + kl;
-            const long long l = i + (long long)L0 * (j + (long long)L1 * k);
-            if (b->color[l] != c) continue;
-            const uint32_t pidx = (uint32_t)((i + halo) + b->PX * ((j + halo) + b->PY * (kl + halo)));
-            uint32_t flags = 0;
-            if (i < halo) flags |= 1;
-            else if (i >= L0 - halo) flags |= 2;
-            if (j < halo) flags |= 4;
-            else if (j >= L1 - halo) flags |= 8;
-            if (kl < halo) flags |= 16;
-            if (kl >= nk - halo) flags |= 32;
-            bank[(pidx >> 2) & 31].push_back({pidx | (flags << 24), (uint32_t)l});
-          }
-      bool more = true;
-      size_t pos = 0;
-      while (more) {
-        more = false;
-        for (int q = 0; q < 32; ++q)
-          if (pos < bank[q].size()) {
-            entries.push_back(bank[q][pos].first);
-            site.push_back(bank[q][pos].second);
-            more = true;
-          }
-        ++pos;
-      }
-    }
-    cstart[(size_t)r * (b->n_colors + 1) + b->n_colors] = (int)entries.size();
-  }
-  if (b->smem > (size_t)(1u << 24) || entries.size() != (size_t)N) {
-    set_error("Error in mg_ce_batch_create: internal site-list construction failed");
-    free_batch(b);
+  // colouring and per-slab, per-colour site lists
+  b->color.assign(N, -1);
+  b->n_colors = color_supercell(L0, L1, L2, m->kind, b->color.data());
+  if (b->n_colors < 1) {
+    set_error("Error in mg_ce_batch_create: colouring needs more than 64 colours");
+    delete b;
     return MG_ERR_INVALID;
   }
-
-  // chain parameters
-  const double KB = 8.6173303E-05;
-  const int ns = m->n_species;
-  b->hcp.resize(n_chains);
-  double wsum = 0.0;
-  for (int k = 0; k < m->n_features; ++k)
-    wsum += std::fabs((double)m->w32[k]) * (double)m->feat_max[k] * dpsi_max(m->kind, m->feat_b[k]);
-  for (int c = 0; c < n_chains; ++c) {
-    mg::CeChainParams& p = b->hcp[c];
-    std::memset(&p, 0, sizeof(p));
-    p.beta = 1.0 / (KB * temperature[c]);
-    p.beta_log2e = (float)(p.beta * 1.4426950408889634);
-    double dmu_max = 0.0;
-    for (int o = 0; o < ns; ++o)
-      for (int o2 = 0; o2 < ns; ++o2) {
-        double r = 0.0;
-        for (int i = 0; i < ns - 1; ++i) {
-          const double d = (o2 == i + 1 ? 1.0 : 0.0) - (o == i + 1 ? 1.0 : 0.0);
-          r += mu[(size_t)c * (ns - 1) + i] * d;
-        }
-        p.dmu64[o * ns + o2] = r;
-        p.dmu32[o * ns + o2] = (float)r;
-        dmu_max = std::max(dmu_max, std::fabs(r));
-      }
-    const double dtol = (m->n_features + 8) * std::ldexp(1.0, -23) * (wsum + dmu_max) + 1e-30;
-    p.dtol = (float)(dtol * 1.0001);
-    p.eps = (float)(1.25 * p.beta * dtol + 8e-6);
-    p.key0 = (uint32_t)seeds[c];
-    p.key1 = (uint32_t)(seeds[c] >> 32);
-    p.chain_id = chain_ids ? chain_ids[c] : (uint32_t)c;
+  std::vector<int> cstart((size_t)S * (b->n_colors + 1), 0);
+  std::vector<uint32_t> entries(N), site(N);
+  build_site_lists(L0, L1, L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(), site.data());
+  if (b->smem > (size_t)(1u << 24)) {
+    set_error("Error in mg_ce_batch_create: slab too large for 24-bit shared-memory indices");
+    delete b;
+    return MG_ERR_INVALID;
   }
+  b->hcp.resize(n_chains);
+  make_chain_params(m, n_chains, temperature, mu, seeds, chain_ids, b->hcp.data());
 
   auto fail = [&](cudaError_t e, const char* what) {
     set_error(std::string("CUDA error in mg_ce_batch_create: ") + what + ": " + cudaGetErrorString(e));
@@ -596,8 +287,9 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   }
   MG_CUDA_TRY(cudaMemsetAsync(b->dout, 0, sizeof(long long) * need, b->stream));
   MG_CUDA_TRY(cudaEventRecord(b->ev0, b->stream));
-  int rc = (b->model->kind == 0) ? launch_sweep<mg::FccBinary, mg::NT_BINARY>(b, n_passes, b->pass)
-                                 : launch_sweep<mg::FccTernary, mg::NT_TERNARY>(b, n_passes, b->pass);
+  SweepLaunch L{b->L0, b->L1, b->L2, b->S, b->n_colors, b->n_chains, b->precision, b->dcstart, b->dentries,
+                b->dsite, b->dcp, b->docc, b->pass, n_passes, b->dout, b->stream};
+  int rc = launch_sweep(b->model, L);
   if (rc != MG_OK) return rc;
   MG_CUDA_TRY(cudaEventRecord(b->ev1, b->stream));
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, b->dout, sizeof(long long) * need, cudaMemcpyDeviceToHost, b->stream));
@@ -738,11 +430,8 @@ int mg_ce_max_active_chains(const mg_ce_model* m, int L0, int L1, int L2, int ct
     set_error("Error in mg_ce_max_active_chains: invalid argument");
     return MG_ERR_INVALID;
   }
-  mg_ce_batch tmp;
-  tmp.n_chains = 1;
-  const size_t smem = (size_t)(L0 + 4) * (L1 + 4) * ((L2 + ctas_per_chain - 1) / ctas_per_chain + 4);
-  int rc = (m->kind == 0) ? max_active_clusters<mg::FccBinary, mg::NT_BINARY>(&tmp, ctas_per_chain, smem, n_chains)
-                          : max_active_clusters<mg::FccTernary, mg::NT_TERNARY>(&tmp, ctas_per_chain, smem, n_chains);
+  const size_t smem = slab_smem(L0, L1, L2, ctas_per_chain);
+  int rc = max_active_chains(m->kind, ctas_per_chain, smem, n_chains);
   return rc;
 }
 

@@ -1,0 +1,367 @@
+// Host-side helpers of the FCC cluster-expansion sweeps, shared by the chain-batch API
+// (ce_api.cu) and the allocation-free entry point (ce_noalloc.cu).  Every helper writes
+// into caller-provided buffers and performs no memory allocation of its own.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/montegpu.h"
+#include "ce_sweep.cuh"
+#include "generated/fcc_binary.cuh"
+#include "generated/fcc_ternary.cuh"
+#include "mg_common.cuh"
+
+namespace mg {
+
+// Adapters from the generated namespaces to the kernel's basis interface.
+#define MG_BASIS_ADAPTER(NAME, NS_)                                                       \
+  struct NAME {                                                                          \
+    static constexpr int NSPECIES = NS_::NSPECIES;                                       \
+    static constexpr int NFUNC = NS_::NFUNC;                                             \
+    static constexpr int NCLASS = NS_::NCLASS;                                           \
+    static constexpr int NFEAT = NS_::NFEAT;                                             \
+    static constexpr int HALO = NS_::HALO;                                               \
+    __host__ __device__ static constexpr int feat_class(int k) { return NS_::feat_class(k); } \
+    __host__ __device__ static constexpr int feat_b(int k) { return NS_::feat_b(k); }     \
+    __host__ __device__ static constexpr int psi(int b, int o) { return NS_::psi(b, o); } \
+    __host__ __device__ static constexpr int8_t code_of_occ(int o) { return NS_::code_of_occ(o); } \
+    __host__ __device__ static constexpr int occ_of_code(int c) { return NS_::occ_of_code(c); } \
+    template <class L>                                                                   \
+    __device__ static __forceinline__ void features(const L& ld, int (&F)[NFEAT]) {      \
+      NS_::features(ld, F);                                                              \
+    }                                                                                    \
+    template <class L>                                                                   \
+    __device__ static __forceinline__ void anchored(const L& ld, long long (&C)[NCLASS]) { \
+      NS_::anchored(ld, C);                                                              \
+    }                                                                                    \
+  };
+
+MG_BASIS_ADAPTER(FccBinary, fcc_binary)
+MG_BASIS_ADAPTER(FccTernary, fcc_ternary)
+#undef MG_BASIS_ADAPTER
+
+constexpr int NT_BINARY = 512;
+constexpr int NT_TERNARY = 256;
+constexpr int CE_HALO = 2;
+constexpr int CE_MAX_COLORS = 64;
+
+struct ClassInfo {
+  long multiplicity;
+  double scale;
+};
+
+namespace host {
+#include "generated/fcc_class_tables.inc"
+}  // namespace host
+
+}  // namespace mg
+
+struct mg_ce_model {
+  int kind = 0;  // 0 binary, 1 ternary
+  int n_species = 2, n_func = 1, n_classes = 0, n_features = 0;
+  std::vector<double> eci;
+  std::vector<long> mult;
+  std::vector<double> scale;
+  std::vector<int> feat_class, feat_b;
+  std::vector<long> feat_max;  // bound on |F_k|
+  std::vector<double> w64;
+  std::vector<float> w32;
+};
+
+namespace mg {
+namespace host {
+
+inline int dpsi_max(int kind, int b) {
+  if (kind == 0) return 1;
+  return b == 0 ? 2 : 3;
+}
+
+inline const int* offsets(int kind, int* n) {
+  *n = kind == 0 ? kFccBinaryNOffsets : kFccTernaryNOffsets;
+  return kind == 0 ? kFccBinaryOffsets : kFccTernaryOffsets;
+}
+
+// Colouring of the periodic conflict graph (sites sharing a cluster get different colours).
+// Linear colouring (a*i + b*j + c*k) mod m when a*L0, b*L1, c*L2 are multiples of m and no
+// neighbour offset maps to 0 mod m (smallest such m); else greedy in lexicographic order.
+// Returns the number of colours, or -1 if more than CE_MAX_COLORS would be needed.
+inline int color_supercell(int L0, int L1, int L2, int kind, int32_t* col) {
+  int noff = 0;
+  const int* off = offsets(kind, &noff);
+  for (int m = 2; m <= 32; ++m)
+    for (int a = 0; a < m; ++a)
+      for (int b = 0; b < m; ++b)
+        for (int c = 0; c < m; ++c) {
+          if ((1LL * a * L0) % m || (1LL * b * L1) % m || (1LL * c * L2) % m) continue;
+          bool ok = true;
+          for (int t = 0; t < noff && ok; ++t) {
+            long long v = (1LL * a * off[3 * t] + 1LL * b * off[3 * t + 1] + 1LL * c * off[3 * t + 2]) % m;
+            if (v < 0) v += m;
+            ok = v != 0;
+          }
+          if (!ok) continue;
+          for (int k = 0; k < L2; ++k)
+            for (int j = 0; j < L1; ++j)
+              for (int i = 0; i < L0; ++i)
+                col[i + (long long)L0 * (j + (long long)L1 * k)] =
+                    (int32_t)((1LL * a * i + 1LL * b * j + 1LL * c * k) % m);
+          return m;
+        }
+  const long long N = (long long)L0 * L1 * L2;
+  for (long long l = 0; l < N; ++l) col[l] = -1;
+  int n_colors = 0;
+  for (int k = 0; k < L2; ++k)
+    for (int j = 0; j < L1; ++j)
+      for (int i = 0; i < L0; ++i) {
+        bool used[CE_MAX_COLORS] = {};
+        for (int t = 0; t < noff; ++t) {
+          const int a = ((i + off[3 * t]) % L0 + L0) % L0, b = ((j + off[3 * t + 1]) % L1 + L1) % L1,
+                    c = ((k + off[3 * t + 2]) % L2 + L2) % L2;
+          const int32_t cc = col[a + (long long)L0 * (b + (long long)L1 * c)];
+          if (cc >= 0) used[cc] = true;
+        }
+        int cc = 0;
+        while (cc < CE_MAX_COLORS && used[cc]) ++cc;
+        if (cc == CE_MAX_COLORS) return -1;
+        col[i + (long long)L0 * (j + (long long)L1 * k)] = cc;
+        n_colors = std::max(n_colors, cc + 1);
+      }
+  return n_colors;
+}
+
+inline int slab_planes(int L2, int S, int r) { return L2 / S + (r < L2 % S ? 1 : 0); }
+inline int slab_start(int L2, int S, int r) { return r * (L2 / S) + std::min(r, L2 % S); }
+inline size_t slab_smem(int L0, int L1, int L2, int S) {
+  return (size_t)(L0 + 2 * CE_HALO) * (L1 + 2 * CE_HALO) * ((L2 + S - 1) / S + 2 * CE_HALO);
+}
+
+// Per-slab, per-colour site lists.  Within one (slab, colour) list the sites are ordered
+// round-robin over shared-memory banks (bank = (padded index / 4) mod 32) so that the 32
+// lanes of a warp start from different banks.  Entry = padded index | mirror flags << 24;
+// site[e] = global linear index.  cstart[S][n_colors + 1].
+inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, int n_colors,
+                             int* cstart, uint32_t* entries, uint32_t* site) {
+  const int PX = L0 + 2 * CE_HALO, PY = L1 + 2 * CE_HALO;
+  long long pos = 0;
+  for (int r = 0; r < S; ++r) {
+    const int nk = slab_planes(L2, S, r), k0 = slab_start(L2, S, r);
+    for (int c = 0; c < n_colors; ++c) {
+      cstart[r * (n_colors + 1) + c] = (int)pos;
+      long long count[32] = {};
+      for (int kl = 0; kl < nk; ++kl)
+        for (int j = 0; j < L1; ++j)
+          for (int i = 0; i < L0; ++i)
+            if (col[i + (long long)L0 * (j + (long long)L1 * (k0 + kl))] == c) {
+              const uint32_t pidx = (uint32_t)((i + CE_HALO) + PX * ((j + CE_HALO) + PY * (kl + CE_HALO)));
+              count[(pidx >> 2) & 31]++;
+            }
+      long long seen[32] = {};
+      long long total = 0;
+      for (int q = 0; q < 32; ++q) total += count[q];
+      for (int kl = 0; kl < nk; ++kl)
+        for (int j = 0; j < L1; ++j)
+          for (int i = 0; i < L0; ++i) {
+            const long long l = i + (long long)L0 * (j + (long long)L1 * (k0 + kl));
+            if (col[l] != c) continue;
+            const uint32_t pidx = (uint32_t)((i + CE_HALO) + PX * ((j + CE_HALO) + PY * (kl + CE_HALO)));
+            const int q = (pidx >> 2) & 31;
+            const long long t = seen[q]++;
+            // round-robin position of the t-th site of bank q
+            long long p = 0;
+            for (int q2 = 0; q2 < 32; ++q2) p += std::min(count[q2], t) + ((q2 < q && count[q2] > t) ? 1 : 0);
+            uint32_t flags = 0;
+            if (i < CE_HALO) flags |= 1;
+            else if (i >= L0 - CE_HALO) flags |= 2;
+            if (j < CE_HALO) flags |= 4;
+            else if (j >= L1 - CE_HALO) flags |= 8;
+            if (kl < CE_HALO) flags |= 16;
+            if (kl >= nk - CE_HALO) flags |= 32;
+            entries[pos + p] = pidx | (flags << 24);
+            site[pos + p] = (uint32_t)l;
+          }
+      pos += total;
+    }
+    cstart[r * (n_colors + 1) + n_colors] = (int)pos;
+  }
+}
+
+// Chain parameters: beta, Philox key, mu . N dx table and the FP32 error bounds.
+inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* temperature,
+                              const double* mu, const uint64_t* seeds, const uint32_t* chain_ids,
+                              CeChainParams* out) {
+  const double KB = 8.6173303E-05;
+  const int ns = m->n_species;
+  double wsum = 0.0;
+  for (int k = 0; k < m->n_features; ++k)
+    wsum += std::fabs((double)m->w32[k]) * (double)m->feat_max[k] * dpsi_max(m->kind, m->feat_b[k]);
+  for (int c = 0; c < n_chains; ++c) {
+    CeChainParams& p = out[c];
+    std::memset(&p, 0, sizeof(p));
+    p.beta = 1.0 / (KB * temperature[c]);
+    p.beta_log2e = (float)(p.beta * 1.4426950408889634);
+    double dmu_max = 0.0;
+    for (int o = 0; o < ns; ++o)
+      for (int o2 = 0; o2 < ns; ++o2) {
+        double r = 0.0;
+        for (int i = 0; i < ns - 1; ++i) {
+          const double d = (o2 == i + 1 ? 1.0 : 0.0) - (o == i + 1 ? 1.0 : 0.0);
+          r += mu[(size_t)c * (ns - 1) + i] * d;
+        }
+        p.dmu64[o * ns + o2] = r;
+        p.dmu32[o * ns + o2] = (float)r;
+        dmu_max = std::max(dmu_max, std::fabs(r));
+      }
+    const double dtol = (m->n_features + 8) * std::ldexp(1.0, -23) * (wsum + dmu_max) + 1e-30;
+    p.dtol = (float)(dtol * 1.0001);
+    p.eps = (float)(1.25 * p.beta * dtol + 8e-6);
+    p.key0 = (uint32_t)seeds[c];
+    p.key1 = (uint32_t)(seeds[c] >> 32);
+    p.chain_id = chain_ids ? chain_ids[c] : (uint32_t)c;
+  }
+}
+
+template <class B, int NT>
+int max_active_clusters(int S, size_t smem, int* out) {
+  auto kern = ce_sweep_kernel<B, NT>;
+  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  if (S == 1) {
+    int nb = 0, dev = 0, sms = 0;
+    MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, NT, smem));
+    MG_CUDA_TRY(cudaGetDevice(&dev));
+    MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    *out = nb * sms;
+    return MG_OK;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)S, 1, 1);
+  cfg.blockDim = dim3(NT, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)S;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  MG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, (void*)kern, &cfg));
+  *out = n;
+  return MG_OK;
+}
+
+inline int max_active_chains(int kind, int S, size_t smem, int* out) {
+  return kind == 0 ? max_active_clusters<FccBinary, NT_BINARY>(S, smem, out)
+                   : max_active_clusters<FccTernary, NT_TERNARY>(S, smem, out);
+}
+
+// CTAs per chain: requested (validated) or the S minimising waves(S)/S over the
+// launchable candidates (ties -> fewer CTAs).  Returns MG_OK and sets *S_out.
+inline int choose_ctas(int kind, int L0, int L1, int L2, int n_chains, int requested, int* S_out) {
+  int dev = 0, max_smem = 0;
+  MG_CUDA_TRY(cudaGetDevice(&dev));
+  MG_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t budget = (size_t)max_smem - 1024;
+  auto ok = [&](int S) { return S >= 1 && S <= 16 && L2 / S >= CE_HALO && slab_smem(L0, L1, L2, S) <= budget; };
+  if (requested > 0) {
+    if (!ok(requested)) {
+      set_error("Error in ce sweep: ctas_per_chain must leave >= 2 planes per CTA and fit in shared memory");
+      return MG_ERR_INVALID;
+    }
+    *S_out = requested;
+    return MG_OK;
+  }
+  double best = 1e300;
+  int S = 0;
+  for (int s = 1; s <= 16; ++s) {
+    if (!ok(s)) continue;
+    int n_active = 0;
+    const int rc = max_active_chains(kind, s, slab_smem(L0, L1, L2, s), &n_active);
+    if (rc != MG_OK) return rc;
+    if (n_active < 1) continue;
+    const double cost = (double)((n_chains + n_active - 1) / n_active) / s;
+    if (cost < best * (1.0 - 1e-9)) {
+      best = cost;
+      S = s;
+    }
+  }
+  if (S == 0) {
+    set_error("Error in ce sweep: supercell slab does not fit in shared memory for any CTA count");
+    return MG_ERR_INVALID;
+  }
+  *S_out = S;
+  return MG_OK;
+}
+
+struct SweepLaunch {
+  int L0, L1, L2, S, n_colors, n_chains, precision;
+  const int* cstart;
+  const uint32_t* entries;
+  const uint32_t* site;
+  const CeChainParams* cp;
+  int8_t* occ;
+  long long pass0;
+  int n_passes;
+  long long* out;
+  cudaStream_t stream;
+};
+
+template <class B, int NT>
+int launch_sweep_t(const mg_ce_model* m, const SweepLaunch& L) {
+  CeSweepArgs<B::NFEAT> A;
+  A.g.L0 = L.L0;
+  A.g.L1 = L.L1;
+  A.g.L2 = L.L2;
+  A.g.S = L.S;
+  A.g.PX = L.L0 + 2 * CE_HALO;
+  A.g.PY = L.L1 + 2 * CE_HALO;
+  A.g.PZ = (L.L2 + L.S - 1) / L.S + 2 * CE_HALO;
+  A.g.n_colors = L.n_colors;
+  A.g.color_start = L.cstart;
+  A.g.entries = L.entries;
+  A.g.site_l = L.site;
+  for (int k = 0; k < B::NFEAT; ++k) {
+    A.w.w32[k] = m->w32[k];
+    A.w.w64[k] = m->w64[k];
+  }
+  A.cp = L.cp;
+  A.occ = L.occ;
+  A.pass0 = L.pass0;
+  A.n_passes = L.n_passes;
+  A.n_chains = L.n_chains;
+  A.precision = L.precision;
+  A.out = L.out;
+  const size_t smem = slab_smem(L.L0, L.L1, L.L2, L.S);
+  auto kern = ce_sweep_kernel<B, NT>;
+  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);
+  cfg.blockDim = dim3(NT, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = L.stream;
+  cudaLaunchAttribute attr[1];
+  if (L.S > 1) {
+    if (L.S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)L.S;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  MG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
+  MG_CUDA_TRY(cudaGetLastError());
+  return MG_OK;
+}
+
+inline int launch_sweep(const mg_ce_model* m, const SweepLaunch& L) {
+  return m->kind == 0 ? launch_sweep_t<FccBinary, NT_BINARY>(m, L) : launch_sweep_t<FccTernary, NT_TERNARY>(m, L);
+}
+
+}  // namespace host
+}  // namespace mg
