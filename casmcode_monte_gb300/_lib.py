@@ -64,6 +64,8 @@ SIGNATURES = {
     "mg_ce_batch_delta_e": (C.c_int, [vp, c_int32_p, c_ll_p, c_int8_p, C.c_longlong, c_double_p]),
     "mg_ce_batch_destroy": (C.c_int, [vp]),
     "mg_ce_max_active_chains": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, c_int_p]),
+    "mg_ce_sweep_noalloc": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p, c_double_p, c_uint64_p,
+                                      vp, C.c_longlong, C.c_int, vp, C.c_int, vp]),
     "mg_equilibration_check": (C.c_int, [c_double_p, C.c_long, C.c_double, c_int_p, c_long_p]),
     "mg_basic_statistics": (C.c_int, [c_double_p, C.c_long, c_double_p, C.c_long, C.c_double,
                                       C.c_long, C.c_long, c_double_p, c_double_p]),

@@ -129,6 +129,28 @@ int mg_ce_batch_destroy(mg_ce_batch* b);
 int mg_ce_max_active_chains(const mg_ce_model* m, int L0, int L1, int L2, int ctas_per_chain,
                             int* n_chains);
 
+/* ---- allocation-free coloured sweep (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc (an embedding framework owns all device
+ * memory, allocation is forbidden during a run, or the device is fully reserved): the
+ * caller passes device pointers to the occupations d_occ[n_chains][N] (in/out) and the
+ * per-pass outputs d_out[n_passes][n_chains][n_classes+2] (same meaning as
+ * mg_ce_batch_run), plus host arrays of temperatures, exchange potentials and seeds.
+ * The site lists and chain parameters go to a fixed file-scope device array of
+ * MG_NOALLOC_SCRATCH_BYTES, resident on every device that loads the library until exit;
+ * nothing is allocated.  Sizes beyond MG_NOALLOC_MAX_SITES sites per chain or
+ * MG_NOALLOC_MAX_CHAINS chains are rejected.  The first call on a device looks up the
+ * array's address (do it before any stream capture).  Calls share the array: calls that
+ * overlap on the GPU race, and host calls must not run concurrently.  Work is enqueued
+ * on `stream` (a cudaStream_t, NULL = legacy default stream) and not synchronised;
+ * pass0 continues the Philox pass counter. */
+#define MG_NOALLOC_MAX_SITES 262144
+#define MG_NOALLOC_MAX_CHAINS 64
+#define MG_NOALLOC_SCRATCH_BYTES 2162688
+int mg_ce_sweep_noalloc(const mg_ce_model* m, int L0, int L1, int L2, int n_chains,
+                        const double* temperature, const double* mu, const uint64_t* seeds,
+                        int8_t* d_occ, long long pass0, int n_passes, long long* d_out,
+                        int precision, void* stream);
+
 /* ---- statistics (host numerics shared with the device convergence kernel) ---- */
 /* _default_equilibration_check (EquilibrationCheck.cc:50-117) */
 int mg_equilibration_check(const double* obs, long n, double prec, int* is_equilibrated,

@@ -1,0 +1,67 @@
+"""The allocation-free sweep entry point (mg_ce_sweep_noalloc) against the batch API.
+
+Callers that cannot allocate device memory (their framework owns the pool, or
+allocation is forbidden while a run is in progress) hand the library their own device
+buffers and get the same coloured sweep, with the library's scratch in a fixed device
+array.  This test allocates the caller's buffers with torch (the caller may allocate;
+the entry point must not), calls the entry point twice in a row through the C-ABI, and
+requires the occupations and per-pass outputs to equal those of mg_ce_batch_run on the
+same inputs exactly (the sweeps are deterministic integer trajectories).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from casmcode_monte_gb300 import _lib, clex
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("kind,L,n_chains", [("fcc_binary", (16, 16, 16), 3), ("fcc_ternary", (12, 8, 10), 2)])
+def test_noalloc_sweep_matches_batch_two_calls(kind, L, n_chains):
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    Lb = _lib.lib()
+    model = clex.ClexModel(kind, clex.make_eci(kind, 21))
+    rng = np.random.default_rng(4)
+    N = L[0] * L[1] * L[2]
+    occ0 = np.stack([clex.random_occupation(model.n_species, N, rng) for _ in range(n_chains)])
+    T = np.ascontiguousarray(np.linspace(500.0, 1500.0, n_chains))
+    mu = np.ascontiguousarray(rng.uniform(-0.2, 0.2, size=(n_chains, model.n_species - 1)))
+    seeds = np.ascontiguousarray(np.arange(7, 7 + n_chains, dtype=np.uint64))
+    nslot = model.n_classes + 2
+
+    ref = clex.ChainBatch(model, L, occ0, T, mu, seeds)
+    d_occ = torch.from_numpy(occ0.copy()).cuda()
+    stream = torch.cuda.current_stream()
+    pass0 = 0
+    for n_passes in (3, 4):
+        d_out = torch.full((n_passes, n_chains, nslot), -7, dtype=torch.int64, device="cuda")
+        rc = Lb.mg_ce_sweep_noalloc(model._h, L[0], L[1], L[2], n_chains, _lib.ptr(T, C.c_double),
+                                    _lib.ptr(mu, C.c_double), _lib.ptr(seeds, C.c_uint64),
+                                    C.c_void_p(d_occ.data_ptr()), pass0, n_passes,
+                                    C.c_void_p(d_out.data_ptr()), 0, C.c_void_p(stream.cuda_stream))
+        _lib.check(rc)
+        torch.cuda.synchronize()
+        want = ref.run(n_passes)
+        assert np.array_equal(d_out.cpu().numpy(), want)
+        assert np.array_equal(d_occ.cpu().numpy(), ref.occupation())
+        pass0 += n_passes
+    ref.close()
+
+
+def test_noalloc_rejects_oversized_inputs():
+    torch = pytest.importorskip("torch")
+    Lb = _lib.lib()
+    model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 1))
+    T = np.array([1000.0])
+    mu = np.zeros((1, 1))
+    seeds = np.array([1], dtype=np.uint64)
+    dummy = torch.zeros(8, dtype=torch.int64, device="cuda")
+    # 96^3 sites exceed the 262144-site scratch limit
+    rc = Lb.mg_ce_sweep_noalloc(model._h, 96, 96, 96, 1, _lib.ptr(T, C.c_double), _lib.ptr(mu, C.c_double),
+                                _lib.ptr(seeds, C.c_uint64), C.c_void_p(dummy.data_ptr()), 0, 1,
+                                C.c_void_p(dummy.data_ptr()), 0, None)
+    assert rc != 0
+    assert b"262144" in Lb.mg_last_error()
