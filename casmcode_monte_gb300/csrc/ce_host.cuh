@@ -140,10 +140,12 @@ inline size_t slab_smem(int L0, int L1, int L2, int S) {
   return (size_t)(L0 + 2 * CE_HALO) * (L1 + 2 * CE_HALO) * ((L2 + S - 1) / S + 2 * CE_HALO);
 }
 
-// Per-slab, per-colour site lists.  Within one (slab, colour) list the sites are ordered
-// round-robin over shared-memory banks (bank = (padded index / 4) mod 32) so that the 32
-// lanes of a warp start from different banks.  Entry = padded index | mirror flags << 24;
-// site[e] = global linear index.  cstart[S][n_colors + 1].
+// Per-slab, per-colour site lists.  Within one (slab, colour) list the sites are grouped
+// by (padded index mod 4) and, inside a group, ordered round-robin over the 32 word banks
+// ((padded index / 4) mod 32).  Lanes of a warp then share the byte offset within their
+// 4-byte word, so every constant neighbour offset keeps their words in distinct banks.
+// Entry = padded index | mirror flags << 24; site[e] = global linear index.
+// cstart[S][n_colors + 1].
 inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, int n_colors,
                              int* cstart, uint32_t* entries, uint32_t* site) {
   const int PX = L0 + 2 * CE_HALO, PY = L1 + 2 * CE_HALO;
@@ -152,28 +154,31 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
     const int nk = slab_planes(L2, S, r), k0 = slab_start(L2, S, r);
     for (int c = 0; c < n_colors; ++c) {
       cstart[r * (n_colors + 1) + c] = (int)pos;
-      long long count[32] = {};
+      long long count[4][32] = {};
       for (int kl = 0; kl < nk; ++kl)
         for (int j = 0; j < L1; ++j)
           for (int i = 0; i < L0; ++i)
             if (col[i + (long long)L0 * (j + (long long)L1 * (k0 + kl))] == c) {
               const uint32_t pidx = (uint32_t)((i + CE_HALO) + PX * ((j + CE_HALO) + PY * (kl + CE_HALO)));
-              count[(pidx >> 2) & 31]++;
+              count[pidx & 3][(pidx >> 2) & 31]++;
             }
-      long long seen[32] = {};
-      long long total = 0;
-      for (int q = 0; q < 32; ++q) total += count[q];
+      long long base[4] = {};
+      for (int g = 1; g < 4; ++g) {
+        base[g] = base[g - 1];
+        for (int q = 0; q < 32; ++q) base[g] += count[g - 1][q];
+      }
+      long long seen[4][32] = {};
       for (int kl = 0; kl < nk; ++kl)
         for (int j = 0; j < L1; ++j)
           for (int i = 0; i < L0; ++i) {
             const long long l = i + (long long)L0 * (j + (long long)L1 * (k0 + kl));
             if (col[l] != c) continue;
             const uint32_t pidx = (uint32_t)((i + CE_HALO) + PX * ((j + CE_HALO) + PY * (kl + CE_HALO)));
-            const int q = (pidx >> 2) & 31;
-            const long long t = seen[q]++;
-            // round-robin position of the t-th site of bank q
-            long long p = 0;
-            for (int q2 = 0; q2 < 32; ++q2) p += std::min(count[q2], t) + ((q2 < q && count[q2] > t) ? 1 : 0);
+            const int g = pidx & 3, q = (pidx >> 2) & 31;
+            const long long t = seen[g][q]++;
+            // round-robin position of the t-th site of bank q within group g
+            long long p = base[g];
+            for (int q2 = 0; q2 < 32; ++q2) p += std::min(count[g][q2], t) + ((q2 < q && count[g][q2] > t) ? 1 : 0);
             uint32_t flags = 0;
             if (i < CE_HALO) flags |= 1;
             else if (i >= L0 - CE_HALO) flags |= 2;
@@ -184,7 +189,8 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
             entries[pos + p] = pidx | (flags << 24);
             site[pos + p] = (uint32_t)l;
           }
-      pos += total;
+      for (int g = 0; g < 4; ++g)
+        for (int q = 0; q < 32; ++q) pos += count[g][q];
     }
     cstart[r * (n_colors + 1) + n_colors] = (int)pos;
   }

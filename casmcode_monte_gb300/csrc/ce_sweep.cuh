@@ -101,6 +101,15 @@ __device__ __forceinline__ float fast_exp2(float x) {
   return y;
 }
 
+// split cluster barrier: arrive (release the CTA's shared and distributed-shared writes),
+// then wait (acquire the other CTAs' writes)
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ int warp_sum(int v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -173,123 +182,157 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
   const int dI = L0, dJ = L1 * PX, dKp = nk_prev * PXY, dKn = nk * PXY;
   (void)PZ;
   const int lane = threadIdx.x & 31;
-  barrier();
-
   int acc[NSLOT];
 #pragma unroll
   for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+
+  // Sweep of one site in two parts: `gather` reads the site and its neighbourhood
+  // (shared-memory loads only) and `decide` draws the decision and writes the flip.
+  auto gather = [&](uint32_t ent, int& o, int (&F)[NF]) {
+    const int8_t* p = s + (int)(ent & 0xFFFFFFu);
+    o = B::occ_of_code(*p);
+    B::features(SmemLoader{p, PX, PXY}, F);
+  };
+  auto decide = [&](uint32_t ent, uint32_t x0, uint32_t x1, int o, const int (&F)[NF]) {
+    const int pidx = (int)(ent & 0xFFFFFFu);
+    const uint32_t flags = ent >> 24;
+    int o2;
+    if (NS == 2)
+      o2 = 1 - o;
+    else
+      o2 = (o + 1 + (int)(x1 >> 31)) % 3;
+    int dpsi[B::NFUNC];
+#pragma unroll
+    for (int b = 0; b < B::NFUNC; ++b) dpsi[b] = B::psi(b, o2) - B::psi(b, o);
+    float G[B::NFUNC];
+#pragma unroll
+    for (int b = 0; b < B::NFUNC; ++b) G[b] = 0.f;
+#pragma unroll
+    for (int k = 0; k < NF; ++k) G[B::feat_b(k)] = fmaf(A.w.w32[k], (float)F[k], G[B::feat_b(k)]);
+    float dE32 = -dmu32_sm[o * NS + o2];
+#pragma unroll
+    for (int b = 0; b < B::NFUNC; ++b) dE32 = fmaf((float)dpsi[b], G[b], dE32);
+
+    const float u32 = __uint2float_rn(x0) * 2.3283064365386963e-10f;
+    bool amb = false, acc32;
+    if (dE32 < -dtol) {
+      acc32 = true;
+    } else {
+      const float P = fast_exp2(-dE32 * beta_log2e);
+      acc32 = (dE32 < 0.f) || (u32 < P);
+      if (dE32 <= dtol || x0 == 0u)
+        amb = true;
+      else if (!(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps)))
+        amb = true;
+    }
+    bool accept = acc32;
+    if (amb) {
+      // exact FP64 decision: dE64 = sum_b dpsi_b * (sum_k w64[k] F[k]) - dmu
+      double G64[B::NFUNC];
+#pragma unroll
+      for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
+#pragma unroll
+      for (int k = 0; k < NF; ++k)
+        G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(A.w.w64[k], (double)F[k]));
+      double dE = 0.0;
+#pragma unroll
+      for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
+      dE = __dsub_rn(dE, dmu64_sm[o * NS + o2]);
+      bool acc64;
+      if (dE < 0.0) {
+        acc64 = true;
+      } else {
+        const double u = __dmul_rn((double)x0, 2.3283064365386962890625e-10);
+        acc64 = u < exp(__dmul_rn(-dE, beta));
+      }
+      acc[NC] += 1;
+      if (A.precision == 0) {
+        accept = acc64;
+      } else if (acc64 != acc32) {
+        acc[NC + 1] += 1;
+      }
+    }
+    if (accept) {
+      const int8_t c2 = B::code_of_occ(o2);
+      const int oi = (flags & 1u) ? dI : ((flags & 2u) ? -dI : 0);
+      const int oj = (flags & 4u) ? dJ : ((flags & 8u) ? -dJ : 0);
+      s[pidx] = c2;
+      if (oi) s[pidx + oi] = c2;
+      if (oj) s[pidx + oj] = c2;
+      if (oi && oj) s[pidx + oi + oj] = c2;
+      if (flags & 16u) {
+        int8_t* r = s_prev + pidx + dKp;
+        r[0] = c2;
+        if (oi) r[oi] = c2;
+        if (oj) r[oj] = c2;
+        if (oi && oj) r[oi + oj] = c2;
+      }
+      if (flags & 32u) {
+        int8_t* r = s_next + pidx - dKn;
+        r[0] = c2;
+        if (oi) r[oi] = c2;
+        if (oj) r[oj] = c2;
+        if (oi && oj) r[oi + oj] = c2;
+      }
+      acc[0] += 1;
+#pragma unroll
+      for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += dpsi[B::feat_b(k)] * F[k];
+    }
+  };
+
+  // The first PRE sites of each thread in the next phase are prepared (list entry and
+  // random numbers, which do not depend on the lattice) while the phase barrier is
+  // pending; further sites of a phase load and draw inline.
+  constexpr int PRE = (NS == 2) ? 3 : 2;
+  uint32_t pre_ent[PRE], pre_x0[PRE], pre_x1[PRE];
+  auto prepare = [&](int cn, uint32_t pass_n) {
+    const int eb = cstart[cn] + threadIdx.x, ee = cstart[cn + 1];
+#pragma unroll
+    for (int q = 0; q < PRE; ++q) {
+      const int e = eb + q * NT;
+      if (e < ee) {
+        pre_ent[q] = __ldg(g.entries + e);
+        const U32x4 x = philox4x32_10(U32x4{__ldg(g.site_l + e), pass_n, chain_id, SWEEP_TAG}, key0, key1);
+        pre_x0[q] = x.x;
+        pre_x1[q] = x.y;
+      }
+    }
+  };
+  prepare(0, (uint32_t)A.pass0);
+  barrier();
 
 #pragma unroll 1
   for (int pass = 0; pass < A.n_passes; ++pass) {
     const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
 #pragma unroll 1
     for (int c = 0; c < g.n_colors; ++c) {
-      const int e_end = cstart[c + 1];
-      int e = cstart[c] + threadIdx.x;
-      uint32_t ent_next = 0u, l_next = 0u;
-      if (e < e_end) {
-        ent_next = __ldg(g.entries + e);
-        l_next = __ldg(g.site_l + e);
-      }
+      const int e0 = cstart[c] + threadIdx.x, e_end = cstart[c + 1];
+#pragma unroll
+      for (int q = 0; q < PRE; ++q)
+        if (e0 + q * NT < e_end) {
+          int o1;
+          int F1[NF];
+          gather(pre_ent[q], o1, F1);
+          decide(pre_ent[q], pre_x0[q], pre_x1[q], o1, F1);
+        }
 #pragma unroll 1
-      for (; e < e_end; e += NT) {
-        const uint32_t ent = ent_next;
-        const uint32_t l = l_next;
-        if (e + NT < e_end) {  // prefetch the next site of this colour
-          ent_next = __ldg(g.entries + e + NT);
-          l_next = __ldg(g.site_l + e + NT);
-        }
-        const int pidx = (int)(ent & 0xFFFFFFu);
-        const uint32_t flags = ent >> 24;
-        const int8_t* p = s + pidx;
-        const int o = B::occ_of_code(*p);
-        const U32x4 x = philox4x32_10(U32x4{l, pass_g, chain_id, SWEEP_TAG}, key0, key1);
-        int o2;
-        if (NS == 2)
-          o2 = 1 - o;
-        else
-          o2 = (o + 1 + (int)(x.y >> 31)) % 3;
-        int F[NF];
-        B::features(SmemLoader{p, PX, PXY}, F);
-        int dpsi[B::NFUNC];
-#pragma unroll
-        for (int b = 0; b < B::NFUNC; ++b) dpsi[b] = B::psi(b, o2) - B::psi(b, o);
-        float G[B::NFUNC];
-#pragma unroll
-        for (int b = 0; b < B::NFUNC; ++b) G[b] = 0.f;
-#pragma unroll
-        for (int k = 0; k < NF; ++k) G[B::feat_b(k)] = fmaf(A.w.w32[k], (float)F[k], G[B::feat_b(k)]);
-        float dE32 = -dmu32_sm[o * NS + o2];
-#pragma unroll
-        for (int b = 0; b < B::NFUNC; ++b) dE32 = fmaf((float)dpsi[b], G[b], dE32);
-
-        const float u32 = __uint2float_rn(x.x) * 2.3283064365386963e-10f;
-        bool amb = false, acc32;
-        if (dE32 < -dtol) {
-          acc32 = true;
-        } else {
-          const float P = fast_exp2(-dE32 * beta_log2e);
-          acc32 = (dE32 < 0.f) || (u32 < P);
-          if (dE32 <= dtol || x.x == 0u)
-            amb = true;
-          else if (!(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps)))
-            amb = true;
-        }
-        bool accept = acc32;
-        if (amb) {
-          // exact FP64 decision: dE64 = sum_b dpsi_b * (sum_k w64[k] F[k]) - dmu
-          double G64[B::NFUNC];
-#pragma unroll
-          for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
-#pragma unroll
-          for (int k = 0; k < NF; ++k)
-            G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(A.w.w64[k], (double)F[k]));
-          double dE = 0.0;
-#pragma unroll
-          for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
-          dE = __dsub_rn(dE, dmu64_sm[o * NS + o2]);
-          bool acc64;
-          if (dE < 0.0) {
-            acc64 = true;
-          } else {
-            const double u = __dmul_rn((double)x.x, 2.3283064365386962890625e-10);
-            acc64 = u < exp(__dmul_rn(-dE, beta));
-          }
-          acc[NC] += 1;
-          if (A.precision == 0) {
-            accept = acc64;
-          } else if (acc64 != acc32) {
-            acc[NC + 1] += 1;
-          }
-        }
-        if (accept) {
-          const int8_t c2 = B::code_of_occ(o2);
-          const int oi = (flags & 1u) ? dI : ((flags & 2u) ? -dI : 0);
-          const int oj = (flags & 4u) ? dJ : ((flags & 8u) ? -dJ : 0);
-          s[pidx] = c2;
-          if (oi) s[pidx + oi] = c2;
-          if (oj) s[pidx + oj] = c2;
-          if (oi && oj) s[pidx + oi + oj] = c2;
-          if (flags & 16u) {
-            int8_t* r = s_prev + pidx + dKp;
-            r[0] = c2;
-            if (oi) r[oi] = c2;
-            if (oj) r[oj] = c2;
-            if (oi && oj) r[oi + oj] = c2;
-          }
-          if (flags & 32u) {
-            int8_t* r = s_next + pidx - dKn;
-            r[0] = c2;
-            if (oi) r[oi] = c2;
-            if (oj) r[oj] = c2;
-            if (oi && oj) r[oi + oj] = c2;
-          }
-          acc[0] += 1;
-#pragma unroll
-          for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += dpsi[B::feat_b(k)] * F[k];
-        }
+      for (int e = e0 + PRE * NT; e < e_end; e += NT) {
+        const U32x4 x = philox4x32_10(U32x4{__ldg(g.site_l + e), pass_g, chain_id, SWEEP_TAG}, key0, key1);
+        const uint32_t ent = __ldg(g.entries + e);
+        int o1;
+        int F1[NF];
+        gather(ent, o1, F1);
+        decide(ent, x.x, x.y, o1, F1);
       }
-      barrier();
+      const bool last = (c + 1 == g.n_colors);
+      if (S > 1) {
+        cluster_arrive_release();
+        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g);
+        cluster_wait_acquire();
+      } else {
+        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g);
+        __syncthreads();
+      }
       if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
         // flush the previous pass (all warps added to it before this barrier)
         int* buf = acc_sm[(pass - 1) & 1];
