@@ -189,6 +189,97 @@ class ChainBatch:
         return out
 
 
+class PoolFull(RuntimeError):
+    """Admission refused: no free chain slot or not enough arena memory."""
+
+
+class ChainPool:
+    """Chains of any supercell shape in one HBM arena (handle to mg_ce_pool).
+
+    ``add`` admits a chain if its occupation fits in the arena (raises ``PoolFull``
+    otherwise); ``run(slots, n_passes)`` sweeps the given chains in one launch of the
+    persistent pool kernel; each chain keeps its own pass counter.
+    """
+
+    def __init__(self, model: ClexModel, arena_bytes: int, max_chains: int, precision: str = "fp64"):
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.model = model
+        h = C.c_void_p()
+        _lib.check(_lib.lib().mg_ce_pool_create(model._h, int(arena_bytes), int(max_chains),
+                                                0 if precision == "fp64" else 1, C.byref(h)))
+        self._h = h
+        self.shapes: dict = {}
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.mg_ce_pool_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def n_slots(self) -> int:
+        return self.model.n_classes + 2
+
+    def add(self, shape, occ, temperature: float, mu, seed: int, chain_id: int) -> int:
+        L0, L1, L2 = (int(x) for x in shape)
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int8).reshape(-1))
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64).reshape(self.model.n_species - 1))
+        slot = C.c_int()
+        rc = _lib.lib().mg_ce_pool_add(self._h, L0, L1, L2, float(temperature), _lib.ptr(mu, C.c_double),
+                                       C.c_uint64(int(seed)), C.c_uint32(int(chain_id)), _lib.ptr(occ, C.c_int8),
+                                       C.byref(slot))
+        if rc == 5:
+            raise PoolFull(_lib.lib().mg_last_error().decode())
+        _lib.check(rc)
+        self.shapes[slot.value] = (L0, L1, L2)
+        return slot.value
+
+    def remove(self, slot: int) -> None:
+        _lib.check(_lib.lib().mg_ce_pool_remove(self._h, int(slot)))
+        self.shapes.pop(slot, None)
+
+    def info(self) -> dict:
+        fb, ab, nu, mc = C.c_longlong(), C.c_longlong(), C.c_int(), C.c_int()
+        _lib.check(_lib.lib().mg_ce_pool_info(self._h, C.byref(fb), C.byref(ab), C.byref(nu), C.byref(mc)))
+        return {"arena_free_bytes": fb.value, "arena_bytes": ab.value, "n_used": nu.value, "max_chains": mc.value}
+
+    def run(self, slots, n_passes: int, want_output: bool = True) -> Optional[np.ndarray]:
+        """Sweep the chains in ``slots``; returns [len(slots), n_passes, n_classes+2] int64."""
+        sl = np.ascontiguousarray(np.asarray(slots, dtype=np.int32).reshape(-1))
+        out = np.zeros((sl.size, n_passes, self.n_slots), dtype=np.int64) if want_output else None
+        _lib.check(_lib.lib().mg_ce_pool_run(self._h, _lib.ptr(sl, C.c_int32), sl.size, int(n_passes),
+                                             _lib.ptr(out, C.c_longlong) if out is not None else None))
+        return out
+
+    def last_kernel_ms(self) -> float:
+        ms = C.c_float()
+        _lib.check(_lib.lib().mg_ce_pool_last_kernel_ms(self._h, C.byref(ms)))
+        return float(ms.value)
+
+    def occupation(self, slot: int) -> np.ndarray:
+        n = int(np.prod(self.shapes[slot]))
+        occ = np.zeros(n, dtype=np.int8)
+        _lib.check(_lib.lib().mg_ce_pool_get_occ(self._h, int(slot), _lib.ptr(occ, C.c_int8)))
+        return occ
+
+    def colors(self, slot: int) -> tuple[np.ndarray, int]:
+        n = int(np.prod(self.shapes[slot]))
+        col = np.zeros(n, dtype=np.int32)
+        nc = _lib.lib().mg_ce_pool_colors(self._h, int(slot), _lib.ptr(col, C.c_int32))
+        if nc <= 0:
+            _lib.check(nc if nc else 1)
+        return col, nc
+
+    def corr(self, slot: int) -> np.ndarray:
+        out = np.zeros(self.model.n_classes, dtype=np.int64)
+        _lib.check(_lib.lib().mg_ce_pool_corr(self._h, int(slot), _lib.ptr(out, C.c_longlong)))
+        return out
+
+
 @dataclass
 class SweepSamples:
     """Per-pass observables of a batch run (arrays [n_passes, n_chains])."""
@@ -231,5 +322,5 @@ def random_occupation(n_species: int, n_sites: int, rng: np.random.Generator,
     return occ
 
 
-__all__ = ["ClexModel", "ChainBatch", "SweepSamples", "accumulate", "basis_description", "make_eci",
+__all__ = ["ClexModel", "ChainBatch", "ChainPool", "PoolFull", "SweepSamples", "accumulate", "basis_description", "make_eci",
            "random_occupation", "KB"]

@@ -116,84 +116,38 @@ __device__ __forceinline__ int warp_sum(int v) {
   return v;
 }
 
-template <class B, int NT>
-__global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__ CeSweepArgs<B::NFEAT> A) {
-  constexpr int NF = B::NFEAT;
-  constexpr int NC = B::NCLASS;
-  constexpr int NS = B::NSPECIES;
-  constexpr int NSLOT = CeSlots<NC>::N;
-  extern __shared__ __align__(16) int8_t s[];
-  __shared__ int acc_sm[2][NSLOT];
-  __shared__ float dmu32_sm[NS * NS];
-  __shared__ double dmu64_sm[NS * NS];
+// Per-CTA context of the site update: shared-memory lattice and its periodic copies,
+// chain constants and the FP32/FP64 decision rule.  Shared by the cluster sweep kernel
+// and the persistent pool kernel.
+template <class B>
+struct SiteSweeper {
+  static constexpr int NF = B::NFEAT;
+  static constexpr int NC = B::NCLASS;
+  static constexpr int NS = B::NSPECIES;
+  static constexpr int NSLOT = CeSlots<NC>::N;
+  int8_t* s;       // own slab (padded)
+  int8_t* s_prev;  // previous CTA's slab (distributed shared memory; == s for one CTA)
+  int8_t* s_next;  // next CTA's slab
+  int PX, PXY;
+  int dI, dJ, dKp, dKn;  // offsets of the periodic / halo copies
+  const float* dmu32;    // shared memory [NS*NS]
+  const double* dmu64;
+  const CeWeights<NF>* w;
+  double beta;
+  float beta_log2e, dtol, eps;
+  int precision;
 
-  const CeGeometry& g = A.g;
-  const int S = g.S;
-  const int chain = blockIdx.x / S;
-  int rank = 0;
-  cg::cluster_group cluster = cg::this_cluster();
-  if (S > 1) rank = (int)cluster.block_rank();
-  auto barrier = [&]() {
-    if (S > 1)
-      cluster.sync();
-    else
-      __syncthreads();
-  };
-
-  const int PX = g.PX, PY = g.PY, PZ = g.PZ, PXY = PX * PY;
-  const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
-  const int nkq = L2 / S, nkr = L2 % S;
-  const int nk = nkq + (rank < nkr ? 1 : 0);
-  const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
-  const int rprev = (rank + S - 1) % S;
-  const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
-  const long long N = (long long)L0 * L1 * L2;
-  int8_t* gocc = A.occ + (size_t)chain * N;
-
-  // ---- load slab + borders
-  for (int idx = threadIdx.x; idx < PXY * (nk + 2 * B::HALO); idx += NT) {
-    const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
-    int i = ip - B::HALO, j = jp - B::HALO, k = k0 + kp - B::HALO;
-    i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
-    j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
-    k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
-    s[idx] = B::code_of_occ(gocc[i + (long long)L0 * (j + (long long)L1 * k)]);
-  }
-  if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
-
-  int8_t* s_prev = s;
-  int8_t* s_next = s;
-  if (S > 1) {
-    s_prev = cluster.map_shared_rank(s, (unsigned)((rank + S - 1) % S));
-    s_next = cluster.map_shared_rank(s, (unsigned)((rank + 1) % S));
-  }
-  const CeChainParams* cpg = A.cp + chain;
-  if (threadIdx.x < NS * NS) {
-    dmu32_sm[threadIdx.x] = cpg->dmu32[threadIdx.x];
-    dmu64_sm[threadIdx.x] = cpg->dmu64[threadIdx.x];
-  }
-  const double beta = cpg->beta;
-  const float beta_log2e = cpg->beta_log2e, dtol = cpg->dtol, eps = cpg->eps;
-  const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
-  const int* cstart = g.color_start + rank * (g.n_colors + 1);
-  // periodic copies: +-L0 in i, +-L1 rows in j; a plane kl < HALO is also the upper
-  // halo of the previous CTA (at kl + nk_prev + HALO), a plane kl >= nk - HALO the
-  // lower halo of the next CTA (at kl - nk + HALO)
-  const int dI = L0, dJ = L1 * PX, dKp = nk_prev * PXY, dKn = nk * PXY;
-  (void)PZ;
-  const int lane = threadIdx.x & 31;
-  int acc[NSLOT];
-#pragma unroll
-  for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
-
-  // Sweep of one site in two parts: `gather` reads the site and its neighbourhood
-  // (shared-memory loads only) and `decide` draws the decision and writes the flip.
-  auto gather = [&](uint32_t ent, int& o, int (&F)[NF]) {
+  // the site's occupant and its integer local features
+  __device__ __forceinline__ void gather(uint32_t ent, int& o, int (&F)[NF]) const {
     const int8_t* p = s + (int)(ent & 0xFFFFFFu);
     o = B::occ_of_code(*p);
     B::features(SmemLoader{p, PX, PXY}, F);
-  };
-  auto decide = [&](uint32_t ent, uint32_t x0, uint32_t x1, int o, const int (&F)[NF]) {
+  }
+
+  // Metropolis decision for the proposal drawn from (x0, x1); on acceptance write the
+  // site and its copies and add the changes of the integer correlation sums to acc.
+  __device__ __forceinline__ void decide(uint32_t ent, uint32_t x0, uint32_t x1, int o, const int (&F)[NF],
+                                         int (&acc)[NSLOT]) const {
     const int pidx = (int)(ent & 0xFFFFFFu);
     const uint32_t flags = ent >> 24;
     int o2;
@@ -208,8 +162,8 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
 #pragma unroll
     for (int b = 0; b < B::NFUNC; ++b) G[b] = 0.f;
 #pragma unroll
-    for (int k = 0; k < NF; ++k) G[B::feat_b(k)] = fmaf(A.w.w32[k], (float)F[k], G[B::feat_b(k)]);
-    float dE32 = -dmu32_sm[o * NS + o2];
+    for (int k = 0; k < NF; ++k) G[B::feat_b(k)] = fmaf(w->w32[k], (float)F[k], G[B::feat_b(k)]);
+    float dE32 = -dmu32[o * NS + o2];
 #pragma unroll
     for (int b = 0; b < B::NFUNC; ++b) dE32 = fmaf((float)dpsi[b], G[b], dE32);
 
@@ -233,11 +187,11 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
       for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
 #pragma unroll
       for (int k = 0; k < NF; ++k)
-        G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(A.w.w64[k], (double)F[k]));
+        G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(w->w64[k], (double)F[k]));
       double dE = 0.0;
 #pragma unroll
       for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
-      dE = __dsub_rn(dE, dmu64_sm[o * NS + o2]);
+      dE = __dsub_rn(dE, dmu64[o * NS + o2]);
       bool acc64;
       if (dE < 0.0) {
         acc64 = true;
@@ -246,7 +200,7 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
         acc64 = u < exp(__dmul_rn(-dE, beta));
       }
       acc[NC] += 1;
-      if (A.precision == 0) {
+      if (precision == 0) {
         accept = acc64;
       } else if (acc64 != acc32) {
         acc[NC + 1] += 1;
@@ -278,27 +232,148 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
 #pragma unroll
       for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += dpsi[B::feat_b(k)] * F[k];
     }
-  };
+  }
+};
 
-  // The first PRE sites of each thread in the next phase are prepared (list entry and
-  // random numbers, which do not depend on the lattice) while the phase barrier is
-  // pending; further sites of a phase load and draw inline.
-  constexpr int PRE = (NS == 2) ? 3 : 2;
-  uint32_t pre_ent[PRE], pre_x0[PRE], pre_x1[PRE];
-  auto prepare = [&](int cn, uint32_t pass_n) {
-    const int eb = cstart[cn] + threadIdx.x, ee = cstart[cn + 1];
+// Philox words of the first PRE sites of a thread in one colour phase, drawn ahead of
+// the phase (they depend on (site, pass, chain) only, not on the lattice).
+template <int PRE>
+struct PhasePrefetch {
+  uint32_t ent[PRE], x0[PRE], x1[PRE];
+
+  template <int NT>
+  __device__ __forceinline__ void prepare(const int* cstart, int c, const uint32_t* entries,
+                                          const uint32_t* site_l, uint32_t pass, uint32_t chain_id,
+                                          uint32_t key0, uint32_t key1) {
+    const int eb = cstart[c] + threadIdx.x, ee = cstart[c + 1];
 #pragma unroll
     for (int q = 0; q < PRE; ++q) {
       const int e = eb + q * NT;
       if (e < ee) {
-        pre_ent[q] = __ldg(g.entries + e);
-        const U32x4 x = philox4x32_10(U32x4{__ldg(g.site_l + e), pass_n, chain_id, SWEEP_TAG}, key0, key1);
-        pre_x0[q] = x.x;
-        pre_x1[q] = x.y;
+        ent[q] = __ldg(entries + e);
+        const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
+        x0[q] = x.x;
+        x1[q] = x.y;
       }
     }
+  }
+};
+
+// One colour phase of one CTA: the prefetched sites, then any further sites inline.
+template <class B, int NT, int PRE>
+__device__ __forceinline__ void sweep_phase(const SiteSweeper<B>& sw, const PhasePrefetch<PRE>& pf,
+                                            const int* cstart, int c, const uint32_t* entries,
+                                            const uint32_t* site_l, uint32_t pass, uint32_t chain_id,
+                                            uint32_t key0, uint32_t key1, int (&acc)[SiteSweeper<B>::NSLOT]) {
+  const int e0 = cstart[c] + threadIdx.x, e_end = cstart[c + 1];
+#pragma unroll
+  for (int q = 0; q < PRE; ++q)
+    if (e0 + q * NT < e_end) {
+      int o;
+      int F[B::NFEAT];
+      sw.gather(pf.ent[q], o, F);
+      sw.decide(pf.ent[q], pf.x0[q], pf.x1[q], o, F, acc);
+    }
+#pragma unroll 1
+  for (int e = e0 + PRE * NT; e < e_end; e += NT) {
+    const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
+    const uint32_t ent = __ldg(entries + e);
+    int o;
+    int F[B::NFEAT];
+    sw.gather(ent, o, F);
+    sw.decide(ent, x.x, x.y, o, F, acc);
+  }
+}
+
+template <int NS>
+__device__ __forceinline__ void load_dmu(const CeChainParams* cp, float* dmu32, double* dmu64) {
+  if (threadIdx.x < NS * NS) {
+    dmu32[threadIdx.x] = cp->dmu32[threadIdx.x];
+    dmu64[threadIdx.x] = cp->dmu64[threadIdx.x];
+  }
+}
+
+template <class B, int NT>
+__global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__ CeSweepArgs<B::NFEAT> A) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  constexpr int PRE = (NS == 2) ? 3 : 2;
+  extern __shared__ __align__(16) int8_t s[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+
+  const CeGeometry& g = A.g;
+  const int S = g.S;
+  const int chain = blockIdx.x / S;
+  int rank = 0;
+  cg::cluster_group cluster = cg::this_cluster();
+  if (S > 1) rank = (int)cluster.block_rank();
+  auto barrier = [&]() {
+    if (S > 1)
+      cluster.sync();
+    else
+      __syncthreads();
   };
-  prepare(0, (uint32_t)A.pass0);
+
+  const int PX = g.PX, PY = g.PY, PXY = PX * PY;
+  const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+  const int nkq = L2 / S, nkr = L2 % S;
+  const int nk = nkq + (rank < nkr ? 1 : 0);
+  const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+  const int rprev = (rank + S - 1) % S;
+  const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
+  const long long N = (long long)L0 * L1 * L2;
+  int8_t* gocc = A.occ + (size_t)chain * N;
+
+  // ---- load slab + borders
+  for (int idx = threadIdx.x; idx < PXY * (nk + 2 * B::HALO); idx += NT) {
+    const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
+    int i = ip - B::HALO, j = jp - B::HALO, k = k0 + kp - B::HALO;
+    i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+    j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+    k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+    s[idx] = B::code_of_occ(gocc[i + (long long)L0 * (j + (long long)L1 * k)]);
+  }
+  if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+
+  const CeChainParams* cpg = A.cp + chain;
+  load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+  const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+  const int* cstart = g.color_start + rank * (g.n_colors + 1);
+
+  // periodic copies: +-L0 in i, +-L1 rows in j; a plane kl < HALO is also the upper
+  // halo of the previous CTA (at kl + nk_prev + HALO), a plane kl >= nk - HALO the
+  // lower halo of the next CTA (at kl - nk + HALO)
+  SiteSweeper<B> sw;
+  sw.s = s;
+  sw.s_prev = s;
+  sw.s_next = s;
+  if (S > 1) {
+    sw.s_prev = cluster.map_shared_rank(s, (unsigned)rprev);
+    sw.s_next = cluster.map_shared_rank(s, (unsigned)((rank + 1) % S));
+  }
+  sw.PX = PX;
+  sw.PXY = PXY;
+  sw.dI = L0;
+  sw.dJ = L1 * PX;
+  sw.dKp = nk_prev * PXY;
+  sw.dKn = nk * PXY;
+  sw.dmu32 = dmu32_sm;
+  sw.dmu64 = dmu64_sm;
+  sw.w = &A.w;
+  sw.beta = cpg->beta;
+  sw.beta_log2e = cpg->beta_log2e;
+  sw.dtol = cpg->dtol;
+  sw.eps = cpg->eps;
+  sw.precision = A.precision;
+  const int lane = threadIdx.x & 31;
+  int acc[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+
+  PhasePrefetch<PRE> pf;
+  pf.template prepare<NT>(cstart, 0, g.entries, g.site_l, (uint32_t)A.pass0, chain_id, key0, key1);
   barrier();
 
 #pragma unroll 1
@@ -306,31 +381,17 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
     const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
 #pragma unroll 1
     for (int c = 0; c < g.n_colors; ++c) {
-      const int e0 = cstart[c] + threadIdx.x, e_end = cstart[c + 1];
-#pragma unroll
-      for (int q = 0; q < PRE; ++q)
-        if (e0 + q * NT < e_end) {
-          int o1;
-          int F1[NF];
-          gather(pre_ent[q], o1, F1);
-          decide(pre_ent[q], pre_x0[q], pre_x1[q], o1, F1);
-        }
-#pragma unroll 1
-      for (int e = e0 + PRE * NT; e < e_end; e += NT) {
-        const U32x4 x = philox4x32_10(U32x4{__ldg(g.site_l + e), pass_g, chain_id, SWEEP_TAG}, key0, key1);
-        const uint32_t ent = __ldg(g.entries + e);
-        int o1;
-        int F1[NF];
-        gather(ent, o1, F1);
-        decide(ent, x.x, x.y, o1, F1);
-      }
+      sweep_phase<B, NT, PRE>(sw, pf, cstart, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
       const bool last = (c + 1 == g.n_colors);
       if (S > 1) {
+        // arrive, draw the next phase's random numbers while others finish, then wait
         cluster_arrive_release();
-        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g);
+        pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, last ? pass_g + 1 : pass_g,
+                                chain_id, key0, key1);
         cluster_wait_acquire();
       } else {
-        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g);
+        pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, last ? pass_g + 1 : pass_g,
+                                chain_id, key0, key1);
         __syncthreads();
       }
       if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
@@ -368,6 +429,137 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
     gocc[i + (long long)L0 * (j + (long long)L1 * (k0 + kl))] = (int8_t)B::occ_of_code(s[pidx]);
   }
   barrier();
+}
+
+// ---- persistent pool kernel: many chains of any shape, one CTA per chain
+
+// geometry of one supercell shape (S = 1): padded dims and colour lists
+struct PoolGeometry {
+  int L0, L1, L2;
+  int n_colors;
+  const int* color_start;   // [n_colors + 1]
+  const uint32_t* entries;  // padded index | flags << 24
+  const uint32_t* site_l;
+};
+
+// one work item: a chain of some geometry
+struct PoolItem {
+  int geom;
+  int param;             // index into the chain-parameter array
+  long long occ_offset;  // into the occupation arena
+  long long out_offset;  // into the output array, [pass][NSLOT] for this item
+  long long pass0;       // the chain's pass count before this launch (Philox counter)
+};
+
+template <int NFEAT>
+struct CePoolArgs {
+  const PoolGeometry* geoms;
+  const PoolItem* items;
+  int n_items;
+  int* next_item;  // work counter (zeroed by the host)
+  CeWeights<NFEAT> w;
+  const CeChainParams* cp;
+  int8_t* occ;  // arena
+  int n_passes;
+  int precision;
+  long long* out;
+};
+
+template <class B, int NT>
+__global__ void __launch_bounds__(NT, 1) ce_pool_kernel(const __grid_constant__ CePoolArgs<B::NFEAT> A) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  constexpr int PRE = (NS == 2) ? 3 : 2;
+  extern __shared__ __align__(16) int8_t s[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+  __shared__ int item_sm;
+  const int lane = threadIdx.x & 31;
+
+#pragma unroll 1
+  while (true) {
+    if (threadIdx.x == 0) item_sm = atomicAdd(A.next_item, 1);
+    __syncthreads();
+    const int it = item_sm;
+    if (it >= A.n_items) break;
+    const PoolItem item = A.items[it];
+    const PoolGeometry g = A.geoms[item.geom];
+    const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+    const int PX = L0 + 2 * B::HALO, PY = L1 + 2 * B::HALO, PXY = PX * PY;
+    int8_t* gocc = A.occ + item.occ_offset;
+    for (int idx = threadIdx.x; idx < PXY * (L2 + 2 * B::HALO); idx += NT) {
+      const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
+      int i = ip - B::HALO, j = jp - B::HALO, k = kp - B::HALO;
+      i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+      s[idx] = B::code_of_occ(gocc[i + (long long)L0 * (j + (long long)L1 * k)]);
+    }
+    if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+    const CeChainParams* cpg = A.cp + item.param;
+    load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+    const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+    SiteSweeper<B> sw;
+    sw.s = s;
+    sw.s_prev = s;
+    sw.s_next = s;
+    sw.PX = PX;
+    sw.PXY = PXY;
+    sw.dI = L0;
+    sw.dJ = L1 * PX;
+    sw.dKp = L2 * PXY;
+    sw.dKn = L2 * PXY;
+    sw.dmu32 = dmu32_sm;
+    sw.dmu64 = dmu64_sm;
+    sw.w = &A.w;
+    sw.beta = cpg->beta;
+    sw.beta_log2e = cpg->beta_log2e;
+    sw.dtol = cpg->dtol;
+    sw.eps = cpg->eps;
+    sw.precision = A.precision;
+    int acc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+    long long* out = A.out + item.out_offset;
+    PhasePrefetch<PRE> pf;
+    pf.template prepare<NT>(g.color_start, 0, g.entries, g.site_l, (uint32_t)item.pass0, chain_id, key0, key1);
+    __syncthreads();
+#pragma unroll 1
+    for (int pass = 0; pass < A.n_passes; ++pass) {
+      const uint32_t pass_g = (uint32_t)(item.pass0 + pass);
+#pragma unroll 1
+      for (int c = 0; c < g.n_colors; ++c) {
+        sweep_phase<B, NT, PRE>(sw, pf, g.color_start, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
+        const bool last = (c + 1 == g.n_colors);
+        pf.template prepare<NT>(g.color_start, last ? 0 : c + 1, g.entries, g.site_l,
+                                last ? pass_g + 1 : pass_g, chain_id, key0, key1);
+        __syncthreads();
+        if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+          int* buf = acc_sm[(pass - 1) & 1];
+          out[(size_t)(pass - 1) * NSLOT + threadIdx.x] = buf[threadIdx.x];
+          buf[threadIdx.x] = 0;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q) {
+        const int v = warp_sum(acc[q]);
+        if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+        acc[q] = 0;
+      }
+    }
+    __syncthreads();
+    if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+      const int pl = A.n_passes - 1;
+      out[(size_t)pl * NSLOT + threadIdx.x] = acc_sm[pl & 1][threadIdx.x];
+    }
+    for (int idx = threadIdx.x; idx < L0 * L1 * L2; idx += NT) {
+      const int i = idx % L0, j = (idx / L0) % L1, k = idx / (L0 * L1);
+      const int pidx = (i + B::HALO) + PX * ((j + B::HALO) + PY * (k + B::HALO));
+      gocc[i + (long long)L0 * (j + (long long)L1 * k)] = (int8_t)B::occ_of_code(s[pidx]);
+    }
+    __syncthreads();
+  }
 }
 
 // ---- global-memory evaluation (per-proposal dE and full correlation sums)

@@ -38,6 +38,7 @@ extern "C" {
 #define MG_ERR_INVALID 1 /* invalid argument (reference: std::runtime_error) */
 #define MG_ERR_CUDA 2    /* CUDA runtime error */
 #define MG_ERR_DEVICE 4  /* a kernel reported an error status */
+#define MG_ERR_FULL 5    /* admission refused: no free slot or arena space */
 
 /* ---- library ---- */
 const char* mg_last_error(void); /* thread-local message of the last failure */
@@ -128,6 +129,31 @@ int mg_ce_batch_destroy(mg_ce_batch* b);
  * (cudaOccupancyMaxActiveClusters on the sweep kernel); used by the autotuner */
 int mg_ce_max_active_chains(const mg_ce_model* m, int L0, int L1, int L2, int ctas_per_chain,
                             int* n_chains);
+
+/* ---- chain pool: many chains of any supercell shape, persistent kernel ----
+ * The batched form of the reference's per-chain run (one `run` call per thermodynamic
+ * state, basic_semigrand_canonical.hh:416-470): an HBM arena of arena_bytes holds the
+ * occupations; chains are admitted while their occupation fits (MG_ERR_FULL otherwise)
+ * and removed when done.  mg_ce_pool_run sweeps the given slots by n_passes each in one
+ * launch of a persistent kernel (one CTA per chain, work queue largest first); every
+ * chain keeps its own pass counter, so results do not depend on how runs are batched.
+ * out (host, may be NULL): [n][n_passes][n_classes+2] in the order of `slots`, same slot
+ * meaning as mg_ce_batch_run. */
+typedef struct mg_ce_pool mg_ce_pool;
+int mg_ce_pool_create(const mg_ce_model* m, long long arena_bytes, int max_chains, int precision,
+                      mg_ce_pool** out);
+int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, const double* mu,
+                   uint64_t seed, uint32_t chain_id, const int8_t* occ, int* slot);
+int mg_ce_pool_remove(mg_ce_pool* p, int slot);
+int mg_ce_pool_info(const mg_ce_pool* p, long long* arena_free_bytes, long long* arena_bytes,
+                    int* n_used, int* max_chains);
+int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, long long* out);
+int mg_ce_pool_last_kernel_ms(const mg_ce_pool* p, float* ms);
+int mg_ce_pool_get_occ(mg_ce_pool* p, int slot, int8_t* occ);
+/* colouring of the slot's supercell [N]; returns the number of colours (>0) or an error */
+int mg_ce_pool_colors(const mg_ce_pool* p, int slot, int32_t* color);
+int mg_ce_pool_corr(mg_ce_pool* p, int slot, long long* out);
+int mg_ce_pool_destroy(mg_ce_pool* p);
 
 /* ---- allocation-free coloured sweep (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc (an embedding framework owns all device

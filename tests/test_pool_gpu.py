@@ -1,0 +1,77 @@
+"""Chain pool (persistent kernel, one CTA per chain, mixed supercell shapes)."""
+import numpy as np
+import pytest
+
+from casmcode_monte_gb300 import clex
+from tests.oracle_lib import OracleCE
+
+pytestmark = pytest.mark.gpu
+
+
+def _chains(model, shapes, seed=1):
+    rng = np.random.default_rng(seed)
+    out = []
+    for c, L in enumerate(shapes):
+        n = L[0] * L[1] * L[2]
+        occ = rng.integers(0, model.n_species, size=n).astype(np.int8)
+        T = float(rng.uniform(300.0, 2000.0))
+        mu = rng.uniform(-0.3, 0.3, size=model.n_species - 1)
+        out.append((L, occ, T, mu, int(rng.integers(1, 2**63)), 1000 + c))
+    return out
+
+
+@pytest.mark.parametrize("kind", ["fcc_binary", "fcc_ternary"])
+def test_pool_matches_oracle_mixed_shapes(gpu_lib, kind):
+    model = clex.ClexModel(kind, clex.make_eci(kind, 5))
+    shapes = [(8, 8, 8), (12, 12, 12), (16, 8, 12), (6, 9, 7), (8, 8, 8)]
+    chains = _chains(model, shapes)
+    pool = clex.ChainPool(model, arena_bytes=1 << 20, max_chains=8)
+    slots = [pool.add(L, occ, T, mu, seed, cid) for (L, occ, T, mu, seed, cid) in chains]
+    corr0 = [pool.corr(s) for s in slots]
+    n_passes = 5
+    out = pool.run(slots, n_passes)
+    for i, ((L, occ, T, mu, seed, cid), s) in enumerate(zip(chains, slots)):
+        col, nc = pool.colors(s)
+        orc = OracleCE(L, model.n_species, model.eci)
+        occ_ref, corr_ref, nacc_ref = orc.colored_sweep(occ, T, mu, seed, cid, col, nc, 0, n_passes,
+                                                        model.n_classes)
+        assert np.array_equal(pool.occupation(s), occ_ref.astype(np.int8)), (i, L)
+        d = out[i, :, : model.n_classes].copy()
+        d[:, 0] = 0
+        ic = corr0[i][None, :] + np.cumsum(d, axis=0)
+        assert np.array_equal(ic, corr_ref), (i, L)
+        assert np.array_equal(out[i, :, 0], nacc_ref)
+        assert np.array_equal(pool.corr(s), corr_ref[-1])
+
+
+def test_pool_results_independent_of_batching(gpu_lib):
+    model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 2))
+    shapes = [(8, 8, 8), (12, 8, 8), (16, 16, 16), (10, 10, 10)]
+    chains = _chains(model, shapes, seed=3)
+    a = clex.ChainPool(model, 1 << 20, 8)
+    b = clex.ChainPool(model, 1 << 20, 8)
+    sa = [a.add(*c[:1], c[1], c[2], c[3], c[4], c[5]) for c in chains]
+    sb = [b.add(*c[:1], c[1], c[2], c[3], c[4], c[5]) for c in chains]
+    a.run(sa, 6)  # all together, 6 passes
+    b.run(sb[:2], 2)  # uneven batching: subsets and splits
+    b.run(sb, 3)
+    b.run(sb[2:], 3)
+    b.run(sb[:2], 1)
+    for x, y in zip(sa, sb):
+        assert np.array_equal(a.occupation(x), b.occupation(y))
+
+
+def test_pool_admission_by_footprint(gpu_lib):
+    model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 2))
+    pool = clex.ChainPool(model, arena_bytes=3 * 4096, max_chains=8)
+    occ = np.zeros(16 * 16 * 16, dtype=np.int8)
+    s0 = pool.add((16, 16, 16), occ, 1000.0, [0.0], 1, 0)
+    s1 = pool.add((16, 16, 16), occ, 1000.0, [0.0], 2, 1)
+    s2 = pool.add((16, 16, 16), occ, 1000.0, [0.0], 3, 2)
+    with pytest.raises(clex.PoolFull):
+        pool.add((16, 16, 16), occ, 1000.0, [0.0], 4, 3)
+    pool.remove(s1)
+    s3 = pool.add((16, 16, 16), occ, 1000.0, [0.0], 4, 3)
+    assert s3 == s1
+    assert pool.info()["arena_free_bytes"] == 0
+    pool.run([s0, s2, s3], 2)
