@@ -68,12 +68,16 @@ SIGNATURES = {
     "mg_ce_pool_add": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_double, c_double_p, C.c_uint64, C.c_uint32,
                                  c_int8_p, c_int_p]),
     "mg_ce_pool_remove": (C.c_int, [vp, C.c_int]),
+    "mg_ce_pool_prepare": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
     "mg_ce_pool_info": (C.c_int, [vp, c_ll_p, c_ll_p, c_int_p, c_int_p]),
     "mg_ce_pool_run": (C.c_int, [vp, c_int32_p, C.c_int, C.c_int, c_ll_p]),
     "mg_ce_pool_last_kernel_ms": (C.c_int, [vp, c_float_p]),
     "mg_ce_pool_get_occ": (C.c_int, [vp, C.c_int, c_int8_p]),
     "mg_ce_pool_colors": (C.c_int, [vp, C.c_int, c_int32_p]),
     "mg_ce_pool_corr": (C.c_int, [vp, C.c_int, c_ll_p]),
+    "mg_ce_pool_enable_series": (C.c_int, [vp, C.c_int]),
+    "mg_ce_pool_series": (C.c_int, [vp, C.c_int, c_double_p, C.c_int, c_int_p]),
+    "mg_ce_pool_check": (C.c_int, [vp, c_int32_p, C.c_int, C.c_double, C.c_double, c_double_p]),
     "mg_ce_pool_destroy": (C.c_int, [vp]),
     "mg_ce_sweep_noalloc": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p, c_double_p, c_uint64_p,
                                       vp, C.c_longlong, C.c_int, vp, C.c_int, vp]),

@@ -41,12 +41,16 @@ def _deps_mtime() -> float:
     return m
 
 
+# per-file flags: the pool's device statistics must round exactly like the host code
+FILE_FLAGS = {"ce_pool.cu": ["-fmad=false"]}
+
+
 def _compile(src: str, verbose: bool, extra: list[str]) -> str:
     obj = os.path.join(OBJDIR, src.replace(".cu", ".o"))
     srcp = os.path.join(CSRC, src)
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(srcp), _deps_mtime()) and not extra:
         return obj
-    cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", srcp, "-o", obj]
+    cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src, []), *extra, "-c", srcp, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -238,6 +238,11 @@ class ChainPool:
         self.shapes[slot.value] = (L0, L1, L2)
         return slot.value
 
+    def prepare(self, shape) -> None:
+        """Build and cache the geometry (colouring, site lists) of a supercell shape."""
+        L0, L1, L2 = (int(x) for x in shape)
+        _lib.check(_lib.lib().mg_ce_pool_prepare(self._h, L0, L1, L2))
+
     def remove(self, slot: int) -> None:
         _lib.check(_lib.lib().mg_ce_pool_remove(self._h, int(slot)))
         self.shapes.pop(slot, None)
@@ -277,6 +282,29 @@ class ChainPool:
     def corr(self, slot: int) -> np.ndarray:
         out = np.zeros(self.model.n_classes, dtype=np.int64)
         _lib.check(_lib.lib().mg_ce_pool_corr(self._h, int(slot), _lib.ptr(out, C.c_longlong)))
+        return out
+
+    def enable_series(self, max_samples: int) -> None:
+        """Keep a device-resident potential-energy-per-site sample per pass (before adds)."""
+        _lib.check(_lib.lib().mg_ce_pool_enable_series(self._h, int(max_samples)))
+        self.max_samples = int(max_samples)
+
+    def series(self, slot: int) -> np.ndarray:
+        buf = np.zeros(self.max_samples, dtype=np.float64)
+        n = C.c_int()
+        _lib.check(_lib.lib().mg_ce_pool_series(self._h, int(slot), _lib.ptr(buf, C.c_double), buf.size,
+                                                C.byref(n)))
+        return buf[: min(n.value, buf.size)].copy()
+
+    def check(self, slots, abs_precision: float, confidence: float = 0.95) -> np.ndarray:
+        """Device equilibration + convergence check of each slot's series.
+
+        Returns [n, 6]: equilibrated, N_equilibration, N_statistics, mean, precision, converged.
+        """
+        sl = np.ascontiguousarray(np.asarray(slots, dtype=np.int32).reshape(-1))
+        out = np.zeros((sl.size, 6), dtype=np.float64)
+        _lib.check(_lib.lib().mg_ce_pool_check(self._h, _lib.ptr(sl, C.c_int32), sl.size, float(abs_precision),
+                                               float(confidence), _lib.ptr(out, C.c_double)))
         return out
 
 

@@ -112,22 +112,45 @@ inline int color_supercell(int L0, int L1, int L2, int kind, int32_t* col) {
                     (int32_t)((1LL * a * i + 1LL * b * j + 1LL * c * k) % m);
           return m;
         }
+  // greedy: neighbour coordinates from per-axis wrap tables (offsets lie in [-HALO, HALO])
   const long long N = (long long)L0 * L1 * L2;
   for (long long l = 0; l < N; ++l) col[l] = -1;
+  const int W = 2 * CE_HALO + 1;
+  auto wrap_table = [&](int L, int* t) {
+    for (int x = 0; x < L; ++x)
+      for (int d = -CE_HALO; d <= CE_HALO; ++d) t[x * W + d + CE_HALO] = ((x + d) % L + L) % L;
+  };
+  // at most 3 * 128 entries per axis for the sizes accepted here; larger sizes fall back
+  // to direct arithmetic
+  int ti[1024 * 5], tj[1024 * 5], tk[1024 * 5];
+  const bool tables = L0 <= 1024 && L1 <= 1024 && L2 <= 1024;
+  if (tables) {
+    wrap_table(L0, ti);
+    wrap_table(L1, tj);
+    wrap_table(L2, tk);
+  }
   int n_colors = 0;
   for (int k = 0; k < L2; ++k)
     for (int j = 0; j < L1; ++j)
       for (int i = 0; i < L0; ++i) {
-        bool used[CE_MAX_COLORS] = {};
+        unsigned long long used = 0ull;  // CE_MAX_COLORS == 64
         for (int t = 0; t < noff; ++t) {
-          const int a = ((i + off[3 * t]) % L0 + L0) % L0, b = ((j + off[3 * t + 1]) % L1 + L1) % L1,
-                    c = ((k + off[3 * t + 2]) % L2 + L2) % L2;
+          int a, b, c;
+          if (tables) {
+            a = ti[i * W + off[3 * t] + CE_HALO];
+            b = tj[j * W + off[3 * t + 1] + CE_HALO];
+            c = tk[k * W + off[3 * t + 2] + CE_HALO];
+          } else {
+            a = ((i + off[3 * t]) % L0 + L0) % L0;
+            b = ((j + off[3 * t + 1]) % L1 + L1) % L1;
+            c = ((k + off[3 * t + 2]) % L2 + L2) % L2;
+          }
           const int32_t cc = col[a + (long long)L0 * (b + (long long)L1 * c)];
-          if (cc >= 0) used[cc] = true;
+          if (cc >= 0) used |= 1ull << cc;
         }
+        if (used == ~0ull) return -1;
         int cc = 0;
-        while (cc < CE_MAX_COLORS && used[cc]) ++cc;
-        if (cc == CE_MAX_COLORS) return -1;
+        while (used >> cc & 1ull) ++cc;
         col[i + (long long)L0 * (j + (long long)L1 * k)] = cc;
         n_colors = std::max(n_colors, cc + 1);
       }
@@ -140,7 +163,8 @@ inline size_t slab_smem(int L0, int L1, int L2, int S) {
   return (size_t)(L0 + 2 * CE_HALO) * (L1 + 2 * CE_HALO) * ((L2 + S - 1) / S + 2 * CE_HALO);
 }
 
-// Per-slab, per-colour site lists.  Within one (slab, colour) list the sites are grouped
+// Per-slab, per-colour site lists (two passes over the slab).  Within one (slab, colour)
+// list the sites are grouped
 // by (padded index mod 4) and, inside a group, ordered round-robin over the 32 word banks
 // ((padded index / 4) mod 32).  Lanes of a warp then share the byte offset within their
 // 4-byte word, so every constant neighbour offset keeps their words in distinct banks.
@@ -149,50 +173,61 @@ inline size_t slab_smem(int L0, int L1, int L2, int S) {
 inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, int n_colors,
                              int* cstart, uint32_t* entries, uint32_t* site) {
   const int PX = L0 + 2 * CE_HALO, PY = L1 + 2 * CE_HALO;
+  // per (colour, residue group, bank): count, then round-robin placement (stack arrays:
+  // n_colors <= CE_MAX_COLORS, at most 2^31 sites per bucket)
+  int count[CE_MAX_COLORS * 128], seen[CE_MAX_COLORS * 128];
+  long long cbase[CE_MAX_COLORS + 1], gbase[CE_MAX_COLORS * 4];
   long long pos = 0;
   for (int r = 0; r < S; ++r) {
     const int nk = slab_planes(L2, S, r), k0 = slab_start(L2, S, r);
-    for (int c = 0; c < n_colors; ++c) {
-      cstart[r * (n_colors + 1) + c] = (int)pos;
-      long long count[4][32] = {};
-      for (int kl = 0; kl < nk; ++kl)
-        for (int j = 0; j < L1; ++j)
-          for (int i = 0; i < L0; ++i)
-            if (col[i + (long long)L0 * (j + (long long)L1 * (k0 + kl))] == c) {
-              const uint32_t pidx = (uint32_t)((i + CE_HALO) + PX * ((j + CE_HALO) + PY * (kl + CE_HALO)));
-              count[pidx & 3][(pidx >> 2) & 31]++;
-            }
-      long long base[4] = {};
-      for (int g = 1; g < 4; ++g) {
-        base[g] = base[g - 1];
-        for (int q = 0; q < 32; ++q) base[g] += count[g - 1][q];
+    std::fill(count, count + n_colors * 128, 0);
+    std::fill(seen, seen + n_colors * 128, 0);
+    for (int kl = 0; kl < nk; ++kl)
+      for (int j = 0; j < L1; ++j) {
+        const long long row = (long long)L0 * (j + (long long)L1 * (k0 + kl));
+        const uint32_t prow = (uint32_t)(CE_HALO + PX * ((j + CE_HALO) + PY * (kl + CE_HALO)));
+        for (int i = 0; i < L0; ++i) {
+          const uint32_t pidx = prow + i;
+          count[(size_t)col[row + i] * 128 + (pidx & 3) * 32 + ((pidx >> 2) & 31)]++;
+        }
       }
-      long long seen[4][32] = {};
-      for (int kl = 0; kl < nk; ++kl)
-        for (int j = 0; j < L1; ++j)
-          for (int i = 0; i < L0; ++i) {
-            const long long l = i + (long long)L0 * (j + (long long)L1 * (k0 + kl));
-            if (col[l] != c) continue;
-            const uint32_t pidx = (uint32_t)((i + CE_HALO) + PX * ((j + CE_HALO) + PY * (kl + CE_HALO)));
-            const int g = pidx & 3, q = (pidx >> 2) & 31;
-            const long long t = seen[g][q]++;
-            // round-robin position of the t-th site of bank q within group g
-            long long p = base[g];
-            for (int q2 = 0; q2 < 32; ++q2) p += std::min(count[g][q2], t) + ((q2 < q && count[g][q2] > t) ? 1 : 0);
-            uint32_t flags = 0;
-            if (i < CE_HALO) flags |= 1;
-            else if (i >= L0 - CE_HALO) flags |= 2;
-            if (j < CE_HALO) flags |= 4;
-            else if (j >= L1 - CE_HALO) flags |= 8;
-            if (kl < CE_HALO) flags |= 16;
-            if (kl >= nk - CE_HALO) flags |= 32;
-            entries[pos + p] = pidx | (flags << 24);
-            site[pos + p] = (uint32_t)l;
-          }
-      for (int g = 0; g < 4; ++g)
-        for (int q = 0; q < 32; ++q) pos += count[g][q];
+    cbase[0] = pos;
+    for (int c = 0; c < n_colors; ++c) {
+      long long b = cbase[c];
+      for (int g = 0; g < 4; ++g) {
+        gbase[(size_t)c * 4 + g] = b;
+        for (int q = 0; q < 32; ++q) b += count[(size_t)c * 128 + g * 32 + q];
+      }
+      cbase[c + 1] = b;
+      cstart[r * (n_colors + 1) + c] = (int)cbase[c];
     }
-    cstart[r * (n_colors + 1) + n_colors] = (int)pos;
+    cstart[r * (n_colors + 1) + n_colors] = (int)cbase[n_colors];
+    for (int kl = 0; kl < nk; ++kl)
+      for (int j = 0; j < L1; ++j) {
+        const long long row = (long long)L0 * (j + (long long)L1 * (k0 + kl));
+        const uint32_t prow = (uint32_t)(CE_HALO + PX * ((j + CE_HALO) + PY * (kl + CE_HALO)));
+        for (int i = 0; i < L0; ++i) {
+          const long long l = row + i;
+          const int c = col[l];
+          const uint32_t pidx = prow + i;
+          const int g = pidx & 3, q = (pidx >> 2) & 31;
+          const int* cnt = &count[(size_t)c * 128 + g * 32];
+          const int t = seen[(size_t)c * 128 + g * 32 + q]++;
+          // round-robin position of the t-th site of bank q within (colour, group)
+          long long p = gbase[(size_t)c * 4 + g];
+          for (int q2 = 0; q2 < 32; ++q2) p += std::min(cnt[q2], t) + ((q2 < q && cnt[q2] > t) ? 1 : 0);
+          uint32_t flags = 0;
+          if (i < CE_HALO) flags |= 1;
+          else if (i >= L0 - CE_HALO) flags |= 2;
+          if (j < CE_HALO) flags |= 4;
+          else if (j >= L1 - CE_HALO) flags |= 8;
+          if (kl < CE_HALO) flags |= 16;
+          if (kl >= nk - CE_HALO) flags |= 32;
+          entries[p] = pidx | (flags << 24);
+          site[p] = (uint32_t)l;
+        }
+      }
+    pos = cbase[n_colors];
   }
 }
 
@@ -225,6 +260,7 @@ inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* 
     const double dtol = (m->n_features + 8) * std::ldexp(1.0, -23) * (wsum + dmu_max) + 1e-30;
     p.dtol = (float)(dtol * 1.0001);
     p.eps = (float)(1.25 * p.beta * dtol + 8e-6);
+    for (int i = 0; i < ns - 1; ++i) p.mu[i] = mu[(size_t)c * (ns - 1) + i];
     p.key0 = (uint32_t)seeds[c];
     p.key1 = (uint32_t)(seeds[c] >> 32);
     p.chain_id = chain_ids ? chain_ids[c] : (uint32_t)c;

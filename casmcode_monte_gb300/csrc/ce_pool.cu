@@ -14,6 +14,7 @@
 #include "../../include/montegpu.h"
 #include "ce_host.cuh"
 #include "mg_common.cuh"
+#include "stats.cuh"
 
 namespace {
 
@@ -21,9 +22,12 @@ using mg::set_error;
 using namespace mg::host;
 
 constexpr int kMaxGeoms = 1024;
+// CTA classes: chains are swept by 1, 2, 4, 8 or 16 CTAs (the smallest whose slab fits)
+constexpr int kClasses = 5;
+constexpr int kClassS[kClasses] = {1, 2, 4, 8, 16};
 
 struct PoolGeom {
-  int L0 = 0, L1 = 0, L2 = 0, n_colors = 0;
+  int L0 = 0, L1 = 0, L2 = 0, S = 1, n_colors = 0;
   int* dcstart = nullptr;
   uint32_t* dentries = nullptr;
   uint32_t* dsite = nullptr;
@@ -32,7 +36,7 @@ struct PoolGeom {
 
 struct PoolSlot {
   bool used = false;
-  int L0 = 0, L1 = 0, L2 = 0;
+  int L0 = 0, L1 = 0, L2 = 0, cls = 0;
   long long N = 0, offset = 0, pass = 0;
   int geom = -1;
 };
@@ -47,17 +51,25 @@ struct mg_ce_pool {
   std::map<long long, long long> free_blocks;  // offset -> size
   std::vector<PoolSlot> slots;
   std::vector<PoolGeom> geoms;
-  std::map<std::tuple<int, int, int>, int> geom_index;
+  std::map<std::tuple<int, int, int, int>, int> geom_index;
   mg::CeChainParams* dcp = nullptr;
   mg::PoolGeometry* dgeoms = nullptr;
   mg::PoolItem* ditems = nullptr;
-  int* dcounter = nullptr;
+  int* dcounter = nullptr;  // one work counter per CTA class
   long long* dcorr = nullptr;
   long long* dout = nullptr;
   size_t out_cap = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t cls_stream[kClasses] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t cls_done[kClasses] = {};
   float last_ms = 0.f;
+  // device-resident sample series (potential energy per site after every pass)
+  int max_samples = 0;
+  long long* dstate = nullptr;  // [slot][n_classes] integer correlation sums
+  double* dseries = nullptr;    // [slot][max_samples]
+  int* dnsamp = nullptr;        // [slot]
+  double* dcheck = nullptr;     // check outputs
 };
 
 namespace {
@@ -76,6 +88,14 @@ void free_pool(mg_ce_pool* p) {
   cudaFree(p->dcounter);
   cudaFree(p->dcorr);
   cudaFree(p->dout);
+  cudaFree(p->dstate);
+  cudaFree(p->dseries);
+  cudaFree(p->dnsamp);
+  cudaFree(p->dcheck);
+  for (int c = 0; c < kClasses; ++c) {
+    if (p->cls_stream[c]) cudaStreamDestroy(p->cls_stream[c]);
+    if (p->cls_done[c]) cudaEventDestroy(p->cls_done[c]);
+  }
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -114,8 +134,8 @@ void arena_free(mg_ce_pool* p, long long off, long long n) {
   }
 }
 
-int geometry(mg_ce_pool* p, int L0, int L1, int L2, int* out) {
-  auto key = std::make_tuple(L0, L1, L2);
+int geometry(mg_ce_pool* p, int L0, int L1, int L2, int S, int* out) {
+  auto key = std::make_tuple(L0, L1, L2, S);
   auto it = p->geom_index.find(key);
   if (it != p->geom_index.end()) {
     *out = it->second;
@@ -130,15 +150,16 @@ int geometry(mg_ce_pool* p, int L0, int L1, int L2, int* out) {
   g.L0 = L0;
   g.L1 = L1;
   g.L2 = L2;
+  g.S = S;
   g.color.assign(N, -1);
   g.n_colors = color_supercell(L0, L1, L2, p->model->kind, g.color.data());
   if (g.n_colors < 1) {
     set_error("Error in mg_ce_pool_add: colouring needs more than 64 colours");
     return MG_ERR_INVALID;
   }
-  std::vector<int> cstart(g.n_colors + 1);
+  std::vector<int> cstart((size_t)S * (g.n_colors + 1));
   std::vector<uint32_t> entries(N), site(N);
-  build_site_lists(L0, L1, L2, 1, g.color.data(), g.n_colors, cstart.data(), entries.data(), site.data());
+  build_site_lists(L0, L1, L2, S, g.color.data(), g.n_colors, cstart.data(), entries.data(), site.data());
   MG_CUDA_TRY(cudaMalloc(&g.dcstart, sizeof(int) * cstart.size()));
   MG_CUDA_TRY(cudaMalloc(&g.dentries, sizeof(uint32_t) * N));
   MG_CUDA_TRY(cudaMalloc(&g.dsite, sizeof(uint32_t) * N));
@@ -156,12 +177,12 @@ int geometry(mg_ce_pool* p, int L0, int L1, int L2, int* out) {
 }
 
 template <class B, int NT>
-int launch_pool(mg_ce_pool* p, const std::vector<mg::PoolItem>& items, int n_passes, size_t smem) {
+int launch_pool(mg_ce_pool* p, int cls, int item0, int n_items, int n_passes, size_t smem) {
   mg::CePoolArgs<B::NFEAT> A;
   A.geoms = p->dgeoms;
-  A.items = p->ditems;
-  A.n_items = (int)items.size();
-  A.next_item = p->dcounter;
+  A.items = p->ditems + item0;
+  A.n_items = n_items;
+  A.next_item = p->dcounter + cls;
   for (int k = 0; k < B::NFEAT; ++k) {
     A.w.w32[k] = p->model->w32[k];
     A.w.w64[k] = p->model->w64[k];
@@ -171,20 +192,115 @@ int launch_pool(mg_ce_pool* p, const std::vector<mg::PoolItem>& items, int n_pas
   A.n_passes = n_passes;
   A.precision = p->precision;
   A.out = p->dout;
-  auto kern = mg::ce_pool_kernel<B, NT>;
+  const int S = kClassS[cls];
+  cudaStream_t st = p->cls_stream[cls];
+  if (S == 1) {
+    auto kern = mg::ce_pool_kernel<B, NT>;
+    MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0, dev = 0, sms = 0;
+    MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    MG_CUDA_TRY(cudaGetDevice(&dev));
+    MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (per_sm < 1) {
+      set_error("Error in mg_ce_pool_run: supercell does not fit in shared memory");
+      return MG_ERR_INVALID;
+    }
+    const int grid = std::max(1, std::min(n_items, per_sm * sms));
+    kern<<<grid, NT, smem, st>>>(A);
+    MG_CUDA_TRY(cudaGetLastError());
+    return MG_OK;
+  }
+  auto kern = mg::ce_pool_cluster_kernel<B, NT>;
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0, dev = 0, sms = 0;
-  MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
-  MG_CUDA_TRY(cudaGetDevice(&dev));
-  MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  if (per_sm < 1) {
-    set_error("Error in mg_ce_pool_run: the largest supercell does not fit in shared memory");
+  if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cfg.blockDim = dim3(NT, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)S;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3((unsigned)S, 1, 1);
+  int n_cl = 0;
+  MG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n_cl, (void*)kern, &cfg));
+  if (n_cl < 1) {
+    set_error("Error in mg_ce_pool_run: no cluster of this size can be scheduled");
     return MG_ERR_INVALID;
   }
-  const int grid = std::max(1, std::min((int)items.size(), per_sm * sms));
-  kern<<<grid, NT, smem, p->stream>>>(A);
+  cfg.gridDim = dim3((unsigned)(S * std::max(1, std::min(n_items, n_cl))), 1, 1);
+  MG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
   MG_CUDA_TRY(cudaGetLastError());
   return MG_OK;
+}
+
+// Append one potential-energy-per-site sample per pass to each item's series: the
+// item's integer correlation sums advance by the pass's changes; E_f = sum_f w_f C_f,
+// E_pot = E_f - mu . N x, divided by N (same operation order as the host code).
+template <int NC, int NSPEC>
+__global__ void pool_series_kernel(const mg::PoolItem* items, int n_items, const mg::PoolGeometry* geoms,
+                                   const mg::CeChainParams* cp, const long long* out, int n_passes,
+                                   long long* state, double* series, int* nsamp, int max_samples,
+                                   mg::CeWeightsClass<NC> wc) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const mg::PoolItem it = items[t];
+  const mg::PoolGeometry g = geoms[it.geom];
+  const long long N = (long long)g.L0 * g.L1 * g.L2;
+  long long* C = state + (size_t)it.param * NC;
+  double* ser = series + (size_t)it.param * max_samples;
+  int ns = nsamp[it.param];
+  const long long* o = out + it.out_offset;
+  for (int p = 0; p < n_passes; ++p) {
+    for (int f = 1; f < NC; ++f) C[f] += o[(size_t)p * (NC + 2) + f];
+    double e = 0.0;
+    for (int f = 0; f < NC; ++f) e = __dadd_rn(e, __dmul_rn(wc.w[f], (double)C[f]));
+    double nx[2] = {0.0, 0.0};
+    if (NSPEC == 2) {
+      nx[0] = (double)C[1];
+    } else {
+      const long long nB = (N - C[2]) / 3;
+      nx[0] = (double)nB;
+      nx[1] = (double)((N - nB + C[1]) / 2);
+    }
+    for (int i = 0; i < NSPEC - 1; ++i) e = __dsub_rn(e, __dmul_rn(cp[it.param].mu[i], nx[i]));
+    if (ns < max_samples) ser[ns] = __ddiv_rn(e, (double)N);
+    ++ns;
+  }
+  nsamp[it.param] = ns;
+}
+
+// The reference's equilibration + convergence rule on one component per slot
+// (EquilibrationCheck.cc:50-117, ConvergenceCheck.hh:74-184, BasicStatistics.cc:114-131):
+// out[slot] = {equilibrated, N_equilibration, N_statistics, mean, precision, converged}.
+__global__ void pool_check_kernel(const int* slots, int n, const double* series, const int* nsamp,
+                                  int max_samples, double abs_precision, double confidence, double* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int slot = slots[t];
+  const int N = min(nsamp[slot], max_samples);
+  double* r = out + (size_t)t * 6;
+  r[0] = 0.0;
+  r[1] = 0.0;
+  r[2] = 0.0;
+  r[3] = 0.0;
+  r[4] = DBL_MAX;
+  r[5] = 0.0;
+  if (N < 1) return;
+  const double* x = series + (size_t)slot * max_samples;
+  const mg::stats::Equilibration eq = mg::stats::equilibration_check(x, N, abs_precision);
+  r[0] = eq.equilibrated ? 1.0 : 0.0;
+  r[1] = (double)eq.n_equilibration;
+  if (!eq.equilibrated || eq.n_equilibration >= N) return;
+  const long n_stat = N - eq.n_equilibration;
+  const mg::stats::MeanPrecision st = mg::stats::basic_statistics(x + eq.n_equilibration, n_stat, confidence);
+  r[2] = (double)n_stat;
+  r[3] = st.mean;
+  r[4] = st.precision;
+  r[5] = (st.precision < abs_precision) ? 1.0 : 0.0;
 }
 
 bool valid_slot(const mg_ce_pool* p, int slot) {
@@ -214,16 +330,47 @@ int mg_ce_pool_create(const mg_ce_model* m, long long arena_bytes, int max_chain
     return MG_ERR_CUDA;
   };
   if ((e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream");
+  for (int c = 0; c < kClasses; ++c) {
+    if ((e = cudaStreamCreateWithFlags(&p->cls_stream[c], cudaStreamNonBlocking)) != cudaSuccess) return fail("stream");
+    if ((e = cudaEventCreateWithFlags(&p->cls_done[c], cudaEventDisableTiming)) != cudaSuccess) return fail("event");
+  }
   if ((e = cudaEventCreate(&p->ev0)) != cudaSuccess) return fail("event");
   if ((e = cudaEventCreate(&p->ev1)) != cudaSuccess) return fail("event");
   if ((e = cudaMalloc(&p->darena, p->arena_bytes)) != cudaSuccess) return fail("arena");
   if ((e = cudaMalloc(&p->dcp, sizeof(mg::CeChainParams) * max_chains)) != cudaSuccess) return fail("params");
   if ((e = cudaMalloc(&p->dgeoms, sizeof(mg::PoolGeometry) * kMaxGeoms)) != cudaSuccess) return fail("geoms");
   if ((e = cudaMalloc(&p->ditems, sizeof(mg::PoolItem) * max_chains)) != cudaSuccess) return fail("items");
-  if ((e = cudaMalloc(&p->dcounter, sizeof(int))) != cudaSuccess) return fail("counter");
+  if ((e = cudaMalloc(&p->dcounter, sizeof(int) * kClasses)) != cudaSuccess) return fail("counter");
   if ((e = cudaMalloc(&p->dcorr, sizeof(long long) * 64)) != cudaSuccess) return fail("corr");
   *out = p;
   return MG_OK;
+}
+
+static int pool_class(int L0, int L1, int L2, int* cls) {
+  int dev = 0, max_smem = 0;
+  MG_CUDA_TRY(cudaGetDevice(&dev));
+  MG_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  *cls = -1;
+  for (int c = 0; c < kClasses && *cls < 0; ++c) {
+    const int S = kClassS[c];
+    if (L2 / S >= mg::CE_HALO && slab_smem(L0, L1, L2, S) <= (size_t)max_smem - 1024) *cls = c;
+  }
+  if (*cls < 0) {
+    set_error("Error in mg_ce_pool_add: supercell slab does not fit in shared memory with 16 CTAs");
+    return MG_ERR_INVALID;
+  }
+  return MG_OK;
+}
+
+int mg_ce_pool_prepare(mg_ce_pool* p, int L0, int L1, int L2) {
+  if (!p || L0 < 4 || L1 < 4 || L2 < 4) {
+    set_error("Error in mg_ce_pool_prepare: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  int cls = 0, gi = 0;
+  int rc = pool_class(L0, L1, L2, &cls);
+  if (rc != MG_OK) return rc;
+  return geometry(p, L0, L1, L2, kClassS[cls], &gi);
 }
 
 int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, const double* mu,
@@ -246,12 +393,10 @@ int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, co
       set_error("Error in mg_ce_pool_add: occupant index out of range");
       return MG_ERR_INVALID;
     }
-  int dev = 0, max_smem = 0;
-  MG_CUDA_TRY(cudaGetDevice(&dev));
-  MG_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  if (slab_smem(L0, L1, L2, 1) > (size_t)max_smem - 1024) {
-    set_error("Error in mg_ce_pool_add: supercell does not fit in one CTA's shared memory (use a batch)");
-    return MG_ERR_INVALID;
+  int cls = -1;
+  {
+    const int rc0 = pool_class(L0, L1, L2, &cls);
+    if (rc0 != MG_OK) return rc0;
   }
   int slot = -1;
   for (int i = 0; i < (int)p->slots.size(); ++i)
@@ -269,7 +414,7 @@ int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, co
     return MG_ERR_FULL;
   }
   int gi = -1;
-  int rc = geometry(p, L0, L1, L2, &gi);
+  int rc = geometry(p, L0, L1, L2, kClassS[cls], &gi);
   if (rc != MG_OK) {
     arena_free(p, off, N);
     return rc;
@@ -278,12 +423,26 @@ int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, co
   make_chain_params(p->model, 1, &temperature, mu, &seed, &chain_id, &cp);
   MG_CUDA_TRY(cudaMemcpyAsync(p->darena + off, occ, N, cudaMemcpyHostToDevice, p->stream));
   MG_CUDA_TRY(cudaMemcpyAsync(p->dcp + slot, &cp, sizeof(cp), cudaMemcpyHostToDevice, p->stream));
+  if (p->max_samples > 0) {
+    // the series starts from the integer correlation sums of the initial occupation
+    const int nc = p->model->n_classes;
+    long long* st = p->dstate + (size_t)slot * nc;
+    MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(long long) * nc, p->stream));
+    MG_CUDA_TRY(cudaMemsetAsync(p->dnsamp + slot, 0, sizeof(int), p->stream));
+    const int nblk = (int)std::min<long long>((N + 255) / 256, 1024);
+    if (p->model->kind == 0)
+      mg::ce_corr_kernel<mg::FccBinary><<<dim3(nblk, 1), 256, 0, p->stream>>>(p->darena + off, L0, L1, L2, 1, st);
+    else
+      mg::ce_corr_kernel<mg::FccTernary><<<dim3(nblk, 1), 256, 0, p->stream>>>(p->darena + off, L0, L1, L2, 1, st);
+    MG_CUDA_TRY(cudaGetLastError());
+  }
   MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
   PoolSlot& s = p->slots[slot];
   s.used = true;
   s.L0 = L0;
   s.L1 = L1;
   s.L2 = L2;
+  s.cls = cls;
   s.N = N;
   s.offset = off;
   s.pass = 0;
@@ -326,26 +485,39 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
     return MG_ERR_INVALID;
   }
   if (n == 0 || n_passes == 0) return MG_OK;
+  if ((size_t)n > p->slots.size()) {
+    set_error("Error in mg_ce_pool_run: more items than slots");
+    return MG_ERR_INVALID;
+  }
   const int nslot = p->model->n_classes + 2;
   std::vector<int> order(n);
+  std::vector<char> seen(p->slots.size(), 0);
   for (int i = 0; i < n; ++i) {
-    if (!valid_slot(p, slots[i])) {
-      set_error("Error in mg_ce_pool_run: invalid slot");
+    if (!valid_slot(p, slots[i]) || seen[slots[i]]) {
+      set_error("Error in mg_ce_pool_run: invalid or repeated slot");
       return MG_ERR_INVALID;
     }
+    seen[slots[i]] = 1;
     order[i] = i;
   }
-  // largest chains first (longest-processing-time order for the work queue)
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int b) { return p->slots[slots[a]].N > p->slots[slots[b]].N; });
+  // grouped by CTA class, largest chains first within a class (LPT work queue)
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const PoolSlot &x = p->slots[slots[a]], &y = p->slots[slots[b]];
+    if (x.cls != y.cls) return x.cls < y.cls;
+    return x.N > y.N;
+  });
   std::vector<mg::PoolItem> items(n);
-  size_t smem = 0;
-  for (int t = 0; t < n; ++t) {
+  int first[kClasses + 1] = {};
+  size_t smem[kClasses] = {};
+  for (int c = 0; c <= kClasses; ++c) first[c] = n;
+  for (int t = n - 1; t >= 0; --t) {
     const int i = order[t];
     const PoolSlot& s = p->slots[slots[i]];
     items[t] = mg::PoolItem{s.geom, slots[i], s.offset, (long long)i * n_passes * nslot, s.pass};
-    smem = std::max(smem, slab_smem(s.L0, s.L1, s.L2, 1));
+    first[s.cls] = t;
+    smem[s.cls] = std::max(smem[s.cls], slab_smem(s.L0, s.L1, s.L2, kClassS[s.cls]));
   }
+  for (int c = kClasses - 1; c >= 0; --c) first[c] = std::min(first[c], first[c + 1]);
   const size_t need = (size_t)n * n_passes * nslot;
   if (need > p->out_cap) {
     cudaFree(p->dout);
@@ -353,21 +525,113 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
     MG_CUDA_TRY(cudaMalloc(&p->dout, sizeof(long long) * need));
     p->out_cap = need;
   }
-  if ((size_t)n > p->slots.size()) {
-    set_error("Error in mg_ce_pool_run: more items than slots");
-    return MG_ERR_INVALID;
-  }
   MG_CUDA_TRY(cudaMemcpyAsync(p->ditems, items.data(), sizeof(mg::PoolItem) * n, cudaMemcpyHostToDevice, p->stream));
-  MG_CUDA_TRY(cudaMemsetAsync(p->dcounter, 0, sizeof(int), p->stream));
+  MG_CUDA_TRY(cudaMemsetAsync(p->dcounter, 0, sizeof(int) * kClasses, p->stream));
+  MG_CUDA_TRY(cudaMemsetAsync(p->dout, 0, sizeof(long long) * need, p->stream));
   MG_CUDA_TRY(cudaEventRecord(p->ev0, p->stream));
-  int rc = p->model->kind == 0 ? launch_pool<mg::FccBinary, mg::NT_BINARY>(p, items, n_passes, smem)
-                               : launch_pool<mg::FccTernary, mg::NT_TERNARY>(p, items, n_passes, smem);
-  if (rc != MG_OK) return rc;
+  // one launch per CTA class, each on its own stream after the set-up copies; the
+  // largest class first so that its long chains start while the others fill in
+  for (int c = kClasses - 1; c >= 0; --c) {
+    const int cnt = first[c + 1] - first[c];
+    if (cnt <= 0) continue;
+    MG_CUDA_TRY(cudaStreamWaitEvent(p->cls_stream[c], p->ev0, 0));
+    int rc = p->model->kind == 0 ? launch_pool<mg::FccBinary, mg::NT_BINARY>(p, c, first[c], cnt, n_passes, smem[c])
+                                 : launch_pool<mg::FccTernary, mg::NT_TERNARY>(p, c, first[c], cnt, n_passes, smem[c]);
+    if (rc != MG_OK) return rc;
+    MG_CUDA_TRY(cudaEventRecord(p->cls_done[c], p->cls_stream[c]));
+    MG_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->cls_done[c], 0));
+  }
   MG_CUDA_TRY(cudaEventRecord(p->ev1, p->stream));
+  if (p->max_samples > 0) {
+    const int nc = p->model->n_classes;
+    const int nt = 128, nb = (n + nt - 1) / nt;
+    if (p->model->kind == 0) {
+      mg::CeWeightsClass<mg::FccBinary::NCLASS> wc;
+      for (int f = 0; f < nc; ++f) wc.w[f] = (p->model->eci[f] / (double)p->model->mult[f]) * p->model->scale[f];
+      pool_series_kernel<mg::FccBinary::NCLASS, 2><<<nb, nt, 0, p->stream>>>(
+          p->ditems, n, p->dgeoms, p->dcp, p->dout, n_passes, p->dstate, p->dseries, p->dnsamp, p->max_samples, wc);
+    } else {
+      mg::CeWeightsClass<mg::FccTernary::NCLASS> wc;
+      for (int f = 0; f < nc; ++f) wc.w[f] = (p->model->eci[f] / (double)p->model->mult[f]) * p->model->scale[f];
+      pool_series_kernel<mg::FccTernary::NCLASS, 3><<<nb, nt, 0, p->stream>>>(
+          p->ditems, n, p->dgeoms, p->dcp, p->dout, n_passes, p->dstate, p->dseries, p->dnsamp, p->max_samples, wc);
+    }
+    MG_CUDA_TRY(cudaGetLastError());
+  }
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, p->dout, sizeof(long long) * need, cudaMemcpyDeviceToHost, p->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
   MG_CUDA_TRY(cudaEventElapsedTime(&p->last_ms, p->ev0, p->ev1));
   for (int i = 0; i < n; ++i) p->slots[slots[i]].pass += n_passes;
+  return MG_OK;
+}
+
+int mg_ce_pool_enable_series(mg_ce_pool* p, int max_samples) {
+  if (!p || max_samples < 1) {
+    set_error("Error in mg_ce_pool_enable_series: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  for (auto& s : p->slots)
+    if (s.used) {
+      set_error("Error in mg_ce_pool_enable_series: enable before adding chains");
+      return MG_ERR_INVALID;
+    }
+  const size_t nslots = p->slots.size();
+  cudaFree(p->dstate);
+  cudaFree(p->dseries);
+  cudaFree(p->dnsamp);
+  cudaFree(p->dcheck);
+  p->dstate = nullptr;
+  p->dseries = nullptr;
+  p->dnsamp = nullptr;
+  p->dcheck = nullptr;
+  p->max_samples = 0;
+  MG_CUDA_TRY(cudaMalloc(&p->dstate, sizeof(long long) * nslots * p->model->n_classes));
+  MG_CUDA_TRY(cudaMalloc(&p->dseries, sizeof(double) * nslots * (size_t)max_samples));
+  MG_CUDA_TRY(cudaMalloc(&p->dnsamp, sizeof(int) * nslots));
+  MG_CUDA_TRY(cudaMalloc(&p->dcheck, sizeof(double) * 6 * nslots + sizeof(int) * nslots));
+  MG_CUDA_TRY(cudaMemset(p->dnsamp, 0, sizeof(int) * nslots));
+  p->max_samples = max_samples;
+  return MG_OK;
+}
+
+int mg_ce_pool_series(mg_ce_pool* p, int slot, double* out, int max_n, int* n_out) {
+  if (!valid_slot(p, slot) || !n_out || p->max_samples < 1 || (max_n > 0 && !out)) {
+    set_error("Error in mg_ce_pool_series: invalid argument (series enabled?)");
+    return MG_ERR_INVALID;
+  }
+  int ns = 0;
+  MG_CUDA_TRY(cudaMemcpyAsync(&ns, p->dnsamp + slot, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+  MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  const int n = std::min(std::min(ns, p->max_samples), max_n);
+  if (n > 0)
+    MG_CUDA_TRY(cudaMemcpyAsync(out, p->dseries + (size_t)slot * p->max_samples, sizeof(double) * n,
+                                cudaMemcpyDeviceToHost, p->stream));
+  MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  *n_out = ns;
+  return MG_OK;
+}
+
+int mg_ce_pool_check(mg_ce_pool* p, const int32_t* slots, int n, double abs_precision, double confidence,
+                     double* out) {
+  if (!p || n < 0 || (n > 0 && (!slots || !out)) || p->max_samples < 1 || (size_t)n > p->slots.size()) {
+    set_error("Error in mg_ce_pool_check: invalid argument (series enabled?)");
+    return MG_ERR_INVALID;
+  }
+  if (n == 0) return MG_OK;
+  for (int i = 0; i < n; ++i)
+    if (!valid_slot(p, slots[i])) {
+      set_error("Error in mg_ce_pool_check: invalid slot");
+      return MG_ERR_INVALID;
+    }
+  double* dres = p->dcheck;
+  int* dslots = reinterpret_cast<int*>(p->dcheck + 6 * p->slots.size());
+  MG_CUDA_TRY(cudaMemcpyAsync(dslots, slots, sizeof(int) * n, cudaMemcpyHostToDevice, p->stream));
+  const int nt = 32, nb = (n + nt - 1) / nt;
+  pool_check_kernel<<<nb, nt, 0, p->stream>>>(dslots, n, p->dseries, p->dnsamp, p->max_samples, abs_precision,
+                                               confidence, dres);
+  MG_CUDA_TRY(cudaGetLastError());
+  MG_CUDA_TRY(cudaMemcpyAsync(out, dres, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, p->stream));
+  MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
   return MG_OK;
 }
 

@@ -48,6 +48,13 @@ struct CeChainParams {
   uint32_t chain_id;
   double dmu64[CE_MAX_SPECIES * CE_MAX_SPECIES];  // mu . N dx for o -> o2
   float dmu32[CE_MAX_SPECIES * CE_MAX_SPECIES];
+  double mu[CE_MAX_SPECIES - 1];  // exchange potentials (for energy samples)
+};
+
+// per-class energy weights w_f = V_f / M_f * C_f (E_f per supercell = sum_f w_f IntCorr_f)
+template <int NCLASS>
+struct CeWeightsClass {
+  double w[NCLASS];
 };
 
 template <int NFEAT>
@@ -433,11 +440,11 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
 
 // ---- persistent pool kernel: many chains of any shape, one CTA per chain
 
-// geometry of one supercell shape (S = 1): padded dims and colour lists
+// geometry of one supercell shape swept by S CTAs: colour lists per slab
 struct PoolGeometry {
   int L0, L1, L2;
   int n_colors;
-  const int* color_start;   // [n_colors + 1]
+  const int* color_start;   // [S][n_colors + 1]
   const uint32_t* entries;  // padded index | flags << 24
   const uint32_t* site_l;
 };
@@ -559,6 +566,127 @@ __global__ void __launch_bounds__(NT, 1) ce_pool_kernel(const __grid_constant__ 
       gocc[i + (long long)L0 * (j + (long long)L1 * k)] = (int8_t)B::occ_of_code(s[pidx]);
     }
     __syncthreads();
+  }
+}
+
+// Persistent pool kernel for chains too large for one CTA: each thread-block cluster of
+// S CTAs takes chains from the work queue (rank 0 draws the item and writes it into every
+// CTA's shared memory) and sweeps them as the batch kernel does (slabs, halo copies
+// through distributed shared memory, split cluster barriers).  Per-pass outputs are
+// accumulated with atomics (the host zeroes them).
+template <class B, int NT>
+__global__ void __launch_bounds__(NT, 1) ce_pool_cluster_kernel(const __grid_constant__ CePoolArgs<B::NFEAT> A) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  constexpr int PRE = (NS == 2) ? 3 : 2;
+  extern __shared__ __align__(16) int8_t s[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+  __shared__ int item_sm;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int S = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int lane = threadIdx.x & 31;
+
+#pragma unroll 1
+  while (true) {
+    if (rank == 0 && threadIdx.x == 0) {
+      const int it = atomicAdd(A.next_item, 1);
+      for (int r = 0; r < S; ++r) *cluster.map_shared_rank(&item_sm, (unsigned)r) = it;
+    }
+    cluster.sync();
+    const int it = item_sm;
+    if (it >= A.n_items) break;
+    const PoolItem item = A.items[it];
+    const PoolGeometry g = A.geoms[item.geom];
+    const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+    const int PX = L0 + 2 * B::HALO, PY = L1 + 2 * B::HALO, PXY = PX * PY;
+    const int nkq = L2 / S, nkr = L2 % S;
+    const int nk = nkq + (rank < nkr ? 1 : 0);
+    const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+    const int rprev = (rank + S - 1) % S;
+    const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
+    int8_t* gocc = A.occ + item.occ_offset;
+    for (int idx = threadIdx.x; idx < PXY * (nk + 2 * B::HALO); idx += NT) {
+      const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
+      int i = ip - B::HALO, j = jp - B::HALO, k = k0 + kp - B::HALO;
+      i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+      s[idx] = B::code_of_occ(gocc[i + (long long)L0 * (j + (long long)L1 * k)]);
+    }
+    if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+    const CeChainParams* cpg = A.cp + item.param;
+    load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+    const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+    const int* cstart = g.color_start + rank * (g.n_colors + 1);
+    SiteSweeper<B> sw;
+    sw.s = s;
+    sw.s_prev = cluster.map_shared_rank(s, (unsigned)rprev);
+    sw.s_next = cluster.map_shared_rank(s, (unsigned)((rank + 1) % S));
+    sw.PX = PX;
+    sw.PXY = PXY;
+    sw.dI = L0;
+    sw.dJ = L1 * PX;
+    sw.dKp = nk_prev * PXY;
+    sw.dKn = nk * PXY;
+    sw.dmu32 = dmu32_sm;
+    sw.dmu64 = dmu64_sm;
+    sw.w = &A.w;
+    sw.beta = cpg->beta;
+    sw.beta_log2e = cpg->beta_log2e;
+    sw.dtol = cpg->dtol;
+    sw.eps = cpg->eps;
+    sw.precision = A.precision;
+    int acc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+    long long* out = A.out + item.out_offset;
+    PhasePrefetch<PRE> pf;
+    pf.template prepare<NT>(cstart, 0, g.entries, g.site_l, (uint32_t)item.pass0, chain_id, key0, key1);
+    cluster.sync();
+#pragma unroll 1
+    for (int pass = 0; pass < A.n_passes; ++pass) {
+      const uint32_t pass_g = (uint32_t)(item.pass0 + pass);
+#pragma unroll 1
+      for (int c = 0; c < g.n_colors; ++c) {
+        sweep_phase<B, NT, PRE>(sw, pf, cstart, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
+        const bool last = (c + 1 == g.n_colors);
+        cluster_arrive_release();
+        pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, last ? pass_g + 1 : pass_g,
+                                chain_id, key0, key1);
+        cluster_wait_acquire();
+        if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+          int* buf = acc_sm[(pass - 1) & 1];
+          const int v = buf[threadIdx.x];
+          buf[threadIdx.x] = 0;
+          if (v)
+            atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)(pass - 1) * NSLOT + threadIdx.x),
+                      (unsigned long long)(long long)v);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q) {
+        const int v = warp_sum(acc[q]);
+        if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+        acc[q] = 0;
+      }
+    }
+    cluster.sync();
+    if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+      const int pl = A.n_passes - 1;
+      const int v = acc_sm[pl & 1][threadIdx.x];
+      if (v)
+        atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)pl * NSLOT + threadIdx.x),
+                  (unsigned long long)(long long)v);
+    }
+    for (int idx = threadIdx.x; idx < L0 * L1 * nk; idx += NT) {
+      const int i = idx % L0, j = (idx / L0) % L1, kl = idx / (L0 * L1);
+      const int pidx = (i + B::HALO) + PX * ((j + B::HALO) + PY * (kl + B::HALO));
+      gocc[i + (long long)L0 * (j + (long long)L1 * (k0 + kl))] = (int8_t)B::occ_of_code(s[pidx]);
+    }
+    cluster.sync();
   }
 }
 

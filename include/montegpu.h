@@ -145,6 +145,9 @@ int mg_ce_pool_create(const mg_ce_model* m, long long arena_bytes, int max_chain
 int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, const double* mu,
                    uint64_t seed, uint32_t chain_id, const int8_t* occ, int* slot);
 int mg_ce_pool_remove(mg_ce_pool* p, int slot);
+/* build (and cache) the colouring and site lists of a supercell shape ahead of its first
+ * chain; a geometry depends only on the shape, so servers prepare the shapes they expect */
+int mg_ce_pool_prepare(mg_ce_pool* p, int L0, int L1, int L2);
 int mg_ce_pool_info(const mg_ce_pool* p, long long* arena_free_bytes, long long* arena_bytes,
                     int* n_used, int* max_chains);
 int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, long long* out);
@@ -153,6 +156,17 @@ int mg_ce_pool_get_occ(mg_ce_pool* p, int slot, int8_t* occ);
 /* colouring of the slot's supercell [N]; returns the number of colours (>0) or an error */
 int mg_ce_pool_colors(const mg_ce_pool* p, int slot, int32_t* color);
 int mg_ce_pool_corr(mg_ce_pool* p, int slot, long long* out);
+/* Device-resident samples: after every pass each chain appends its potential energy per
+ * site (E_f - mu . N x)/N to a series of up to max_samples values (call before adding
+ * chains).  mg_ce_pool_check runs the reference's equilibration + convergence rule on one
+ * component (EquilibrationCheck.cc:50-117 with the absolute precision, then
+ * BasicStatisticsCalculator on the equilibrated tail, ConvergenceCheck.hh:74-90) on the
+ * device for each slot: out[n][6] = {equilibrated, N_equilibration, N_statistics, mean,
+ * calculated_precision, converged}. */
+int mg_ce_pool_enable_series(mg_ce_pool* p, int max_samples);
+int mg_ce_pool_series(mg_ce_pool* p, int slot, double* out, int max_n, int* n_samples);
+int mg_ce_pool_check(mg_ce_pool* p, const int32_t* slots, int n, double abs_precision, double confidence,
+                     double* out);
 int mg_ce_pool_destroy(mg_ce_pool* p);
 
 /* ---- allocation-free coloured sweep (no counterpart in the reference) ----

@@ -75,3 +75,54 @@ def test_pool_admission_by_footprint(gpu_lib):
     assert s3 == s1
     assert pool.info()["arena_free_bytes"] == 0
     pool.run([s0, s2, s3], 2)
+
+
+@pytest.mark.parametrize("kind,L", [("fcc_binary", (64, 64, 64)), ("fcc_binary", (72, 72, 72)),
+                                    ("fcc_ternary", (64, 64, 60))])
+def test_pool_large_chains_match_batch(gpu_lib, kind, L):
+    """Chains too large for one CTA run in the pool's cluster classes; same trajectory as the
+    (oracle-validated) batch path."""
+    model = clex.ClexModel(kind, clex.make_eci(kind, 8))
+    chains = _chains(model, [L, (16, 16, 16)], seed=9)
+    pool = clex.ChainPool(model, arena_bytes=2 * L[0] * L[1] * L[2] + (1 << 16), max_chains=4)
+    slots = [pool.add(c[0], c[1], c[2], c[3], c[4], c[5]) for c in chains]
+    out = pool.run(slots, 3)
+    out2 = pool.run(slots, 2)
+    for i, c in enumerate(chains):
+        b = clex.ChainBatch(model, c[0], c[1][None, :], [c[2]], c[3][None, :], [c[4]], chain_ids=[c[5]])
+        ref = b.run(3)
+        ref2 = b.run(2)
+        assert np.array_equal(out[i], ref[:, 0, :])
+        assert np.array_equal(out2[i], ref2[:, 0, :])
+        assert np.array_equal(pool.occupation(slots[i]), b.occupation()[0])
+        b.close()
+
+
+def test_pool_device_series_and_check_match_host(gpu_lib):
+    from casmcode_monte_gb300 import sampling
+
+    model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 3))
+    chains = _chains(model, [(12, 12, 12), (64, 64, 64), (8, 8, 8)], seed=11)
+    pool = clex.ChainPool(model, arena_bytes=(1 << 19), max_chains=4)
+    pool.enable_series(400)
+    slots = [pool.add(c[0], c[1], c[2], c[3], c[4], c[5]) for c in chains]
+    corr0 = [pool.corr(s) for s in slots]
+    outs = [pool.run(slots, 150), pool.run(slots, 150)]
+    for i, (c, s) in enumerate(zip(chains, slots)):
+        n = int(np.prod(c[0]))
+        o = np.concatenate([x[i] for x in outs])[:, None, :]
+        smp = clex.accumulate(model, corr0[i][None, :], o, np.asarray(c[3])[None, :], n)
+        ser = pool.series(s)
+        assert ser.size == 300
+        assert np.array_equal(ser, smp.potential_energy[:, 0])
+    for prec in (1e-4, 1e-3, 5e-3):
+        res = pool.check(slots, prec)
+        for i, s in enumerate(slots):
+            ser = pool.series(s)
+            eq = sampling.default_equilibration_check(ser, None, sampling.RequestedPrecision(abs=prec))
+            assert bool(res[i, 0]) == eq.is_equilibrated
+            assert int(res[i, 1]) == eq.N_samples_for_equilibration
+            if eq.is_equilibrated and eq.N_samples_for_equilibration < ser.size:
+                st = sampling.BasicStatisticsCalculator()(ser[eq.N_samples_for_equilibration:])
+                assert res[i, 3] == st.mean and res[i, 4] == st.calculated_precision
+                assert bool(res[i, 5]) == (st.calculated_precision < prec)
