@@ -56,6 +56,9 @@ SIGNATURES = {
                                      c_uint64_p, c_uint32_p, c_int8_p, C.c_int, C.c_int, vpp]),
     "mg_ce_batch_info": (C.c_int, [vp, c_int_p, c_int_p, c_int_p, c_size_p]),
     "mg_ce_batch_colors": (C.c_int, [vp, c_int32_p]),
+    "mg_ce_batch_layout": (C.c_int, [vp, c_int_p]),
+    "mg_ce_color_supercell": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, c_int32_p, c_int_p]),
+    "mg_ce_batch_set_layout": (C.c_int, [vp, C.c_int]),
     "mg_ce_batch_run": (C.c_int, [vp, C.c_int, c_ll_p]),
     "mg_ce_batch_last_kernel_ms": (C.c_int, [vp, c_float_p]),
     "mg_ce_batch_get_occ": (C.c_int, [vp, c_int8_p]),

@@ -94,6 +94,18 @@ class ClexModel:
         return np.stack([nB, nC], axis=-1).astype(np.float64)
 
 
+def color_supercell(kind: str, shape) -> tuple[np.ndarray, int, bool]:
+    """The sweep's colouring of a supercell (host only): (colour per site, number of
+    colours, whether the four-sites-per-word layout applies)."""
+    L0, L1, L2 = (int(x) for x in shape)
+    col = np.zeros(L0 * L1 * L2, dtype=np.int32)
+    word = C.c_int()
+    n = _lib.lib().mg_ce_color_supercell(BASIS_KINDS[kind], L0, L1, L2, _lib.ptr(col, C.c_int32), C.byref(word))
+    if n <= 0:
+        _lib.check(-n if n else 1)
+    return col, n, bool(word.value)
+
+
 class ChainBatch:
     """Chains of one L0 x L1 x L2 supercell resident on the GPU (handle to mg_ce_batch).
 
@@ -125,10 +137,23 @@ class ChainBatch:
             _lib.ptr(seeds, C.c_uint64), _lib.ptr(ids, C.c_uint32) if ids is not None else None,
             _lib.ptr(occ, C.c_int8), 0 if precision == "fp64" else 1, int(ctas_per_chain), C.byref(h)))
         self._h = h
-        S, nc, nt, sm = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
-        _lib.check(_lib.lib().mg_ce_batch_info(h, C.byref(S), C.byref(nc), C.byref(nt), C.byref(sm)))
-        self.ctas_per_chain, self.n_colors, self.threads, self.smem_bytes = S.value, nc.value, nt.value, sm.value
+        self._read_info()
         self.pass_count = 0
+
+    def _read_info(self) -> None:
+        S, nc, nt, sm, lay = C.c_int(), C.c_int(), C.c_int(), C.c_size_t(), C.c_int()
+        _lib.check(_lib.lib().mg_ce_batch_info(self._h, C.byref(S), C.byref(nc), C.byref(nt), C.byref(sm)))
+        _lib.check(_lib.lib().mg_ce_batch_layout(self._h, C.byref(lay)))
+        self.ctas_per_chain, self.n_colors, self.threads, self.smem_bytes = S.value, nc.value, nt.value, sm.value
+        self.layout = "word" if lay.value == 1 else "byte"
+
+    def set_layout(self, layout: str) -> None:
+        """Sweep with one site per byte ("byte") or four sites per word ("word", binary
+        basis with L0 a multiple of 4); trajectories are identical."""
+        if layout not in ("byte", "word"):
+            raise ValueError("layout must be 'byte' or 'word'")
+        _lib.check(_lib.lib().mg_ce_batch_set_layout(self._h, 1 if layout == "word" else 0))
+        self._read_info()
 
     def close(self) -> None:
         h = getattr(self, "_h", None)

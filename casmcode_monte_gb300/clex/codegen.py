@@ -54,6 +54,55 @@ def _var(off) -> str:
     return "v_" + "_".join(("m" + str(-x)) if x < 0 else str(x) for x in off)
 
 
+def _quad_features(bs, offs) -> list:
+    """Byte-parallel features for an occupation basis: every loaded word holds the 0/1
+    occupants of four sites (one per byte) and every F[k] the four sites' local sums.
+
+    A product of 0/1 values is a bitwise AND; sums stay below 256 per byte (the largest
+    feature of the FCC binary set counts 72 clusters), so byte lanes never carry into each
+    other.  Pair products that share a site a are factored as mask(a) & (sum of the
+    partners), mask(a) = a * 0xFF (0x00 or 0xFF per byte)."""
+    out = ["// Byte-parallel features: ld(di,dj,dk) returns a word of four sites' occupants (one",
+           "// per byte); F[k] receives the four sites' local sums, one per byte.",
+           "template <class Loader>",
+           "__device__ __forceinline__ void features_quad(const Loader& ld, uint32_t (&F)[NFEAT]) {"]
+    for o in offs:
+        out.append(f"  const uint32_t {_var(o)} = ld({o[0]}, {o[1]}, {o[2]});")
+    masks = set()
+    body = []
+    for k, f in enumerate(bs.features):
+        terms = [tuple(_var(o) for o, _ in t) for t in f.terms]
+        if all(len(t) == 0 for t in terms):
+            body.append(f"  F[{k}] = {len(terms)}u * 0x01010101u;")
+            continue
+        parts = []
+        singles = [t[0] for t in terms if len(t) == 1]
+        parts += singles
+        pairs = [t for t in terms if len(t) == 2]
+        while pairs:
+            count: dict = {}
+            for a, b in pairs:
+                count[a] = count.get(a, 0) + 1
+                count[b] = count.get(b, 0) + 1
+            v = max(sorted(count), key=lambda x: count[x])
+            if count[v] < 3:
+                parts += [f"({a} & {b})" for a, b in pairs]
+                break
+            partners = [b if a == v else a for a, b in pairs if v in (a, b)]
+            pairs = [t for t in pairs if v not in t]
+            masks.add(v)
+            parts.append(f"(m_{v} & ({' + '.join(partners)}))")
+        for t in terms:
+            if len(t) >= 3:
+                parts.append("(" + " & ".join(t) + ")")
+        body.append(f"  F[{k}] = " + _sum_expr(parts) + ";")
+    for v in sorted(masks):
+        out.append(f"  const uint32_t m_{v} = {v} * 0xFFu;")
+    out += body
+    out.append("}")
+    return out
+
+
 def generate(kind: str) -> tuple[str, dict]:
     bs = O.make_basis_set(kind)
     basis = bs.basis
@@ -127,6 +176,9 @@ def generate(kind: str) -> tuple[str, dict]:
                 terms.append(" * ".join(_psi_expr(basis, b, _var(o)) for o, b in t))
         lines.append(f"  F[{k}] = " + _sum_expr(terms) + ";")
     lines.append("}")
+
+    if basis.name == "occupation":
+        lines += _quad_features(bs, offs)
 
     # anchored correlations
     anc_offs = sorted({o for cls in bs.anchored for t in cls for o, _ in t})

@@ -18,6 +18,8 @@ struct mg_ce_batch {
   int L0 = 0, L1 = 0, L2 = 0, n_chains = 0, precision = 0;
   long long N = 0;
   int S = 1, PX = 0, PY = 0, PZ = 0, n_colors = 0, threads = 0;
+  int layout = 0;          // 0: one site per byte; 1: four sites per word (binary basis)
+  int ctas_requested = 0;  // 0: chosen by occupancy
   size_t smem = 0;
   long long pass = 0;
   std::vector<int32_t> color;
@@ -99,6 +101,48 @@ void free_batch(mg_ce_batch* b) {
   if (b->ev1) cudaEventDestroy(b->ev1);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
+}
+
+// CTA count, shared-memory size and site (or word) lists of the batch's layout, uploaded
+// to the device (replacing earlier lists).
+int setup_layout(mg_ce_batch* b, int layout) {
+  const mg_ce_model* m = b->model;
+  int S = 0;
+  int rc = choose_ctas(m->kind, b->L0, b->L1, b->L2, b->n_chains, b->ctas_requested, &S, layout);
+  if (rc != MG_OK) return rc;
+  const size_t smem = layout_smem(layout, b->L0, b->L1, b->L2, S);
+  if (smem > (size_t)(1u << 24)) {
+    set_error("Error in mg_ce_batch_create: slab too large for 24-bit shared-memory indices");
+    return MG_ERR_INVALID;
+  }
+  const long long n_entries = layout == 1 ? b->N / 4 : b->N;
+  std::vector<int> cstart((size_t)S * (b->n_colors + 1), 0);
+  std::vector<uint32_t> entries(n_entries), site(n_entries);
+  if (layout == 1)
+    build_word_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
+                     site.data());
+  else
+    build_site_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
+                     site.data());
+  cudaFree(b->dcstart);
+  cudaFree(b->dentries);
+  cudaFree(b->dsite);
+  b->dcstart = nullptr;
+  b->dentries = nullptr;
+  b->dsite = nullptr;
+  MG_CUDA_TRY(cudaMalloc(&b->dcstart, sizeof(int) * cstart.size()));
+  MG_CUDA_TRY(cudaMalloc(&b->dentries, sizeof(uint32_t) * entries.size()));
+  MG_CUDA_TRY(cudaMalloc(&b->dsite, sizeof(uint32_t) * site.size()));
+  MG_CUDA_TRY(cudaMemcpyAsync(b->dcstart, cstart.data(), sizeof(int) * cstart.size(), cudaMemcpyHostToDevice, b->stream));
+  MG_CUDA_TRY(cudaMemcpyAsync(b->dentries, entries.data(), sizeof(uint32_t) * entries.size(), cudaMemcpyHostToDevice, b->stream));
+  MG_CUDA_TRY(cudaMemcpyAsync(b->dsite, site.data(), sizeof(uint32_t) * site.size(), cudaMemcpyHostToDevice, b->stream));
+  MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->layout = layout;
+  b->S = S;
+  b->smem = smem;
+  b->PZ = (b->L2 + S - 1) / S + 2 * mg::CE_HALO;
+  b->threads = layout == 1 ? mg::host::NT_QUAD : (m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY);
+  return MG_OK;
 }
 
 }  // namespace
@@ -191,19 +235,9 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   const int halo = 2;
   b->PX = L0 + 2 * halo;
   b->PY = L1 + 2 * halo;
-  b->threads = m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY;
+  b->ctas_requested = ctas_per_chain;
 
-  int S = 0;
-  int rc = choose_ctas(m->kind, L0, L1, L2, n_chains, ctas_per_chain, &S);
-  if (rc != MG_OK) {
-    delete b;
-    return rc;
-  }
-  b->S = S;
-  b->PZ = (L2 + S - 1) / S + 2 * halo;
-  b->smem = slab_smem(L0, L1, L2, S);
-
-  // colouring and per-slab, per-colour site lists
+  // colouring, then the layout (word layout where the basis and colouring allow it)
   b->color.assign(N, -1);
   b->n_colors = color_supercell(L0, L1, L2, m->kind, b->color.data());
   if (b->n_colors < 1) {
@@ -211,14 +245,7 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
     delete b;
     return MG_ERR_INVALID;
   }
-  std::vector<int> cstart((size_t)S * (b->n_colors + 1), 0);
-  std::vector<uint32_t> entries(N), site(N);
-  build_site_lists(L0, L1, L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(), site.data());
-  if (b->smem > (size_t)(1u << 24)) {
-    set_error("Error in mg_ce_batch_create: slab too large for 24-bit shared-memory indices");
-    delete b;
-    return MG_ERR_INVALID;
-  }
+  const int layout = quad_eligible(m->kind, L0, L1, L2, b->color.data()) ? 1 : 0;
   b->hcp.resize(n_chains);
   make_chain_params(m, n_chains, temperature, mu, seeds, chain_ids, b->hcp.data());
 
@@ -235,16 +262,15 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   MGX(cudaEventCreate(&b->ev1), "event");
   MGX(cudaMalloc(&b->docc, (size_t)N * n_chains), "malloc occ");
   MGX(cudaMalloc(&b->dcp, sizeof(mg::CeChainParams) * n_chains), "malloc params");
-  MGX(cudaMalloc(&b->dcstart, sizeof(int) * cstart.size()), "malloc lists");
-  MGX(cudaMalloc(&b->dentries, sizeof(uint32_t) * entries.size()), "malloc lists");
-  MGX(cudaMalloc(&b->dsite, sizeof(uint32_t) * site.size()), "malloc lists");
   MGX(cudaMemcpyAsync(b->docc, occ, (size_t)N * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
   MGX(cudaMemcpyAsync(b->dcp, b->hcp.data(), sizeof(mg::CeChainParams) * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
-  MGX(cudaMemcpyAsync(b->dcstart, cstart.data(), sizeof(int) * cstart.size(), cudaMemcpyHostToDevice, b->stream), "copy");
-  MGX(cudaMemcpyAsync(b->dentries, entries.data(), sizeof(uint32_t) * entries.size(), cudaMemcpyHostToDevice, b->stream), "copy");
-  MGX(cudaMemcpyAsync(b->dsite, site.data(), sizeof(uint32_t) * site.size(), cudaMemcpyHostToDevice, b->stream), "copy");
-  MGX(cudaStreamSynchronize(b->stream), "sync");
 #undef MGX
+  int rc = setup_layout(b, layout);
+  if (rc == MG_ERR_INVALID && layout == 1) rc = setup_layout(b, 0);  // e.g. a CTA count only the byte layout fits
+  if (rc != MG_OK) {
+    free_batch(b);
+    return rc;
+  }
   *out = b;
   return MG_OK;
 }
@@ -260,6 +286,44 @@ int mg_ce_batch_info(const mg_ce_batch* b, int* ctas_per_chain, int* n_colors, i
   if (threads) *threads = b->threads;
   if (smem_bytes) *smem_bytes = b->smem;
   return MG_OK;
+}
+
+int mg_ce_color_supercell(int basis_kind, int L0, int L1, int L2, int32_t* color, int* word_layout) {
+  if (!color || (basis_kind != 0 && basis_kind != 1) || L0 < 4 || L1 < 4 || L2 < 4 ||
+      (long long)L0 * L1 * L2 > (1LL << 31)) {
+    set_error("Error in mg_ce_color_supercell: invalid argument");
+    return -MG_ERR_INVALID;
+  }
+  const int n = color_supercell(L0, L1, L2, basis_kind, color);
+  if (n < 1) {
+    set_error("Error in mg_ce_color_supercell: colouring needs more than 64 colours");
+    return -MG_ERR_INVALID;
+  }
+  if (word_layout) *word_layout = quad_eligible(basis_kind, L0, L1, L2, color) ? 1 : 0;
+  return n;
+}
+
+int mg_ce_batch_layout(const mg_ce_batch* b, int* layout) {
+  if (!b || !layout) {
+    set_error("Error in mg_ce_batch_layout: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  *layout = b->layout;
+  return MG_OK;
+}
+
+int mg_ce_batch_set_layout(mg_ce_batch* b, int layout) {
+  if (!b || (layout != 0 && layout != 1)) {
+    set_error("Error in mg_ce_batch_set_layout: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  if (layout == 1 && !quad_eligible(b->model->kind, b->L0, b->L1, b->L2, b->color.data())) {
+    set_error("Error in mg_ce_batch_set_layout: the word layout needs the binary basis, L0 = 4Q with Q >= 4 "
+              "and a colouring with colour(i + Q) = colour(i)");
+    return MG_ERR_INVALID;
+  }
+  if (layout == b->layout) return MG_OK;
+  return setup_layout(b, layout);
 }
 
 int mg_ce_batch_colors(const mg_ce_batch* b, int32_t* color) {
@@ -289,7 +353,7 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   MG_CUDA_TRY(cudaEventRecord(b->ev0, b->stream));
   SweepLaunch L{b->L0, b->L1, b->L2, b->S, b->n_colors, b->n_chains, b->precision, b->dcstart, b->dentries,
                 b->dsite, b->dcp, b->docc, b->pass, n_passes, b->dout, b->stream};
-  int rc = launch_sweep(b->model, L);
+  int rc = b->layout == 1 ? launch_sweep_quad(b->model, L) : launch_sweep(b->model, L);
   if (rc != MG_OK) return rc;
   MG_CUDA_TRY(cudaEventRecord(b->ev1, b->stream));
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, b->dout, sizeof(long long) * need, cudaMemcpyDeviceToHost, b->stream));

@@ -19,7 +19,7 @@
 namespace mg {
 
 // Adapters from the generated namespaces to the kernel's basis interface.
-#define MG_BASIS_ADAPTER(NAME, NS_)                                                       \
+#define MG_BASIS_ADAPTER(NAME, NS_, EXTRA)                                                \
   struct NAME {                                                                          \
     static constexpr int NSPECIES = NS_::NSPECIES;                                       \
     static constexpr int NFUNC = NS_::NFUNC;                                             \
@@ -39,10 +39,18 @@ namespace mg {
     __device__ static __forceinline__ void anchored(const L& ld, long long (&C)[NCLASS]) { \
       NS_::anchored(ld, C);                                                              \
     }                                                                                    \
+    EXTRA                                                                                \
   };
 
-MG_BASIS_ADAPTER(FccBinary, fcc_binary)
-MG_BASIS_ADAPTER(FccTernary, fcc_ternary)
+// the binary occupation basis also has byte-parallel features (word layout)
+#define MG_QUAD_FEATURES                                                                  \
+  template <class L>                                                                     \
+  __device__ static __forceinline__ void features_quad(const L& ld, uint32_t(&F)[NFEAT]) { \
+    fcc_binary::features_quad(ld, F);                                                    \
+  }
+MG_BASIS_ADAPTER(FccBinary, fcc_binary, MG_QUAD_FEATURES)
+MG_BASIS_ADAPTER(FccTernary, fcc_ternary, )
+#undef MG_QUAD_FEATURES
 #undef MG_BASIS_ADAPTER
 
 constexpr int NT_BINARY = 512;
@@ -93,11 +101,16 @@ inline const int* offsets(int kind, int* n) {
 inline int color_supercell(int L0, int L1, int L2, int kind, int32_t* col) {
   int noff = 0;
   const int* off = offsets(kind, &noff);
+  // binary basis: prefer, at each m, a colouring with colour(i + L0/4) = colour(i) (the
+  // word layout groups the four sites i0 + t*L0/4 of a row)
+  const bool want_quad = kind == 0 && L0 % 4 == 0;
   for (int m = 2; m <= 32; ++m)
+    for (int pref = want_quad ? 1 : 0; pref >= 0; --pref)
     for (int a = 0; a < m; ++a)
       for (int b = 0; b < m; ++b)
         for (int c = 0; c < m; ++c) {
           if ((1LL * a * L0) % m || (1LL * b * L1) % m || (1LL * c * L2) % m) continue;
+          if (pref && (1LL * a * (L0 / 4)) % m) continue;
           bool ok = true;
           for (int t = 0; t < noff && ok; ++t) {
             long long v = (1LL * a * off[3 * t] + 1LL * b * off[3 * t + 1] + 1LL * c * off[3 * t + 2]) % m;
@@ -231,6 +244,91 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
   }
 }
 
+// ---- word layout (four sites per 32-bit word, binary basis)
+
+constexpr int NT_QUAD = 384;
+
+// padded words per row: Q + 2 * HALO, made odd so that consecutive rows start in
+// different shared-memory banks
+inline int quad_row_stride(int Q) {
+  const int r = Q + 2 * CE_HALO;
+  return (r & 1) ? r : r + 1;
+}
+inline size_t quad_smem(int L0, int L1, int L2, int S) {
+  return sizeof(uint32_t) * (size_t)quad_row_stride(L0 / 4) * (L1 + 2 * CE_HALO) *
+         ((L2 + S - 1) / S + 2 * CE_HALO);
+}
+
+// The word layout applies to the binary basis when L0 = 4Q with Q >= 4 and the colouring
+// gives the four sites i0 + tQ of every row one colour.
+inline bool quad_eligible(int kind, int L0, int L1, int L2, const int32_t* col) {
+  if (kind != 0 || L0 % 4 != 0 || L0 / 4 < 4) return false;
+  const int Q = L0 / 4;
+  const long long rows = (long long)L1 * L2;
+  for (long long r = 0; r < rows; ++r) {
+    const int32_t* c = col + r * L0;
+    for (int i = 0; i < L0 - Q; ++i)
+      if (c[i] != c[i + Q]) return false;
+  }
+  return true;
+}
+
+// Per-slab, per-colour word lists.  Within one (slab, colour) list the words are ordered
+// round-robin over the 32 banks (padded word index mod 32), so that the lanes of a warp
+// load from distinct banks at every constant neighbour offset.
+// Entry = padded word index | mirror flags << 24 (1: w < 2, 2: w >= Q-2, 4: j < 2,
+// 8: j >= L1-2, 16: kl < 2, 32: kl >= nk-2); site[e] = linear index of byte 0's site.
+inline void build_word_lists(int L0, int L1, int L2, int S, const int32_t* col, int n_colors, int* cstart,
+                             uint32_t* entries, uint32_t* site) {
+  const int Q = L0 / 4, RS = quad_row_stride(Q), RY = L1 + 2 * CE_HALO;
+  int count[CE_MAX_COLORS * 32], seen[CE_MAX_COLORS * 32];
+  long long cbase[CE_MAX_COLORS + 1];
+  long long pos = 0;
+  for (int r = 0; r < S; ++r) {
+    const int nk = slab_planes(L2, S, r), k0 = slab_start(L2, S, r);
+    std::fill(count, count + n_colors * 32, 0);
+    std::fill(seen, seen + n_colors * 32, 0);
+    for (int kl = 0; kl < nk; ++kl)
+      for (int j = 0; j < L1; ++j) {
+        const long long row = (long long)L0 * (j + (long long)L1 * (k0 + kl));
+        const uint32_t prow = (uint32_t)(CE_HALO + RS * ((j + CE_HALO) + RY * (kl + CE_HALO)));
+        for (int w = 0; w < Q; ++w) count[(size_t)col[row + w] * 32 + ((prow + w) & 31)]++;
+      }
+    cbase[0] = pos;
+    for (int c = 0; c < n_colors; ++c) {
+      long long b = cbase[c];
+      for (int q = 0; q < 32; ++q) b += count[(size_t)c * 32 + q];
+      cbase[c + 1] = b;
+      cstart[r * (n_colors + 1) + c] = (int)cbase[c];
+    }
+    cstart[r * (n_colors + 1) + n_colors] = (int)cbase[n_colors];
+    for (int kl = 0; kl < nk; ++kl)
+      for (int j = 0; j < L1; ++j) {
+        const long long row = (long long)L0 * (j + (long long)L1 * (k0 + kl));
+        const uint32_t prow = (uint32_t)(CE_HALO + RS * ((j + CE_HALO) + RY * (kl + CE_HALO)));
+        for (int w = 0; w < Q; ++w) {
+          const int c = col[row + w];
+          const uint32_t pw = prow + w;
+          const int q = pw & 31;
+          const int* cnt = &count[(size_t)c * 32];
+          const int t = seen[(size_t)c * 32 + q]++;
+          long long p = cbase[c];
+          for (int q2 = 0; q2 < 32; ++q2) p += std::min(cnt[q2], t) + ((q2 < q && cnt[q2] > t) ? 1 : 0);
+          uint32_t flags = 0;
+          if (w < CE_HALO) flags |= 1;
+          else if (w >= Q - CE_HALO) flags |= 2;
+          if (j < CE_HALO) flags |= 4;
+          else if (j >= L1 - CE_HALO) flags |= 8;
+          if (kl < CE_HALO) flags |= 16;
+          if (kl >= nk - CE_HALO) flags |= 32;
+          entries[p] = pw | (flags << 24);
+          site[p] = (uint32_t)(row + w);
+        }
+      }
+    pos = cbase[n_colors];
+  }
+}
+
 // Chain parameters: beta, Philox key, mu . N dx table and the FP32 error bounds.
 inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* temperature,
                               const double* mu, const uint64_t* seeds, const uint32_t* chain_ids,
@@ -267,9 +365,8 @@ inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* 
   }
 }
 
-template <class B, int NT>
-int max_active_clusters(int S, size_t smem, int* out) {
-  auto kern = ce_sweep_kernel<B, NT>;
+template <class Kern>
+int max_active_clusters_k(Kern kern, int NT, int S, size_t smem, int* out) {
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   if (S == 1) {
@@ -297,19 +394,29 @@ int max_active_clusters(int S, size_t smem, int* out) {
   return MG_OK;
 }
 
-inline int max_active_chains(int kind, int S, size_t smem, int* out) {
-  return kind == 0 ? max_active_clusters<FccBinary, NT_BINARY>(S, smem, out)
-                   : max_active_clusters<FccTernary, NT_TERNARY>(S, smem, out);
+// layout 0: one site per byte (ce_sweep_kernel); layout 1: four sites per word
+// (ce_sweep_quad_kernel, binary basis)
+inline int max_active_chains(int kind, int S, size_t smem, int* out, int layout = 0) {
+  if (layout == 1)
+    return max_active_clusters_k(ce_sweep_quad_kernel<FccBinary, NT_QUAD>, NT_QUAD, S, smem, out);
+  return kind == 0 ? max_active_clusters_k(ce_sweep_kernel<FccBinary, NT_BINARY>, NT_BINARY, S, smem, out)
+                   : max_active_clusters_k(ce_sweep_kernel<FccTernary, NT_TERNARY>, NT_TERNARY, S, smem, out);
+}
+
+inline size_t layout_smem(int layout, int L0, int L1, int L2, int S) {
+  return layout == 1 ? quad_smem(L0, L1, L2, S) : slab_smem(L0, L1, L2, S);
 }
 
 // CTAs per chain: requested (validated) or the S minimising waves(S)/S over the
 // launchable candidates (ties -> fewer CTAs).  Returns MG_OK and sets *S_out.
-inline int choose_ctas(int kind, int L0, int L1, int L2, int n_chains, int requested, int* S_out) {
+inline int choose_ctas(int kind, int L0, int L1, int L2, int n_chains, int requested, int* S_out, int layout = 0) {
   int dev = 0, max_smem = 0;
   MG_CUDA_TRY(cudaGetDevice(&dev));
   MG_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t budget = (size_t)max_smem - 1024;
-  auto ok = [&](int S) { return S >= 1 && S <= 16 && L2 / S >= CE_HALO && slab_smem(L0, L1, L2, S) <= budget; };
+  auto ok = [&](int S) {
+    return S >= 1 && S <= 16 && L2 / S >= CE_HALO && layout_smem(layout, L0, L1, L2, S) <= budget;
+  };
   if (requested > 0) {
     if (!ok(requested)) {
       set_error("Error in ce sweep: ctas_per_chain must leave >= 2 planes per CTA and fit in shared memory");
@@ -323,7 +430,7 @@ inline int choose_ctas(int kind, int L0, int L1, int L2, int n_chains, int reque
   for (int s = 1; s <= 16; ++s) {
     if (!ok(s)) continue;
     int n_active = 0;
-    const int rc = max_active_chains(kind, s, slab_smem(L0, L1, L2, s), &n_active);
+    const int rc = max_active_chains(kind, s, layout_smem(layout, L0, L1, L2, s), &n_active, layout);
     if (rc != MG_OK) return rc;
     if (n_active < 1) continue;
     const double cost = (double)((n_chains + n_active - 1) / n_active) / s;
@@ -384,6 +491,54 @@ int launch_sweep_t(const mg_ce_model* m, const SweepLaunch& L) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);
   cfg.blockDim = dim3(NT, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = L.stream;
+  cudaLaunchAttribute attr[1];
+  if (L.S > 1) {
+    if (L.S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)L.S;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  MG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
+  MG_CUDA_TRY(cudaGetLastError());
+  return MG_OK;
+}
+
+inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L) {
+  using B = FccBinary;
+  CeQuadArgs<B::NFEAT> A;
+  A.g.L0 = L.L0;
+  A.g.L1 = L.L1;
+  A.g.L2 = L.L2;
+  A.g.Q = L.L0 / 4;
+  A.g.S = L.S;
+  A.g.RS = quad_row_stride(L.L0 / 4);
+  A.g.RY = L.L1 + 2 * CE_HALO;
+  A.g.n_colors = L.n_colors;
+  A.g.color_start = L.cstart;
+  A.g.entries = L.entries;
+  A.g.site_l = L.site;
+  for (int k = 0; k < B::NFEAT; ++k) {
+    A.w.w32[k] = m->w32[k];
+    A.w.w64[k] = m->w64[k];
+  }
+  A.cp = L.cp;
+  A.occ = L.occ;
+  A.pass0 = L.pass0;
+  A.n_passes = L.n_passes;
+  A.n_chains = L.n_chains;
+  A.precision = L.precision;
+  A.out = L.out;
+  const size_t smem = quad_smem(L.L0, L.L1, L.L2, L.S);
+  auto kern = ce_sweep_quad_kernel<B, NT_QUAD>;
+  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);
+  cfg.blockDim = dim3(NT_QUAD, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = L.stream;
   cudaLaunchAttribute attr[1];

@@ -123,6 +123,80 @@ __device__ __forceinline__ int warp_sum(int v) {
   return v;
 }
 
+// Metropolis decision of one proposal o -> o2 from its integer local features: the FP32
+// fast path, and the exact FP64 decision whenever the FP32 one could differ (|dE32|
+// within the rounding bound, or u within the relative bound of exp(-beta dE)).  Counts
+// FP64 re-decisions in acc[NCLASS] and, in FP32 mode, flipped decisions in
+// acc[NCLASS+1].  Ff[k] is F[k] as a float (exact); Fi(k) returns F[k] as an int and is
+// only called on the FP64 path.
+template <class B>
+struct MetropolisRule {
+  static constexpr int NF = B::NFEAT;
+  static constexpr int NC = B::NCLASS;
+  static constexpr int NS = B::NSPECIES;
+  static constexpr int NSLOT = CeSlots<NC>::N;
+  const float* dmu32;  // shared memory [NS*NS]
+  const double* dmu64;
+  const CeWeights<NF>* w;
+  double beta;
+  float beta_log2e, dtol, eps;
+  int precision;
+
+  template <class FI>
+  __device__ __forceinline__ bool operator()(int o, int o2, const int (&dpsi)[B::NFUNC], const float (&Ff)[NF],
+                                             const FI& Fi, uint32_t x0, int (&acc)[NSLOT]) const {
+    float G[B::NFUNC];
+#pragma unroll
+    for (int b = 0; b < B::NFUNC; ++b) G[b] = 0.f;
+#pragma unroll
+    for (int k = 0; k < NF; ++k) G[B::feat_b(k)] = fmaf(w->w32[k], Ff[k], G[B::feat_b(k)]);
+    float dE32 = -dmu32[o * NS + o2];
+#pragma unroll
+    for (int b = 0; b < B::NFUNC; ++b) dE32 = fmaf((float)dpsi[b], G[b], dE32);
+
+    const float u32 = __uint2float_rn(x0) * 2.3283064365386963e-10f;
+    bool amb = false, acc32;
+    if (dE32 < -dtol) {
+      acc32 = true;
+    } else {
+      const float P = fast_exp2(-dE32 * beta_log2e);
+      acc32 = (dE32 < 0.f) || (u32 < P);
+      if (dE32 <= dtol || x0 == 0u)
+        amb = true;
+      else if (!(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps)))
+        amb = true;
+    }
+    bool accept = acc32;
+    if (amb) {
+      // exact FP64 decision: dE64 = sum_b dpsi_b * (sum_k w64[k] F[k]) - dmu
+      double G64[B::NFUNC];
+#pragma unroll
+      for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
+#pragma unroll
+      for (int k = 0; k < NF; ++k)
+        G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(w->w64[k], (double)Fi(k)));
+      double dE = 0.0;
+#pragma unroll
+      for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
+      dE = __dsub_rn(dE, dmu64[o * NS + o2]);
+      bool acc64;
+      if (dE < 0.0) {
+        acc64 = true;
+      } else {
+        const double u = __dmul_rn((double)x0, 2.3283064365386962890625e-10);
+        acc64 = u < exp(__dmul_rn(-dE, beta));
+      }
+      acc[NC] += 1;
+      if (precision == 0) {
+        accept = acc64;
+      } else if (acc64 != acc32) {
+        acc[NC + 1] += 1;
+      }
+    }
+    return accept;
+  }
+};
+
 // Per-CTA context of the site update: shared-memory lattice and its periodic copies,
 // chain constants and the FP32/FP64 decision rule.  Shared by the cluster sweep kernel
 // and the persistent pool kernel.
@@ -165,54 +239,11 @@ struct SiteSweeper {
     int dpsi[B::NFUNC];
 #pragma unroll
     for (int b = 0; b < B::NFUNC; ++b) dpsi[b] = B::psi(b, o2) - B::psi(b, o);
-    float G[B::NFUNC];
+    float Ff[NF];
 #pragma unroll
-    for (int b = 0; b < B::NFUNC; ++b) G[b] = 0.f;
-#pragma unroll
-    for (int k = 0; k < NF; ++k) G[B::feat_b(k)] = fmaf(w->w32[k], (float)F[k], G[B::feat_b(k)]);
-    float dE32 = -dmu32[o * NS + o2];
-#pragma unroll
-    for (int b = 0; b < B::NFUNC; ++b) dE32 = fmaf((float)dpsi[b], G[b], dE32);
-
-    const float u32 = __uint2float_rn(x0) * 2.3283064365386963e-10f;
-    bool amb = false, acc32;
-    if (dE32 < -dtol) {
-      acc32 = true;
-    } else {
-      const float P = fast_exp2(-dE32 * beta_log2e);
-      acc32 = (dE32 < 0.f) || (u32 < P);
-      if (dE32 <= dtol || x0 == 0u)
-        amb = true;
-      else if (!(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps)))
-        amb = true;
-    }
-    bool accept = acc32;
-    if (amb) {
-      // exact FP64 decision: dE64 = sum_b dpsi_b * (sum_k w64[k] F[k]) - dmu
-      double G64[B::NFUNC];
-#pragma unroll
-      for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
-#pragma unroll
-      for (int k = 0; k < NF; ++k)
-        G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(w->w64[k], (double)F[k]));
-      double dE = 0.0;
-#pragma unroll
-      for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
-      dE = __dsub_rn(dE, dmu64[o * NS + o2]);
-      bool acc64;
-      if (dE < 0.0) {
-        acc64 = true;
-      } else {
-        const double u = __dmul_rn((double)x0, 2.3283064365386962890625e-10);
-        acc64 = u < exp(__dmul_rn(-dE, beta));
-      }
-      acc[NC] += 1;
-      if (precision == 0) {
-        accept = acc64;
-      } else if (acc64 != acc32) {
-        acc[NC + 1] += 1;
-      }
-    }
+    for (int k = 0; k < NF; ++k) Ff[k] = (float)F[k];
+    const MetropolisRule<B> rule{dmu32, dmu64, w, beta, beta_log2e, dtol, eps, precision};
+    const bool accept = rule(o, o2, dpsi, Ff, [&](int k) { return F[k]; }, x0, acc);
     if (accept) {
       const int8_t c2 = B::code_of_occ(o2);
       const int oi = (flags & 1u) ? dI : ((flags & 2u) ? -dI : 0);
@@ -434,6 +465,295 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
     const int i = idx % L0, j = (idx / L0) % L1, kl = idx / (L0 * L1);
     const int pidx = (i + B::HALO) + PX * ((j + B::HALO) + PY * (kl + B::HALO));
     gocc[i + (long long)L0 * (j + (long long)L1 * (k0 + kl))] = (int8_t)B::occ_of_code(s[pidx]);
+  }
+  barrier();
+}
+
+// ---- word layout (binary occupation basis): four sites per 32-bit word
+//
+// A supercell row (fixed j, k) of L0 = 4Q sites is held as Q words; word w in [0, Q)
+// holds the sites i = w + tQ in byte t (t = 0..3).  The padded row has words
+// w in [-2, Q + 2): words -2, -1 are words Q-2, Q-1 rotated left by one byte and words
+// Q, Q+1 are words 0, 1 rotated right by one byte, so that byte t of padded word w is
+// always site (w + tQ) mod L0.  A neighbour offset (di, dj, dk) of the four sites of a
+// word is then the word at constant offset di + dj*RS + dk*RS*RY, with the four
+// neighbours in matching bytes.  With a colouring in which colour(i + Q) = colour(i), a
+// word's four sites share a colour and are proposed together: the features of all four
+// come out of one pass of byte-parallel integer code, the four decisions are taken one
+// by one (same random numbers, same arithmetic as the per-site kernel, so trajectories
+// are identical), and accepted flips are written back as one word.
+struct QuadGeometry {
+  int L0, L1, L2, Q;
+  int S;
+  int RS, RY;  // padded words per row (odd: rows start in different banks), rows per plane
+  int n_colors;
+  const int* color_start;   // [S][n_colors + 1]
+  const uint32_t* entries;  // padded word index | flags << 24
+  const uint32_t* site_l;   // linear index of the word's byte-0 site
+};
+
+template <int NFEAT>
+struct CeQuadArgs {
+  QuadGeometry g;
+  CeWeights<NFEAT> w;
+  const CeChainParams* cp;
+  int8_t* occ;
+  long long pass0;
+  int n_passes;
+  int n_chains;
+  int precision;
+  long long* out;
+};
+
+struct WordLoader {
+  const uint32_t* p;
+  int RS, RSY;
+  __device__ __forceinline__ uint32_t operator()(int di, int dj, int dk) const {
+    return p[di + dj * RS + dk * RSY];
+  }
+};
+
+// byte t of w as a float (exact): 2^23 + byte, minus 2^23
+__device__ __forceinline__ float byte_as_float(uint32_t w, int t) {
+  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + (unsigned)t)) - 8388608.0f;
+}
+
+template <class B>
+struct QuadSweeper {
+  static constexpr int NF = B::NFEAT;
+  static constexpr int NC = B::NCLASS;
+  static constexpr int NSLOT = CeSlots<NC>::N;
+  static_assert(B::NSPECIES == 2 && B::NFUNC == 1, "word layout needs a binary occupation basis");
+  uint32_t* s;
+  uint32_t* s_prev;
+  uint32_t* s_next;
+  int RS, RSY;
+  int Q, dJ, dKp, dKn;
+  MetropolisRule<B> rule;
+
+  // one word: features of its four sites, four decisions, write-back of the flips
+  __device__ __forceinline__ void update(uint32_t ent, const uint32_t (&x0)[4], int (&acc)[NSLOT]) const {
+    const int pw = (int)(ent & 0xFFFFFFu);
+    const uint32_t flags = ent >> 24;
+    const uint32_t* p = s + pw;
+    uint32_t F[NF];
+    B::features_quad(WordLoader{p, RS, RSY}, F);
+    const uint32_t v = *p;
+    uint32_t flip = 0u, sgn = 0u;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int o = (int)((v >> (8 * t)) & 1u);
+      const int dpsi[1] = {1 - 2 * o};
+      float Ff[NF];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) Ff[k] = byte_as_float(F[k], t);
+      const bool accept =
+          rule(o, 1 - o, dpsi, Ff, [&](int k) { return (int)((F[k] >> (8 * t)) & 0xFFu); }, x0[t], acc);
+      if (accept) {
+        flip |= 1u << (8 * t);
+        sgn |= (o ? 0xFFu : 0x01u) << (8 * t);
+      }
+    }
+    if (flip) {
+      const uint32_t nv = v ^ flip;
+      uint32_t vi = nv;
+      int oi = 0;
+      if (flags & 1u) {
+        oi = Q;
+        vi = __funnelshift_r(nv, nv, 8);
+      } else if (flags & 2u) {
+        oi = -Q;
+        vi = __funnelshift_l(nv, nv, 8);
+      }
+      const int oj = (flags & 4u) ? dJ : ((flags & 8u) ? -dJ : 0);
+      auto put = [&](uint32_t* r) {
+        r[0] = nv;
+        if (oi) r[oi] = vi;
+        if (oj) r[oj] = nv;
+        if (oi && oj) r[oi + oj] = vi;
+      };
+      put(s + pw);
+      if (flags & 16u) put(s_prev + pw + dKp);
+      if (flags & 32u) put(s_next + pw - dKn);
+      acc[0] += __popc(flip);
+      // sum over the four sites of dpsi * F[k]: signed byte dot product
+#pragma unroll
+      for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += __dp4a((int)F[k], (int)sgn, 0);
+    }
+  }
+};
+
+// Philox words of the first word of a thread in one colour phase (four sites)
+struct QuadPrefetch {
+  uint32_t ent, x0[4];
+
+  template <int NT>
+  __device__ __forceinline__ void prepare(const int* cstart, int c, const uint32_t* entries,
+                                          const uint32_t* site_l, int Q, uint32_t pass, uint32_t chain_id,
+                                          uint32_t key0, uint32_t key1) {
+    const int e = cstart[c] + threadIdx.x;
+    if (e < cstart[c + 1]) {
+      ent = __ldg(entries + e);
+      const uint32_t l0 = __ldg(site_l + e);
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        x0[t] = philox4x32_10(U32x4{l0 + (uint32_t)(t * Q), pass, chain_id, SWEEP_TAG}, key0, key1).x;
+    }
+  }
+};
+
+template <class B, int NT>
+__device__ __forceinline__ void sweep_phase_quad(const QuadSweeper<B>& sw, const QuadPrefetch& pf, const int* cstart,
+                                                 int c, const uint32_t* entries, const uint32_t* site_l,
+                                                 uint32_t pass, uint32_t chain_id, uint32_t key0, uint32_t key1,
+                                                 int (&acc)[QuadSweeper<B>::NSLOT]) {
+  const int e0 = cstart[c] + threadIdx.x, e_end = cstart[c + 1];
+  if (e0 < e_end) sw.update(pf.ent, pf.x0, acc);
+#pragma unroll 1
+  for (int e = e0 + NT; e < e_end; e += NT) {
+    const uint32_t ent = __ldg(entries + e);
+    const uint32_t l0 = __ldg(site_l + e);
+    uint32_t x0[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      x0[t] = philox4x32_10(U32x4{l0 + (uint32_t)(t * sw.Q), pass, chain_id, SWEEP_TAG}, key0, key1).x;
+    sw.update(ent, x0, acc);
+  }
+}
+
+template <class B, int NT>
+__global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_constant__ CeQuadArgs<B::NFEAT> A) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  extern __shared__ __align__(16) uint32_t sq[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+
+  const QuadGeometry& g = A.g;
+  const int S = g.S;
+  const int chain = blockIdx.x / S;
+  int rank = 0;
+  cg::cluster_group cluster = cg::this_cluster();
+  if (S > 1) rank = (int)cluster.block_rank();
+  auto barrier = [&]() {
+    if (S > 1)
+      cluster.sync();
+    else
+      __syncthreads();
+  };
+
+  const int Q = g.Q, RS = g.RS, RY = g.RY, RSY = RS * RY;
+  const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+  const int nkq = L2 / S, nkr = L2 % S;
+  const int nk = nkq + (rank < nkr ? 1 : 0);
+  const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+  const int rprev = (rank + S - 1) % S;
+  const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
+  const long long N = (long long)L0 * L1 * L2;
+  int8_t* gocc = A.occ + (size_t)chain * N;
+
+  // ---- load slab + borders (padding words beyond Q + 2 are zero and never read)
+  for (int idx = threadIdx.x; idx < RSY * (nk + 2 * B::HALO); idx += NT) {
+    const int wp = idx % RS, jp = (idx / RS) % RY, kp = idx / RSY;
+    const int w = wp - B::HALO;
+    uint32_t word = 0u;
+    if (w < Q + B::HALO) {
+      int j = jp - B::HALO, k = k0 + kp - B::HALO;
+      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+      const int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        int i = w + t * Q;
+        i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+        word |= (uint32_t)(uint8_t)row[i] << (8 * t);
+      }
+    }
+    sq[idx] = word;
+  }
+  if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+
+  const CeChainParams* cpg = A.cp + chain;
+  load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+  const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+  const int* cstart = g.color_start + rank * (g.n_colors + 1);
+
+  QuadSweeper<B> sw;
+  sw.s = sq;
+  sw.s_prev = sq;
+  sw.s_next = sq;
+  if (S > 1) {
+    sw.s_prev = cluster.map_shared_rank(sq, (unsigned)rprev);
+    sw.s_next = cluster.map_shared_rank(sq, (unsigned)((rank + 1) % S));
+  }
+  sw.RS = RS;
+  sw.RSY = RSY;
+  sw.Q = Q;
+  sw.dJ = L1 * RS;
+  sw.dKp = nk_prev * RSY;
+  sw.dKn = nk * RSY;
+  sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
+                              A.precision};
+  const int lane = threadIdx.x & 31;
+  int acc[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+
+  QuadPrefetch pf;
+  pf.template prepare<NT>(cstart, 0, g.entries, g.site_l, Q, (uint32_t)A.pass0, chain_id, key0, key1);
+  barrier();
+
+#pragma unroll 1
+  for (int pass = 0; pass < A.n_passes; ++pass) {
+    const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
+#pragma unroll 1
+    for (int c = 0; c < g.n_colors; ++c) {
+      sweep_phase_quad<B, NT>(sw, pf, cstart, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
+      const bool last = (c + 1 == g.n_colors);
+      if (S > 1) {
+        cluster_arrive_release();
+        pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, Q, last ? pass_g + 1 : pass_g,
+                                chain_id, key0, key1);
+        cluster_wait_acquire();
+      } else {
+        pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, Q, last ? pass_g + 1 : pass_g,
+                                chain_id, key0, key1);
+        __syncthreads();
+      }
+      if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+        int* buf = acc_sm[(pass - 1) & 1];
+        const int v = buf[threadIdx.x];
+        buf[threadIdx.x] = 0;
+        if (v)
+          atomicAdd(reinterpret_cast<unsigned long long*>(
+                        A.out + ((size_t)(pass - 1) * A.n_chains + chain) * NSLOT + threadIdx.x),
+                    (unsigned long long)(long long)v);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) {
+      const int v = warp_sum(acc[q]);
+      if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+      acc[q] = 0;
+    }
+  }
+  barrier();
+  if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+    const int pl = A.n_passes - 1;
+    int* buf = acc_sm[pl & 1];
+    const int v = buf[threadIdx.x];
+    if (v)
+      atomicAdd(reinterpret_cast<unsigned long long*>(A.out + ((size_t)pl * A.n_chains + chain) * NSLOT + threadIdx.x),
+                (unsigned long long)(long long)v);
+  }
+  // ---- write back own words
+  for (int idx = threadIdx.x; idx < Q * L1 * nk; idx += NT) {
+    const int w = idx % Q, j = (idx / Q) % L1, kl = idx / (Q * L1);
+    const uint32_t word = sq[(w + B::HALO) + RS * ((j + B::HALO) + RY * (kl + B::HALO))];
+    int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * (k0 + kl));
+#pragma unroll
+    for (int t = 0; t < 4; ++t) row[w + t * Q] = (int8_t)((word >> (8 * t)) & 0xFFu);
   }
   barrier();
 }

@@ -93,6 +93,86 @@ __device__ __forceinline__ void features(const Loader& ld, int (&F)[NFEAT]) {
   F[7] = ((v_m2_0_1 * v_m1_0_0 + v_m2_1_1 * v_m1_0_1 + v_m1_m1_2 * v_m1_0_1 + v_m1_0_0 * v_0_0_1 + v_m1_0_1 * v_m1_0_2 + v_m1_0_1 * v_1_0_0 + v_m1_1_0 * v_0_m1_0 + v_m1_2_m1 * v_0_1_m1 + v_0_m1_m1 * v_0_m1_0 + v_0_m1_0 * v_1_m2_0 + v_0_m1_1 * v_0_1_0 + v_0_0_m1 * v_0_1_m2 + v_0_0_1 * v_0_1_m1 + v_0_1_m2 * v_0_1_m1 + v_0_1_0 * v_0_1_1 + v_1_m2_0 * v_1_m1_0 + v_1_0_m2 * v_1_0_m1 + v_1_0_0 * v_1_0_1) + (v_m2_0_1 * v_m1_0_1 + v_m2_1_1 * v_m1_1_0 + v_m1_m1_2 * v_0_m1_1 + v_m1_0_0 * v_0_1_0 + v_m1_0_1 * v_0_0_m1 + v_m1_0_2 * v_0_0_1 + v_m1_1_0 * v_0_m1_1 + v_m1_2_0 * v_0_1_0 + v_0_m1_m1 * v_0_0_m1 + v_0_m1_0 * v_1_0_0 + v_0_m1_1 * v_1_m2_1 + v_0_0_m1 * v_0_1_0 + v_0_0_1 * v_0_1_1 + v_0_1_m1 * v_0_2_m1 + v_0_1_0 * v_0_2_m1 + v_1_m2_1 * v_1_m1_0 + v_1_0_m1 * v_1_1_m2 + v_1_0_0 * v_1_1_0)) + ((v_m2_1_0 * v_m1_0_0 + v_m1_m1_0 * v_m1_0_0 + v_m1_0_m1 * v_m1_0_0 + v_m1_0_0 * v_1_m1_0 + v_m1_0_1 * v_0_1_m1 + v_m1_1_0 * v_m1_2_m1 + v_m1_1_0 * v_1_0_m1 + v_0_m2_1 * v_0_m1_0 + v_0_m1_0 * v_0_0_1 + v_0_m1_1 * v_0_m1_2 + v_0_m1_1 * v_1_0_m1 + v_0_0_m1 * v_1_0_m2 + v_0_0_1 * v_1_0_m1 + v_0_1_m1 * v_1_m1_0 + v_0_1_0 * v_1_m1_0 + v_1_m1_0 * v_2_m1_m1 + v_1_0_m1 * v_2_m1_m1 + v_1_0_0 * v_2_m1_0) + (v_m2_1_0 * v_m1_1_0 + v_m1_m1_0 * v_0_m1_0 + v_m1_0_m1 * v_0_0_m1 + v_m1_0_0 * v_1_0_m1 + v_m1_0_1 * v_1_m1_0 + v_m1_1_0 * v_m1_2_0 + v_m1_1_0 * v_1_0_0 + v_0_m2_1 * v_0_m1_1 + v_0_m1_0 * v_0_1_m1 + v_0_m1_1 * v_0_0_m1 + v_0_m1_2 * v_0_0_1 + v_0_0_m1 * v_1_0_0 + v_0_0_1 * v_1_0_1 + v_0_1_m1 * v_1_1_m2 + v_0_1_0 * v_1_1_0 + v_1_m1_0 * v_2_m1_0 + v_1_0_m1 * v_2_0_m1 + v_1_0_0 * v_2_0_m1));
   F[8] = ((v_m1_0_0 * v_m1_0_1 * v_m1_1_0 + v_0_m1_0 * v_0_m1_1 * v_1_m1_0) + (v_m1_0_0 * v_0_m1_0 * v_0_0_m1 + v_0_0_m1 * v_0_1_m1 * v_1_0_m1)) + ((v_m1_0_1 * v_0_m1_1 * v_0_0_1 + v_0_0_1 * v_0_1_0 * v_1_0_0) + (v_m1_1_0 * v_0_1_m1 * v_0_1_0 + v_1_m1_0 * v_1_0_m1 * v_1_0_0));
 }
+// Byte-parallel features: ld(di,dj,dk) returns a word of four sites' occupants (one
+// per byte); F[k] receives the four sites' local sums, one per byte.
+template <class Loader>
+__device__ __forceinline__ void features_quad(const Loader& ld, uint32_t (&F)[NFEAT]) {
+  const uint32_t v_m2_0_0 = ld(-2, 0, 0);
+  const uint32_t v_m2_0_1 = ld(-2, 0, 1);
+  const uint32_t v_m2_0_2 = ld(-2, 0, 2);
+  const uint32_t v_m2_1_0 = ld(-2, 1, 0);
+  const uint32_t v_m2_1_1 = ld(-2, 1, 1);
+  const uint32_t v_m2_2_0 = ld(-2, 2, 0);
+  const uint32_t v_m1_m1_0 = ld(-1, -1, 0);
+  const uint32_t v_m1_m1_1 = ld(-1, -1, 1);
+  const uint32_t v_m1_m1_2 = ld(-1, -1, 2);
+  const uint32_t v_m1_0_m1 = ld(-1, 0, -1);
+  const uint32_t v_m1_0_0 = ld(-1, 0, 0);
+  const uint32_t v_m1_0_1 = ld(-1, 0, 1);
+  const uint32_t v_m1_0_2 = ld(-1, 0, 2);
+  const uint32_t v_m1_1_m1 = ld(-1, 1, -1);
+  const uint32_t v_m1_1_0 = ld(-1, 1, 0);
+  const uint32_t v_m1_1_1 = ld(-1, 1, 1);
+  const uint32_t v_m1_2_m1 = ld(-1, 2, -1);
+  const uint32_t v_m1_2_0 = ld(-1, 2, 0);
+  const uint32_t v_0_m2_0 = ld(0, -2, 0);
+  const uint32_t v_0_m2_1 = ld(0, -2, 1);
+  const uint32_t v_0_m2_2 = ld(0, -2, 2);
+  const uint32_t v_0_m1_m1 = ld(0, -1, -1);
+  const uint32_t v_0_m1_0 = ld(0, -1, 0);
+  const uint32_t v_0_m1_1 = ld(0, -1, 1);
+  const uint32_t v_0_m1_2 = ld(0, -1, 2);
+  const uint32_t v_0_0_m2 = ld(0, 0, -2);
+  const uint32_t v_0_0_m1 = ld(0, 0, -1);
+  const uint32_t v_0_0_1 = ld(0, 0, 1);
+  const uint32_t v_0_0_2 = ld(0, 0, 2);
+  const uint32_t v_0_1_m2 = ld(0, 1, -2);
+  const uint32_t v_0_1_m1 = ld(0, 1, -1);
+  const uint32_t v_0_1_0 = ld(0, 1, 0);
+  const uint32_t v_0_1_1 = ld(0, 1, 1);
+  const uint32_t v_0_2_m2 = ld(0, 2, -2);
+  const uint32_t v_0_2_m1 = ld(0, 2, -1);
+  const uint32_t v_0_2_0 = ld(0, 2, 0);
+  const uint32_t v_1_m2_0 = ld(1, -2, 0);
+  const uint32_t v_1_m2_1 = ld(1, -2, 1);
+  const uint32_t v_1_m1_m1 = ld(1, -1, -1);
+  const uint32_t v_1_m1_0 = ld(1, -1, 0);
+  const uint32_t v_1_m1_1 = ld(1, -1, 1);
+  const uint32_t v_1_0_m2 = ld(1, 0, -2);
+  const uint32_t v_1_0_m1 = ld(1, 0, -1);
+  const uint32_t v_1_0_0 = ld(1, 0, 0);
+  const uint32_t v_1_0_1 = ld(1, 0, 1);
+  const uint32_t v_1_1_m2 = ld(1, 1, -2);
+  const uint32_t v_1_1_m1 = ld(1, 1, -1);
+  const uint32_t v_1_1_0 = ld(1, 1, 0);
+  const uint32_t v_2_m2_0 = ld(2, -2, 0);
+  const uint32_t v_2_m1_m1 = ld(2, -1, -1);
+  const uint32_t v_2_m1_0 = ld(2, -1, 0);
+  const uint32_t v_2_0_m2 = ld(2, 0, -2);
+  const uint32_t v_2_0_m1 = ld(2, 0, -1);
+  const uint32_t v_2_0_0 = ld(2, 0, 0);
+  const uint32_t m_v_0_0_1 = v_0_0_1 * 0xFFu;
+  const uint32_t m_v_0_0_m1 = v_0_0_m1 * 0xFFu;
+  const uint32_t m_v_0_1_0 = v_0_1_0 * 0xFFu;
+  const uint32_t m_v_0_1_m1 = v_0_1_m1 * 0xFFu;
+  const uint32_t m_v_0_m1_0 = v_0_m1_0 * 0xFFu;
+  const uint32_t m_v_0_m1_1 = v_0_m1_1 * 0xFFu;
+  const uint32_t m_v_1_0_0 = v_1_0_0 * 0xFFu;
+  const uint32_t m_v_1_0_m1 = v_1_0_m1 * 0xFFu;
+  const uint32_t m_v_1_m1_0 = v_1_m1_0 * 0xFFu;
+  const uint32_t m_v_m1_0_0 = v_m1_0_0 * 0xFFu;
+  const uint32_t m_v_m1_0_1 = v_m1_0_1 * 0xFFu;
+  const uint32_t m_v_m1_1_0 = v_m1_1_0 * 0xFFu;
+  F[0] = 1u * 0x01010101u;
+  F[1] = ((v_m1_0_0 + v_0_m1_1 + v_0_1_0) + (v_m1_0_1 + v_0_0_m1 + v_1_m1_0)) + ((v_m1_1_0 + v_0_0_1 + v_1_0_m1) + (v_0_m1_0 + v_0_1_m1 + v_1_0_0));
+  F[2] = ((v_m1_m1_1 + v_1_m1_1) + (v_m1_1_m1 + v_1_1_m1)) + ((v_m1_1_1) + (v_1_m1_m1));
+  F[3] = ((v_m2_0_1 + v_m1_m1_2 + v_m1_2_0 + v_0_1_m2 + v_1_m2_1 + v_1_1_0) + (v_m2_1_0 + v_m1_0_m1 + v_0_m2_1 + v_0_1_1 + v_1_0_m2 + v_2_m1_m1)) + ((v_m2_1_1 + v_m1_0_2 + v_0_m1_m1 + v_0_2_m1 + v_1_0_1 + v_2_m1_0) + (v_m1_m1_0 + v_m1_2_m1 + v_0_m1_2 + v_1_m2_0 + v_1_1_m2 + v_2_0_m1));
+  F[4] = ((v_m2_0_0 + v_0_m2_2 + v_0_2_0) + (v_m2_0_2 + v_0_0_m2 + v_2_m2_0)) + ((v_m2_2_0 + v_0_0_2 + v_2_0_m2) + (v_0_m2_0 + v_0_2_m2 + v_2_0_0));
+  F[5] = (((m_v_0_0_1 & (v_m1_0_1 + v_0_m1_1 + v_0_1_0 + v_1_0_0)) + (v_m1_0_0 & v_m1_0_1) + (v_0_1_m1 & v_0_1_0)) + ((m_v_0_0_m1 & (v_m1_0_0 + v_0_m1_0 + v_0_1_m1 + v_1_0_m1)) + (v_m1_0_0 & v_0_m1_0) + (v_0_1_m1 & v_1_0_m1))) + (((m_v_1_m1_0 & (v_0_m1_0 + v_0_m1_1 + v_1_0_m1 + v_1_0_0)) + (v_m1_0_1 & v_0_m1_1) + (v_0_1_0 & v_1_0_0)) + ((m_v_m1_1_0 & (v_m1_0_0 + v_m1_0_1 + v_0_1_m1 + v_0_1_0)) + (v_0_m1_0 & v_0_m1_1) + (v_1_0_m1 & v_1_0_0)));
+  F[6] = (((m_v_0_0_1 & (v_m1_1_0 + v_m1_1_1 + v_1_m1_0 + v_1_m1_1)) + (m_v_0_m1_0 & (v_m1_m1_1 + v_m1_0_1 + v_1_m1_m1 + v_1_0_m1)) + (v_m1_0_0 & v_m1_1_m1) + (v_1_m1_m1 & v_1_m1_0) + (v_1_0_m1 & v_1_1_m1)) + ((m_v_0_0_m1 & (v_m1_1_m1 + v_m1_1_0 + v_1_m1_m1 + v_1_m1_0)) + (m_v_0_m1_1 & (v_m1_m1_1 + v_m1_0_0 + v_1_m1_1 + v_1_0_0)) + (v_m1_0_1 & v_m1_1_1) + (v_1_m1_m1 & v_1_0_m1) + (v_1_0_0 & v_1_1_m1))) + (((m_v_0_1_0 & (v_m1_0_1 + v_m1_1_1 + v_1_0_m1 + v_1_1_m1)) + (v_m1_m1_1 & v_m1_0_0) + (v_m1_1_m1 & v_m1_1_0) + (v_1_m1_0 & v_1_m1_1)) + ((m_v_0_1_m1 & (v_m1_0_0 + v_m1_1_m1 + v_1_0_0 + v_1_1_m1)) + (v_m1_m1_1 & v_m1_0_1) + (v_m1_1_0 & v_m1_1_1) + (v_1_m1_1 & v_1_0_0)));
+  F[7] = (((m_v_0_0_1 & (v_m1_0_0 + v_m1_0_2 + v_0_m1_0 + v_0_m1_2 + v_0_1_m1 + v_0_1_1 + v_1_0_m1 + v_1_0_1)) + (m_v_0_1_0 & (v_m1_0_0 + v_m1_2_0 + v_0_m1_1 + v_0_1_1 + v_0_2_m1 + v_1_1_0)) + (m_v_0_m1_0 & (v_m1_m1_0 + v_0_m2_1 + v_0_m1_m1 + v_1_m2_0))) + ((m_v_0_0_m1 & (v_m1_0_m1 + v_m1_0_1 + v_0_m1_m1 + v_0_m1_1 + v_0_1_m2 + v_0_1_0 + v_1_0_m2 + v_1_0_0)) + (m_v_0_1_m1 & (v_m1_0_1 + v_m1_2_m1 + v_0_m1_0 + v_0_1_m2 + v_0_2_m1 + v_1_1_m2)) + (m_v_0_m1_1 & (v_m1_m1_2 + v_0_m2_1 + v_0_m1_2 + v_1_m2_1)))) + (((m_v_1_m1_0 & (v_m1_0_0 + v_m1_0_1 + v_0_1_m1 + v_0_1_0 + v_1_m2_0 + v_1_m2_1 + v_2_m1_m1 + v_2_m1_0)) + (m_v_1_0_0 & (v_m1_0_1 + v_0_m1_0 + v_1_0_1 + v_1_1_0 + v_2_m1_0 + v_2_0_m1)) + (m_v_m1_0_0 & (v_m2_0_1 + v_m2_1_0 + v_m1_m1_0 + v_m1_0_m1))) + ((m_v_m1_1_0 & (v_m2_1_0 + v_m2_1_1 + v_m1_2_m1 + v_m1_2_0 + v_0_m1_0 + v_0_m1_1 + v_1_0_m1 + v_1_0_0)) + (m_v_1_0_m1 & (v_m1_0_0 + v_0_m1_1 + v_1_0_m2 + v_1_1_m2 + v_2_m1_m1 + v_2_0_m1)) + (m_v_m1_0_1 & (v_m2_0_1 + v_m2_1_1 + v_m1_m1_2 + v_m1_0_2))));
+  F[8] = (((v_m1_0_0 & v_m1_0_1 & v_m1_1_0) + (v_0_m1_0 & v_0_m1_1 & v_1_m1_0)) + ((v_m1_0_0 & v_0_m1_0 & v_0_0_m1) + (v_0_0_m1 & v_0_1_m1 & v_1_0_m1))) + (((v_m1_0_1 & v_0_m1_1 & v_0_0_1) + (v_0_0_1 & v_0_1_0 & v_1_0_0)) + ((v_m1_1_0 & v_0_1_m1 & v_0_1_0) + (v_1_m1_0 & v_1_0_m1 & v_1_0_0)));
+}
 // C[f] += sum over decorated clusters of class f anchored at this site (its
 // lexicographically smallest member) of the product of integer psi values.
 template <class Loader>

@@ -140,3 +140,26 @@ def test_statistics_edge_cases():
     # no precision requested: equilibrated immediately
     r = sampling.default_equilibration_check(np.arange(5.0), None, sampling.RequestedPrecision())
     assert r.is_equilibrated and r.N_samples_for_equilibration == 0
+
+
+@pytest.mark.parametrize("kind,L,word", [("fcc_binary", (64, 64, 64), True), ("fcc_binary", (20, 12, 10), True),
+                                         ("fcc_binary", (8, 8, 8), False), ("fcc_ternary", (16, 16, 16), False),
+                                         ("fcc_binary", (13, 11, 7), False)])
+def test_colouring_is_proper_host(kind, L, word):
+    """The sweep's colouring (host entry point, no device): no neighbour offset of the
+    basis set joins two sites of one colour; the word layout applies exactly where the
+    four sites i0 + t*L0/4 of every row share a colour."""
+    from casmcode_monte_gb300 import clex
+    import casmcode_monte_gb300.clex.orbits as O
+
+    col, n, w = clex.color_supercell(kind, L)
+    assert w == word
+    assert col.min() == 0 and col.max() == n - 1
+    col3 = col.reshape(L[2], L[1], L[0])
+    for (di, dj, dk) in O.make_basis_set(kind).neighbour_offsets():
+        shifted = np.roll(col3, shift=(-dk, -dj, -di), axis=(0, 1, 2))
+        assert not np.any(shifted == col3)
+    if w:
+        Q = L[0] // 4
+        assert np.array_equal(col3[:, :, :Q], col3[:, :, Q:2 * Q])
+        assert np.array_equal(col3[:, :, :Q], col3[:, :, 3 * Q:])
