@@ -122,7 +122,7 @@ int setup_layout(mg_ce_batch* b, int layout) {
     build_word_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
                      site.data());
   else
-    build_site_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
+    build_site_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, b->model->kind, cstart.data(), entries.data(),
                      site.data());
   cudaFree(b->dcstart);
   cudaFree(b->dentries);

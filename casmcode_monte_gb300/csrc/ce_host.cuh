@@ -181,10 +181,14 @@ inline size_t slab_smem(int L0, int L1, int L2, int S) {
 // by (padded index mod 4) and, inside a group, ordered round-robin over the 32 word banks
 // ((padded index / 4) mod 32).  Lanes of a warp then share the byte offset within their
 // 4-byte word, so every constant neighbour offset keeps their words in distinct banks.
-// Entry = padded index | mirror flags << 24; site[e] = global linear index.
+// Entry = padded index | mirror flags << 24 | Philox word << 30; site[e] = Philox counter
+// word of the site (see sweep_counter: binary basis with L0 = 4Q: the row's sites
+// i0 + tQ share counter i0 + L0 (j + L1 k) and take word t; otherwise counter l, word 0).
 // cstart[S][n_colors + 1].
-inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, int n_colors,
+inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, int n_colors, int kind,
                              int* cstart, uint32_t* entries, uint32_t* site) {
+  const bool word_rng = kind == 0 && L0 % 4 == 0;
+  const int Q = word_rng ? L0 / 4 : L0;
   const int PX = L0 + 2 * CE_HALO, PY = L1 + 2 * CE_HALO;
   // per (colour, residue group, bank): count, then round-robin placement (stack arrays:
   // n_colors <= CE_MAX_COLORS, at most 2^31 sites per bucket)
@@ -236,8 +240,9 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
           else if (j >= L1 - CE_HALO) flags |= 8;
           if (kl < CE_HALO) flags |= 16;
           if (kl >= nk - CE_HALO) flags |= 32;
-          entries[p] = pidx | (flags << 24);
-          site[p] = (uint32_t)l;
+          const int lane = i / Q;
+          entries[p] = pidx | (flags << 24) | ((uint32_t)lane << 30);
+          site[p] = (uint32_t)(l - (long long)lane * Q);
         }
       }
     pos = cbase[n_colors];

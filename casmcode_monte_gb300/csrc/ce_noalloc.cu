@@ -107,7 +107,7 @@ extern "C" int mg_ce_sweep_noalloc(const mg_ce_model* m, int L0, int L1, int L2,
     mg::set_error("Error in mg_ce_sweep_noalloc: colouring needs more than 64 colours");
     return MG_ERR_INVALID;
   }
-  build_site_lists(L0, L1, L2, S, h_color, n_colors, h_cstart, h_entries, h_site);
+  build_site_lists(L0, L1, L2, S, h_color, n_colors, m->kind, h_cstart, h_entries, h_site);
   make_chain_params(m, n_chains, temperature, mu, seeds, nullptr, h_cp);
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);

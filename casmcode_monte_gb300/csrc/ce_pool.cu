@@ -159,7 +159,7 @@ int geometry(mg_ce_pool* p, int L0, int L1, int L2, int S, int* out) {
   }
   std::vector<int> cstart((size_t)S * (g.n_colors + 1));
   std::vector<uint32_t> entries(N), site(N);
-  build_site_lists(L0, L1, L2, S, g.color.data(), g.n_colors, cstart.data(), entries.data(), site.data());
+  build_site_lists(L0, L1, L2, S, g.color.data(), g.n_colors, p->model->kind, cstart.data(), entries.data(), site.data());
   MG_CUDA_TRY(cudaMalloc(&g.dcstart, sizeof(int) * cstart.size()));
   MG_CUDA_TRY(cudaMalloc(&g.dentries, sizeof(uint32_t) * N));
   MG_CUDA_TRY(cudaMalloc(&g.dsite, sizeof(uint32_t) * N));

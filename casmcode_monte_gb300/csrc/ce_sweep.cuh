@@ -6,9 +6,10 @@
 // that same-colour sites share no cluster and are updated concurrently); the change
 // of semi-grand canonical energy is dE = dE_f - mu.(N dx) (basic_semigrand_canonical.hh:
 // 178-192); a proposal is accepted if dE < 0 or u < exp(-beta dE).  Random numbers are
-// Philox4x32-10 keyed by the chain's seed with counter (site, pass, chain, tag), so a
-// trajectory is a pure function of (seed, chain, initial state) independent of the
-// thread mapping.
+// Philox4x32-10 keyed by the chain's seed with counter (q, pass, chain, tag): for the
+// binary basis with L0 = 4Q the four sites i0 + tQ of a row share q = i0 + L0 (j + L1 k)
+// and take words t = 0..3; otherwise q = l (words 0 and 1).  A trajectory is a pure
+// function of (seed, chain, initial state), independent of the thread mapping.
 //
 // Layout: a chain is owned by a cluster of S CTAs; CTA r holds planes
 // [k0(r), k0(r) + nk(r)) of the L0 x L1 x L2 supercell (l = i + L0*(j + L1*k)) plus a
@@ -123,12 +124,12 @@ __device__ __forceinline__ int warp_sum(int v) {
   return v;
 }
 
-// Metropolis decision of one proposal o -> o2 from its integer local features: the FP32
-// fast path, and the exact FP64 decision whenever the FP32 one could differ (|dE32|
-// within the rounding bound, or u within the relative bound of exp(-beta dE)).  Counts
-// FP64 re-decisions in acc[NCLASS] and, in FP32 mode, flipped decisions in
-// acc[NCLASS+1].  Ff[k] is F[k] as a float (exact); Fi(k) returns F[k] as an int and is
-// only called on the FP64 path.
+// Metropolis decision of one proposal o -> o2 from its integer local features, in two
+// parts: fast() is the branch-free FP32 decision and says whether it is ambiguous (|dE32|
+// within the rounding bound, or u within the relative bound of exp(-beta dE)); exact()
+// takes the FP64 decision of an ambiguous proposal, counts it in acc[NCLASS] and, in
+// FP32 mode, counts a flipped decision in acc[NCLASS+1] (the FP32 decision stands there).
+// Ff[k] is F[k] as a float (exact); Fi(k) returns F[k] as an int.
 template <class B>
 struct MetropolisRule {
   static constexpr int NF = B::NFEAT;
@@ -142,9 +143,8 @@ struct MetropolisRule {
   float beta_log2e, dtol, eps;
   int precision;
 
-  template <class FI>
-  __device__ __forceinline__ bool operator()(int o, int o2, const int (&dpsi)[B::NFUNC], const float (&Ff)[NF],
-                                             const FI& Fi, uint32_t x0, int (&acc)[NSLOT]) const {
+  __device__ __forceinline__ bool fast(int o, int o2, const int (&dpsi)[B::NFUNC], const float (&Ff)[NF],
+                                       uint32_t x0, bool& amb) const {
     float G[B::NFUNC];
 #pragma unroll
     for (int b = 0; b < B::NFUNC; ++b) G[b] = 0.f;
@@ -153,47 +153,47 @@ struct MetropolisRule {
     float dE32 = -dmu32[o * NS + o2];
 #pragma unroll
     for (int b = 0; b < B::NFUNC; ++b) dE32 = fmaf((float)dpsi[b], G[b], dE32);
-
     const float u32 = __uint2float_rn(x0) * 2.3283064365386963e-10f;
-    bool amb = false, acc32;
-    if (dE32 < -dtol) {
-      acc32 = true;
+    const float P = fast_exp2(-dE32 * beta_log2e);
+    const bool band = !(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps));
+    amb = !(dE32 < -dtol) && ((dE32 <= dtol) || (x0 == 0u) || band);
+    return (dE32 < 0.f) || (u32 < P);
+  }
+
+  template <class FI>
+  __device__ __forceinline__ bool exact(int o, int o2, const int (&dpsi)[B::NFUNC], const FI& Fi, uint32_t x0,
+                                     bool acc32, int (&acc)[NSLOT]) const {
+    // dE64 = sum_b dpsi_b * (sum_k w64[k] F[k]) - dmu
+    double G64[B::NFUNC];
+#pragma unroll
+    for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
+#pragma unroll
+    for (int k = 0; k < NF; ++k)
+      G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(w->w64[k], (double)Fi(k)));
+    double dE = 0.0;
+#pragma unroll
+    for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
+    dE = __dsub_rn(dE, dmu64[o * NS + o2]);
+    bool acc64;
+    if (dE < 0.0) {
+      acc64 = true;
     } else {
-      const float P = fast_exp2(-dE32 * beta_log2e);
-      acc32 = (dE32 < 0.f) || (u32 < P);
-      if (dE32 <= dtol || x0 == 0u)
-        amb = true;
-      else if (!(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps)))
-        amb = true;
+      const double u = __dmul_rn((double)x0, 2.3283064365386962890625e-10);
+      acc64 = u < exp(__dmul_rn(-dE, beta));
     }
-    bool accept = acc32;
-    if (amb) {
-      // exact FP64 decision: dE64 = sum_b dpsi_b * (sum_k w64[k] F[k]) - dmu
-      double G64[B::NFUNC];
-#pragma unroll
-      for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
-#pragma unroll
-      for (int k = 0; k < NF; ++k)
-        G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(w->w64[k], (double)Fi(k)));
-      double dE = 0.0;
-#pragma unroll
-      for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
-      dE = __dsub_rn(dE, dmu64[o * NS + o2]);
-      bool acc64;
-      if (dE < 0.0) {
-        acc64 = true;
-      } else {
-        const double u = __dmul_rn((double)x0, 2.3283064365386962890625e-10);
-        acc64 = u < exp(__dmul_rn(-dE, beta));
-      }
-      acc[NC] += 1;
-      if (precision == 0) {
-        accept = acc64;
-      } else if (acc64 != acc32) {
-        acc[NC + 1] += 1;
-      }
-    }
-    return accept;
+    acc[NC] += 1;
+    if (precision == 0) return acc64;
+    if (acc64 != acc32) acc[NC + 1] += 1;
+    return acc32;
+  }
+
+  template <class FI>
+  __device__ __forceinline__ bool operator()(int o, int o2, const int (&dpsi)[B::NFUNC], const float (&Ff)[NF],
+                                             const FI& Fi, uint32_t x0, int (&acc)[NSLOT]) const {
+    bool amb;
+    const bool acc32 = fast(o, o2, dpsi, Ff, x0, amb);
+    if (amb) return exact(o, o2, dpsi, Fi, x0, acc32, acc);
+    return acc32;
   }
 };
 
@@ -273,8 +273,14 @@ struct SiteSweeper {
   }
 };
 
+// word `w` (0..3) of a Philox block
+__device__ __forceinline__ uint32_t philox_word(const U32x4& x, uint32_t w) {
+  return w == 0u ? x.x : (w == 1u ? x.y : (w == 2u ? x.z : x.w));
+}
+
 // Philox words of the first PRE sites of a thread in one colour phase, drawn ahead of
-// the phase (they depend on (site, pass, chain) only, not on the lattice).
+// the phase (they depend on (site, pass, chain) only, not on the lattice).  The list
+// holds each site's counter word and, in the entry's top two bits, the word it takes.
 template <int PRE>
 struct PhasePrefetch {
   uint32_t ent[PRE], x0[PRE], x1[PRE];
@@ -290,7 +296,7 @@ struct PhasePrefetch {
       if (e < ee) {
         ent[q] = __ldg(entries + e);
         const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
-        x0[q] = x.x;
+        x0[q] = philox_word(x, ent[q] >> 30);
         x1[q] = x.y;
       }
     }
@@ -319,7 +325,7 @@ __device__ __forceinline__ void sweep_phase(const SiteSweeper<B>& sw, const Phas
     int o;
     int F[B::NFEAT];
     sw.gather(ent, o, F);
-    sw.decide(ent, x.x, x.y, o, F, acc);
+    sw.decide(ent, philox_word(x, ent >> 30), x.y, o, F, acc);
   }
 }
 
@@ -518,6 +524,14 @@ __device__ __forceinline__ float byte_as_float(uint32_t w, int t) {
   return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + (unsigned)t)) - 8388608.0f;
 }
 
+// F[k] of one byte lane, as an int (FP64 re-decisions)
+template <int NF>
+struct QuadFeature {
+  const uint32_t (&F)[NF];
+  int shift;
+  __device__ __forceinline__ int operator()(int k) const { return (int)((F[k] >> shift) & 0xFFu); }
+};
+
 template <class B>
 struct QuadSweeper {
   static constexpr int NF = B::NFEAT;
@@ -539,7 +553,8 @@ struct QuadSweeper {
     uint32_t F[NF];
     B::features_quad(WordLoader{p, RS, RSY}, F);
     const uint32_t v = *p;
-    uint32_t flip = 0u, sgn = 0u;
+    // FP32 decisions of the four sites (branch-free, interleaved)
+    bool acc32[4], amb[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int o = (int)((v >> (8 * t)) & 1u);
@@ -547,11 +562,26 @@ struct QuadSweeper {
       float Ff[NF];
 #pragma unroll
       for (int k = 0; k < NF; ++k) Ff[k] = byte_as_float(F[k], t);
-      const bool accept =
-          rule(o, 1 - o, dpsi, Ff, [&](int k) { return (int)((F[k] >> (8 * t)) & 0xFFu); }, x0[t], acc);
-      if (accept) {
-        flip |= 1u << (8 * t);
-        sgn |= (o ? 0xFFu : 0x01u) << (8 * t);
+      acc32[t] = rule.fast(o, 1 - o, dpsi, Ff, x0[t], amb[t]);
+    }
+    // exact FP64 decisions where the FP32 one is ambiguous (rare)
+    if (amb[0] || amb[1] || amb[2] || amb[3]) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (amb[t]) {
+          const int o = (int)((v >> (8 * t)) & 1u);
+          const int dpsi[1] = {1 - 2 * o};
+          acc32[t] = rule.exact(o, 1 - o, dpsi, QuadFeature<NF>{F, 8 * t}, x0[t], acc32[t], acc);
+        }
+      }
+    }
+    uint32_t flip = 0u, sgn = 0u;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const uint32_t bit = 1u << (8 * t);
+      if (acc32[t]) {
+        flip |= bit;
+        sgn |= (v & bit) ? (0xFFu << (8 * t)) : bit;
       }
     }
     if (flip) {
@@ -583,7 +613,8 @@ struct QuadSweeper {
   }
 };
 
-// Philox words of the first word of a thread in one colour phase (four sites)
+// Philox block of the first word of a thread in one colour phase: its four sites take
+// words 0..3 of the block with counter (site of byte 0, pass, chain, tag)
 struct QuadPrefetch {
   uint32_t ent, x0[4];
 
@@ -594,10 +625,11 @@ struct QuadPrefetch {
     const int e = cstart[c] + threadIdx.x;
     if (e < cstart[c + 1]) {
       ent = __ldg(entries + e);
-      const uint32_t l0 = __ldg(site_l + e);
-#pragma unroll
-      for (int t = 0; t < 4; ++t)
-        x0[t] = philox4x32_10(U32x4{l0 + (uint32_t)(t * Q), pass, chain_id, SWEEP_TAG}, key0, key1).x;
+      const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
+      x0[0] = x.x;
+      x0[1] = x.y;
+      x0[2] = x.z;
+      x0[3] = x.w;
     }
   }
 };
@@ -612,11 +644,8 @@ __device__ __forceinline__ void sweep_phase_quad(const QuadSweeper<B>& sw, const
 #pragma unroll 1
   for (int e = e0 + NT; e < e_end; e += NT) {
     const uint32_t ent = __ldg(entries + e);
-    const uint32_t l0 = __ldg(site_l + e);
-    uint32_t x0[4];
-#pragma unroll
-    for (int t = 0; t < 4; ++t)
-      x0[t] = philox4x32_10(U32x4{l0 + (uint32_t)(t * sw.Q), pass, chain_id, SWEEP_TAG}, key0, key1).x;
+    const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
+    const uint32_t x0[4] = {x.x, x.y, x.z, x.w};
     sw.update(ent, x0, acc);
   }
 }

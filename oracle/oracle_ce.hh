@@ -17,8 +17,8 @@
 // distances, canonical form).
 //
 // Also here: a restatement of the coloured-sweep algorithm of the GPU kernels (Philox4x32-10
-// keyed by (seed), counter (site, pass, chain, tag); one visit per site per pass in colour
-// order), used to check those kernels trajectory-for-trajectory.
+// keyed by (seed), counters as in sweep_counter below; one visit per site per pass in
+// colour order), used to check those kernels trajectory-for-trajectory.
 #pragma once
 #include <algorithm>
 #include <array>
@@ -380,10 +380,26 @@ struct ColoredRun {
   std::vector<long long> n_accept;           // [pass]
 };
 
+// Philox block of a site and the word of it the site uses.  Binary basis with L0 = 4Q:
+// the four sites i0 + tQ (0 <= i0 < Q) of a row share the block with counter word
+// q = i0 + L0 (j + L1 k) and site i0 + tQ takes word t.  Otherwise (ternary basis, or L0
+// not a multiple of 4) site l has its own block (counter word l) and takes words 0
+// (acceptance) and 1 (choice of the new species).
+inline void sweep_counter(const CESupercell& S, long l, uint32_t* q, int* word) {
+  if (S.basis.n_species == 2 && S.L0 % 4 == 0) {
+    const long Q = S.L0 / 4, i = l % S.L0;
+    *q = (uint32_t)(l - (i / Q) * Q);
+    *word = (int)(i / Q);
+  } else {
+    *q = (uint32_t)l;
+    *word = 0;
+  }
+}
+
 // Coloured semi-grand canonical sweep: pass p, colour c = 0..nc-1, every site of colour c
 // visited once (order irrelevant: same-colour sites share no cluster).  Proposal:
 // binary o -> 1-o; ternary o -> (o + 1 + (x1 >> 31)) % 3.  Acceptance (metropolis.hh:26-35
-// with u = x0 * 2^-32 from the site's Philox block): dE < 0 or u < exp(-beta dE).
+// with u = x0 * 2^-32, x0 the site's word of its Philox block): dE < 0 or u < exp(-beta dE).
 inline ColoredRun colored_sweep(const CESupercell& S, int* occ, double T,
                                 const std::vector<double>& mu, uint64_t seed, uint32_t chain,
                                 const std::vector<int>& color, int n_colors, long pass0,
@@ -397,7 +413,11 @@ inline ColoredRun colored_sweep(const CESupercell& S, int* occ, double T,
     long long nacc = 0;
     for (int c = 0; c < n_colors; ++c) {
       for (long l : by_color[c]) {
-        auto x = philox4x32_10({(uint32_t)l, (uint32_t)p, chain, SWEEP_TAG}, key);
+        uint32_t q;
+        int word;
+        sweep_counter(S, l, &q, &word);
+        auto x = philox4x32_10({q, (uint32_t)p, chain, SWEEP_TAG}, key);
+        const uint32_t x0 = x[word];
         int o = occ[l];
         int o2 = (S.basis.n_species == 2) ? 1 - o : (o + 1 + (int)(x[1] >> 31)) % 3;
         double dE = S.delta_formation(occ, l, o2) - S.mu_dot_Ndx(mu, o, o2);
@@ -405,7 +425,7 @@ inline ColoredRun colored_sweep(const CESupercell& S, int* occ, double T,
         if (dE < 0.0) {
           acc = true;
         } else {
-          double u = (double)x[0] * (1.0 / 4294967296.0);
+          double u = (double)x0 * (1.0 / 4294967296.0);
           acc = u < std::exp(-dE * beta);
         }
         if (acc) {
