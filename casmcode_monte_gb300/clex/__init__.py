@@ -94,16 +94,19 @@ class ClexModel:
         return np.stack([nB, nC], axis=-1).astype(np.float64)
 
 
-def color_supercell(kind: str, shape) -> tuple[np.ndarray, int, bool]:
+LAYOUTS = {0: "byte", 1: "word", 2: "word_pipelined"}
+
+
+def color_supercell(kind: str, shape) -> tuple[np.ndarray, int, str]:
     """The sweep's colouring of a supercell (host only): (colour per site, number of
-    colours, whether the four-sites-per-word layout applies)."""
+    colours, the layout a batch of this shape uses: "byte", "word" or "word_pipelined")."""
     L0, L1, L2 = (int(x) for x in shape)
     col = np.zeros(L0 * L1 * L2, dtype=np.int32)
     word = C.c_int()
     n = _lib.lib().mg_ce_color_supercell(BASIS_KINDS[kind], L0, L1, L2, _lib.ptr(col, C.c_int32), C.byref(word))
     if n <= 0:
         _lib.check(-n if n else 1)
-    return col, n, bool(word.value)
+    return col, n, LAYOUTS[word.value]
 
 
 class ChainBatch:
@@ -145,14 +148,16 @@ class ChainBatch:
         _lib.check(_lib.lib().mg_ce_batch_info(self._h, C.byref(S), C.byref(nc), C.byref(nt), C.byref(sm)))
         _lib.check(_lib.lib().mg_ce_batch_layout(self._h, C.byref(lay)))
         self.ctas_per_chain, self.n_colors, self.threads, self.smem_bytes = S.value, nc.value, nt.value, sm.value
-        self.layout = "word" if lay.value == 1 else "byte"
+        self.layout = LAYOUTS[lay.value]
 
     def set_layout(self, layout: str) -> None:
-        """Sweep with one site per byte ("byte") or four sites per word ("word", binary
-        basis with L0 a multiple of 4); trajectories are identical."""
-        if layout not in ("byte", "word"):
-            raise ValueError("layout must be 'byte' or 'word'")
-        _lib.check(_lib.lib().mg_ce_batch_set_layout(self._h, 1 if layout == "word" else 0))
+        """Sweep with one site per byte ("byte"), four sites per word ("word", binary
+        basis with L0 a multiple of 4) or four sites per word with the features split
+        around the phase barrier ("word_pipelined"); trajectories are identical."""
+        codes = {v: k for k, v in LAYOUTS.items()}
+        if layout not in codes:
+            raise ValueError(f"layout must be one of {sorted(codes)}")
+        _lib.check(_lib.lib().mg_ce_batch_set_layout(self._h, codes[layout]))
         self._read_info()
 
     def close(self) -> None:

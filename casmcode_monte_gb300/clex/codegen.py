@@ -103,6 +103,140 @@ def _quad_features(bs, offs) -> list:
     return out
 
 
+# Linear colourings (a i + b j + c k) mod m of the word-layout pipelines: a = 4 keeps the
+# four sites i0 + tQ of a row in one colour whenever L0 is a multiple of 16; (b, c) are
+# chosen so that a site has the fewest neighbours in the colour proposed just before its
+# own.  Valid when a L0, b L1, c L2 are multiples of m (L0, L1 multiples of 16 and L2 of 8
+# for the first; L0, L2 of 16 and L1 of 8 for the second).
+PIPELINE_COLOURINGS = [(4, 5, 14, 16), (4, 6, 15, 16)]
+
+
+def late_offsets(offs, colouring) -> list:
+    """Neighbour offsets whose colour is one less (mod m) than the site's own."""
+    a, b, c, m = colouring
+    assert all((a * o[0] + b * o[1] + c * o[2]) % m for o in offs), "colouring is not proper"
+    return [o for o in offs if (a * o[0] + b * o[1] + c * o[2]) % m == m - 1]
+
+
+def _factor_pairs(pairs, prefer=None) -> tuple[list, set]:
+    """Sum of (x & y) pair products as masked partner sums: mask(v) & (sum of v's
+    partners), for the variable v in most remaining pairs (or only variables in
+    ``prefer``); returns the expression parts and the masks used."""
+    parts, masks = [], set()
+    pairs = list(pairs)
+    while pairs:
+        count: dict = {}
+        for a, b in pairs:
+            for v in (a, b):
+                if prefer is None or v in prefer:
+                    count[v] = count.get(v, 0) + 1
+        if not count:
+            parts += [f"({a} & {b})" for a, b in pairs]
+            break
+        v = max(sorted(count), key=lambda x: count[x])
+        if count[v] < 2 and prefer is None:
+            parts += [f"({a} & {b})" for a, b in pairs]
+            break
+        partners = [b if a == v else a for a, b in pairs if v in (a, b)]
+        pairs = [t for t in pairs if v not in t]
+        if len(partners) == 1:
+            parts.append(f"({v} & {partners[0]})")
+        else:
+            masks.add(v)
+            parts.append(f"(m_{v} & ({' + '.join(partners)}))")
+    return parts, masks
+
+
+def _and(vs) -> str:
+    return vs[0] if len(vs) == 1 else "(" + " & ".join(vs) + ")"
+
+
+def _quad_pipelines(bs, offs) -> list:
+    """Split byte-parallel features for the word-layout pipelines (see PIPELINE_COLOURINGS).
+
+    For colouring p, early() runs while the previous colour's phase may still be writing:
+    it loads every neighbour except the late ones (colour one less than the site's) and
+    sums the cluster terms free of late neighbours into E[k].  A term with late part L
+    and stable part R contributes AND(L) * AND(R); the terms of feature k that share L
+    are summed early into one kept word K = sum AND(R), so that late() only loads the late
+    neighbours and adds mask(AND(L)) & K (mask = 0xFF per set byte)."""
+    out = ["// ---- word-layout pipelines (early / late split of features_quad)",
+           f"constexpr int NPIPE = {len(PIPELINE_COLOURINGS)};",
+           "__host__ __device__ constexpr int pipe_colouring(int p, int q) {",
+           "  constexpr int t[NPIPE * 4] = {" + ", ".join(str(x) for col in PIPELINE_COLOURINGS for x in col) + "};",
+           "  return t[p * 4 + q];  // a, b, c, m",
+           "}",
+           "template <int P>",
+           "struct Pipe;"]
+    for p, col in enumerate(PIPELINE_COLOURINGS):
+        late_offs = late_offsets(offs, col)
+        late = set(_var(o) for o in late_offs)
+        stable = [o for o in offs if _var(o) not in late]
+        early_lines, masks = [], set()
+        kept = []    # (name, expression) computed early
+        late_lines = []
+        for k, f in enumerate(bs.features):
+            terms = [tuple(_var(o) for o, _ in t) for t in f.terms]
+            if all(len(t) == 0 for t in terms):
+                early_lines.append(f"    s.E[{k}] = {len(terms)}u * 0x01010101u;")
+                late_lines.append(f"    F[{k}] = s.E[{k}];")
+                continue
+            early_t = [t for t in terms if not (set(t) & late)]
+            parts = [t[0] for t in early_t if len(t) == 1]
+            pp, mm = _factor_pairs([t for t in early_t if len(t) == 2])
+            parts += pp
+            masks |= mm
+            parts += [_and(t) for t in early_t if len(t) >= 3]
+            early_lines.append(f"    s.E[{k}] = " + (_sum_expr(parts) if parts else "0u") + ";")
+            groups: dict = {}
+            for t in terms:
+                Lp = tuple(v for v in t if v in late)
+                if Lp:
+                    groups.setdefault(Lp, []).append(tuple(v for v in t if v not in late))
+            lparts = []
+            for Lp, Rs in sorted(groups.items()):
+                if all(len(R) == 0 for R in Rs):
+                    lparts += [_and(list(Lp))] * len(Rs)
+                elif len(Rs) == 1:
+                    # one term: AND(L) & AND(R), AND(R) kept
+                    kept.append((f"K{len(kept)}", _and(list(Rs[0]))))
+                    lparts.append(f"({_and(list(Lp))} & s.K[{len(kept) - 1}])")
+                else:
+                    kexpr = " + ".join(_and(list(R)) if R else "0x01010101u" for R in Rs)
+                    kept.append((f"K{len(kept)}", kexpr))
+                    lparts.append(f"((({_and(list(Lp))}) * 0xFFu) & s.K[{len(kept) - 1}])")
+            late_lines.append(f"    F[{k}] = s.E[{k}]" + ("".join(" + " + x for x in lparts)) + ";")
+        out.append(f"// colouring ({col[0]} i + {col[1]} j + {col[2]} k) mod {col[3]}: late neighbours "
+                   + ", ".join(str(tuple(o)) for o in late_offs))
+        out.append("template <>")
+        out.append(f"struct Pipe<{p}> {{")
+        out.append(f"  static constexpr int NKEEP = {max(1, len(kept))};")
+        out.append("  struct State {")
+        out.append("    uint32_t E[NFEAT];")
+        out.append("    uint32_t K[NKEEP];")
+        out.append("    uint32_t own;")
+        out.append("  };")
+        out.append("  template <class Loader>")
+        out.append("  __device__ static __forceinline__ void early(const Loader& ld, State& s) {")
+        for o in stable:
+            out.append(f"    const uint32_t {_var(o)} = ld({o[0]}, {o[1]}, {o[2]});")
+        out.append("    s.own = ld(0, 0, 0);")
+        for v in sorted(masks):
+            out.append(f"    const uint32_t m_{v} = {v} * 0xFFu;")
+        out += early_lines
+        for i, (_, kexpr) in enumerate(kept):
+            out.append(f"    s.K[{i}] = {kexpr};")
+        out.append("  }")
+        out.append("  template <class Loader>")
+        out.append("  __device__ static __forceinline__ void late(const Loader& ld, const State& s, uint32_t (&F)[NFEAT]) {")
+        for o in late_offs:
+            out.append(f"    const uint32_t {_var(o)} = ld({o[0]}, {o[1]}, {o[2]});")
+        out += late_lines
+        out.append("  }")
+        out.append("};")
+    return out
+
+
 def generate(kind: str) -> tuple[str, dict]:
     bs = O.make_basis_set(kind)
     basis = bs.basis
@@ -179,6 +313,7 @@ def generate(kind: str) -> tuple[str, dict]:
 
     if basis.name == "occupation":
         lines += _quad_features(bs, offs)
+        lines += _quad_pipelines(bs, offs)
 
     # anchored correlations
     anc_offs = sorted({o for cls in bs.anchored for t in cls for o, _ in t})

@@ -18,7 +18,8 @@ struct mg_ce_batch {
   int L0 = 0, L1 = 0, L2 = 0, n_chains = 0, precision = 0;
   long long N = 0;
   int S = 1, PX = 0, PY = 0, PZ = 0, n_colors = 0, threads = 0;
-  int layout = 0;          // 0: one site per byte; 1: four sites per word (binary basis)
+  int layout = 0;          // 0: one site per byte; 1: four sites per word (binary basis); 2: 1 pipelined
+  int pipe = -1;           // pipeline colouring id of the colouring, or -1
   int ctas_requested = 0;  // 0: chosen by occupancy
   size_t smem = 0;
   long long pass = 0;
@@ -115,10 +116,10 @@ int setup_layout(mg_ce_batch* b, int layout) {
     set_error("Error in mg_ce_batch_create: slab too large for 24-bit shared-memory indices");
     return MG_ERR_INVALID;
   }
-  const long long n_entries = layout == 1 ? b->N / 4 : b->N;
+  const long long n_entries = layout >= 1 ? b->N / 4 : b->N;
   std::vector<int> cstart((size_t)S * (b->n_colors + 1), 0);
   std::vector<uint32_t> entries(n_entries), site(n_entries);
-  if (layout == 1)
+  if (layout >= 1)
     build_word_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
                      site.data());
   else
@@ -141,7 +142,7 @@ int setup_layout(mg_ce_batch* b, int layout) {
   b->S = S;
   b->smem = smem;
   b->PZ = (b->L2 + S - 1) / S + 2 * mg::CE_HALO;
-  b->threads = layout == 1 ? mg::host::NT_QUAD : (m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY);
+  b->threads = layout >= 1 ? mg::host::NT_QUAD : (m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY);
   return MG_OK;
 }
 
@@ -239,13 +240,13 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
 
   // colouring, then the layout (word layout where the basis and colouring allow it)
   b->color.assign(N, -1);
-  b->n_colors = color_supercell(L0, L1, L2, m->kind, b->color.data());
+  b->n_colors = color_supercell(L0, L1, L2, m->kind, b->color.data(), &b->pipe);
   if (b->n_colors < 1) {
     set_error("Error in mg_ce_batch_create: colouring needs more than 64 colours");
     delete b;
     return MG_ERR_INVALID;
   }
-  const int layout = quad_eligible(m->kind, L0, L1, L2, b->color.data()) ? 1 : 0;
+  const int layout = !quad_eligible(m->kind, L0, L1, L2, b->color.data()) ? 0 : (b->pipe >= 0 ? 2 : 1);
   b->hcp.resize(n_chains);
   make_chain_params(m, n_chains, temperature, mu, seeds, chain_ids, b->hcp.data());
 
@@ -266,7 +267,7 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   MGX(cudaMemcpyAsync(b->dcp, b->hcp.data(), sizeof(mg::CeChainParams) * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
 #undef MGX
   int rc = setup_layout(b, layout);
-  if (rc == MG_ERR_INVALID && layout == 1) rc = setup_layout(b, 0);  // e.g. a CTA count only the byte layout fits
+  if (rc == MG_ERR_INVALID && layout >= 1) rc = setup_layout(b, 0);  // e.g. a CTA count only the byte layout fits
   if (rc != MG_OK) {
     free_batch(b);
     return rc;
@@ -294,12 +295,13 @@ int mg_ce_color_supercell(int basis_kind, int L0, int L1, int L2, int32_t* color
     set_error("Error in mg_ce_color_supercell: invalid argument");
     return -MG_ERR_INVALID;
   }
-  const int n = color_supercell(L0, L1, L2, basis_kind, color);
+  int pipe = -1;
+  const int n = color_supercell(L0, L1, L2, basis_kind, color, &pipe);
   if (n < 1) {
     set_error("Error in mg_ce_color_supercell: colouring needs more than 64 colours");
     return -MG_ERR_INVALID;
   }
-  if (word_layout) *word_layout = quad_eligible(basis_kind, L0, L1, L2, color) ? 1 : 0;
+  if (word_layout) *word_layout = !quad_eligible(basis_kind, L0, L1, L2, color) ? 0 : (pipe >= 0 ? 2 : 1);
   return n;
 }
 
@@ -313,13 +315,18 @@ int mg_ce_batch_layout(const mg_ce_batch* b, int* layout) {
 }
 
 int mg_ce_batch_set_layout(mg_ce_batch* b, int layout) {
-  if (!b || (layout != 0 && layout != 1)) {
+  if (!b || layout < 0 || layout > 2) {
     set_error("Error in mg_ce_batch_set_layout: invalid argument");
     return MG_ERR_INVALID;
   }
-  if (layout == 1 && !quad_eligible(b->model->kind, b->L0, b->L1, b->L2, b->color.data())) {
+  if (layout >= 1 && !quad_eligible(b->model->kind, b->L0, b->L1, b->L2, b->color.data())) {
     set_error("Error in mg_ce_batch_set_layout: the word layout needs the binary basis, L0 = 4Q with Q >= 4 "
               "and a colouring with colour(i + Q) = colour(i)");
+    return MG_ERR_INVALID;
+  }
+  if (layout == 2 && b->pipe < 0) {
+    set_error("Error in mg_ce_batch_set_layout: the pipelined word layout needs one of the generated pipeline "
+              "colourings");
     return MG_ERR_INVALID;
   }
   if (layout == b->layout) return MG_OK;
@@ -353,7 +360,7 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   MG_CUDA_TRY(cudaEventRecord(b->ev0, b->stream));
   SweepLaunch L{b->L0, b->L1, b->L2, b->S, b->n_colors, b->n_chains, b->precision, b->dcstart, b->dentries,
                 b->dsite, b->dcp, b->docc, b->pass, n_passes, b->dout, b->stream};
-  int rc = b->layout == 1 ? launch_sweep_quad(b->model, L) : launch_sweep(b->model, L);
+  int rc = b->layout >= 1 ? launch_sweep_quad(b->model, L, b->layout == 2 ? b->pipe : -1) : launch_sweep(b->model, L);
   if (rc != MG_OK) return rc;
   MG_CUDA_TRY(cudaEventRecord(b->ev1, b->stream));
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, b->dout, sizeof(long long) * need, cudaMemcpyDeviceToHost, b->stream));

@@ -47,7 +47,9 @@ namespace mg {
   template <class L>                                                                     \
   __device__ static __forceinline__ void features_quad(const L& ld, uint32_t(&F)[NFEAT]) { \
     fcc_binary::features_quad(ld, F);                                                    \
-  }
+  }                                                                                      \
+  template <int P>                                                                       \
+  using Pipe = fcc_binary::Pipe<P>;
 MG_BASIS_ADAPTER(FccBinary, fcc_binary, MG_QUAD_FEATURES)
 MG_BASIS_ADAPTER(FccTernary, fcc_ternary, )
 #undef MG_QUAD_FEATURES
@@ -98,13 +100,31 @@ inline const int* offsets(int kind, int* n) {
 // Linear colouring (a*i + b*j + c*k) mod m when a*L0, b*L1, c*L2 are multiples of m and no
 // neighbour offset maps to 0 mod m (smallest such m); else greedy in lexicographic order.
 // Returns the number of colours, or -1 if more than CE_MAX_COLORS would be needed.
-inline int color_supercell(int L0, int L1, int L2, int kind, int32_t* col) {
+// Binary basis: at each m, the colourings of the word-layout pipelines come first (their
+// id is returned in *pipe, else -1), then colourings with colour(i + L0/4) = colour(i)
+// (the word layout groups the four sites i0 + t*L0/4 of a row).
+inline int color_supercell(int L0, int L1, int L2, int kind, int32_t* col, int* pipe = nullptr) {
   int noff = 0;
   const int* off = offsets(kind, &noff);
-  // binary basis: prefer, at each m, a colouring with colour(i + L0/4) = colour(i) (the
-  // word layout groups the four sites i0 + t*L0/4 of a row)
   const bool want_quad = kind == 0 && L0 % 4 == 0;
-  for (int m = 2; m <= 32; ++m)
+  if (pipe) *pipe = -1;
+  auto fill_linear = [&](long long a, long long b, long long c, int m) {
+    for (int k = 0; k < L2; ++k)
+      for (int j = 0; j < L1; ++j)
+        for (int i = 0; i < L0; ++i)
+          col[i + (long long)L0 * (j + (long long)L1 * k)] = (int32_t)((a * i + b * j + c * k) % m);
+  };
+  for (int m = 2; m <= 32; ++m) {
+    if (want_quad)
+      for (int p = 0; p < fcc_binary::NPIPE; ++p) {
+        const long long a = fcc_binary::pipe_colouring(p, 0), b = fcc_binary::pipe_colouring(p, 1),
+                        c = fcc_binary::pipe_colouring(p, 2);
+        if (fcc_binary::pipe_colouring(p, 3) != m) continue;
+        if ((a * L0) % m || (b * L1) % m || (c * L2) % m || (a * (L0 / 4)) % m) continue;
+        fill_linear(a, b, c, m);
+        if (pipe) *pipe = p;
+        return m;
+      }
     for (int pref = want_quad ? 1 : 0; pref >= 0; --pref)
     for (int a = 0; a < m; ++a)
       for (int b = 0; b < m; ++b)
@@ -118,13 +138,10 @@ inline int color_supercell(int L0, int L1, int L2, int kind, int32_t* col) {
             ok = v != 0;
           }
           if (!ok) continue;
-          for (int k = 0; k < L2; ++k)
-            for (int j = 0; j < L1; ++j)
-              for (int i = 0; i < L0; ++i)
-                col[i + (long long)L0 * (j + (long long)L1 * k)] =
-                    (int32_t)((1LL * a * i + 1LL * b * j + 1LL * c * k) % m);
+          fill_linear(a, b, c, m);
           return m;
         }
+  }
   // greedy: neighbour coordinates from per-axis wrap tables (offsets lie in [-HALO, HALO])
   const long long N = (long long)L0 * L1 * L2;
   for (long long l = 0; l < N; ++l) col[l] = -1;
@@ -400,16 +417,18 @@ int max_active_clusters_k(Kern kern, int NT, int S, size_t smem, int* out) {
 }
 
 // layout 0: one site per byte (ce_sweep_kernel); layout 1: four sites per word
-// (ce_sweep_quad_kernel, binary basis)
+// (ce_sweep_quad_kernel, binary basis); layout 2: the same with pipelined features
 inline int max_active_chains(int kind, int S, size_t smem, int* out, int layout = 0) {
   if (layout == 1)
-    return max_active_clusters_k(ce_sweep_quad_kernel<FccBinary, NT_QUAD>, NT_QUAD, S, smem, out);
+    return max_active_clusters_k(ce_sweep_quad_kernel<FccBinary, NT_QUAD, -1>, NT_QUAD, S, smem, out);
+  if (layout == 2)
+    return max_active_clusters_k(ce_sweep_quad_kernel<FccBinary, NT_QUAD, 0>, NT_QUAD, S, smem, out);
   return kind == 0 ? max_active_clusters_k(ce_sweep_kernel<FccBinary, NT_BINARY>, NT_BINARY, S, smem, out)
                    : max_active_clusters_k(ce_sweep_kernel<FccTernary, NT_TERNARY>, NT_TERNARY, S, smem, out);
 }
 
 inline size_t layout_smem(int layout, int L0, int L1, int L2, int S) {
-  return layout == 1 ? quad_smem(L0, L1, L2, S) : slab_smem(L0, L1, L2, S);
+  return layout >= 1 ? quad_smem(L0, L1, L2, S) : slab_smem(L0, L1, L2, S);
 }
 
 // CTAs per chain: requested (validated) or the S minimising waves(S)/S over the
@@ -513,7 +532,8 @@ int launch_sweep_t(const mg_ce_model* m, const SweepLaunch& L) {
   return MG_OK;
 }
 
-inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L) {
+// pipe < 0: generic word-layout kernel; pipe >= 0: pipelined kernel of that colouring
+inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L, int pipe) {
   using B = FccBinary;
   CeQuadArgs<B::NFEAT> A;
   A.g.L0 = L.L0;
@@ -539,7 +559,9 @@ inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L) {
   A.precision = L.precision;
   A.out = L.out;
   const size_t smem = quad_smem(L.L0, L.L1, L.L2, L.S);
-  auto kern = ce_sweep_quad_kernel<B, NT_QUAD>;
+  static_assert(fcc_binary::NPIPE == 2, "one kernel instance per pipeline colouring");
+  auto kern = pipe == 0 ? ce_sweep_quad_kernel<B, NT_QUAD, 0>
+                        : (pipe == 1 ? ce_sweep_quad_kernel<B, NT_QUAD, 1> : ce_sweep_quad_kernel<B, NT_QUAD, -1>);
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);

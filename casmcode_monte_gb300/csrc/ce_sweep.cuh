@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "mg_common.cuh"
 
@@ -545,14 +546,22 @@ struct QuadSweeper {
   int Q, dJ, dKp, dKn;
   MetropolisRule<B> rule;
 
-  // one word: features of its four sites, four decisions, write-back of the flips
+  __device__ __forceinline__ WordLoader loader(uint32_t ent) const {
+    return WordLoader{s + (int)(ent & 0xFFFFFFu), RS, RSY};
+  }
+
+  // one word: features of its four sites, then finish()
   __device__ __forceinline__ void update(uint32_t ent, const uint32_t (&x0)[4], int (&acc)[NSLOT]) const {
+    uint32_t F[NF];
+    B::features_quad(loader(ent), F);
+    finish(ent, s[(int)(ent & 0xFFFFFFu)], F, x0, acc);
+  }
+
+  // four decisions from the word's features F and value v, write-back of the flips
+  __device__ __forceinline__ void finish(uint32_t ent, uint32_t v, const uint32_t (&F)[NF], const uint32_t (&x0)[4],
+                                         int (&acc)[NSLOT]) const {
     const int pw = (int)(ent & 0xFFFFFFu);
     const uint32_t flags = ent >> 24;
-    const uint32_t* p = s + pw;
-    uint32_t F[NF];
-    B::features_quad(WordLoader{p, RS, RSY}, F);
-    const uint32_t v = *p;
     // FP32 decisions of the four sites (branch-free, interleaved)
     bool acc32[4], amb[4];
 #pragma unroll
@@ -634,6 +643,53 @@ struct QuadPrefetch {
   }
 };
 
+// Pipelined variant (colouring with a generated early/late split, B::Pipe<P>): besides
+// the Philox block, the first word's early() part (every neighbour not of the colour
+// proposed just before) is computed between the cluster arrive and wait of the previous
+// phase; after the wait only late() remains.
+template <class B, int P>
+struct QuadPipePrefetch {
+  uint32_t ent, x0[4];
+  typename B::template Pipe<P>::State st;
+
+  template <int NT>
+  __device__ __forceinline__ void prepare(const QuadSweeper<B>& sw, const int* cstart, int c, const uint32_t* entries,
+                                          const uint32_t* site_l, uint32_t pass, uint32_t chain_id, uint32_t key0,
+                                          uint32_t key1) {
+    const int e = cstart[c] + threadIdx.x;
+    if (e < cstart[c + 1]) {
+      ent = __ldg(entries + e);
+      const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
+      x0[0] = x.x;
+      x0[1] = x.y;
+      x0[2] = x.z;
+      x0[3] = x.w;
+      B::template Pipe<P>::early(sw.loader(ent), st);
+    }
+  }
+};
+
+template <class B, int NT, int P>
+__device__ __forceinline__ void sweep_phase_quad_pipe(const QuadSweeper<B>& sw, const QuadPipePrefetch<B, P>& pf,
+                                                      const int* cstart, int c, const uint32_t* entries,
+                                                      const uint32_t* site_l, uint32_t pass, uint32_t chain_id,
+                                                      uint32_t key0, uint32_t key1,
+                                                      int (&acc)[QuadSweeper<B>::NSLOT]) {
+  const int e0 = cstart[c] + threadIdx.x, e_end = cstart[c + 1];
+  if (e0 < e_end) {
+    uint32_t F[B::NFEAT];
+    B::template Pipe<P>::late(sw.loader(pf.ent), pf.st, F);
+    sw.finish(pf.ent, pf.st.own, F, pf.x0, acc);
+  }
+#pragma unroll 1
+  for (int e = e0 + NT; e < e_end; e += NT) {
+    const uint32_t ent = __ldg(entries + e);
+    const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
+    const uint32_t x0[4] = {x.x, x.y, x.z, x.w};
+    sw.update(ent, x0, acc);
+  }
+}
+
 template <class B, int NT>
 __device__ __forceinline__ void sweep_phase_quad(const QuadSweeper<B>& sw, const QuadPrefetch& pf, const int* cstart,
                                                  int c, const uint32_t* entries, const uint32_t* site_l,
@@ -650,7 +706,8 @@ __device__ __forceinline__ void sweep_phase_quad(const QuadSweeper<B>& sw, const
   }
 }
 
-template <class B, int NT>
+// PIPE < 0: generic word layout; PIPE >= 0: pipelined features for colouring B::Pipe<PIPE>
+template <class B, int NT, int PIPE>
 __global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_constant__ CeQuadArgs<B::NFEAT> A) {
   constexpr int NS = B::NSPECIES;
   constexpr int NSLOT = CeSlots<B::NCLASS>::N;
@@ -729,26 +786,38 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_const
 #pragma unroll
   for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
 
-  QuadPrefetch pf;
-  pf.template prepare<NT>(cstart, 0, g.entries, g.site_l, Q, (uint32_t)A.pass0, chain_id, key0, key1);
+  using Prefetch =
+      typename std::conditional<(PIPE >= 0), QuadPipePrefetch<B, (PIPE >= 0 ? PIPE : 0)>, QuadPrefetch>::type;
+  Prefetch pf;
+  auto prepare = [&](int c, uint32_t pass) {
+    if constexpr (PIPE >= 0)
+      pf.template prepare<NT>(sw, cstart, c, g.entries, g.site_l, pass, chain_id, key0, key1);
+    else
+      pf.template prepare<NT>(cstart, c, g.entries, g.site_l, Q, pass, chain_id, key0, key1);
+  };
   barrier();
+  prepare(0, (uint32_t)A.pass0);  // the pipelined prefetch reads the loaded slab
 
 #pragma unroll 1
   for (int pass = 0; pass < A.n_passes; ++pass) {
     const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
 #pragma unroll 1
     for (int c = 0; c < g.n_colors; ++c) {
-      sweep_phase_quad<B, NT>(sw, pf, cstart, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
+      if constexpr (PIPE >= 0)
+        sweep_phase_quad_pipe<B, NT, (PIPE >= 0 ? PIPE : 0)>(sw, pf, cstart, c, g.entries, g.site_l, pass_g,
+                                                             chain_id, key0, key1, acc);
+      else
+        sweep_phase_quad<B, NT>(sw, pf, cstart, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
       const bool last = (c + 1 == g.n_colors);
+      // arrive, prepare the next phase (Philox block; pipelined: the early features,
+      // which read no word of colour c) while other threads finish, then wait
       if (S > 1) {
         cluster_arrive_release();
-        pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, Q, last ? pass_g + 1 : pass_g,
-                                chain_id, key0, key1);
+        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g);
         cluster_wait_acquire();
       } else {
-        pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, Q, last ? pass_g + 1 : pass_g,
-                                chain_id, key0, key1);
         __syncthreads();
+        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g);
       }
       if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
         int* buf = acc_sm[(pass - 1) & 1];

@@ -142,18 +142,24 @@ def test_statistics_edge_cases():
     assert r.is_equilibrated and r.N_samples_for_equilibration == 0
 
 
-@pytest.mark.parametrize("kind,L,word", [("fcc_binary", (64, 64, 64), True), ("fcc_binary", (20, 12, 10), True),
-                                         ("fcc_binary", (8, 8, 8), False), ("fcc_ternary", (16, 16, 16), False),
-                                         ("fcc_binary", (13, 11, 7), False)])
-def test_colouring_is_proper_host(kind, L, word):
+@pytest.mark.parametrize("kind,L,layout", [("fcc_binary", (64, 64, 64), "word_pipelined"),
+                                           ("fcc_binary", (16, 16, 8), "word_pipelined"),
+                                           ("fcc_binary", (16, 8, 16), "word_pipelined"),
+                                           ("fcc_binary", (20, 12, 10), "word"),
+                                           ("fcc_binary", (8, 8, 8), "byte"), ("fcc_ternary", (16, 16, 16), "byte"),
+                                           ("fcc_binary", (13, 11, 7), "byte")])
+def test_colouring_is_proper_host(kind, L, layout):
     """The sweep's colouring (host entry point, no device): no neighbour offset of the
-    basis set joins two sites of one colour; the word layout applies exactly where the
-    four sites i0 + t*L0/4 of every row share a colour."""
+    basis set joins two sites of one colour; the word layouts apply exactly where the
+    four sites i0 + t*L0/4 of every row share a colour; the pipelined one uses a
+    generated colouring whose late neighbours are those of the previous colour."""
     from casmcode_monte_gb300 import clex
     import casmcode_monte_gb300.clex.orbits as O
+    from casmcode_monte_gb300.clex import codegen
 
-    col, n, w = clex.color_supercell(kind, L)
-    assert w == word
+    col, n, lay = clex.color_supercell(kind, L)
+    assert lay == layout
+    w = lay != "byte"
     assert col.min() == 0 and col.max() == n - 1
     col3 = col.reshape(L[2], L[1], L[0])
     for (di, dj, dk) in O.make_basis_set(kind).neighbour_offsets():
@@ -163,3 +169,13 @@ def test_colouring_is_proper_host(kind, L, word):
         Q = L[0] // 4
         assert np.array_equal(col3[:, :, :Q], col3[:, :, Q:2 * Q])
         assert np.array_equal(col3[:, :, :Q], col3[:, :, 3 * Q:])
+    if lay == "word_pipelined":
+        offs = O.make_basis_set(kind).neighbour_offsets()
+        a, b, c = int(col3[0, 0, 1]), int(col3[0, 1, 0]), int(col3[1, 0, 0])
+        assert (a, b, c, n) in codegen.PIPELINE_COLOURINGS
+        late = codegen.late_offsets(offs, (a, b, c, n))
+        assert len(late) == 2
+        for (di, dj, dk) in offs:
+            shifted = np.roll(col3, shift=(-dk, -dj, -di), axis=(0, 1, 2))
+            is_late = (di, dj, dk) in [tuple(o) for o in late]
+            assert np.all((shifted == (col3 - 1) % n) == is_late)

@@ -1,7 +1,7 @@
-"""Word layout (four sites per 32-bit word) of the binary sweep against the byte layout
-and the oracle.
+"""Word layouts (four sites per 32-bit word, generic and pipelined) of the binary sweep
+against the byte layout and the oracle.
 
-The two layouts implement the same coloured sweep (same colouring, same Philox counters,
+The layouts implement the same coloured sweep (same colouring, same Philox counters,
 same FP32/FP64 decision arithmetic), so occupations and every per-pass output slot must
 be identical, in FP64 and in FP32 decision mode, for every CTA split.
 """
@@ -27,7 +27,12 @@ def _setup(L, n_chains, seed):
 
 def test_layout_selection(gpu_lib):
     model, occ, T, mu, seeds = _setup((16, 16, 16), 1, 1)
-    assert clex.ChainBatch(model, (16, 16, 16), occ, T, mu, seeds).layout == "word"
+    assert clex.ChainBatch(model, (16, 16, 16), occ, T, mu, seeds).layout == "word_pipelined"
+    m20, occ20, T20, mu20, s20 = _setup((20, 12, 10), 1, 1)
+    b20 = clex.ChainBatch(m20, (20, 12, 10), occ20, T20, mu20, s20)
+    assert b20.layout == "word"
+    with pytest.raises(RuntimeError):
+        b20.set_layout("word_pipelined")
     model8, occ8, T8, mu8, seeds8 = _setup((8, 8, 8), 1, 1)
     b8 = clex.ChainBatch(model8, (8, 8, 8), occ8, T8, mu8, seeds8)
     assert b8.layout == "byte"
@@ -48,16 +53,23 @@ WORD_SHAPES = [((16, 16, 16), 1), ((16, 16, 16), 2), ((16, 16, 8), 3), ((32, 16,
 def test_word_equals_byte_layout(gpu_lib, L, S, precision):
     n_chains = 3
     model, occ, T, mu, seeds = _setup(L, n_chains, seed=L[0] + S)
-    bw = clex.ChainBatch(model, L, occ, T, mu, seeds, precision=precision, ctas_per_chain=S)
-    bb = clex.ChainBatch(model, L, occ, T, mu, seeds, precision=precision, ctas_per_chain=S)
-    assert bw.layout == "word"
-    bb.set_layout("byte")
-    assert bb.layout == "byte" and bb.ctas_per_chain == S and bw.ctas_per_chain == S
+    auto = clex.ChainBatch(model, L, occ, T, mu, seeds, precision=precision, ctas_per_chain=S)
+    assert auto.layout in ("word", "word_pipelined")
+    layouts = ["byte", "word"] + (["word_pipelined"] if auto.layout == "word_pipelined" else [])
+    batches = []
+    for lay in layouts:
+        b = clex.ChainBatch(model, L, occ, T, mu, seeds, precision=precision, ctas_per_chain=S)
+        b.set_layout(lay)
+        assert b.layout == lay and b.ctas_per_chain == S
+        batches.append(b)
     for n in (5, 3):
-        ow, ob = bw.run(n), bb.run(n)
-        assert np.array_equal(ow, ob)
-        assert np.array_equal(bw.occupation(), bb.occupation())
-    assert np.array_equal(bw.corr(), bb.corr())
+        outs = [b.run(n) for b in batches]
+        occs = [b.occupation() for b in batches]
+        for o, oc in zip(outs[1:], occs[1:]):
+            assert np.array_equal(o, outs[0])
+            assert np.array_equal(oc, occs[0])
+    for b in batches[1:]:
+        assert np.array_equal(b.corr(), batches[0].corr())
 
 
 @pytest.mark.parametrize("L,S", [((16, 16, 16), 4), ((20, 12, 10), 1)])
@@ -65,7 +77,7 @@ def test_word_layout_matches_oracle(gpu_lib, L, S):
     n_chains = 2
     model, occ, T, mu, seeds = _setup(L, n_chains, seed=21)
     b = clex.ChainBatch(model, L, occ, T, mu, seeds, ctas_per_chain=S)
-    assert b.layout == "word"
+    assert b.layout in ("word", "word_pipelined")
     corr0 = b.corr()
     n_passes = 4
     out = b.run(n_passes)
@@ -87,12 +99,15 @@ def test_word_layout_full_size(gpu_lib):
     model, occ, T, _, seeds = _setup(L, 8, seed=3)
     mu = np.zeros((8, 1))
     bw = clex.ChainBatch(model, L, occ, T, mu, seeds, precision="fp32")
-    assert bw.layout == "word"
+    assert bw.layout == "word_pipelined"
     bb = clex.ChainBatch(model, L, occ, T, mu, seeds, precision="fp32", ctas_per_chain=bw.ctas_per_chain)
     bb.set_layout("byte")
+    bg = clex.ChainBatch(model, L, occ, T, mu, seeds, precision="fp32", ctas_per_chain=bw.ctas_per_chain)
+    bg.set_layout("word")
     corr0 = bw.corr()
-    ow, ob = bw.run(10), bb.run(10)
-    assert np.array_equal(ow, ob)
+    ow, ob, og = bw.run(10), bb.run(10), bg.run(10)
+    assert np.array_equal(ow, ob) and np.array_equal(og, ob)
     assert np.array_equal(bw.occupation(), bb.occupation())
+    assert np.array_equal(bg.occupation(), bb.occupation())
     s = clex.accumulate(model, corr0, ow, mu, bw.n_sites)
     assert np.array_equal(bw.corr(), s.int_corr[-1])
