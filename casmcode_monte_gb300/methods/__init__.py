@@ -1,0 +1,153 @@
+"""Monte Carlo methods (libcasm.monte.methods, python/libcasm/monte/methods/__init__.py:3-9).
+
+* ``metropolis_acceptance`` (python/libcasm/monte/methods/_metropolis.py:6-48,
+  include/casm/monte/methods/metropolis.hh:26-35): accept if dE < 0 without drawing,
+  else accept if ``random_real(1.0) < exp(-dE * beta)``.
+* ``BasicOccupationMetropolisData`` and ``basic_occupation_metropolis``
+  (include/casm/monte/methods/basic_occupation_metropolis.hh:18-115, 354-425): the
+  reference's generic Metropolis loop, parameterised by caller-supplied functions for the
+  potential change, the proposal and the application of an event.  Because those
+  functions are the caller's (any system, any event type), this loop is driven from the
+  host and calls them once per step, as the reference's Python binding does through
+  std::function (python/src/monte_methods.cpp).  The built-in systems run their loops on
+  the GPU instead: ``casmcode_monte_gb300.ising_cpp.semigrand_canonical`` (serial replay
+  of the reference's trajectory) and ``casmcode_monte_gb300.clex`` (coloured sweeps).
+"""
+from __future__ import annotations
+
+import math
+import sys
+from typing import Callable, Optional
+
+from .. import MethodLog, RandomNumberEngine, RandomNumberGenerator
+from ..sampling import (CompletionCheck, CompletionCheckParams, Sampler, get_n_samples, jsonSampler,
+                        jsonStateSamplingFunctionMap, StateSamplingFunctionMap)
+
+__all__ = ["KB", "BasicOccupationMetropolisData", "basic_occupation_metropolis", "default_write_status",
+           "metropolis_acceptance", "write_no_status"]
+
+KB = 8.6173303e-05  # eV/K (the reference's libcasm-global constant)
+
+
+def metropolis_acceptance(delta_potential_energy: float, beta: float, random_number_generator) -> bool:
+    """Metropolis acceptance (metropolis.hh:26-35): no random number is drawn for a
+    decrease of the potential."""
+    if delta_potential_energy < 0.0:
+        return True
+    return random_number_generator.random_real(1.0) < math.exp(-delta_potential_energy * beta)
+
+
+class BasicOccupationMetropolisData:
+    """Samplers, counters and completion check of a basic occupation Metropolis run
+    (basic_occupation_metropolis.hh:18-115)."""
+
+    def __init__(self, sampling_functions: StateSamplingFunctionMap,
+                 json_sampling_functions: jsonStateSamplingFunctionMap, n_steps_per_pass: int,
+                 completion_check_params: CompletionCheckParams):
+        self.sampling_functions = sampling_functions
+        self.json_sampling_functions = json_sampling_functions
+        self.samplers = {f.name: Sampler(f.shape, f.component_names) for f in sampling_functions.values()}
+        self.json_samplers = {f.name: jsonSampler() for f in json_sampling_functions.values()}
+        self.sample_weight = Sampler([])
+        self.n_pass = 0
+        self.n_steps_per_pass = int(n_steps_per_pass)
+        self.n_accept = 0
+        self.n_reject = 0
+        self.completion_check = CompletionCheck(completion_check_params)
+
+    def acceptance_rate(self) -> float:
+        total = float(self.n_accept) + float(self.n_reject)
+        return float(self.n_accept) / total if total else float("nan")
+
+    def rejection_rate(self) -> float:
+        total = float(self.n_accept) + float(self.n_reject)
+        return float(self.n_reject) / total if total else float("nan")
+
+    def reset(self) -> None:
+        for s in self.samplers.values():
+            s.clear()
+        for s in self.json_samplers.values():
+            s.values.clear()
+        self.sample_weight.clear()
+        self.n_pass = 0
+        self.n_accept = 0
+        self.n_reject = 0
+        self.completion_check.reset()
+
+    def to_dict(self) -> dict:
+        return {"completion_check_results": self.completion_check.results().to_dict(), "n_pass": self.n_pass,
+                "n_steps_per_pass": self.n_steps_per_pass, "n_accept": int(self.n_accept),
+                "n_reject": int(self.n_reject), "acceptance_rate": self.acceptance_rate(),
+                "rejection_rate": self.rejection_rate()}
+
+
+def write_no_status(data: BasicOccupationMetropolisData, method_log: MethodLog) -> None:
+    method_log.begin_lap()
+
+
+def default_write_status(data: BasicOccupationMetropolisData, method_log: MethodLog) -> None:
+    """Run status (passes, samples, clock time, steps per second) and the latest
+    completion-check results to stdout; the results to the method log's file."""
+    n_samples = get_n_samples(data.samplers)
+    t = method_log.time_s()
+    steps = float(data.n_pass) * float(data.n_steps_per_pass)
+    print(f"Passes={data.n_pass}, Samples={n_samples}, ClockTime(s)={t}, "
+          f"Steps/Second={steps / t if t > 0 else float('inf')}, Seconds/Step={t / steps if steps else 0.0}")
+    results = data.completion_check.results()
+    print(f"  AllEquilibrated={int(results.equilibration_check_results.all_equilibrated)}")
+    if results.equilibration_check_results.all_equilibrated:
+        print(f"  AllConverged={int(results.convergence_check_results.all_converged)}")
+    sys.stdout.flush()
+    if method_log.logfile_path():
+        method_log.reset()
+        method_log.write_json(results.to_dict())
+    method_log.begin_lap()
+
+
+def basic_occupation_metropolis(data: BasicOccupationMetropolisData, temperature: float,
+                                potential_occ_delta_per_supercell_f: Callable, propose_event_f: Callable,
+                                apply_event_f: Callable, sample_period: int = 1,
+                                method_log: Optional[MethodLog] = None,
+                                random_engine: Optional[RandomNumberEngine] = None,
+                                write_status_f: Optional[Callable] = None) -> None:
+    """Occupation Metropolis loop (basic_occupation_metropolis.hh:354-425).
+
+    Until the completion check (with count = passes, checked before every step): propose an
+    event with ``propose_event_f(rng)``, compute ``potential_occ_delta_per_supercell_f(e)``,
+    accept by ``metropolis_acceptance`` and apply with ``apply_event_f(e)``; every
+    ``n_steps_per_pass`` steps is a pass, and every ``sample_period`` passes each
+    sampling function is sampled (status written when the method log's frequency is due).
+    """
+    beta = 1.0 / (KB * temperature)
+    rng = RandomNumberGenerator(random_engine if random_engine is not None else RandomNumberEngine())
+    if write_status_f is None:
+        write_status_f = default_write_status
+    if method_log is None:
+        method_log = MethodLog(logfile_path="status.json", log_frequency=600.0)
+    method_log.restart_clock()
+    method_log.begin_lap()
+    n_pass_next_sample = sample_period
+    n_step = 0
+    cc = data.completion_check
+    while not cc.count_check(data.samplers, data.sample_weight, data.n_pass, method_log):
+        event = propose_event_f(rng)
+        dE = potential_occ_delta_per_supercell_f(event)
+        if metropolis_acceptance(dE, beta, rng):
+            data.n_accept += 1
+            apply_event_f(event)
+        else:
+            data.n_reject += 1
+        n_step += 1
+        if n_step == data.n_steps_per_pass:
+            n_step = 0
+            data.n_pass += 1
+        if data.n_pass == n_pass_next_sample:
+            n_pass_next_sample += sample_period
+            for f in data.sampling_functions.values():
+                data.samplers[f.name].push_back(f())
+            for f in data.json_sampling_functions.values():
+                data.json_samplers[f.name].values.append(f())
+            freq = method_log.log_frequency()
+            if freq is not None and method_log.lap_time() >= freq:
+                write_status_f(data, method_log)
+    write_status_f(data, method_log)

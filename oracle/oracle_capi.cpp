@@ -84,6 +84,55 @@ int orc_rng_draws(const char* state_in, int kind, long max_i, double max_r, long
   return 0;
 }
 
+// Semi-grand canonical proposals with the reference's occupant tracking, for a supercell
+// whose n_sites sites all allow the same n_species occupants (one asymmetric unit):
+// candidates (asym 0, species s) in species order; swaps a -> b for every ordered pair
+// a != b (OccCandidate.cc:125-140); each step draws the swap type with
+// random_real(sum of cand_size(a)) against the running sums and the site with
+// random_int(cand_size(a) - 1) (OccEventProposal.hh:168-247), then (if apply) applies the
+// event by swap-remove (OccLocation.cc:212-245).  Writes the proposed (site, new occupant).
+int orc_sgc_proposals(long n_sites, int n_species, const int* occ_in, unsigned long long seed, long n_steps,
+                      int apply, long* l_out, int* new_occ_out) {
+  std::mt19937_64 e(seed);
+  RNG rng{&e};
+  std::vector<std::vector<long>> loc(n_species);
+  std::vector<long> mol_loc(n_sites);
+  std::vector<int> species(occ_in, occ_in + n_sites);
+  for (long l = 0; l < n_sites; ++l) {
+    if (species[l] < 0 || species[l] >= n_species) return -1;
+    mol_loc[l] = (long)loc[species[l]].size();
+    loc[species[l]].push_back(l);
+  }
+  std::vector<std::pair<int, int>> swaps;
+  for (int a = 0; a < n_species; ++a)
+    for (int b = 0; b < n_species; ++b)
+      if (a != b) swaps.push_back({a, b});
+  std::vector<double> tsum(swaps.size() + 1);
+  for (long t = 0; t < n_steps; ++t) {
+    tsum[0] = 0.0;
+    for (size_t i = 0; i < swaps.size(); ++i) tsum[i + 1] = tsum[i] + (double)loc[swaps[i].first].size();
+    if (tsum.back() == 0.0) return -2;
+    const double r = rng.random_real(tsum.back());
+    size_t k = 0;
+    while (k < swaps.size() && !(r < tsum[k + 1])) ++k;
+    if (k == swaps.size()) return -3;
+    const int a = swaps[k].first, b = swaps[k].second;
+    const long l = loc[a][rng.random_int((long)loc[a].size() - 1)];
+    l_out[t] = l;
+    new_occ_out[t] = b;
+    if (apply) {
+      const long back = loc[a].back();
+      loc[a][mol_loc[l]] = back;
+      mol_loc[back] = mol_loc[l];
+      loc[a].pop_back();
+      mol_loc[l] = (long)loc[b].size();
+      loc[b].push_back(l);
+      species[l] = b;
+    }
+  }
+  return 0;
+}
+
 int orc_engine_seed(unsigned long long seed, char* state_out, long state_len) {
   std::mt19937_64 e(seed);
   std::stringstream ss;

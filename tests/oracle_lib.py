@@ -44,6 +44,7 @@ def load():
         L.orc_mt19937_64_10000th.restype = C.c_ulonglong
         L.orc_rng_draws.argtypes = [C.c_char_p, C.c_int, C.c_long, C.c_double, C.c_long, lp, dp, C.c_char_p, C.c_long]
         L.orc_engine_seed.argtypes = [C.c_ulonglong, C.c_char_p, C.c_long]
+        L.orc_sgc_proposals.argtypes = [C.c_long, C.c_int, ip, C.c_ulonglong, C.c_long, C.c_int, lp, ip]
         L.orc_ising_run.argtypes = [C.c_long, C.c_long, C.c_double, C.c_int, C.c_double, C.c_double, ip,
                                     C.POINTER(OrcCCParams), C.c_int, C.c_char_p, dp, C.c_long,
                                     C.POINTER(OrcRunOut), C.c_char_p, C.c_long]
@@ -180,3 +181,14 @@ class OracleCE:
         nacc = load().orc_ce_random_site_run(self.h, p(occ, C.c_int), T, p(mu, C.c_double), mu.size,
                                              C.c_ulonglong(seed), C.c_longlong(n_steps), C.byref(secs))
         return occ, nacc, secs.value
+
+
+def sgc_proposals(occ, n_species, seed, n_steps, apply=True):
+    """The oracle's semi-grand canonical proposal sequence: (sites, new occupants)."""
+    occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32))
+    l_out = np.zeros(n_steps, dtype=np.int64)
+    o_out = np.zeros(n_steps, dtype=np.int32)
+    rc = load().orc_sgc_proposals(occ.size, n_species, p(occ, C.c_int), C.c_ulonglong(seed), n_steps, int(apply),
+                                  p(l_out, C.c_long), p(o_out, C.c_int))
+    assert rc == 0, rc
+    return l_out, o_out

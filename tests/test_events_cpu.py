@@ -1,0 +1,248 @@
+"""Events and methods modules on the CPU.
+
+* Conversions: the reference's own cases (python/tests/events/test_Conversions.py:8-72):
+  site counts, the b-major linear index, translations, the asymmetric unit with
+  molecule orientations and occupant order.
+* OccLocation: the invariants the reference checks after every proposal and application
+  (tests/unit/monte/OccLocation_test.cpp:16-104), for FCC ternary random and dilute
+  configurations with canonical and semi-grand canonical proposals.
+* Semi-grand canonical proposals: draw-for-draw equal to the oracle's restatement of
+  OccEventProposal.hh:168-247 with std::mt19937_64 and libstdc++'s distributions.
+* basic_occupation_metropolis driving the Ising model through user functions: the same
+  trajectory, counters and samples as the oracle's Ising semi-grand canonical run.
+"""
+import numpy as np
+import pytest
+
+import casmcode_monte_gb300 as monte
+import casmcode_monte_gb300.events as ev
+import casmcode_monte_gb300.methods as methods
+import casmcode_monte_gb300.sampling as sampling
+from tests import oracle_lib
+
+
+def bijk(b, i, j, k):
+    return ev.IntegralSiteCoordinate.from_list([b, i, j, k])
+
+
+def test_conversions_cubic():
+    convert = ev.Conversions(ev.Prim.cubic(1.0, ["A", "B"]), np.eye(3, dtype=int) * 3)
+    assert convert.l_size() == 27
+    assert convert.asym_size() == 1
+    assert convert.occ_size(0) == 2 and convert.species_size() == 2
+
+
+def test_conversions_two_sites():
+    prim = ev.Prim(np.eye(3), np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5]]).T, [["A", "B"], ["B", "C"]])
+    convert = ev.Conversions(prim, np.eye(3, dtype=int) * 3)
+    assert convert.l_size() == 54
+    f = convert.site_index_converter()
+    assert f.total_sites() == 54
+    assert f.linear_site_index(bijk(1, 0, 0, 0)) == 27
+    assert convert.bijk_to_l(bijk(1, 0, 0, 0)) == 27
+    assert convert.l_to_bijk(27) == bijk(1, 0, 0, 0)
+    assert convert.bijk_to_l(bijk(1, 0, 0, 0) + np.array([1, 0, 0])) == convert.bijk_to_l(bijk(1, 1, 0, 0))
+    # periodic images and round trips
+    assert convert.bijk_to_l(bijk(0, 3, -3, 6)) == 0
+    for l in range(convert.l_size()):
+        assert convert.bijk_to_l(convert.l_to_bijk(l)) == l
+    # sites differ in occupants: two asymmetric units; species A, B, C
+    assert convert.asym_size() == 2
+    assert [convert.species_name(i) for i in range(convert.species_size())] == ["A", "B", "C"]
+    assert convert.species_index(1, 0) == 1 and convert.occ_index(1, 2) == 1
+    assert not convert.species_allowed(0, 2) and convert.occ_index(0, 2) == convert.occ_size(0)
+
+
+def _mol_prim(orders):
+    occupants = {"A": ev.Occupant.atom("A")}
+    for axis, name in enumerate(("mol.x", "mol.y", "mol.z")):
+        d = np.zeros(3)
+        d[axis] = 0.1
+        occupants[name] = ev.Occupant("mol", [("B", -d), ("B", d)])
+    coords = np.array([[0.0, 0.0, 0.0], [0.0, 0.5, 0.5], [0.5, 0.0, 0.5], [0.5, 0.5, 0.0]]).T
+    return ev.Prim(np.eye(3), coords, orders, occupants)
+
+
+def test_conversions_molecules_and_occupant_order():
+    full = ["A", "mol.x", "mol.y", "mol.z"]
+    convert = ev.Conversions(_mol_prim([["A"], full, full, full]), np.eye(3, dtype=int) * 3)
+    assert convert.l_size() == 27 * 4
+    assert convert.asym_size() == 2
+    shuffled = ["mol.x", "mol.y", "mol.z", "A"]
+    convert = ev.Conversions(_mol_prim([["A"], full, shuffled, full]), np.eye(3, dtype=int) * 3)
+    assert convert.l_size() == 27 * 4
+    assert convert.asym_size() == 3
+
+
+def test_nondiagonal_supercell_indexing():
+    T = np.array([[1, 1, 0], [-1, 1, 0], [0, 0, 2]])
+    convert = ev.Conversions(ev.Prim.fcc(4.0, ["A", "B"]), T)
+    assert convert.l_size() == 4
+    seen = {convert.bijk_to_l(convert.l_to_bijk(l)) for l in range(4)}
+    assert seen == {0, 1, 2, 3}
+    # translations by supercell lattice vectors map a site onto itself
+    for l in range(4):
+        x = convert.l_to_bijk(l)
+        for n in np.eye(3, dtype=int):
+            assert convert.bijk_to_l(x + T @ n) == l
+
+
+def test_swaps():
+    convert = ev.Conversions(ev.Prim.fcc(4.0, ["A", "B", "C"]), np.eye(3, dtype=int) * 2)
+    cands = ev.OccCandidateList(convert)
+    assert len(cands) == 3 and [cands.index(c) for c in cands] == [0, 1, 2]
+    sgc = ev.make_semigrand_canonical_swaps(convert, cands)
+    assert [(s.cand_a.species_index, s.cand_b.species_index) for s in sgc] == [(0, 1), (0, 2), (1, 0), (1, 2),
+                                                                               (2, 0), (2, 1)]
+    can = ev.make_canonical_swaps(convert, cands)
+    assert [(s.cand_a.species_index, s.cand_b.species_index) for s in can] == [(0, 1), (0, 2), (1, 2)]
+    assert ev.swaps_allowed_per_unitcell(convert, sgc) == 5
+    binary = ev.Conversions(ev.Prim.fcc(4.0, ["A", "B"]), np.eye(3, dtype=int) * 2)
+    assert ev.swaps_allowed_per_unitcell(binary, ev.make_semigrand_canonical_swaps(binary,
+                                                                                    ev.OccCandidateList(binary))) == 1
+    multis = ev.make_multiswaps(sgc, 2)
+    assert len(multis) == 6 + 21  # one swap, or a multiset of two of the six
+    assert all(m.total_count in (1, 2) for m in multis)
+    assert ev.OccSwap(cands[1], cands[0]).sorted() == ev.OccSwap(cands[0], cands[1])
+
+
+def _check_init(occ, loc, convert, cands):
+    for mol_id in range(loc.mol_size()):
+        assert loc.mol(mol_id).id == mol_id
+    for l in range(occ.size):
+        mol_id = loc.l_to_mol_id(l)
+        if mol_id == loc.mol_size():
+            continue
+        mol = loc.mol(mol_id)
+        assert mol.l == l and mol.id == mol_id
+        asym = convert.l_to_asym(l)
+        assert asym == mol.asym
+        assert occ[l] == convert.occ_index(asym, mol.species_index)
+        assert convert.species_index(asym, int(occ[l])) == mol.species_index
+        assert loc.mol_id(cands.index(mol.asym, mol.species_index), mol.loc) == mol.id
+
+
+def _check_event(occ, e, loc, convert, cands):
+    for t in e.occ_transform:
+        mol_id = loc.l_to_mol_id(t.l)
+        mol = loc.mol(mol_id)
+        assert mol.l == t.l and mol.id == mol_id and t.mol_id == mol_id
+        asym = convert.l_to_asym(t.l)
+        assert asym == mol.asym
+        assert occ[t.l] == convert.occ_index(asym, mol.species_index)
+        assert loc.mol_id(cands.index(mol.asym, mol.species_index), mol.loc) == mol.id
+
+
+@pytest.mark.parametrize("dilute", [False, True])
+@pytest.mark.parametrize("kind", ["canonical", "semigrand_canonical"])
+def test_occ_location_invariants(dilute, kind):
+    convert = ev.Conversions(ev.Prim.fcc(4.0, ["A", "B", "C"]), np.eye(3, dtype=int) * 9)
+    n = convert.l_size()
+    rng_np = np.random.default_rng(7)
+    occ = np.zeros(n, dtype=np.int32) if dilute else rng_np.integers(0, 3, size=n).astype(np.int32)
+    if dilute:
+        occ[rng_np.choice(n, size=3, replace=False)] = [1, 2, 1]
+    cands = ev.OccCandidateList(convert)
+    swaps = (ev.make_canonical_swaps if kind == "canonical" else ev.make_semigrand_canonical_swaps)(convert, cands)
+    propose = ev.propose_canonical_event if kind == "canonical" else ev.propose_semigrand_canonical_event
+    loc = ev.OccLocation(convert, cands)
+    loc.initialize(occ)
+    _check_init(occ, loc, convert, cands)
+    engine = monte.RandomNumberEngine()
+    engine.seed(11)
+    rng = monte.RandomNumberGenerator(engine)
+    e = ev.OccEvent()
+    counts0 = np.bincount(occ, minlength=3)
+    for _ in range(3000):
+        propose(e, loc, swaps, rng)
+        _check_event(occ, e, loc, convert, cands)
+        loc.apply(e, occ)
+        _check_event(occ, e, loc, convert, cands)
+    _check_init(occ, loc, convert, cands)
+    if kind == "canonical":
+        assert np.array_equal(np.bincount(occ, minlength=3), counts0)
+
+
+def test_semigrand_canonical_proposals_match_oracle(oracle):
+    convert = ev.Conversions(ev.Prim.fcc(4.0, ["A", "B", "C"]), np.eye(3, dtype=int) * 6)
+    n = convert.l_size()
+    occ = np.random.default_rng(3).integers(0, 3, size=n).astype(np.int32)
+    ref_l, ref_o = oracle_lib.sgc_proposals(occ, 3, 2024, 4000, apply=True)
+    cands = ev.OccCandidateList(convert)
+    swaps = ev.make_semigrand_canonical_swaps(convert, cands)
+    loc = ev.OccLocation(convert, cands)
+    work = occ.copy()
+    loc.initialize(work)
+    engine = monte.RandomNumberEngine()
+    engine.seed(2024)
+    rng = monte.RandomNumberGenerator(engine)
+    e = ev.OccEvent()
+    got_l, got_o = [], []
+    for _ in range(4000):
+        ev.propose_semigrand_canonical_event(e, loc, swaps, rng)
+        got_l.append(e.linear_site_index[0])
+        got_o.append(e.new_occ[0])
+        loc.apply(e, work)
+    assert got_l == ref_l.tolist()
+    assert got_o == ref_o.tolist()
+
+
+def test_metropolis_acceptance_draws_only_uphill():
+    engine = monte.RandomNumberEngine()
+    engine.seed(5)
+    rng = monte.RandomNumberGenerator(engine)
+    s0 = engine.dump()
+    assert methods.metropolis_acceptance(-1e-3, 10.0, rng)
+    assert engine.dump() == s0
+    methods.metropolis_acceptance(1e-3, 10.0, rng)
+    assert engine.dump() != s0
+
+
+def test_basic_occupation_metropolis_matches_oracle(oracle):
+    import casmcode_monte_gb300.ising_cpp as ising
+    import casmcode_monte_gb300.ising_cpp.semigrand_canonical as sgc
+
+    rows = cols = 8
+    J, T, mu, n_pass = 0.1, 2000.0, 0.0, 25
+    system = ising.IsingSystem(formation_energy_calculator=ising.IsingFormationEnergy(J=J, lattice_type=1,
+                                                                                      use_nlist=True),
+                               param_composition_calculator=ising.IsingParamComposition())
+    state = ising.IsingState(configuration=ising.IsingConfiguration(shape=(rows, cols)),
+                             conditions=monte.ValueMap.from_dict({"temperature": T, "exchange_potential": [mu]}))
+    occ0 = state.configuration.occupation().copy()
+    potential = sgc.SemiGrandCanonicalPotential(system)
+    potential.set_state(state, sgc.SemiGrandCanonicalConditions.from_values(state.conditions))
+    N = rows * cols
+
+    def propose(rng):
+        e = ev.OccEvent()
+        l = rng.random_int(N - 1)
+        e.linear_site_index = [l]
+        e.new_occ = [-state.configuration.occ(l)]
+        return e
+
+    def delta(e):
+        return potential.occ_delta_per_supercell(e.linear_site_index, e.new_occ)
+
+    def apply(e):
+        state.configuration.set_occ(e.linear_site_index[0], e.new_occ[0])
+
+    fmap = sampling.StateSamplingFunctionMap()
+    fmap["potential_energy"] = sampling.StateSamplingFunction(
+        "potential_energy", "", [], lambda: np.array([potential.per_unitcell()]))
+    params = sampling.CompletionCheckParams()
+    params.cutoff_params.max_count = n_pass
+    data = methods.BasicOccupationMetropolisData(fmap, sampling.jsonStateSamplingFunctionMap(), N, params)
+    engine = monte.RandomNumberEngine()
+    engine.seed(77)
+    methods.basic_occupation_metropolis(data, T, delta, propose, apply, sample_period=1,
+                                        method_log=monte.MethodLog(None, None), random_engine=engine,
+                                        write_status_f=methods.write_no_status)
+    ref = oracle_lib.ising_run(rows, cols, J, True, T, mu, occ0, oracle_lib.make_cc_params(max_count=n_pass), 1,
+                               oracle_lib.engine_state(77))
+    assert data.n_pass == n_pass
+    assert data.n_accept == ref["out"].n_accept and data.n_reject == ref["out"].n_reject
+    assert state.configuration.occupation().tolist() == ref["occ"].tolist()
+    pe = data.samplers["potential_energy"].component(0)
+    assert [float.hex(float(x)) for x in pe] == [float.hex(float(x)) for x in ref["potential_energy"]]
+    assert engine.dump() == ref["engine"]
