@@ -358,4 +358,70 @@ long long orc_ce_random_site_run(void* h, int* occ, double T, const double* mu, 
   return nacc;
 }
 
+// Semi-grand canonical run of the cluster expansion with the reference's proposal and
+// acceptance (one asymmetric unit, all species allowed): swap type a -> b drawn with
+// random_real against running sums of cand_size(a), site with random_int(cand_size(a)-1)
+// (OccEventProposal.hh:168-247), metropolis_acceptance (metropolis.hh:26-35), occupant
+// lists updated by swap-remove (OccLocation.cc:212-245).  After every pass of N steps:
+// e_out[p] = potential energy per site (E_f - sum_i mu_i N_(i+1)) / N, x_out[p][i] =
+// N_(i+1) / N (E_f tracked by adding the FP64 change of every accepted proposal).  Returns
+// the accepted count, or -1 on bad input.
+long long orc_ce_sgc_samples(void* h, int* occ, double T, const double* mu, int n_mu, unsigned long long seed,
+                             long n_passes, double* e_out, double* x_out) {
+  auto* S = static_cast<CESupercell*>(h);
+  const int ns = S->basis.n_species;
+  if (n_mu != ns - 1) return -1;
+  std::vector<double> m(mu, mu + n_mu);
+  std::mt19937_64 e(seed);
+  RNG rng{&e};
+  const double beta = 1.0 / (KB * T);
+  const long N = S->n();
+  std::vector<std::vector<long>> loc(ns);
+  std::vector<long> mol_loc(N);
+  for (long l = 0; l < N; ++l) {
+    if (occ[l] < 0 || occ[l] >= ns) return -1;
+    mol_loc[l] = (long)loc[occ[l]].size();
+    loc[occ[l]].push_back(l);
+  }
+  std::vector<std::pair<int, int>> swaps;
+  for (int a = 0; a < ns; ++a)
+    for (int b = 0; b < ns; ++b)
+      if (a != b) swaps.push_back({a, b});
+  std::vector<double> tsum(swaps.size() + 1);
+  long long nacc = 0;
+  double Ef = S->formation_per_supercell(occ);  // tracked by accepted changes
+  for (long p = 0; p < n_passes; ++p) {
+    for (long t = 0; t < N; ++t) {
+      tsum[0] = 0.0;
+      for (size_t i = 0; i < swaps.size(); ++i) tsum[i + 1] = tsum[i] + (double)loc[swaps[i].first].size();
+      const double r = rng.random_real(tsum.back());
+      size_t k = 0;
+      while (k + 1 < swaps.size() && !(r < tsum[k + 1])) ++k;
+      const int a = swaps[k].first, b = swaps[k].second;
+      const long l = loc[a][rng.random_int((long)loc[a].size() - 1)];
+      const double dEf = S->delta_formation(occ, l, b);
+      const double dE = dEf - S->mu_dot_Ndx(m, a, b);
+      if (metropolis_acceptance(dE, beta, rng)) {
+        ++nacc;
+        Ef += dEf;
+        const long back = loc[a].back();
+        loc[a][mol_loc[l]] = back;
+        mol_loc[back] = mol_loc[l];
+        loc[a].pop_back();
+        mol_loc[l] = (long)loc[b].size();
+        loc[b].push_back(l);
+        occ[l] = b;
+      }
+    }
+    double Esgc = Ef;
+    for (int i = 0; i < ns - 1; ++i) {
+      const double Ni = (double)loc[i + 1].size();
+      Esgc -= m[i] * Ni;
+      x_out[p * (ns - 1) + i] = Ni / (double)N;
+    }
+    e_out[p] = Esgc / (double)N;
+  }
+  return nacc;
+}
+
 }  // extern "C"

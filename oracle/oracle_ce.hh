@@ -298,9 +298,12 @@ struct CESupercell {
   }
 
   // clexulator-style FP64 change of formation energy per supercell (real phi)
+  mutable std::vector<double> acc_scratch;  // per-class sums of delta_formation
+
   double delta_formation(const int* occ, long l, int new_occ) const {
     int o = occ[l];
-    std::vector<double> acc(classes.size(), 0.0);
+    std::vector<double>& acc = acc_scratch;
+    acc.assign(classes.size(), 0.0);
     const int32_t* nb = nbr.data() + l * (long)slots.size();
     for (auto& M : tmpl) {
       double prod = basis.phi(M.b_l, new_occ) - basis.phi(M.b_l, o);

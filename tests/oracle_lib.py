@@ -44,6 +44,8 @@ def load():
         L.orc_mt19937_64_10000th.restype = C.c_ulonglong
         L.orc_rng_draws.argtypes = [C.c_char_p, C.c_int, C.c_long, C.c_double, C.c_long, lp, dp, C.c_char_p, C.c_long]
         L.orc_engine_seed.argtypes = [C.c_ulonglong, C.c_char_p, C.c_long]
+        L.orc_ce_sgc_samples.restype = C.c_longlong
+        L.orc_ce_sgc_samples.argtypes = [C.c_void_p, ip, C.c_double, dp, C.c_int, C.c_ulonglong, C.c_long, dp, dp]
         L.orc_sgc_proposals.argtypes = [C.c_long, C.c_int, ip, C.c_ulonglong, C.c_long, C.c_int, lp, ip]
         L.orc_ising_run.argtypes = [C.c_long, C.c_long, C.c_double, C.c_int, C.c_double, C.c_double, ip,
                                     C.POINTER(OrcCCParams), C.c_int, C.c_char_p, dp, C.c_long,
@@ -173,6 +175,18 @@ class OracleCE:
                                     C.c_uint(chain), p(colors, C.c_int), n_colors, pass0, n_passes,
                                     p(corr, C.c_longlong), p(nacc, C.c_longlong))
         return occ, corr, nacc
+
+    def sgc_samples(self, occ, T, mu, seed, n_passes):
+        """Reference-dynamics SGC run: per-pass potential energy per site [n_passes] and
+        composition [n_passes, n_species-1], accepted count."""
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64))
+        e = np.zeros(n_passes, dtype=np.float64)
+        x = np.zeros((n_passes, self.n_species - 1), dtype=np.float64)
+        nacc = load().orc_ce_sgc_samples(self.h, p(occ, C.c_int), T, p(mu, C.c_double), mu.size, C.c_ulonglong(seed),
+                                         n_passes, p(e, C.c_double), p(x, C.c_double))
+        assert nacc >= 0
+        return e, x, nacc
 
     def random_site_run(self, occ, T, mu, seed, n_steps):
         occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
