@@ -94,7 +94,7 @@ class ClexModel:
         return np.stack([nB, nC], axis=-1).astype(np.float64)
 
 
-LAYOUTS = {0: "byte", 1: "word", 2: "word_pipelined"}
+LAYOUTS = {0: "byte", 1: "word", 2: "word_pipelined", 3: "word_specialised"}
 
 
 def color_supercell(kind: str, shape) -> tuple[np.ndarray, int, str]:
@@ -152,8 +152,9 @@ class ChainBatch:
 
     def set_layout(self, layout: str) -> None:
         """Sweep with one site per byte ("byte"), four sites per word ("word", binary
-        basis with L0 a multiple of 4) or four sites per word with the features split
-        around the phase barrier ("word_pipelined"); trajectories are identical."""
+        basis with L0 a multiple of 4), four sites per word with the features split around
+        the phase barrier ("word_pipelined") or the same with warp-specialised CTAs
+        ("word_specialised"); trajectories are identical."""
         codes = {v: k for k, v in LAYOUTS.items()}
         if layout not in codes:
             raise ValueError(f"layout must be one of {sorted(codes)}")

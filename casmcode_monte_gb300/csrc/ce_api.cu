@@ -18,7 +18,7 @@ struct mg_ce_batch {
   int L0 = 0, L1 = 0, L2 = 0, n_chains = 0, precision = 0;
   long long N = 0;
   int S = 1, PX = 0, PY = 0, PZ = 0, n_colors = 0, threads = 0;
-  int layout = 0;          // 0: one site per byte; 1: four sites per word (binary basis); 2: 1 pipelined
+  int layout = 0;  // 0: one site per byte; 1: four sites per word (binary); 2: 1 pipelined; 3: 2 warp-specialised
   int pipe = -1;           // pipeline colouring id of the colouring, or -1
   int ctas_requested = 0;  // 0: chosen by occupancy
   size_t smem = 0;
@@ -119,7 +119,18 @@ int setup_layout(mg_ce_batch* b, int layout) {
   const long long n_entries = layout >= 1 ? b->N / 4 : b->N;
   std::vector<int> cstart((size_t)S * (b->n_colors + 1), 0);
   std::vector<uint32_t> entries(n_entries), site(n_entries);
-  if (layout >= 1)
+  if (layout == 3) {
+    // the warp-specialised kernel stages at most NW_WS words per (CTA, colour)
+    build_word_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
+                     site.data());
+    for (int r = 0; r < S; ++r)
+      for (int c = 0; c < b->n_colors; ++c)
+        if (cstart[r * (b->n_colors + 1) + c + 1] - cstart[r * (b->n_colors + 1) + c] > mg::host::NW_WS) {
+          set_error("Error in mg_ce_batch_set_layout: more words per CTA and colour than the warp-specialised "
+                    "kernel stages");
+          return MG_ERR_INVALID;
+        }
+  } else if (layout >= 1)
     build_word_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
                      site.data());
   else
@@ -142,7 +153,8 @@ int setup_layout(mg_ce_batch* b, int layout) {
   b->S = S;
   b->smem = smem;
   b->PZ = (b->L2 + S - 1) / S + 2 * mg::CE_HALO;
-  b->threads = layout >= 1 ? mg::host::NT_QUAD : (m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY);
+  b->threads = layout == 3 ? 2 * mg::host::NW_WS
+                           : (layout >= 1 ? mg::host::NT_QUAD : (m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY));
   return MG_OK;
 }
 
@@ -246,7 +258,7 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
     delete b;
     return MG_ERR_INVALID;
   }
-  const int layout = !quad_eligible(m->kind, L0, L1, L2, b->color.data()) ? 0 : (b->pipe >= 0 ? 2 : 1);
+  const int layout = !quad_eligible(m->kind, L0, L1, L2, b->color.data()) ? 0 : (b->pipe >= 0 ? 3 : 1);
   b->hcp.resize(n_chains);
   make_chain_params(m, n_chains, temperature, mu, seeds, chain_ids, b->hcp.data());
 
@@ -266,8 +278,13 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   MGX(cudaMemcpyAsync(b->docc, occ, (size_t)N * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
   MGX(cudaMemcpyAsync(b->dcp, b->hcp.data(), sizeof(mg::CeChainParams) * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
 #undef MGX
-  int rc = setup_layout(b, layout);
-  if (rc == MG_ERR_INVALID && layout >= 1) rc = setup_layout(b, 0);  // e.g. a CTA count only the byte layout fits
+  // the best layout that applies; a layout can still be refused for this CTA count (shared
+  // memory, staged words), then the next one is tried
+  int rc = MG_ERR_INVALID;
+  for (int lay = layout; lay >= 0 && rc == MG_ERR_INVALID; --lay) {
+    if (lay == 1 && layout >= 2) continue;  // a pipeline colouring: layout 2 is always at least as fast
+    rc = setup_layout(b, lay);
+  }
   if (rc != MG_OK) {
     free_batch(b);
     return rc;
@@ -302,6 +319,7 @@ int mg_ce_color_supercell(int basis_kind, int L0, int L1, int L2, int32_t* color
     return -MG_ERR_INVALID;
   }
   if (word_layout) *word_layout = !quad_eligible(basis_kind, L0, L1, L2, color) ? 0 : (pipe >= 0 ? 2 : 1);
+  // (a batch may further use layout 3 when its CTA split stages few enough words)
   return n;
 }
 
@@ -315,7 +333,7 @@ int mg_ce_batch_layout(const mg_ce_batch* b, int* layout) {
 }
 
 int mg_ce_batch_set_layout(mg_ce_batch* b, int layout) {
-  if (!b || layout < 0 || layout > 2) {
+  if (!b || layout < 0 || layout > 3) {
     set_error("Error in mg_ce_batch_set_layout: invalid argument");
     return MG_ERR_INVALID;
   }
@@ -324,7 +342,7 @@ int mg_ce_batch_set_layout(mg_ce_batch* b, int layout) {
               "and a colouring with colour(i + Q) = colour(i)");
     return MG_ERR_INVALID;
   }
-  if (layout == 2 && b->pipe < 0) {
+  if (layout >= 2 && b->pipe < 0) {
     set_error("Error in mg_ce_batch_set_layout: the pipelined word layout needs one of the generated pipeline "
               "colourings");
     return MG_ERR_INVALID;
@@ -360,7 +378,13 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   MG_CUDA_TRY(cudaEventRecord(b->ev0, b->stream));
   SweepLaunch L{b->L0, b->L1, b->L2, b->S, b->n_colors, b->n_chains, b->precision, b->dcstart, b->dentries,
                 b->dsite, b->dcp, b->docc, b->pass, n_passes, b->dout, b->stream};
-  int rc = b->layout >= 1 ? launch_sweep_quad(b->model, L, b->layout == 2 ? b->pipe : -1) : launch_sweep(b->model, L);
+  int rc;
+  if (b->layout == 3)
+    rc = launch_sweep_ws(b->model, L, b->pipe);
+  else if (b->layout >= 1)
+    rc = launch_sweep_quad(b->model, L, b->layout == 2 ? b->pipe : -1);
+  else
+    rc = launch_sweep(b->model, L);
   if (rc != MG_OK) return rc;
   MG_CUDA_TRY(cudaEventRecord(b->ev1, b->stream));
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, b->dout, sizeof(long long) * need, cudaMemcpyDeviceToHost, b->stream));

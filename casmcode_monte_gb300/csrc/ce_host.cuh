@@ -269,6 +269,7 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
 // ---- word layout (four sites per 32-bit word, binary basis)
 
 constexpr int NT_QUAD = 384;
+constexpr int NW_WS = 384;  // threads per role of the warp-specialised kernel
 
 // padded words per row: Q + 2 * HALO, made odd so that consecutive rows start in
 // different shared-memory banks
@@ -279,6 +280,11 @@ inline int quad_row_stride(int Q) {
 inline size_t quad_smem(int L0, int L1, int L2, int S) {
   return sizeof(uint32_t) * (size_t)quad_row_stride(L0 / 4) * (L1 + 2 * CE_HALO) *
          ((L2 + S - 1) / S + 2 * CE_HALO);
+}
+// warp-specialised kernel: the lattice (rounded to 16 bytes) and two stage slots
+inline size_t ws_smem(int L0, int L1, int L2, int S) {
+  const size_t lattice = (quad_smem(L0, L1, L2, S) + 15) & ~(size_t)15;
+  return lattice + sizeof(uint32_t) * 2 * (size_t)WsStage<FccBinary, 0>::NFIELD * NW_WS;
 }
 
 // The word layout applies to the binary basis when L0 = 4Q with Q >= 4 and the colouring
@@ -423,11 +429,14 @@ inline int max_active_chains(int kind, int S, size_t smem, int* out, int layout 
     return max_active_clusters_k(ce_sweep_quad_kernel<FccBinary, NT_QUAD, -1>, NT_QUAD, S, smem, out);
   if (layout == 2)
     return max_active_clusters_k(ce_sweep_quad_kernel<FccBinary, NT_QUAD, 0>, NT_QUAD, S, smem, out);
+  if (layout == 3)
+    return max_active_clusters_k(ce_sweep_ws_kernel<FccBinary, NW_WS, 0>, 2 * NW_WS, S, smem, out);
   return kind == 0 ? max_active_clusters_k(ce_sweep_kernel<FccBinary, NT_BINARY>, NT_BINARY, S, smem, out)
                    : max_active_clusters_k(ce_sweep_kernel<FccTernary, NT_TERNARY>, NT_TERNARY, S, smem, out);
 }
 
 inline size_t layout_smem(int layout, int L0, int L1, int L2, int S) {
+  if (layout == 3) return ws_smem(L0, L1, L2, S);
   return layout >= 1 ? quad_smem(L0, L1, L2, S) : slab_smem(L0, L1, L2, S);
 }
 
@@ -566,6 +575,56 @@ inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L, int pip
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);
   cfg.blockDim = dim3(NT_QUAD, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = L.stream;
+  cudaLaunchAttribute attr[1];
+  if (L.S > 1) {
+    if (L.S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)L.S;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  MG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
+  MG_CUDA_TRY(cudaGetLastError());
+  return MG_OK;
+}
+
+// warp-specialised kernel (pipeline colouring `pipe`, at most NW_WS words per CTA and colour)
+inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe) {
+  using B = FccBinary;
+  CeQuadArgs<B::NFEAT> A;
+  A.g.L0 = L.L0;
+  A.g.L1 = L.L1;
+  A.g.L2 = L.L2;
+  A.g.Q = L.L0 / 4;
+  A.g.S = L.S;
+  A.g.RS = quad_row_stride(L.L0 / 4);
+  A.g.RY = L.L1 + 2 * CE_HALO;
+  A.g.n_colors = L.n_colors;
+  A.g.color_start = L.cstart;
+  A.g.entries = L.entries;
+  A.g.site_l = L.site;
+  for (int k = 0; k < B::NFEAT; ++k) {
+    A.w.w32[k] = m->w32[k];
+    A.w.w64[k] = m->w64[k];
+  }
+  A.cp = L.cp;
+  A.occ = L.occ;
+  A.pass0 = L.pass0;
+  A.n_passes = L.n_passes;
+  A.n_chains = L.n_chains;
+  A.precision = L.precision;
+  A.out = L.out;
+  const size_t smem = ws_smem(L.L0, L.L1, L.L2, L.S);
+  static_assert(fcc_binary::NPIPE == 2, "one kernel instance per pipeline colouring");
+  auto kern = pipe == 0 ? ce_sweep_ws_kernel<B, NW_WS, 0> : ce_sweep_ws_kernel<B, NW_WS, 1>;
+  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);
+  cfg.blockDim = dim3(2 * NW_WS, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = L.stream;
   cudaLaunchAttribute attr[1];

@@ -856,6 +856,216 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_const
   barrier();
 }
 
+// ---- warp-specialised pipelined word sweep
+//
+// Two roles of NW threads each share a CTA.  During colour phase g the finish role takes
+// the decisions of phase g's words (late features, four FP32/FP64 decisions, write-back,
+// correlation changes) while the early role prepares phase g+1's words (Philox block and
+// early feature sums, which read no word of colour g) into a double-buffered staging area
+// in shared memory.  Both roles meet at the phase's cluster barrier, so a phase costs about
+// the longer of the two roles rather than their sum.  Requires at most NW words per
+// (CTA, colour) and a generated pipeline colouring; trajectories equal the other kernels'.
+template <class B, int P>
+struct WsStage {
+  using State = typename B::template Pipe<P>::State;
+  static constexpr int NF = B::NFEAT;
+  static constexpr int NK = B::template Pipe<P>::NKEEP;
+  static constexpr int NFIELD = NF + NK + 1 + 4 + 1;  // E, K, own, x0[4], entry
+
+  // field-major: base[field * NW + word]
+  template <int NW>
+  __device__ __forceinline__ static void store(uint32_t* base, int w, const State& st, const uint32_t (&x0)[4],
+                                               uint32_t ent) {
+#pragma unroll
+    for (int k = 0; k < NF; ++k) base[k * NW + w] = st.E[k];
+#pragma unroll
+    for (int k = 0; k < NK; ++k) base[(NF + k) * NW + w] = st.K[k];
+    base[(NF + NK) * NW + w] = st.own;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) base[(NF + NK + 1 + t) * NW + w] = x0[t];
+    base[(NF + NK + 5) * NW + w] = ent;
+  }
+  template <int NW>
+  __device__ __forceinline__ static void load(const uint32_t* base, int w, State& st, uint32_t (&x0)[4],
+                                              uint32_t& ent) {
+#pragma unroll
+    for (int k = 0; k < NF; ++k) st.E[k] = base[k * NW + w];
+#pragma unroll
+    for (int k = 0; k < NK; ++k) st.K[k] = base[(NF + k) * NW + w];
+    st.own = base[(NF + NK) * NW + w];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) x0[t] = base[(NF + NK + 1 + t) * NW + w];
+    ent = base[(NF + NK + 5) * NW + w];
+  }
+};
+
+template <class B, int NW, int PIPE>
+__global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_constant__ CeQuadArgs<B::NFEAT> A) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  using Stage = WsStage<B, PIPE>;
+  using State = typename Stage::State;
+  extern __shared__ __align__(16) uint32_t sq[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+
+  const QuadGeometry& g = A.g;
+  const int S = g.S;
+  const int chain = blockIdx.x / S;
+  int rank = 0;
+  cg::cluster_group cluster = cg::this_cluster();
+  if (S > 1) rank = (int)cluster.block_rank();
+  auto barrier = [&]() {
+    if (S > 1)
+      cluster.sync();
+    else
+      __syncthreads();
+  };
+  const bool finisher = threadIdx.x < NW;
+  const int tid = finisher ? threadIdx.x : threadIdx.x - NW;
+
+  const int Q = g.Q, RS = g.RS, RY = g.RY, RSY = RS * RY;
+  const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+  const int nkq = L2 / S, nkr = L2 % S;
+  const int nk = nkq + (rank < nkr ? 1 : 0);
+  const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+  const int rprev = (rank + S - 1) % S;
+  const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
+  const long long N = (long long)L0 * L1 * L2;
+  int8_t* gocc = A.occ + (size_t)chain * N;
+  const int lattice_words = RSY * (nkq + (nkr ? 1 : 0) + 2 * B::HALO);
+  uint32_t* stage = sq + ((lattice_words + 3) & ~3);  // [2][NFIELD][NW]
+
+  // ---- load slab + borders (as ce_sweep_quad_kernel)
+  for (int idx = threadIdx.x; idx < RSY * (nk + 2 * B::HALO); idx += 2 * NW) {
+    const int wp = idx % RS, jp = (idx / RS) % RY, kp = idx / RSY;
+    const int w = wp - B::HALO;
+    uint32_t word = 0u;
+    if (w < Q + B::HALO) {
+      int j = jp - B::HALO, k = k0 + kp - B::HALO;
+      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+      const int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        int i = w + t * Q;
+        i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+        word |= (uint32_t)(uint8_t)row[i] << (8 * t);
+      }
+    }
+    sq[idx] = word;
+  }
+  if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+
+  const CeChainParams* cpg = A.cp + chain;
+  load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+  const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+  const int* cstart = g.color_start + rank * (g.n_colors + 1);
+
+  QuadSweeper<B> sw;
+  sw.s = sq;
+  sw.s_prev = sq;
+  sw.s_next = sq;
+  if (S > 1) {
+    sw.s_prev = cluster.map_shared_rank(sq, (unsigned)rprev);
+    sw.s_next = cluster.map_shared_rank(sq, (unsigned)((rank + 1) % S));
+  }
+  sw.RS = RS;
+  sw.RSY = RSY;
+  sw.Q = Q;
+  sw.dJ = L1 * RS;
+  sw.dKp = nk_prev * RSY;
+  sw.dKn = nk * RSY;
+  sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
+                              A.precision};
+  const int lane = threadIdx.x & 31;
+  int acc[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+
+  // early role: Philox block and early features of word tid of colour c into a stage slot
+  auto prepare = [&](int c, uint32_t pass, uint32_t* slot) {
+    const int e = cstart[c] + tid;
+    if (e < cstart[c + 1]) {
+      const uint32_t ent = __ldg(A.g.entries + e);
+      const U32x4 x = philox4x32_10(U32x4{__ldg(A.g.site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
+      const uint32_t x0[4] = {x.x, x.y, x.z, x.w};
+      State st;
+      B::template Pipe<PIPE>::early(sw.loader(ent), st);
+      Stage::template store<NW>(slot, tid, st, x0, ent);
+    }
+  };
+  constexpr int SLOT = Stage::NFIELD * NW;
+
+  barrier();  // slab loaded
+  if (!finisher) prepare(0, (uint32_t)A.pass0, stage);
+  barrier();  // stage 0 ready
+
+  int parity = 0;
+#pragma unroll 1
+  for (int pass = 0; pass < A.n_passes; ++pass) {
+    const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
+#pragma unroll 1
+    for (int c = 0; c < g.n_colors; ++c) {
+      const bool last = (c + 1 == g.n_colors);
+      if (finisher) {
+        if (cstart[c] + tid < cstart[c + 1]) {
+          State st;
+          uint32_t x0[4], ent;
+          Stage::template load<NW>(stage + parity * SLOT, tid, st, x0, ent);
+          uint32_t F[B::NFEAT];
+          B::template Pipe<PIPE>::late(sw.loader(ent), st, F);
+          sw.finish(ent, st.own, F, x0, acc);
+        }
+      } else {
+        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g, stage + (parity ^ 1) * SLOT);
+      }
+      if (S > 1) {
+        cluster_arrive_release();
+        cluster_wait_acquire();
+      } else {
+        __syncthreads();
+      }
+      parity ^= 1;
+      if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+        int* buf = acc_sm[(pass - 1) & 1];
+        const int v = buf[threadIdx.x];
+        buf[threadIdx.x] = 0;
+        if (v)
+          atomicAdd(reinterpret_cast<unsigned long long*>(
+                        A.out + ((size_t)(pass - 1) * A.n_chains + chain) * NSLOT + threadIdx.x),
+                    (unsigned long long)(long long)v);
+      }
+    }
+    if (finisher) {
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q) {
+        const int v = warp_sum(acc[q]);
+        if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+        acc[q] = 0;
+      }
+    }
+  }
+  barrier();
+  if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+    const int pl = A.n_passes - 1;
+    int* buf = acc_sm[pl & 1];
+    const int v = buf[threadIdx.x];
+    if (v)
+      atomicAdd(reinterpret_cast<unsigned long long*>(A.out + ((size_t)pl * A.n_chains + chain) * NSLOT + threadIdx.x),
+                (unsigned long long)(long long)v);
+  }
+  for (int idx = threadIdx.x; idx < Q * L1 * nk; idx += 2 * NW) {
+    const int w = idx % Q, j = (idx / Q) % L1, kl = idx / (Q * L1);
+    const uint32_t word = sq[(w + B::HALO) + RS * ((j + B::HALO) + RY * (kl + B::HALO))];
+    int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * (k0 + kl));
+#pragma unroll
+    for (int t = 0; t < 4; ++t) row[w + t * Q] = (int8_t)((word >> (8 * t)) & 0xFFu);
+  }
+  barrier();
+}
+
 // ---- persistent pool kernel: many chains of any shape, one CTA per chain
 
 // geometry of one supercell shape swept by S CTAs: colour lists per slab

@@ -112,13 +112,16 @@ int mg_ce_batch_colors(const mg_ce_batch* b, int32_t* color /* [N] */);
 /* Shared-memory layout of the sweep: 0 = one site per byte (any basis and shape);
  * 1 = four sites per 32-bit word (binary basis, L0 = 4Q with Q >= 4, colour(i+Q) =
  * colour(i)); 2 = layout 1 with the feature sums split around the phase barrier (the
- * colourings generated for it: L0 a multiple of 16, L1/L2 multiples of 16/8).  The best
- * one that applies is chosen automatically.  All give identical trajectories; set_layout
- * rebuilds the site lists (MG_ERR_INVALID where the layout does not apply). */
+ * colourings generated for it: L0 a multiple of 16, L1/L2 multiples of 16/8); 3 = layout 2
+ * with warp-specialised CTAs (one role prepares the next colour while the other decides the
+ * current one; at most 384 words per CTA and colour).  The best one that applies is
+ * chosen automatically.  All give identical trajectories; set_layout rebuilds the site
+ * lists (MG_ERR_INVALID where the layout does not apply). */
 int mg_ce_batch_layout(const mg_ce_batch* b, int* layout);
 /* The sweep's colouring of an L0 x L1 x L2 supercell (host only, no device needed):
  * writes color[N], returns the number of colours (or -status); word_layout (may be
- * NULL) receives the layout a batch of this shape and basis uses (0, 1 or 2). */
+ * NULL) receives 0, 1 or 2 (a batch of this shape uses that layout, or layout 3 where its
+ * CTA split allows). */
 int mg_ce_color_supercell(int basis_kind, int L0, int L1, int L2, int32_t* color, int* word_layout);
 int mg_ce_batch_set_layout(mg_ce_batch* b, int layout);
 /* Run n_passes passes.  out (host, may be NULL) receives [n_passes][n_chains][n_classes+2]

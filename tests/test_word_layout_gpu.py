@@ -27,7 +27,7 @@ def _setup(L, n_chains, seed):
 
 def test_layout_selection(gpu_lib):
     model, occ, T, mu, seeds = _setup((16, 16, 16), 1, 1)
-    assert clex.ChainBatch(model, (16, 16, 16), occ, T, mu, seeds).layout == "word_pipelined"
+    assert clex.ChainBatch(model, (16, 16, 16), occ, T, mu, seeds).layout == "word_specialised"
     m20, occ20, T20, mu20, s20 = _setup((20, 12, 10), 1, 1)
     b20 = clex.ChainBatch(m20, (20, 12, 10), occ20, T20, mu20, s20)
     assert b20.layout == "word"
@@ -54,8 +54,12 @@ def test_word_equals_byte_layout(gpu_lib, L, S, precision):
     n_chains = 3
     model, occ, T, mu, seeds = _setup(L, n_chains, seed=L[0] + S)
     auto = clex.ChainBatch(model, L, occ, T, mu, seeds, precision=precision, ctas_per_chain=S)
-    assert auto.layout in ("word", "word_pipelined")
-    layouts = ["byte", "word"] + (["word_pipelined"] if auto.layout == "word_pipelined" else [])
+    assert auto.layout in ("word", "word_pipelined", "word_specialised")
+    layouts = ["byte", "word"]
+    if auto.layout in ("word_pipelined", "word_specialised"):
+        layouts.append("word_pipelined")
+    if auto.layout == "word_specialised":
+        layouts.append("word_specialised")
     batches = []
     for lay in layouts:
         b = clex.ChainBatch(model, L, occ, T, mu, seeds, precision=precision, ctas_per_chain=S)
@@ -77,7 +81,7 @@ def test_word_layout_matches_oracle(gpu_lib, L, S):
     n_chains = 2
     model, occ, T, mu, seeds = _setup(L, n_chains, seed=21)
     b = clex.ChainBatch(model, L, occ, T, mu, seeds, ctas_per_chain=S)
-    assert b.layout in ("word", "word_pipelined")
+    assert b.layout in ("word", "word_pipelined", "word_specialised")
     corr0 = b.corr()
     n_passes = 4
     out = b.run(n_passes)
@@ -99,15 +103,18 @@ def test_word_layout_full_size(gpu_lib):
     model, occ, T, _, seeds = _setup(L, 8, seed=3)
     mu = np.zeros((8, 1))
     bw = clex.ChainBatch(model, L, occ, T, mu, seeds, precision="fp32")
-    assert bw.layout == "word_pipelined"
+    assert bw.layout == "word_specialised"
     bb = clex.ChainBatch(model, L, occ, T, mu, seeds, precision="fp32", ctas_per_chain=bw.ctas_per_chain)
     bb.set_layout("byte")
     bg = clex.ChainBatch(model, L, occ, T, mu, seeds, precision="fp32", ctas_per_chain=bw.ctas_per_chain)
     bg.set_layout("word")
+    bp = clex.ChainBatch(model, L, occ, T, mu, seeds, precision="fp32", ctas_per_chain=bw.ctas_per_chain)
+    bp.set_layout("word_pipelined")
     corr0 = bw.corr()
-    ow, ob, og = bw.run(10), bb.run(10), bg.run(10)
-    assert np.array_equal(ow, ob) and np.array_equal(og, ob)
+    ow, ob, og, op = bw.run(10), bb.run(10), bg.run(10), bp.run(10)
+    assert np.array_equal(ow, ob) and np.array_equal(og, ob) and np.array_equal(op, ob)
     assert np.array_equal(bw.occupation(), bb.occupation())
     assert np.array_equal(bg.occupation(), bb.occupation())
+    assert np.array_equal(bp.occupation(), bb.occupation())
     s = clex.accumulate(model, corr0, ow, mu, bw.n_sites)
     assert np.array_equal(bw.corr(), s.int_corr[-1])
