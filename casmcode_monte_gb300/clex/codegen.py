@@ -175,6 +175,8 @@ def _quad_pipelines(bs, offs) -> list:
         early_lines, masks = [], set()
         kept = []    # (name, expression) computed early
         late_lines = []
+        groups_all: list = []  # distinct late parts L (tuples of late variables)
+        terms_tab = []         # (group, feature, kept index or -1, count)
         for k, f in enumerate(bs.features):
             terms = [tuple(_var(o) for o, _ in t) for t in f.terms]
             if all(len(t) == 0 for t in terms):
@@ -195,22 +197,37 @@ def _quad_pipelines(bs, offs) -> list:
                     groups.setdefault(Lp, []).append(tuple(v for v in t if v not in late))
             lparts = []
             for Lp, Rs in sorted(groups.items()):
+                if Lp not in groups_all:
+                    groups_all.append(Lp)
+                gi = groups_all.index(Lp)
                 if all(len(R) == 0 for R in Rs):
                     lparts += [_and(list(Lp))] * len(Rs)
+                    terms_tab.append((gi, k, -1, len(Rs)))
                 elif len(Rs) == 1:
                     # one term: AND(L) & AND(R), AND(R) kept
                     kept.append((f"K{len(kept)}", _and(list(Rs[0]))))
                     lparts.append(f"({_and(list(Lp))} & s.K[{len(kept) - 1}])")
+                    terms_tab.append((gi, k, len(kept) - 1, 1))
                 else:
                     kexpr = " + ".join(_and(list(R)) if R else "0x01010101u" for R in Rs)
                     kept.append((f"K{len(kept)}", kexpr))
                     lparts.append(f"((({_and(list(Lp))}) * 0xFFu) & s.K[{len(kept) - 1}])")
+                    terms_tab.append((gi, k, len(kept) - 1, 1))
             late_lines.append(f"    F[{k}] = s.E[{k}]" + ("".join(" + " + x for x in lparts)) + ";")
         out.append(f"// colouring ({col[0]} i + {col[1]} j + {col[2]} k) mod {col[3]}: late neighbours "
                    + ", ".join(str(tuple(o)) for o in late_offs))
         out.append("template <>")
         out.append(f"struct Pipe<{p}> {{")
         out.append(f"  static constexpr int NKEEP = {max(1, len(kept))};")
+        out.append("  // late groups g (AND of late neighbours); F[k] gains sum over terms (g, k, keep, n) of")
+        out.append("  // n * group_g * (keep < 0 ? 1 : K[keep]) per byte")
+        out.append(f"  static constexpr int NGROUP = {len(groups_all)};")
+        out.append(f"  static constexpr int NTERM = {len(terms_tab)};")
+        for name, col_i in (("term_group", 0), ("term_feature", 1), ("term_keep", 2), ("term_count", 3)):
+            out.append(f"  __host__ __device__ static constexpr int {name}(int i) {{")
+            out.append("    constexpr int t[NTERM] = {" + ", ".join(str(t[col_i]) for t in terms_tab) + "};")
+            out.append("    return t[i];")
+            out.append("  }")
         out.append("  struct State {")
         out.append("    uint32_t E[NFEAT];")
         out.append("    uint32_t K[NKEEP];")
@@ -228,10 +245,13 @@ def _quad_pipelines(bs, offs) -> list:
             out.append(f"    s.K[{i}] = {kexpr};")
         out.append("  }")
         out.append("  template <class Loader>")
-        out.append("  __device__ static __forceinline__ void late(const Loader& ld, const State& s, uint32_t (&F)[NFEAT]) {")
+        out.append("  __device__ static __forceinline__ void late(const Loader& ld, const State& s, uint32_t (&F)[NFEAT],")
+        out.append("                                              uint32_t (&Lw)[NGROUP]) {")
         for o in late_offs:
             out.append(f"    const uint32_t {_var(o)} = ld({o[0]}, {o[1]}, {o[2]});")
         out += late_lines
+        for gi, Lp in enumerate(groups_all):
+            out.append(f"    Lw[{gi}] = {_and(list(Lp))};")
         out.append("  }")
         out.append("};")
     return out

@@ -87,6 +87,7 @@ bool make_model(int kind, const double* eci, int n, mg_ce_model* m, std::string&
     m->w64.push_back(w);
     m->w32.push_back((float)w);
   }
+  mg::host::quantise_weights(m);
   return true;
 }
 
@@ -485,17 +486,11 @@ int mg_ce_batch_delta_e(mg_ce_batch* b, const int32_t* chain, const long long* s
     const unsigned nb = (unsigned)((n + nt - 1) / nt);
     if (b->model->kind == 0) {
       mg::CeWeights<mg::FccBinary::NFEAT> w;
-      for (int k = 0; k < mg::FccBinary::NFEAT; ++k) {
-        w.w32[k] = b->model->w32[k];
-        w.w64[k] = b->model->w64[k];
-      }
+      mg::host::fill_weights(b->model, w);
       mg::ce_delta_e_kernel<mg::FccBinary><<<nb, nt, 0, b->stream>>>(w, b->docc, b->L0, b->L1, b->L2, b->dcp, dc, ds, dn, n, dout);
     } else {
       mg::CeWeights<mg::FccTernary::NFEAT> w;
-      for (int k = 0; k < mg::FccTernary::NFEAT; ++k) {
-        w.w32[k] = b->model->w32[k];
-        w.w64[k] = b->model->w64[k];
-      }
+      mg::host::fill_weights(b->model, w);
       mg::ce_delta_e_kernel<mg::FccTernary><<<nb, nt, 0, b->stream>>>(w, b->docc, b->L0, b->L1, b->L2, b->dcp, dc, ds, dn, n, dout);
     }
     e = cudaGetLastError();

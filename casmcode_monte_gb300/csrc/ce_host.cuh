@@ -81,6 +81,11 @@ struct mg_ce_model {
   std::vector<long> feat_max;  // bound on |F_k|
   std::vector<double> w64;
   std::vector<float> w32;
+  // fast-path quantisation: wq[k] = round(w64[k] * 2^qshift); qerr bounds
+  // |sum_b dpsi_b sum_k (w64[k] - wq[k] 2^-qshift) F[k]|; qmax bounds |dE_f| of a flip
+  std::vector<int32_t> wq;
+  int qshift = 0;
+  double qerr = 0.0, qmax = 0.0;
 };
 
 namespace mg {
@@ -89,6 +94,36 @@ namespace host {
 inline int dpsi_max(int kind, int b) {
   if (kind == 0) return 1;
   return b == 0 ? 2 : 3;
+}
+
+// Quantised weights of the fast path: the largest shift s (<= 60) for which
+// sum_b dpsi_max_b sum_k |w[k]| max|F[k]| 2^s stays below 2^30 (int32 with margin).
+inline void quantise_weights(mg_ce_model* m) {
+  double T = 0.0;
+  for (int k = 0; k < m->n_features; ++k)
+    T += dpsi_max(m->kind, m->feat_b[k]) * std::fabs(m->w64[k]) * (double)m->feat_max[k];
+  int s = 0;
+  while (s < 60 && std::ldexp(T, s + 1) < std::ldexp(1.0, 30)) ++s;
+  m->qshift = s;
+  m->wq.assign(m->n_features, 0);
+  double err = 0.0, qmax = 0.0;
+  for (int k = 0; k < m->n_features; ++k) {
+    m->wq[k] = (int32_t)std::llround(std::ldexp(m->w64[k], s));
+    const double c = dpsi_max(m->kind, m->feat_b[k]) * (double)m->feat_max[k];
+    err += c * std::fabs(m->w64[k] - std::ldexp((double)m->wq[k], -s));
+    qmax += c * std::fabs(std::ldexp((double)m->wq[k], -s));
+  }
+  m->qerr = err;
+  m->qmax = qmax;
+}
+
+template <int NF>
+inline void fill_weights(const mg_ce_model* m, CeWeights<NF>& w) {
+  for (int k = 0; k < NF; ++k) {
+    w.wq[k] = m->wq[k];
+    w.w64[k] = m->w64[k];
+  }
+  w.qscale = (float)std::ldexp(1.0, -m->qshift);
 }
 
 inline const int* offsets(int kind, int* n) {
@@ -282,9 +317,14 @@ inline size_t quad_smem(int L0, int L1, int L2, int S) {
          ((L2 + S - 1) / S + 2 * CE_HALO);
 }
 // warp-specialised kernel: the lattice (rounded to 16 bytes) and two stage slots
-inline size_t ws_smem(int L0, int L1, int L2, int S) {
+static_assert(WsStage<FccBinary, 0>::NFIELD == WsStage<FccBinary, 1>::NFIELD, "one stage size for all pipelines");
+// warp-specialised kernel: the lattice (rounded to 16 bytes), two stage slots, the CTA's
+// site lists (entry and Philox counter word per word) and its colour starts
+inline size_t ws_smem(int L0, int L1, int L2, int S, int n_colors = CE_MAX_COLORS) {
   const size_t lattice = (quad_smem(L0, L1, L2, S) + 15) & ~(size_t)15;
-  return lattice + sizeof(uint32_t) * 2 * (size_t)WsStage<FccBinary, 0>::NFIELD * NW_WS;
+  const size_t words = (size_t)(L0 / 4) * L1 * ((L2 + S - 1) / S);
+  return lattice + sizeof(uint32_t) * (2 * (size_t)WsStage<FccBinary, 0>::NFIELD * NW_WS + 2 * words) +
+         sizeof(int) * (n_colors + 1);
 }
 
 // The word layout applies to the binary basis when L0 = 4Q with Q >= 4 and the colouring
@@ -363,9 +403,6 @@ inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* 
                               CeChainParams* out) {
   const double KB = 8.6173303E-05;
   const int ns = m->n_species;
-  double wsum = 0.0;
-  for (int k = 0; k < m->n_features; ++k)
-    wsum += std::fabs((double)m->w32[k]) * (double)m->feat_max[k] * dpsi_max(m->kind, m->feat_b[k]);
   for (int c = 0; c < n_chains; ++c) {
     CeChainParams& p = out[c];
     std::memset(&p, 0, sizeof(p));
@@ -383,7 +420,8 @@ inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* 
         p.dmu32[o * ns + o2] = (float)r;
         dmu_max = std::max(dmu_max, std::fabs(r));
       }
-    const double dtol = (m->n_features + 8) * std::ldexp(1.0, -23) * (wsum + dmu_max) + 1e-30;
+    // quantisation error + FP32 rounding of the integer change, of mu.N dx and of the sum
+    const double dtol = m->qerr + 2.0 * std::ldexp(1.0, -23) * (m->qmax + dmu_max) + 1e-30;
     p.dtol = (float)(dtol * 1.0001);
     p.eps = (float)(1.25 * p.beta * dtol + 8e-6);
     for (int i = 0; i < ns - 1; ++i) p.mu[i] = mu[(size_t)c * (ns - 1) + i];
@@ -507,10 +545,7 @@ int launch_sweep_t(const mg_ce_model* m, const SweepLaunch& L) {
   A.g.color_start = L.cstart;
   A.g.entries = L.entries;
   A.g.site_l = L.site;
-  for (int k = 0; k < B::NFEAT; ++k) {
-    A.w.w32[k] = m->w32[k];
-    A.w.w64[k] = m->w64[k];
-  }
+  fill_weights(m, A.w);
   A.cp = L.cp;
   A.occ = L.occ;
   A.pass0 = L.pass0;
@@ -556,10 +591,7 @@ inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L, int pip
   A.g.color_start = L.cstart;
   A.g.entries = L.entries;
   A.g.site_l = L.site;
-  for (int k = 0; k < B::NFEAT; ++k) {
-    A.w.w32[k] = m->w32[k];
-    A.w.w64[k] = m->w64[k];
-  }
+  fill_weights(m, A.w);
   A.cp = L.cp;
   A.occ = L.occ;
   A.pass0 = L.pass0;
@@ -607,10 +639,7 @@ inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe)
   A.g.color_start = L.cstart;
   A.g.entries = L.entries;
   A.g.site_l = L.site;
-  for (int k = 0; k < B::NFEAT; ++k) {
-    A.w.w32[k] = m->w32[k];
-    A.w.w64[k] = m->w64[k];
-  }
+  fill_weights(m, A.w);
   A.cp = L.cp;
   A.occ = L.occ;
   A.pass0 = L.pass0;
@@ -618,7 +647,7 @@ inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe)
   A.n_chains = L.n_chains;
   A.precision = L.precision;
   A.out = L.out;
-  const size_t smem = ws_smem(L.L0, L.L1, L.L2, L.S);
+  const size_t smem = ws_smem(L.L0, L.L1, L.L2, L.S, L.n_colors);
   static_assert(fcc_binary::NPIPE == 2, "one kernel instance per pipeline colouring");
   auto kern = pipe == 0 ? ce_sweep_ws_kernel<B, NW_WS, 0> : ce_sweep_ws_kernel<B, NW_WS, 1>;
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

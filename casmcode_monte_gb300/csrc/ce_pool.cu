@@ -183,10 +183,7 @@ int launch_pool(mg_ce_pool* p, int cls, int item0, int n_items, int n_passes, si
   A.items = p->ditems + item0;
   A.n_items = n_items;
   A.next_item = p->dcounter + cls;
-  for (int k = 0; k < B::NFEAT; ++k) {
-    A.w.w32[k] = p->model->w32[k];
-    A.w.w64[k] = p->model->w64[k];
-  }
+  mg::host::fill_weights(p->model, A.w);
   A.cp = p->dcp;
   A.occ = p->darena;
   A.n_passes = n_passes;

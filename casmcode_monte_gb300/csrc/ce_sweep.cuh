@@ -21,7 +21,8 @@
 // (release/acquire).
 //
 // Energies: the generated feature function yields integer local sums F[k]; the FP32
-// fast path computes dE32 = sum_b dpsi_b * (sum_k w32[k] F[k]) - dmu.  A proposal whose
+// fast path computes dE32 = qscale * sum_b dpsi_b * (sum_k wq[k] F[k]) - dmu, the sum an
+// exact integer of quantised weights (any split of it gives the same value).  A proposal whose
 // FP32 decision could differ from the FP64 one (|dE32| within the rounding bound, or u
 // within the relative bound of exp(-beta dE)) is re-decided exactly in FP64.  Accepted
 // changes of the integer correlation sums are accumulated exactly (int32 per thread per
@@ -59,9 +60,13 @@ struct CeWeightsClass {
   double w[NCLASS];
 };
 
+// Energy weights: FP64 for the exact decision; quantised integers wq[k] = round(w[k] * 2^s)
+// for the fast path, whose change of energy sum_b dpsi_b * sum_k wq[k] F[k] is an exact
+// int32 (s chosen so it cannot overflow) scaled by qscale = 2^-s.
 template <int NFEAT>
 struct CeWeights {
-  float w32[NFEAT];
+  int wq[NFEAT];
+  float qscale;
   double w64[NFEAT];
 };
 
@@ -126,11 +131,11 @@ __device__ __forceinline__ int warp_sum(int v) {
 }
 
 // Metropolis decision of one proposal o -> o2 from its integer local features, in two
-// parts: fast() is the branch-free FP32 decision and says whether it is ambiguous (|dE32|
-// within the rounding bound, or u within the relative bound of exp(-beta dE)); exact()
-// takes the FP64 decision of an ambiguous proposal, counts it in acc[NCLASS] and, in
-// FP32 mode, counts a flipped decision in acc[NCLASS+1] (the FP32 decision stands there).
-// Ff[k] is F[k] as a float (exact); Fi(k) returns F[k] as an int.
+// parts: fast() is the branch-free FP32 decision from the exact integer change dEq and
+// says whether it is ambiguous (|dE32| within the quantisation and rounding bound, or u
+// within the relative bound of exp(-beta dE)); exact() takes the FP64 decision of an
+// ambiguous proposal, counts it in acc[NCLASS] and, in FP32 mode, counts a flipped
+// decision in acc[NCLASS+1] (the FP32 decision stands there).  Fi(k) returns F[k].
 template <class B>
 struct MetropolisRule {
   static constexpr int NF = B::NFEAT;
@@ -144,16 +149,22 @@ struct MetropolisRule {
   float beta_log2e, dtol, eps;
   int precision;
 
-  __device__ __forceinline__ bool fast(int o, int o2, const int (&dpsi)[B::NFUNC], const float (&Ff)[NF],
-                                       uint32_t x0, bool& amb) const {
-    float G[B::NFUNC];
+  // exact integer change of energy sum_b dpsi_b * sum_k wq[k] F[k] (F[k] = Fi(k))
+  template <class FI>
+  __device__ __forceinline__ int dEq(const int (&dpsi)[B::NFUNC], const FI& Fi) const {
+    int G[B::NFUNC];
 #pragma unroll
-    for (int b = 0; b < B::NFUNC; ++b) G[b] = 0.f;
+    for (int b = 0; b < B::NFUNC; ++b) G[b] = 0;
 #pragma unroll
-    for (int k = 0; k < NF; ++k) G[B::feat_b(k)] = fmaf(w->w32[k], Ff[k], G[B::feat_b(k)]);
-    float dE32 = -dmu32[o * NS + o2];
+    for (int k = 0; k < NF; ++k) G[B::feat_b(k)] += w->wq[k] * Fi(k);
+    int d = 0;
 #pragma unroll
-    for (int b = 0; b < B::NFUNC; ++b) dE32 = fmaf((float)dpsi[b], G[b], dE32);
+    for (int b = 0; b < B::NFUNC; ++b) d += dpsi[b] * G[b];
+    return d;
+  }
+
+  __device__ __forceinline__ bool fast(int o, int o2, int dEq, uint32_t x0, bool& amb) const {
+    const float dE32 = fmaf((float)dEq, w->qscale, -dmu32[o * NS + o2]);
     const float u32 = __uint2float_rn(x0) * 2.3283064365386963e-10f;
     const float P = fast_exp2(-dE32 * beta_log2e);
     const bool band = !(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps));
@@ -189,10 +200,10 @@ struct MetropolisRule {
   }
 
   template <class FI>
-  __device__ __forceinline__ bool operator()(int o, int o2, const int (&dpsi)[B::NFUNC], const float (&Ff)[NF],
-                                             const FI& Fi, uint32_t x0, int (&acc)[NSLOT]) const {
+  __device__ __forceinline__ bool operator()(int o, int o2, const int (&dpsi)[B::NFUNC], const FI& Fi, uint32_t x0,
+                                             int (&acc)[NSLOT]) const {
     bool amb;
-    const bool acc32 = fast(o, o2, dpsi, Ff, x0, amb);
+    const bool acc32 = fast(o, o2, dEq(dpsi, Fi), x0, amb);
     if (amb) return exact(o, o2, dpsi, Fi, x0, acc32, acc);
     return acc32;
   }
@@ -240,11 +251,8 @@ struct SiteSweeper {
     int dpsi[B::NFUNC];
 #pragma unroll
     for (int b = 0; b < B::NFUNC; ++b) dpsi[b] = B::psi(b, o2) - B::psi(b, o);
-    float Ff[NF];
-#pragma unroll
-    for (int k = 0; k < NF; ++k) Ff[k] = (float)F[k];
     const MetropolisRule<B> rule{dmu32, dmu64, w, beta, beta_log2e, dtol, eps, precision};
-    const bool accept = rule(o, o2, dpsi, Ff, [&](int k) { return F[k]; }, x0, acc);
+    const bool accept = rule(o, o2, dpsi, [&](int k) { return F[k]; }, x0, acc);
     if (accept) {
       const int8_t c2 = B::code_of_occ(o2);
       const int oi = (flags & 1u) ? dI : ((flags & 2u) ? -dI : 0);
@@ -520,11 +528,6 @@ struct WordLoader {
   }
 };
 
-// byte t of w as a float (exact): 2^23 + byte, minus 2^23
-__device__ __forceinline__ float byte_as_float(uint32_t w, int t) {
-  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + (unsigned)t)) - 8388608.0f;
-}
-
 // F[k] of one byte lane, as an int (FP64 re-decisions)
 template <int NF>
 struct QuadFeature {
@@ -557,9 +560,28 @@ struct QuadSweeper {
     finish(ent, s[(int)(ent & 0xFFFFFFu)], F, x0, acc);
   }
 
+  // integer energy sums G[t] = sum_k wq[k] F[k][t] of the four sites (flip of site t
+  // changes the energy by (1 - 2 o_t) G[t] quantised units)
+  __device__ __forceinline__ void word_sums(const uint32_t (&F)[NF], int (&G)[4]) const {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      G[t] = 0;
+#pragma unroll
+      for (int k = 0; k < NF; ++k) G[t] += rule.w->wq[k] * (int)((F[k] >> (8 * t)) & 0xFFu);
+    }
+  }
+
   // four decisions from the word's features F and value v, write-back of the flips
   __device__ __forceinline__ void finish(uint32_t ent, uint32_t v, const uint32_t (&F)[NF], const uint32_t (&x0)[4],
                                          int (&acc)[NSLOT]) const {
+    int G[4];
+    word_sums(F, G);
+    finish_g(ent, v, F, G, x0, acc);
+  }
+
+  // the same with the integer energy sums given
+  __device__ __forceinline__ void finish_g(uint32_t ent, uint32_t v, const uint32_t (&F)[NF], const int (&G)[4],
+                                           const uint32_t (&x0)[4], int (&acc)[NSLOT]) const {
     const int pw = (int)(ent & 0xFFFFFFu);
     const uint32_t flags = ent >> 24;
     // FP32 decisions of the four sites (branch-free, interleaved)
@@ -567,11 +589,7 @@ struct QuadSweeper {
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int o = (int)((v >> (8 * t)) & 1u);
-      const int dpsi[1] = {1 - 2 * o};
-      float Ff[NF];
-#pragma unroll
-      for (int k = 0; k < NF; ++k) Ff[k] = byte_as_float(F[k], t);
-      acc32[t] = rule.fast(o, 1 - o, dpsi, Ff, x0[t], amb[t]);
+      acc32[t] = rule.fast(o, 1 - o, o ? -G[t] : G[t], x0[t], amb[t]);
     }
     // exact FP64 decisions where the FP32 one is ambiguous (rare)
     if (amb[0] || amb[1] || amb[2] || amb[3]) {
@@ -677,8 +695,8 @@ __device__ __forceinline__ void sweep_phase_quad_pipe(const QuadSweeper<B>& sw, 
                                                       int (&acc)[QuadSweeper<B>::NSLOT]) {
   const int e0 = cstart[c] + threadIdx.x, e_end = cstart[c + 1];
   if (e0 < e_end) {
-    uint32_t F[B::NFEAT];
-    B::template Pipe<P>::late(sw.loader(pf.ent), pf.st, F);
+    uint32_t F[B::NFEAT], Lw[B::template Pipe<P>::NGROUP];
+    B::template Pipe<P>::late(sw.loader(pf.ent), pf.st, F, Lw);
     sw.finish(pf.ent, pf.st.own, F, pf.x0, acc);
   }
 #pragma unroll 1
@@ -859,9 +877,9 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_const
 // ---- warp-specialised pipelined word sweep
 //
 // Two roles of NW threads each share a CTA.  During colour phase g the finish role takes
-// the decisions of phase g's words (late features, four FP32/FP64 decisions, write-back,
-// correlation changes) while the early role prepares phase g+1's words (Philox block and
-// early feature sums, which read no word of colour g) into a double-buffered staging area
+// the decisions of phase g's words (Philox block, late features, four FP32/FP64 decisions,
+// write-back, correlation changes) while the early role prepares phase g+1's words (early
+// feature sums, which read no word of colour g) into a double-buffered staging area
 // in shared memory.  Both roles meet at the phase's cluster barrier, so a phase costs about
 // the longer of the two roles rather than their sum.  Requires at most NW words per
 // (CTA, colour) and a generated pipeline colouring; trajectories equal the other kernels'.
@@ -870,32 +888,65 @@ struct WsStage {
   using State = typename B::template Pipe<P>::State;
   static constexpr int NF = B::NFEAT;
   static constexpr int NK = B::template Pipe<P>::NKEEP;
-  static constexpr int NFIELD = NF + NK + 1 + 4 + 1;  // E, K, own, x0[4], entry
+  static constexpr int NG = B::template Pipe<P>::NGROUP;
+  // E, K, own, entry, Philox counter word, early energy sums GE[4], late-group coefficients A[NG][4]
+  static constexpr int NFIELD = NF + NK + 3 + 4 + 4 * NG;
+
+  // the early part of the integer energy sums and, per late group g, the amount it adds
+  // to a site's sum when set: GE[t] = sum_k wq[k] E[k][t], A[g][t] = sum over the group's
+  // terms (feature k, kept word K or none, count n) of wq[k] n (K[t] or 1)
+  __device__ __forceinline__ static void sums(const State& st, const int* wq, int (&GE)[4], int (&A)[NG][4]) {
+    using PP = typename B::template Pipe<P>;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      GE[t] = 0;
+#pragma unroll
+      for (int k = 0; k < NF; ++k) GE[t] += wq[k] * (int)((st.E[k] >> (8 * t)) & 0xFFu);
+#pragma unroll
+      for (int g = 0; g < NG; ++g) A[g][t] = 0;
+#pragma unroll
+      for (int i = 0; i < PP::NTERM; ++i) {
+        const int kk = PP::term_keep(i);
+        const int val = kk < 0 ? 1 : (int)((st.K[kk < 0 ? 0 : kk] >> (8 * t)) & 0xFFu);
+        A[PP::term_group(i)][t] += wq[PP::term_feature(i)] * PP::term_count(i) * val;
+      }
+    }
+  }
 
   // field-major: base[field * NW + word]
   template <int NW>
-  __device__ __forceinline__ static void store(uint32_t* base, int w, const State& st, const uint32_t (&x0)[4],
-                                               uint32_t ent) {
+  __device__ __forceinline__ static void store(uint32_t* base, int w, const State& st, uint32_t ent, uint32_t q,
+                                               const int (&GE)[4], const int (&A)[NG][4]) {
 #pragma unroll
     for (int k = 0; k < NF; ++k) base[k * NW + w] = st.E[k];
 #pragma unroll
     for (int k = 0; k < NK; ++k) base[(NF + k) * NW + w] = st.K[k];
     base[(NF + NK) * NW + w] = st.own;
+    base[(NF + NK + 1) * NW + w] = ent;
+    base[(NF + NK + 2) * NW + w] = q;
 #pragma unroll
-    for (int t = 0; t < 4; ++t) base[(NF + NK + 1 + t) * NW + w] = x0[t];
-    base[(NF + NK + 5) * NW + w] = ent;
+    for (int t = 0; t < 4; ++t) base[(NF + NK + 3 + t) * NW + w] = (uint32_t)GE[t];
+#pragma unroll
+    for (int g = 0; g < NG; ++g)
+#pragma unroll
+      for (int t = 0; t < 4; ++t) base[(NF + NK + 7 + 4 * g + t) * NW + w] = (uint32_t)A[g][t];
   }
   template <int NW>
-  __device__ __forceinline__ static void load(const uint32_t* base, int w, State& st, uint32_t (&x0)[4],
-                                              uint32_t& ent) {
+  __device__ __forceinline__ static void load(const uint32_t* base, int w, State& st, uint32_t& ent, uint32_t& q,
+                                              int (&GE)[4], int (&A)[NG][4]) {
 #pragma unroll
     for (int k = 0; k < NF; ++k) st.E[k] = base[k * NW + w];
 #pragma unroll
     for (int k = 0; k < NK; ++k) st.K[k] = base[(NF + k) * NW + w];
     st.own = base[(NF + NK) * NW + w];
+    ent = base[(NF + NK + 1) * NW + w];
+    q = base[(NF + NK + 2) * NW + w];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) x0[t] = base[(NF + NK + 1 + t) * NW + w];
-    ent = base[(NF + NK + 5) * NW + w];
+    for (int t = 0; t < 4; ++t) GE[t] = (int)base[(NF + NK + 3 + t) * NW + w];
+#pragma unroll
+    for (int g = 0; g < NG; ++g)
+#pragma unroll
+      for (int t = 0; t < 4; ++t) A[g][t] = (int)base[(NF + NK + 7 + 4 * g + t) * NW + w];
   }
 };
 
@@ -936,6 +987,11 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
   int8_t* gocc = A.occ + (size_t)chain * N;
   const int lattice_words = RSY * (nkq + (nkr ? 1 : 0) + 2 * B::HALO);
   uint32_t* stage = sq + ((lattice_words + 3) & ~3);  // [2][NFIELD][NW]
+  // the CTA's site lists (entries, Philox counter words) and colour starts, copied once
+  const int max_words = Q * L1 * (nkq + (nkr ? 1 : 0));
+  uint32_t* ents = stage + 2 * Stage::NFIELD * NW;
+  uint32_t* sites = ents + max_words;
+  int* cst = reinterpret_cast<int*>(sites + max_words);
 
   // ---- load slab + borders (as ce_sweep_quad_kernel)
   for (int idx = threadIdx.x; idx < RSY * (nk + 2 * B::HALO); idx += 2 * NW) {
@@ -961,7 +1017,16 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
   const CeChainParams* cpg = A.cp + chain;
   load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
   const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
-  const int* cstart = g.color_start + rank * (g.n_colors + 1);
+  {
+    const int* cg0 = g.color_start + rank * (g.n_colors + 1);
+    const int base = cg0[0], n = cg0[g.n_colors] - base;
+    for (int i = threadIdx.x; i <= g.n_colors; i += 2 * NW) cst[i] = cg0[i] - base;
+    for (int i = threadIdx.x; i < n; i += 2 * NW) {
+      ents[i] = __ldg(g.entries + base + i);
+      sites[i] = __ldg(g.site_l + base + i);
+    }
+  }
+  const int* cstart = cst;
 
   QuadSweeper<B> sw;
   sw.s = sq;
@@ -984,22 +1049,22 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
 #pragma unroll
   for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
 
-  // early role: Philox block and early features of word tid of colour c into a stage slot
-  auto prepare = [&](int c, uint32_t pass, uint32_t* slot) {
+  // early role: early features and energy sums of word tid of colour c into a stage slot
+  auto prepare = [&](int c, uint32_t* slot) {
     const int e = cstart[c] + tid;
     if (e < cstart[c + 1]) {
-      const uint32_t ent = __ldg(A.g.entries + e);
-      const U32x4 x = philox4x32_10(U32x4{__ldg(A.g.site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
-      const uint32_t x0[4] = {x.x, x.y, x.z, x.w};
+      const uint32_t ent = ents[e];
       State st;
       B::template Pipe<PIPE>::early(sw.loader(ent), st);
-      Stage::template store<NW>(slot, tid, st, x0, ent);
+      int GE[4], Ac[Stage::NG][4];
+      Stage::sums(st, A.w.wq, GE, Ac);
+      Stage::template store<NW>(slot, tid, st, ent, sites[e], GE, Ac);
     }
   };
   constexpr int SLOT = Stage::NFIELD * NW;
 
   barrier();  // slab loaded
-  if (!finisher) prepare(0, (uint32_t)A.pass0, stage);
+  if (!finisher) prepare(0, stage);
   barrier();  // stage 0 ready
 
   int parity = 0;
@@ -1012,14 +1077,21 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
       if (finisher) {
         if (cstart[c] + tid < cstart[c + 1]) {
           State st;
-          uint32_t x0[4], ent;
-          Stage::template load<NW>(stage + parity * SLOT, tid, st, x0, ent);
-          uint32_t F[B::NFEAT];
-          B::template Pipe<PIPE>::late(sw.loader(ent), st, F);
-          sw.finish(ent, st.own, F, x0, acc);
+          uint32_t ent, q;
+          int G[4], Ac[Stage::NG][4];
+          Stage::template load<NW>(stage + parity * SLOT, tid, st, ent, q, G, Ac);
+          const U32x4 x = philox4x32_10(U32x4{q, pass_g, chain_id, SWEEP_TAG}, key0, key1);
+          const uint32_t x0[4] = {x.x, x.y, x.z, x.w};
+          uint32_t F[B::NFEAT], Lw[Stage::NG];
+          B::template Pipe<PIPE>::late(sw.loader(ent), st, F, Lw);
+#pragma unroll
+          for (int t = 0; t < 4; ++t)
+#pragma unroll
+            for (int gi = 0; gi < Stage::NG; ++gi) G[t] += (int)((Lw[gi] >> (8 * t)) & 1u) * Ac[gi][t];
+          sw.finish_g(ent, st.own, F, G, x0, acc);
         }
       } else {
-        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g, stage + (parity ^ 1) * SLOT);
+        prepare(last ? 0 : c + 1, stage + (parity ^ 1) * SLOT);
       }
       if (S > 1) {
         cluster_arrive_release();

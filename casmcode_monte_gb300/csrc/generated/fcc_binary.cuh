@@ -185,6 +185,26 @@ struct Pipe;
 template <>
 struct Pipe<0> {
   static constexpr int NKEEP = 5;
+  // late groups g (AND of late neighbours); F[k] gains sum over terms (g, k, keep, n) of
+  // n * group_g * (keep < 0 ? 1 : K[keep]) per byte
+  static constexpr int NGROUP = 2;
+  static constexpr int NTERM = 7;
+  __host__ __device__ static constexpr int term_group(int i) {
+    constexpr int t[NTERM] = {0, 1, 0, 0, 1, 0, 0};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int term_feature(int i) {
+    constexpr int t[NTERM] = {1, 2, 5, 6, 6, 7, 8};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int term_keep(int i) {
+    constexpr int t[NTERM] = {-1, -1, 0, 1, 2, 3, 4};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int term_count(int i) {
+    constexpr int t[NTERM] = {1, 1, 1, 1, 1, 1, 1};
+    return t[i];
+  }
   struct State {
     uint32_t E[NFEAT];
     uint32_t K[NKEEP];
@@ -272,7 +292,8 @@ struct Pipe<0> {
     s.K[4] = (v_0_m1_0 & v_0_m1_1) + (v_1_0_m1 & v_1_0_0);
   }
   template <class Loader>
-  __device__ static __forceinline__ void late(const Loader& ld, const State& s, uint32_t (&F)[NFEAT]) {
+  __device__ static __forceinline__ void late(const Loader& ld, const State& s, uint32_t (&F)[NFEAT],
+                                              uint32_t (&Lw)[NGROUP]) {
     const uint32_t v_m1_1_1 = ld(-1, 1, 1);
     const uint32_t v_1_m1_0 = ld(1, -1, 0);
     F[0] = s.E[0];
@@ -284,12 +305,34 @@ struct Pipe<0> {
     F[6] = s.E[6] + (((v_1_m1_0) * 0xFFu) & s.K[1]) + (((v_m1_1_1) * 0xFFu) & s.K[2]);
     F[7] = s.E[7] + (((v_1_m1_0) * 0xFFu) & s.K[3]);
     F[8] = s.E[8] + (((v_1_m1_0) * 0xFFu) & s.K[4]);
+    Lw[0] = v_1_m1_0;
+    Lw[1] = v_m1_1_1;
   }
 };
 // colouring (4 i + 6 j + 15 k) mod 16: late neighbours (0, 0, 1), (1, -1, -1)
 template <>
 struct Pipe<1> {
   static constexpr int NKEEP = 5;
+  // late groups g (AND of late neighbours); F[k] gains sum over terms (g, k, keep, n) of
+  // n * group_g * (keep < 0 ? 1 : K[keep]) per byte
+  static constexpr int NGROUP = 2;
+  static constexpr int NTERM = 7;
+  __host__ __device__ static constexpr int term_group(int i) {
+    constexpr int t[NTERM] = {0, 1, 0, 0, 1, 0, 0};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int term_feature(int i) {
+    constexpr int t[NTERM] = {1, 2, 5, 6, 6, 7, 8};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int term_keep(int i) {
+    constexpr int t[NTERM] = {-1, -1, 0, 1, 2, 3, 4};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int term_count(int i) {
+    constexpr int t[NTERM] = {1, 1, 1, 1, 1, 1, 1};
+    return t[i];
+  }
   struct State {
     uint32_t E[NFEAT];
     uint32_t K[NKEEP];
@@ -377,7 +420,8 @@ struct Pipe<1> {
     s.K[4] = (v_m1_0_1 & v_0_m1_1) + (v_0_1_0 & v_1_0_0);
   }
   template <class Loader>
-  __device__ static __forceinline__ void late(const Loader& ld, const State& s, uint32_t (&F)[NFEAT]) {
+  __device__ static __forceinline__ void late(const Loader& ld, const State& s, uint32_t (&F)[NFEAT],
+                                              uint32_t (&Lw)[NGROUP]) {
     const uint32_t v_0_0_1 = ld(0, 0, 1);
     const uint32_t v_1_m1_m1 = ld(1, -1, -1);
     F[0] = s.E[0];
@@ -389,6 +433,8 @@ struct Pipe<1> {
     F[6] = s.E[6] + (((v_0_0_1) * 0xFFu) & s.K[1]) + (((v_1_m1_m1) * 0xFFu) & s.K[2]);
     F[7] = s.E[7] + (((v_0_0_1) * 0xFFu) & s.K[3]);
     F[8] = s.E[8] + (((v_0_0_1) * 0xFFu) & s.K[4]);
+    Lw[0] = v_0_0_1;
+    Lw[1] = v_1_m1_m1;
   }
 };
 // C[f] += sum over decorated clusters of class f anchored at this site (its
