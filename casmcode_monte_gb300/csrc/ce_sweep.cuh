@@ -163,11 +163,16 @@ struct MetropolisRule {
     return d;
   }
 
+  // The band around P = 2^a, a = -beta log2(e) dE32, holds every u whose FP64 decision
+  // could differ: relative half-width eps (dE32's error bound through exp, the ex2.approx
+  // error and the roundings of u and of the band) plus |a| 1e-7 (rounding of a itself).
   __device__ __forceinline__ bool fast(int o, int o2, int dEq, uint32_t x0, bool& amb) const {
     const float dE32 = fmaf((float)dEq, w->qscale, -dmu32[o * NS + o2]);
     const float u32 = __uint2float_rn(x0) * 2.3283064365386963e-10f;
-    const float P = fast_exp2(-dE32 * beta_log2e);
-    const bool band = !(u32 < P * (1.f - eps)) && !(u32 > P * (1.f + eps));
+    const float a = -dE32 * beta_log2e;
+    const float P = fast_exp2(a);
+    const float e = fmaf(fabsf(a), 1.0e-7f, eps);
+    const bool band = !(u32 < P * (1.f - e)) && !(u32 > P * (1.f + e));
     amb = !(dE32 < -dtol) && ((dE32 <= dtol) || (x0 == 0u) || band);
     return (dE32 < 0.f) || (u32 < P);
   }
