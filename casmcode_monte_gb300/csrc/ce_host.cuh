@@ -423,9 +423,11 @@ inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* 
     // quantisation error + FP32 rounding of the integer change, of mu.N dx and of the sum
     const double dtol = m->qerr + 2.0 * std::ldexp(1.0, -23) * (m->qmax + dmu_max) + 1e-30;
     p.dtol = (float)(dtol * 1.0001);
-    // exp of dE32's error bound, ex2.approx (relative error below 2^-20), roundings of u
-    // and of the band edges (a few 2^-24); the kernel adds |a| 1e-7 for the rounding of a
-    p.eps = (float)(1.25 * p.beta * dtol + 1.2e-6);
+    // exp of the quantisation error and of mu.N dx's FP32 rounding, ex2.approx (measured
+    // relative error below 2^-22.7 on [-60, 0]; 2^-21 taken), roundings of u and of the band
+    // edges (2^-24 + 2^-23); the kernel adds 2e-7 |a| for the roundings that scale with dE32
+    p.eps = (float)(1.25 * p.beta * (m->qerr + 1.01 * std::ldexp(dmu_max, -23)) + std::ldexp(1.0, -21) +
+                    std::ldexp(1.0, -23) + std::ldexp(1.0, -24) + 1e-8);
     for (int i = 0; i < ns - 1; ++i) p.mu[i] = mu[(size_t)c * (ns - 1) + i];
     p.key0 = (uint32_t)seeds[c];
     p.key1 = (uint32_t)(seeds[c] >> 32);

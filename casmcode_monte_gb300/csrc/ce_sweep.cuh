@@ -164,14 +164,16 @@ struct MetropolisRule {
   }
 
   // The band around P = 2^a, a = -beta log2(e) dE32, holds every u whose FP64 decision
-  // could differ: relative half-width eps (dE32's error bound through exp, the ex2.approx
-  // error and the roundings of u and of the band) plus |a| 1e-7 (rounding of a itself).
+  // could differ: relative half-width eps (per chain: the quantisation error and the
+  // rounding of mu.N dx through exp, the ex2.approx error, the roundings of u and of the
+  // band edges) plus 2e-7 |a| (the FP32 roundings of dE32, of order 2^-23 |dE32|, through
+  // exp, and the rounding of a itself).
   __device__ __forceinline__ bool fast(int o, int o2, int dEq, uint32_t x0, bool& amb) const {
     const float dE32 = fmaf((float)dEq, w->qscale, -dmu32[o * NS + o2]);
     const float u32 = __uint2float_rn(x0) * 2.3283064365386963e-10f;
     const float a = -dE32 * beta_log2e;
     const float P = fast_exp2(a);
-    const float e = fmaf(fabsf(a), 1.0e-7f, eps);
+    const float e = fmaf(fabsf(a), 2.0e-7f, eps);
     const bool band = !(u32 < P * (1.f - e)) && !(u32 > P * (1.f + e));
     amb = !(dE32 < -dtol) && ((dE32 <= dtol) || (x0 == 0u) || band);
     return (dE32 < 0.f) || (u32 < P);
@@ -185,12 +187,10 @@ struct MetropolisRule {
 #pragma unroll
     for (int b = 0; b < B::NFUNC; ++b) G64[b] = 0.0;
 #pragma unroll
-    for (int k = 0; k < NF; ++k)
-      G64[B::feat_b(k)] = __dadd_rn(G64[B::feat_b(k)], __dmul_rn(w->w64[k], (double)Fi(k)));
-    double dE = 0.0;
+    for (int k = 0; k < NF; ++k) G64[B::feat_b(k)] = __fma_rn(w->w64[k], (double)Fi(k), G64[B::feat_b(k)]);
+    double dE = -dmu64[o * NS + o2];
 #pragma unroll
-    for (int b = 0; b < B::NFUNC; ++b) dE = __dadd_rn(dE, __dmul_rn((double)dpsi[b], G64[b]));
-    dE = __dsub_rn(dE, dmu64[o * NS + o2]);
+    for (int b = 0; b < B::NFUNC; ++b) dE = __fma_rn((double)dpsi[b], G64[b], dE);
     bool acc64;
     if (dE < 0.0) {
       acc64 = true;
