@@ -882,9 +882,10 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_const
 // ---- warp-specialised pipelined word sweep
 //
 // Two roles of NW threads each share a CTA.  During colour phase g the finish role takes
-// the decisions of phase g's words (Philox block, late features, four FP32/FP64 decisions,
-// write-back, correlation changes) while the early role prepares phase g+1's words (early
-// feature sums, which read no word of colour g) into a double-buffered staging area
+// the decisions of phase g's words (late features, four FP32/FP64 decisions, write-back,
+// correlation changes) while the early role prepares phase g+1's words (Philox block,
+// early feature and energy sums, which read no word of colour g) into a double-buffered
+// staging area
 // in shared memory.  Both roles meet at the phase's cluster barrier, so a phase costs about
 // the longer of the two roles rather than their sum.  Requires at most NW words per
 // (CTA, colour) and a generated pipeline colouring; trajectories equal the other kernels'.
@@ -894,8 +895,8 @@ struct WsStage {
   static constexpr int NF = B::NFEAT;
   static constexpr int NK = B::template Pipe<P>::NKEEP;
   static constexpr int NG = B::template Pipe<P>::NGROUP;
-  // E, K, own, entry, Philox counter word, early energy sums GE[4], late-group coefficients A[NG][4]
-  static constexpr int NFIELD = NF + NK + 3 + 4 + 4 * NG;
+  // E, K, own, entry, Philox words x0[4], early energy sums GE[4], late-group coefficients A[NG][4]
+  static constexpr int NFIELD = NF + NK + 2 + 4 + 4 + 4 * NG;
 
   // the early part of the integer energy sums and, per late group g, the amount it adds
   // to a site's sum when set: GE[t] = sum_k wq[k] E[k][t], A[g][t] = sum over the group's
@@ -920,38 +921,40 @@ struct WsStage {
 
   // field-major: base[field * NW + word]
   template <int NW>
-  __device__ __forceinline__ static void store(uint32_t* base, int w, const State& st, uint32_t ent, uint32_t q,
-                                               const int (&GE)[4], const int (&A)[NG][4]) {
+  __device__ __forceinline__ static void store(uint32_t* base, int w, const State& st, uint32_t ent,
+                                               const uint32_t (&x0)[4], const int (&GE)[4], const int (&A)[NG][4]) {
 #pragma unroll
     for (int k = 0; k < NF; ++k) base[k * NW + w] = st.E[k];
 #pragma unroll
     for (int k = 0; k < NK; ++k) base[(NF + k) * NW + w] = st.K[k];
     base[(NF + NK) * NW + w] = st.own;
     base[(NF + NK + 1) * NW + w] = ent;
-    base[(NF + NK + 2) * NW + w] = q;
 #pragma unroll
-    for (int t = 0; t < 4; ++t) base[(NF + NK + 3 + t) * NW + w] = (uint32_t)GE[t];
+    for (int t = 0; t < 4; ++t) base[(NF + NK + 2 + t) * NW + w] = x0[t];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) base[(NF + NK + 6 + t) * NW + w] = (uint32_t)GE[t];
 #pragma unroll
     for (int g = 0; g < NG; ++g)
 #pragma unroll
-      for (int t = 0; t < 4; ++t) base[(NF + NK + 7 + 4 * g + t) * NW + w] = (uint32_t)A[g][t];
+      for (int t = 0; t < 4; ++t) base[(NF + NK + 10 + 4 * g + t) * NW + w] = (uint32_t)A[g][t];
   }
   template <int NW>
-  __device__ __forceinline__ static void load(const uint32_t* base, int w, State& st, uint32_t& ent, uint32_t& q,
-                                              int (&GE)[4], int (&A)[NG][4]) {
+  __device__ __forceinline__ static void load(const uint32_t* base, int w, State& st, uint32_t& ent,
+                                              uint32_t (&x0)[4], int (&GE)[4], int (&A)[NG][4]) {
 #pragma unroll
     for (int k = 0; k < NF; ++k) st.E[k] = base[k * NW + w];
 #pragma unroll
     for (int k = 0; k < NK; ++k) st.K[k] = base[(NF + k) * NW + w];
     st.own = base[(NF + NK) * NW + w];
     ent = base[(NF + NK + 1) * NW + w];
-    q = base[(NF + NK + 2) * NW + w];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) GE[t] = (int)base[(NF + NK + 3 + t) * NW + w];
+    for (int t = 0; t < 4; ++t) x0[t] = base[(NF + NK + 2 + t) * NW + w];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) GE[t] = (int)base[(NF + NK + 6 + t) * NW + w];
 #pragma unroll
     for (int g = 0; g < NG; ++g)
 #pragma unroll
-      for (int t = 0; t < 4; ++t) A[g][t] = (int)base[(NF + NK + 7 + 4 * g + t) * NW + w];
+      for (int t = 0; t < 4; ++t) A[g][t] = (int)base[(NF + NK + 10 + 4 * g + t) * NW + w];
   }
 };
 
@@ -1054,22 +1057,25 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
 #pragma unroll
   for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
 
-  // early role: early features and energy sums of word tid of colour c into a stage slot
-  auto prepare = [&](int c, uint32_t* slot) {
+  // early role: Philox block, early features and energy sums of word tid of colour c
+  // (pass `pass`) into a stage slot
+  auto prepare = [&](int c, uint32_t pass, uint32_t* slot) {
     const int e = cstart[c] + tid;
     if (e < cstart[c + 1]) {
       const uint32_t ent = ents[e];
+      const U32x4 x = philox4x32_10(U32x4{sites[e], pass, chain_id, SWEEP_TAG}, key0, key1);
+      const uint32_t x0[4] = {x.x, x.y, x.z, x.w};
       State st;
       B::template Pipe<PIPE>::early(sw.loader(ent), st);
       int GE[4], Ac[Stage::NG][4];
       Stage::sums(st, A.w.wq, GE, Ac);
-      Stage::template store<NW>(slot, tid, st, ent, sites[e], GE, Ac);
+      Stage::template store<NW>(slot, tid, st, ent, x0, GE, Ac);
     }
   };
   constexpr int SLOT = Stage::NFIELD * NW;
 
   barrier();  // slab loaded
-  if (!finisher) prepare(0, stage);
+  if (!finisher) prepare(0, (uint32_t)A.pass0, stage);
   barrier();  // stage 0 ready
 
   int parity = 0;
@@ -1082,11 +1088,9 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
       if (finisher) {
         if (cstart[c] + tid < cstart[c + 1]) {
           State st;
-          uint32_t ent, q;
+          uint32_t ent, x0[4];
           int G[4], Ac[Stage::NG][4];
-          Stage::template load<NW>(stage + parity * SLOT, tid, st, ent, q, G, Ac);
-          const U32x4 x = philox4x32_10(U32x4{q, pass_g, chain_id, SWEEP_TAG}, key0, key1);
-          const uint32_t x0[4] = {x.x, x.y, x.z, x.w};
+          Stage::template load<NW>(stage + parity * SLOT, tid, st, ent, x0, G, Ac);
           uint32_t F[B::NFEAT], Lw[Stage::NG];
           B::template Pipe<PIPE>::late(sw.loader(ent), st, F, Lw);
 #pragma unroll
@@ -1096,7 +1100,7 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
           sw.finish_g(ent, st.own, F, G, x0, acc);
         }
       } else {
-        prepare(last ? 0 : c + 1, stage + (parity ^ 1) * SLOT);
+        prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g, stage + (parity ^ 1) * SLOT);
       }
       if (S > 1) {
         cluster_arrive_release();
