@@ -25,18 +25,25 @@ constexpr int kMaxGeoms = 1024;
 // CTA classes: chains are swept by 1, 2, 4, 8 or 16 CTAs (the smallest whose slab fits)
 constexpr int kClasses = 5;
 constexpr int kClassS[kClasses] = {1, 2, 4, 8, 16};
+// launch groups: (CTA class, layout) with layout 0 = one site per byte, 1 = four per word
+constexpr int kGroups = 2 * kClasses;
 
 struct PoolGeom {
-  int L0 = 0, L1 = 0, L2 = 0, S = 1, n_colors = 0;
+  int L0 = 0, L1 = 0, L2 = 0, S = 1, layout = 0, n_colors = 0;
   int* dcstart = nullptr;
   uint32_t* dentries = nullptr;
   uint32_t* dsite = nullptr;
+};
+
+// per supercell shape: colouring, layout and CTA class (computed once)
+struct ShapePlan {
   std::vector<int32_t> color;
+  int n_colors = 0, layout = 0, cls = 0;
 };
 
 struct PoolSlot {
   bool used = false;
-  int L0 = 0, L1 = 0, L2 = 0, cls = 0;
+  int L0 = 0, L1 = 0, L2 = 0, cls = 0, layout = 0;
   long long N = 0, offset = 0, pass = 0;
   int geom = -1;
 };
@@ -52,17 +59,18 @@ struct mg_ce_pool {
   std::vector<PoolSlot> slots;
   std::vector<PoolGeom> geoms;
   std::map<std::tuple<int, int, int, int>, int> geom_index;
+  std::map<std::tuple<int, int, int>, ShapePlan> plans;
   mg::CeChainParams* dcp = nullptr;
   mg::PoolGeometry* dgeoms = nullptr;
   mg::PoolItem* ditems = nullptr;
-  int* dcounter = nullptr;  // one work counter per CTA class
+  int* dcounter = nullptr;  // one work counter per launch group
   long long* dcorr = nullptr;
   long long* dout = nullptr;
   size_t out_cap = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t cls_stream[kClasses] = {};
+  cudaStream_t cls_stream[kGroups] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t cls_done[kClasses] = {};
+  cudaEvent_t cls_done[kGroups] = {};
   float last_ms = 0.f;
   // device-resident sample series (potential energy per site after every pass)
   int max_samples = 0;
@@ -92,7 +100,7 @@ void free_pool(mg_ce_pool* p) {
   cudaFree(p->dseries);
   cudaFree(p->dnsamp);
   cudaFree(p->dcheck);
-  for (int c = 0; c < kClasses; ++c) {
+  for (int c = 0; c < kGroups; ++c) {
     if (p->cls_stream[c]) cudaStreamDestroy(p->cls_stream[c]);
     if (p->cls_done[c]) cudaEventDestroy(p->cls_done[c]);
   }
@@ -134,7 +142,50 @@ void arena_free(mg_ce_pool* p, long long off, long long n) {
   }
 }
 
-int geometry(mg_ce_pool* p, int L0, int L1, int L2, int S, int* out) {
+// Colouring, layout and CTA class of a supercell shape (cached): the word layout where the
+// basis and colouring allow it and some class fits it, else the byte layout; the class is
+// the smallest CTA count whose slab fits in shared memory.
+int shape_plan(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan** out) {
+  auto key = std::make_tuple(L0, L1, L2);
+  auto it = p->plans.find(key);
+  if (it != p->plans.end()) {
+    *out = &it->second;
+    return MG_OK;
+  }
+  int dev = 0, max_smem = 0;
+  MG_CUDA_TRY(cudaGetDevice(&dev));
+  MG_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  ShapePlan sp;
+  sp.color.assign((size_t)L0 * L1 * L2, -1);
+  sp.n_colors = color_supercell(L0, L1, L2, p->model->kind, sp.color.data());
+  if (sp.n_colors < 1) {
+    set_error("Error in mg_ce_pool_add: colouring needs more than 64 colours");
+    return MG_ERR_INVALID;
+  }
+  auto fit = [&](int layout) {
+    for (int c = 0; c < kClasses; ++c) {
+      const int S = kClassS[c];
+      if (L2 / S >= mg::CE_HALO && layout_smem(layout, L0, L1, L2, S) <= (size_t)max_smem - 1024) return c;
+    }
+    return -1;
+  };
+  sp.layout = 0;
+  sp.cls = -1;
+  if (quad_eligible(p->model->kind, L0, L1, L2, sp.color.data())) {
+    sp.cls = fit(1);
+    if (sp.cls >= 0) sp.layout = 1;
+  }
+  if (sp.cls < 0) sp.cls = fit(0);
+  if (sp.cls < 0) {
+    set_error("Error in mg_ce_pool_add: supercell slab does not fit in shared memory with 16 CTAs");
+    return MG_ERR_INVALID;
+  }
+  *out = &(p->plans[key] = std::move(sp));
+  return MG_OK;
+}
+
+int geometry(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan& sp, int* out) {
+  const int S = kClassS[sp.cls];
   auto key = std::make_tuple(L0, L1, L2, S);
   auto it = p->geom_index.find(key);
   if (it != p->geom_index.end()) {
@@ -146,26 +197,27 @@ int geometry(mg_ce_pool* p, int L0, int L1, int L2, int S, int* out) {
     return MG_ERR_INVALID;
   }
   const long long N = (long long)L0 * L1 * L2;
+  const long long n_entries = sp.layout == 1 ? N / 4 : N;
   PoolGeom g;
   g.L0 = L0;
   g.L1 = L1;
   g.L2 = L2;
   g.S = S;
-  g.color.assign(N, -1);
-  g.n_colors = color_supercell(L0, L1, L2, p->model->kind, g.color.data());
-  if (g.n_colors < 1) {
-    set_error("Error in mg_ce_pool_add: colouring needs more than 64 colours");
-    return MG_ERR_INVALID;
-  }
+  g.layout = sp.layout;
+  g.n_colors = sp.n_colors;
   std::vector<int> cstart((size_t)S * (g.n_colors + 1));
-  std::vector<uint32_t> entries(N), site(N);
-  build_site_lists(L0, L1, L2, S, g.color.data(), g.n_colors, p->model->kind, cstart.data(), entries.data(), site.data());
+  std::vector<uint32_t> entries(n_entries), site(n_entries);
+  if (sp.layout == 1)
+    build_word_lists(L0, L1, L2, S, sp.color.data(), g.n_colors, cstart.data(), entries.data(), site.data());
+  else
+    build_site_lists(L0, L1, L2, S, sp.color.data(), g.n_colors, p->model->kind, cstart.data(), entries.data(),
+                     site.data());
   MG_CUDA_TRY(cudaMalloc(&g.dcstart, sizeof(int) * cstart.size()));
-  MG_CUDA_TRY(cudaMalloc(&g.dentries, sizeof(uint32_t) * N));
-  MG_CUDA_TRY(cudaMalloc(&g.dsite, sizeof(uint32_t) * N));
+  MG_CUDA_TRY(cudaMalloc(&g.dentries, sizeof(uint32_t) * n_entries));
+  MG_CUDA_TRY(cudaMalloc(&g.dsite, sizeof(uint32_t) * n_entries));
   MG_CUDA_TRY(cudaMemcpyAsync(g.dcstart, cstart.data(), sizeof(int) * cstart.size(), cudaMemcpyHostToDevice, p->stream));
-  MG_CUDA_TRY(cudaMemcpyAsync(g.dentries, entries.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice, p->stream));
-  MG_CUDA_TRY(cudaMemcpyAsync(g.dsite, site.data(), sizeof(uint32_t) * N, cudaMemcpyHostToDevice, p->stream));
+  MG_CUDA_TRY(cudaMemcpyAsync(g.dentries, entries.data(), sizeof(uint32_t) * n_entries, cudaMemcpyHostToDevice, p->stream));
+  MG_CUDA_TRY(cudaMemcpyAsync(g.dsite, site.data(), sizeof(uint32_t) * n_entries, cudaMemcpyHostToDevice, p->stream));
   mg::PoolGeometry dg{L0, L1, L2, g.n_colors, g.dcstart, g.dentries, g.dsite};
   const int gi = (int)p->geoms.size();
   MG_CUDA_TRY(cudaMemcpyAsync(p->dgeoms + gi, &dg, sizeof(dg), cudaMemcpyHostToDevice, p->stream));
@@ -177,12 +229,12 @@ int geometry(mg_ce_pool* p, int L0, int L1, int L2, int S, int* out) {
 }
 
 template <class B, int NT>
-int launch_pool(mg_ce_pool* p, int cls, int item0, int n_items, int n_passes, size_t smem) {
+int launch_pool(mg_ce_pool* p, int cls, int layout, int item0, int n_items, int n_passes, size_t smem) {
   mg::CePoolArgs<B::NFEAT> A;
   A.geoms = p->dgeoms;
   A.items = p->ditems + item0;
   A.n_items = n_items;
-  A.next_item = p->dcounter + cls;
+  A.next_item = p->dcounter + 2 * cls + layout;
   mg::host::fill_weights(p->model, A.w);
   A.cp = p->dcp;
   A.occ = p->darena;
@@ -190,12 +242,14 @@ int launch_pool(mg_ce_pool* p, int cls, int item0, int n_items, int n_passes, si
   A.precision = p->precision;
   A.out = p->dout;
   const int S = kClassS[cls];
-  cudaStream_t st = p->cls_stream[cls];
+  cudaStream_t st = p->cls_stream[2 * cls + layout];
   if (S == 1) {
-    auto kern = mg::ce_pool_kernel<B, NT>;
+    const void* kern = (const void*)mg::ce_pool_kernel<B, NT>;
+    if (layout == 1) kern = (const void*)mg::ce_pool_quad_kernel<mg::FccBinary, NT_QUAD, false>;
+    const int nt = layout == 1 ? NT_QUAD : NT;
     MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0, dev = 0, sms = 0;
-    MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+    MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
     MG_CUDA_TRY(cudaGetDevice(&dev));
     MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (per_sm < 1) {
@@ -203,15 +257,18 @@ int launch_pool(mg_ce_pool* p, int cls, int item0, int n_items, int n_passes, si
       return MG_ERR_INVALID;
     }
     const int grid = std::max(1, std::min(n_items, per_sm * sms));
-    kern<<<grid, NT, smem, st>>>(A);
+    void* args[] = {(void*)&A};
+    MG_CUDA_TRY(cudaLaunchKernel(kern, dim3(grid), dim3(nt), args, smem, st));
     MG_CUDA_TRY(cudaGetLastError());
     return MG_OK;
   }
-  auto kern = mg::ce_pool_cluster_kernel<B, NT>;
+  const void* kern = (const void*)mg::ce_pool_cluster_kernel<B, NT>;
+  if (layout == 1) kern = (const void*)mg::ce_pool_quad_kernel<mg::FccBinary, NT_QUAD, true>;
+  const int nt = layout == 1 ? NT_QUAD : NT;
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
-  cfg.blockDim = dim3(NT, 1, 1);
+  cfg.blockDim = dim3(nt, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -223,13 +280,14 @@ int launch_pool(mg_ce_pool* p, int cls, int item0, int n_items, int n_passes, si
   cfg.numAttrs = 1;
   cfg.gridDim = dim3((unsigned)S, 1, 1);
   int n_cl = 0;
-  MG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n_cl, (void*)kern, &cfg));
+  MG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n_cl, kern, &cfg));
   if (n_cl < 1) {
     set_error("Error in mg_ce_pool_run: no cluster of this size can be scheduled");
     return MG_ERR_INVALID;
   }
   cfg.gridDim = dim3((unsigned)(S * std::max(1, std::min(n_items, n_cl))), 1, 1);
-  MG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
+  void* args[] = {(void*)&A};
+  MG_CUDA_TRY(cudaLaunchKernelExC(&cfg, kern, args));
   MG_CUDA_TRY(cudaGetLastError());
   return MG_OK;
 }
@@ -327,7 +385,7 @@ int mg_ce_pool_create(const mg_ce_model* m, long long arena_bytes, int max_chain
     return MG_ERR_CUDA;
   };
   if ((e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail("stream");
-  for (int c = 0; c < kClasses; ++c) {
+  for (int c = 0; c < kGroups; ++c) {
     if ((e = cudaStreamCreateWithFlags(&p->cls_stream[c], cudaStreamNonBlocking)) != cudaSuccess) return fail("stream");
     if ((e = cudaEventCreateWithFlags(&p->cls_done[c], cudaEventDisableTiming)) != cudaSuccess) return fail("event");
   }
@@ -337,25 +395,9 @@ int mg_ce_pool_create(const mg_ce_model* m, long long arena_bytes, int max_chain
   if ((e = cudaMalloc(&p->dcp, sizeof(mg::CeChainParams) * max_chains)) != cudaSuccess) return fail("params");
   if ((e = cudaMalloc(&p->dgeoms, sizeof(mg::PoolGeometry) * kMaxGeoms)) != cudaSuccess) return fail("geoms");
   if ((e = cudaMalloc(&p->ditems, sizeof(mg::PoolItem) * max_chains)) != cudaSuccess) return fail("items");
-  if ((e = cudaMalloc(&p->dcounter, sizeof(int) * kClasses)) != cudaSuccess) return fail("counter");
+  if ((e = cudaMalloc(&p->dcounter, sizeof(int) * kGroups)) != cudaSuccess) return fail("counter");
   if ((e = cudaMalloc(&p->dcorr, sizeof(long long) * 64)) != cudaSuccess) return fail("corr");
   *out = p;
-  return MG_OK;
-}
-
-static int pool_class(int L0, int L1, int L2, int* cls) {
-  int dev = 0, max_smem = 0;
-  MG_CUDA_TRY(cudaGetDevice(&dev));
-  MG_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  *cls = -1;
-  for (int c = 0; c < kClasses && *cls < 0; ++c) {
-    const int S = kClassS[c];
-    if (L2 / S >= mg::CE_HALO && slab_smem(L0, L1, L2, S) <= (size_t)max_smem - 1024) *cls = c;
-  }
-  if (*cls < 0) {
-    set_error("Error in mg_ce_pool_add: supercell slab does not fit in shared memory with 16 CTAs");
-    return MG_ERR_INVALID;
-  }
   return MG_OK;
 }
 
@@ -364,10 +406,11 @@ int mg_ce_pool_prepare(mg_ce_pool* p, int L0, int L1, int L2) {
     set_error("Error in mg_ce_pool_prepare: invalid argument");
     return MG_ERR_INVALID;
   }
-  int cls = 0, gi = 0;
-  int rc = pool_class(L0, L1, L2, &cls);
+  const ShapePlan* sp = nullptr;
+  int gi = 0;
+  int rc = shape_plan(p, L0, L1, L2, &sp);
   if (rc != MG_OK) return rc;
-  return geometry(p, L0, L1, L2, kClassS[cls], &gi);
+  return geometry(p, L0, L1, L2, *sp, &gi);
 }
 
 int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, const double* mu,
@@ -390,9 +433,9 @@ int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, co
       set_error("Error in mg_ce_pool_add: occupant index out of range");
       return MG_ERR_INVALID;
     }
-  int cls = -1;
+  const ShapePlan* sp = nullptr;
   {
-    const int rc0 = pool_class(L0, L1, L2, &cls);
+    const int rc0 = shape_plan(p, L0, L1, L2, &sp);
     if (rc0 != MG_OK) return rc0;
   }
   int slot = -1;
@@ -411,7 +454,7 @@ int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, co
     return MG_ERR_FULL;
   }
   int gi = -1;
-  int rc = geometry(p, L0, L1, L2, kClassS[cls], &gi);
+  int rc = geometry(p, L0, L1, L2, *sp, &gi);
   if (rc != MG_OK) {
     arena_free(p, off, N);
     return rc;
@@ -439,7 +482,8 @@ int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, co
   s.L0 = L0;
   s.L1 = L1;
   s.L2 = L2;
-  s.cls = cls;
+  s.cls = sp->cls;
+  s.layout = sp->layout;
   s.N = N;
   s.offset = off;
   s.pass = 0;
@@ -497,24 +541,26 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
     seen[slots[i]] = 1;
     order[i] = i;
   }
-  // grouped by CTA class, largest chains first within a class (LPT work queue)
+  // grouped by launch group (CTA class, layout), largest chains first within a group
+  // (LPT work queue)
+  auto group = [&](const PoolSlot& x) { return 2 * x.cls + x.layout; };
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     const PoolSlot &x = p->slots[slots[a]], &y = p->slots[slots[b]];
-    if (x.cls != y.cls) return x.cls < y.cls;
+    if (group(x) != group(y)) return group(x) < group(y);
     return x.N > y.N;
   });
   std::vector<mg::PoolItem> items(n);
-  int first[kClasses + 1] = {};
-  size_t smem[kClasses] = {};
-  for (int c = 0; c <= kClasses; ++c) first[c] = n;
+  int first[kGroups + 1] = {};
+  size_t smem[kGroups] = {};
+  for (int c = 0; c <= kGroups; ++c) first[c] = n;
   for (int t = n - 1; t >= 0; --t) {
     const int i = order[t];
     const PoolSlot& s = p->slots[slots[i]];
     items[t] = mg::PoolItem{s.geom, slots[i], s.offset, (long long)i * n_passes * nslot, s.pass};
-    first[s.cls] = t;
-    smem[s.cls] = std::max(smem[s.cls], slab_smem(s.L0, s.L1, s.L2, kClassS[s.cls]));
+    first[group(s)] = t;
+    smem[group(s)] = std::max(smem[group(s)], layout_smem(s.layout, s.L0, s.L1, s.L2, kClassS[s.cls]));
   }
-  for (int c = kClasses - 1; c >= 0; --c) first[c] = std::min(first[c], first[c + 1]);
+  for (int c = kGroups - 1; c >= 0; --c) first[c] = std::min(first[c], first[c + 1]);
   const size_t need = (size_t)n * n_passes * nslot;
   if (need > p->out_cap) {
     cudaFree(p->dout);
@@ -523,17 +569,19 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
     p->out_cap = need;
   }
   MG_CUDA_TRY(cudaMemcpyAsync(p->ditems, items.data(), sizeof(mg::PoolItem) * n, cudaMemcpyHostToDevice, p->stream));
-  MG_CUDA_TRY(cudaMemsetAsync(p->dcounter, 0, sizeof(int) * kClasses, p->stream));
+  MG_CUDA_TRY(cudaMemsetAsync(p->dcounter, 0, sizeof(int) * kGroups, p->stream));
   MG_CUDA_TRY(cudaMemsetAsync(p->dout, 0, sizeof(long long) * need, p->stream));
   MG_CUDA_TRY(cudaEventRecord(p->ev0, p->stream));
   // one launch per CTA class, each on its own stream after the set-up copies; the
   // largest class first so that its long chains start while the others fill in
-  for (int c = kClasses - 1; c >= 0; --c) {
+  for (int c = kGroups - 1; c >= 0; --c) {
     const int cnt = first[c + 1] - first[c];
     if (cnt <= 0) continue;
     MG_CUDA_TRY(cudaStreamWaitEvent(p->cls_stream[c], p->ev0, 0));
-    int rc = p->model->kind == 0 ? launch_pool<mg::FccBinary, mg::NT_BINARY>(p, c, first[c], cnt, n_passes, smem[c])
-                                 : launch_pool<mg::FccTernary, mg::NT_TERNARY>(p, c, first[c], cnt, n_passes, smem[c]);
+    const int cls = c / 2, layout = c % 2;
+    int rc = p->model->kind == 0
+                 ? launch_pool<mg::FccBinary, mg::NT_BINARY>(p, cls, layout, first[c], cnt, n_passes, smem[c])
+                 : launch_pool<mg::FccTernary, mg::NT_TERNARY>(p, cls, layout, first[c], cnt, n_passes, smem[c]);
     if (rc != MG_OK) return rc;
     MG_CUDA_TRY(cudaEventRecord(p->cls_done[c], p->cls_stream[c]));
     MG_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->cls_done[c], 0));
@@ -657,9 +705,10 @@ int mg_ce_pool_colors(const mg_ce_pool* p, int slot, int32_t* color) {
     set_error("Error in mg_ce_pool_colors: invalid argument");
     return MG_ERR_INVALID;
   }
-  const PoolGeom& g = p->geoms[p->slots[slot].geom];
-  std::copy(g.color.begin(), g.color.end(), color);
-  return g.n_colors;
+  const PoolSlot& sl = p->slots[slot];
+  const ShapePlan& sp = p->plans.at(std::make_tuple(sl.L0, sl.L1, sl.L2));
+  std::copy(sp.color.begin(), sp.color.end(), color);
+  return sp.n_colors;
 }
 
 int mg_ce_pool_corr(mg_ce_pool* p, int slot, long long* out) {

@@ -1399,6 +1399,151 @@ __global__ void __launch_bounds__(NT, 1) ce_pool_cluster_kernel(const __grid_con
   }
 }
 
+// Persistent pool kernel over word-layout geometries (binary basis): as ce_pool_kernel
+// (CLUSTER = false, one CTA per chain) or ce_pool_cluster_kernel (CLUSTER = true, S CTAs
+// per chain), with the lattice held four sites per word (see ce_sweep_quad_kernel).
+// Per-pass outputs are accumulated with atomics (the host zeroes them).
+template <class B, int NT, bool CLUSTER>
+__global__ void __launch_bounds__(NT, 1) ce_pool_quad_kernel(const __grid_constant__ CePoolArgs<B::NFEAT> A) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  extern __shared__ __align__(16) uint32_t sq[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+  __shared__ int item_sm;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int S = CLUSTER ? (int)cluster.num_blocks() : 1;
+  const int rank = CLUSTER ? (int)cluster.block_rank() : 0;
+  const int lane = threadIdx.x & 31;
+  auto sync_all = [&]() {
+    if (CLUSTER)
+      cluster.sync();
+    else
+      __syncthreads();
+  };
+
+#pragma unroll 1
+  while (true) {
+    if (rank == 0 && threadIdx.x == 0) {
+      const int it = atomicAdd(A.next_item, 1);
+      if (CLUSTER) {
+        for (int r = 0; r < S; ++r) *cluster.map_shared_rank(&item_sm, (unsigned)r) = it;
+      } else {
+        item_sm = it;
+      }
+    }
+    sync_all();
+    const int it = item_sm;
+    if (it >= A.n_items) break;
+    const PoolItem item = A.items[it];
+    const PoolGeometry g = A.geoms[item.geom];
+    const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+    const int Q = L0 / 4, RS = (Q + 2 * B::HALO) | 1, RY = L1 + 2 * B::HALO, RSY = RS * RY;
+    const int nkq = L2 / S, nkr = L2 % S;
+    const int nk = nkq + (rank < nkr ? 1 : 0);
+    const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+    const int rprev = (rank + S - 1) % S;
+    const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
+    int8_t* gocc = A.occ + item.occ_offset;
+    for (int idx = threadIdx.x; idx < RSY * (nk + 2 * B::HALO); idx += NT) {
+      const int wp = idx % RS, jp = (idx / RS) % RY, kp = idx / RSY;
+      const int w = wp - B::HALO;
+      uint32_t word = 0u;
+      if (w < Q + B::HALO) {
+        int j = jp - B::HALO, k = k0 + kp - B::HALO;
+        j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+        k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+        const int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          int i = w + t * Q;
+          i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+          word |= (uint32_t)(uint8_t)row[i] << (8 * t);
+        }
+      }
+      sq[idx] = word;
+    }
+    if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+    const CeChainParams* cpg = A.cp + item.param;
+    load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+    const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+    const int* cstart = g.color_start + rank * (g.n_colors + 1);
+    QuadSweeper<B> sw;
+    sw.s = sq;
+    sw.s_prev = sq;
+    sw.s_next = sq;
+    if (CLUSTER) {
+      sw.s_prev = cluster.map_shared_rank(sq, (unsigned)rprev);
+      sw.s_next = cluster.map_shared_rank(sq, (unsigned)((rank + 1) % S));
+    }
+    sw.RS = RS;
+    sw.RSY = RSY;
+    sw.Q = Q;
+    sw.dJ = L1 * RS;
+    sw.dKp = nk_prev * RSY;
+    sw.dKn = nk * RSY;
+    sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
+                                A.precision};
+    int acc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+    long long* out = A.out + item.out_offset;
+    QuadPrefetch pf;
+    pf.template prepare<NT>(cstart, 0, g.entries, g.site_l, Q, (uint32_t)item.pass0, chain_id, key0, key1);
+    sync_all();
+#pragma unroll 1
+    for (int pass = 0; pass < A.n_passes; ++pass) {
+      const uint32_t pass_g = (uint32_t)(item.pass0 + pass);
+#pragma unroll 1
+      for (int c = 0; c < g.n_colors; ++c) {
+        sweep_phase_quad<B, NT>(sw, pf, cstart, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
+        const bool last = (c + 1 == g.n_colors);
+        if (CLUSTER) {
+          cluster_arrive_release();
+          pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, Q, last ? pass_g + 1 : pass_g,
+                                  chain_id, key0, key1);
+          cluster_wait_acquire();
+        } else {
+          pf.template prepare<NT>(cstart, last ? 0 : c + 1, g.entries, g.site_l, Q, last ? pass_g + 1 : pass_g,
+                                  chain_id, key0, key1);
+          __syncthreads();
+        }
+        if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+          int* buf = acc_sm[(pass - 1) & 1];
+          const int v = buf[threadIdx.x];
+          buf[threadIdx.x] = 0;
+          if (v)
+            atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)(pass - 1) * NSLOT + threadIdx.x),
+                      (unsigned long long)(long long)v);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q) {
+        const int v = warp_sum(acc[q]);
+        if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+        acc[q] = 0;
+      }
+    }
+    sync_all();
+    if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+      const int pl = A.n_passes - 1;
+      const int v = acc_sm[pl & 1][threadIdx.x];
+      if (v)
+        atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)pl * NSLOT + threadIdx.x),
+                  (unsigned long long)(long long)v);
+    }
+    for (int idx = threadIdx.x; idx < Q * L1 * nk; idx += NT) {
+      const int w = idx % Q, j = (idx / Q) % L1, kl = idx / (Q * L1);
+      const uint32_t word = sq[(w + B::HALO) + RS * ((j + B::HALO) + RY * (kl + B::HALO))];
+      int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * (k0 + kl));
+#pragma unroll
+      for (int t = 0; t < 4; ++t) row[w + t * Q] = (int8_t)((word >> (8 * t)) & 0xFFu);
+    }
+    sync_all();
+  }
+}
+
 // ---- global-memory evaluation (per-proposal dE and full correlation sums)
 
 struct GlobalLoader {
