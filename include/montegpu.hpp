@@ -1,0 +1,185 @@
+/* C++ facade over the montegpu C-ABI: RAII handles whose methods throw std::runtime_error
+ * with the library's "Error in ..." message (the reference reports failures the same way,
+ * include/casm/monte/definitions.hh:108-113, and pybind maps them to RuntimeError).
+ * Header-only; link libmontegpu.so. */
+#ifndef MONTEGPU_HPP
+#define MONTEGPU_HPP
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "montegpu.h"
+
+namespace montegpu {
+
+inline void check(int status) {
+  if (status != MG_OK) throw std::runtime_error(mg_last_error());
+}
+
+/* A handle owning a library object, released by `Destroy`. */
+template <class T, int (*Destroy)(T*)>
+class Handle {
+ public:
+  Handle() = default;
+  explicit Handle(T* p) : p_(p) {}
+  Handle(const Handle&) = delete;
+  Handle& operator=(const Handle&) = delete;
+  Handle(Handle&& o) noexcept : p_(std::exchange(o.p_, nullptr)) {}
+  Handle& operator=(Handle&& o) noexcept {
+    if (this != &o) {
+      reset();
+      p_ = std::exchange(o.p_, nullptr);
+    }
+    return *this;
+  }
+  ~Handle() { reset(); }
+  T* get() const { return p_; }
+  void reset() {
+    if (p_) Destroy(p_);
+    p_ = nullptr;
+  }
+
+ private:
+  T* p_ = nullptr;
+};
+
+/* std::mt19937_64 with the reference's RandomNumberGenerator semantics
+ * (RandomNumberGenerator.hh:15-42): random_int(max) in [0, max], random_real(max) in
+ * [0, max). */
+class RandomNumberEngine {
+ public:
+  explicit RandomNumberEngine(bool seed_from_device = true) {
+    mg_engine* e = nullptr;
+    check(mg_engine_create(seed_from_device ? 1 : 0, &e));
+    h_ = H(e);
+  }
+  void seed(uint64_t value) { check(mg_engine_seed(h_.get(), value)); }
+  void seed_seq(const std::vector<uint64_t>& values) {
+    check(mg_engine_seed_seq(h_.get(), values.data(), values.size()));
+  }
+  std::string dump() const {
+    std::vector<char> buf(16384);
+    check(mg_engine_dump(h_.get(), buf.data(), buf.size()));
+    return std::string(buf.data());
+  }
+  void load(const std::string& state) { check(mg_engine_load(h_.get(), state.c_str())); }
+  uint64_t random_int(uint64_t max) {
+    uint64_t v = 0;
+    check(mg_engine_random_int(h_.get(), max, &v));
+    return v;
+  }
+  double random_real(double max) {
+    double v = 0.0;
+    check(mg_engine_random_real(h_.get(), max, &v));
+    return v;
+  }
+  mg_engine* get() const { return h_.get(); }
+
+ private:
+  using H = Handle<mg_engine, mg_engine_destroy>;
+  H h_;
+};
+
+/* Cluster-expansion model: basis kind 0 (FCC binary, occupation basis) or 1 (FCC
+ * ternary, Chebyshev basis) and one ECI per class. */
+class CeModel {
+ public:
+  CeModel(int basis_kind, const std::vector<double>& eci) {
+    mg_ce_model* m = nullptr;
+    check(mg_ce_model_create(basis_kind, eci.data(), (int)eci.size(), &m));
+    h_ = H(m);
+    check(mg_ce_model_info(m, &n_classes_, &n_features_, &n_species_));
+  }
+  int n_classes() const { return n_classes_; }
+  int n_species() const { return n_species_; }
+  const mg_ce_model* get() const { return h_.get(); }
+
+ private:
+  using H = Handle<mg_ce_model, mg_ce_model_destroy>;
+  H h_;
+  int n_classes_ = 0, n_features_ = 0, n_species_ = 0;
+};
+
+/* Chains of one supercell shape resident on the GPU (mg_ce_batch_*). */
+class CeBatch {
+ public:
+  CeBatch(const CeModel& m, int L0, int L1, int L2, const std::vector<double>& temperature,
+          const std::vector<double>& mu, const std::vector<uint64_t>& seeds, const std::vector<int8_t>& occ,
+          bool fp32_decisions = false, int ctas_per_chain = 0)
+      : n_chains_((int)temperature.size()), n_sites_((long long)L0 * L1 * L2), n_slots_(m.n_classes() + 2) {
+    mg_ce_batch* b = nullptr;
+    check(mg_ce_batch_create(m.get(), L0, L1, L2, n_chains_, temperature.data(), mu.data(), seeds.data(), nullptr,
+                             occ.data(), fp32_decisions ? 1 : 0, ctas_per_chain, &b));
+    h_ = H(b);
+  }
+  /* per-pass outputs [n_passes][n_chains][n_classes + 2] */
+  std::vector<long long> run(int n_passes) {
+    std::vector<long long> out((size_t)n_passes * n_chains_ * n_slots_);
+    check(mg_ce_batch_run(h_.get(), n_passes, out.data()));
+    return out;
+  }
+  std::vector<int8_t> occupation() {
+    std::vector<int8_t> occ((size_t)n_sites_ * n_chains_);
+    check(mg_ce_batch_get_occ(h_.get(), occ.data()));
+    return occ;
+  }
+  int layout() const {
+    int l = 0;
+    check(mg_ce_batch_layout(h_.get(), &l));
+    return l;
+  }
+  void set_layout(int layout) { check(mg_ce_batch_set_layout(h_.get(), layout)); }
+  float last_kernel_ms() const {
+    float ms = 0.f;
+    check(mg_ce_batch_last_kernel_ms(h_.get(), &ms));
+    return ms;
+  }
+  mg_ce_batch* get() const { return h_.get(); }
+
+ private:
+  using H = Handle<mg_ce_batch, mg_ce_batch_destroy>;
+  H h_;
+  int n_chains_;
+  long long n_sites_;
+  int n_slots_;
+};
+
+/* The sweep's colouring of a supercell (host only): colours per site, number of
+ * colours, layout (0 byte, 1 word, 2 pipelined word). */
+struct Colouring {
+  std::vector<int32_t> color;
+  int n_colors = 0;
+  int layout = 0;
+};
+inline Colouring color_supercell(int basis_kind, int L0, int L1, int L2) {
+  Colouring c;
+  c.color.resize((size_t)L0 * L1 * L2);
+  const int n = mg_ce_color_supercell(basis_kind, L0, L1, L2, c.color.data(), &c.layout);
+  if (n <= 0) throw std::runtime_error(mg_last_error());
+  c.n_colors = n;
+  return c;
+}
+
+/* BasicStatisticsCalculator (BasicStatistics.cc:114-188), unweighted: mean and the
+ * autocorrelation-corrected precision of the mean. */
+inline std::pair<double, double> basic_statistics(const std::vector<double>& obs, double confidence = 0.95) {
+  double mean = 0.0, precision = 0.0;
+  check(mg_basic_statistics(obs.data(), (long)obs.size(), nullptr, 0, confidence, 1, 10000, &mean, &precision));
+  return {mean, precision};
+}
+
+/* _default_equilibration_check (EquilibrationCheck.cc:50-117): (equilibrated, samples
+ * needed to equilibrate). */
+inline std::pair<bool, long> equilibration_check(const std::vector<double>& obs, double precision) {
+  int eq = 0;
+  long n = 0;
+  check(mg_equilibration_check(obs.data(), (long)obs.size(), precision, &eq, &n));
+  return {eq != 0, n};
+}
+
+}  // namespace montegpu
+
+#endif /* MONTEGPU_HPP */
