@@ -150,6 +150,14 @@ class ChainBatch:
         self.ctas_per_chain, self.n_colors, self.threads, self.smem_bytes = S.value, nc.value, nt.value, sm.value
         self.layout = LAYOUTS[lay.value]
 
+    def autotune(self, probe_passes: int = 3) -> dict:
+        """Time every applicable layout and CTA count on these chains (state restored after
+        each trial) and keep the fastest; returns the choice and its ms per pass."""
+        lay, S, ms = C.c_int(), C.c_int(), C.c_float()
+        _lib.check(_lib.lib().mg_ce_batch_autotune(self._h, int(probe_passes), C.byref(lay), C.byref(S), C.byref(ms)))
+        self._read_info()
+        return {"layout": LAYOUTS[lay.value], "ctas_per_chain": S.value, "ms_per_pass": float(ms.value)}
+
     def set_layout(self, layout: str) -> None:
         """Sweep with one site per byte ("byte"), four sites per word ("word", binary
         basis with L0 a multiple of 4), four sites per word with the features split around

@@ -352,6 +352,73 @@ int mg_ce_batch_set_layout(mg_ce_batch* b, int layout) {
   return setup_layout(b, layout);
 }
 
+int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout_out, int* ctas_out, float* ms_out) {
+  if (!b || probe_passes < 1) {
+    set_error("Error in mg_ce_batch_autotune: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  const mg_ce_model* m = b->model;
+  const bool word = quad_eligible(m->kind, b->L0, b->L1, b->L2, b->color.data());
+  std::vector<int> layouts = {0};
+  if (word) layouts.push_back(1);
+  if (word && b->pipe >= 0) {
+    layouts.push_back(2);
+    layouts.push_back(3);
+  }
+  const int keep_layout = b->layout, keep_req = b->ctas_requested;
+  const size_t occ_bytes = (size_t)b->N * b->n_chains;
+  int8_t* saved = nullptr;
+  MG_CUDA_TRY(cudaMalloc(&saved, occ_bytes));
+  cudaError_t e = cudaMemcpyAsync(saved, b->docc, occ_bytes, cudaMemcpyDeviceToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) {
+    cudaFree(saved);
+    set_error(std::string("CUDA error in mg_ce_batch_autotune: ") + cudaGetErrorString(e));
+    return MG_ERR_CUDA;
+  }
+  float best = 1e30f;
+  int best_layout = keep_layout, best_S = b->S;
+  const long long pass_keep = b->pass;
+  int rc = MG_OK;
+  // every layout that applies, each at every CTA count from 1 to 16 that it accepts
+  for (int lay : layouts) {
+    for (int S = 1; S <= 16 && rc == MG_OK; ++S) {
+      b->ctas_requested = S;
+      if (setup_layout(b, lay) != MG_OK) continue;  // this CTA count does not fit this layout
+      int n_active = 0;
+      if (max_active_chains(m->kind, S, b->smem, &n_active, lay) != MG_OK || n_active < 1) continue;
+      float ms = 0.f;
+      rc = mg_ce_batch_run(b, probe_passes, nullptr);
+      if (rc == MG_OK) rc = mg_ce_batch_run(b, probe_passes, nullptr);  // second run timed (warm)
+      if (rc != MG_OK) break;
+      ms = b->last_ms;
+      b->pass = pass_keep;
+      e = cudaMemcpyAsync(b->docc, saved, occ_bytes, cudaMemcpyDeviceToDevice, b->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+      if (e != cudaSuccess) {
+        rc = MG_ERR_CUDA;
+        set_error(std::string("CUDA error in mg_ce_batch_autotune: ") + cudaGetErrorString(e));
+        break;
+      }
+      if (ms < best) {
+        best = ms;
+        best_layout = lay;
+        best_S = S;
+      }
+    }
+  }
+  cudaFree(saved);
+  b->ctas_requested = best_S;
+  const int rc2 = setup_layout(b, best_layout);
+  if (rc != MG_OK) return rc;
+  if (rc2 != MG_OK) return rc2;
+  (void)keep_req;
+  if (layout_out) *layout_out = best_layout;
+  if (ctas_out) *ctas_out = best_S;
+  if (ms_out) *ms_out = best / (float)probe_passes;
+  return MG_OK;
+}
+
 int mg_ce_batch_colors(const mg_ce_batch* b, int32_t* color) {
   if (!b || !color) {
     set_error("Error in mg_ce_batch_colors: invalid argument");

@@ -587,6 +587,27 @@ struct QuadSweeper {
   // the same with the integer energy sums given
   __device__ __forceinline__ void finish_g(uint32_t ent, uint32_t v, const uint32_t (&F)[NF], const int (&G)[4],
                                            const uint32_t (&x0)[4], int (&acc)[NSLOT]) const {
+    uint32_t sgn;
+    const uint32_t flip = decide_store(ent, v, F, G, x0, acc, sgn);
+    accumulate(F, flip, sgn, acc);
+  }
+
+  // correlation changes of the accepted flips (flip: set bit per accepted site, sgn: its
+  // signed change of the site function per byte)
+  __device__ __forceinline__ void accumulate(const uint32_t (&F)[NF], uint32_t flip, uint32_t sgn,
+                                             int (&acc)[NSLOT]) const {
+    if (flip) {
+      acc[0] += __popc(flip);
+      // sum over the four sites of dpsi * F[k]: signed byte dot product
+#pragma unroll
+      for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += __dp4a((int)F[k], (int)sgn, 0);
+    }
+  }
+
+  // decisions and write-back of the flips; returns the flip mask and sets sgn
+  __device__ __forceinline__ uint32_t decide_store(uint32_t ent, uint32_t v, const uint32_t (&F)[NF],
+                                                   const int (&G)[4], const uint32_t (&x0)[4], int (&acc)[NSLOT],
+                                                   uint32_t& sgn) const {
     const int pw = (int)(ent & 0xFFFFFFu);
     const uint32_t flags = ent >> 24;
     // FP32 decisions of the four sites (branch-free, interleaved)
@@ -607,7 +628,8 @@ struct QuadSweeper {
         }
       }
     }
-    uint32_t flip = 0u, sgn = 0u;
+    uint32_t flip = 0u;
+    sgn = 0u;
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const uint32_t bit = 1u << (8 * t);
@@ -637,11 +659,8 @@ struct QuadSweeper {
       put(s + pw);
       if (flags & 16u) put(s_prev + pw + dKp);
       if (flags & 32u) put(s_next + pw - dKn);
-      acc[0] += __popc(flip);
-      // sum over the four sites of dpsi * F[k]: signed byte dot product
-#pragma unroll
-      for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += __dp4a((int)F[k], (int)sgn, 0);
     }
+    return flip;
   }
 };
 
@@ -1085,27 +1104,32 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
 #pragma unroll 1
     for (int c = 0; c < g.n_colors; ++c) {
       const bool last = (c + 1 == g.n_colors);
+      // finish role: decisions and write-back before the arrive; the correlation changes
+      // (needed only at the end of the pass) while the barrier completes
+      uint32_t F[B::NFEAT], flip = 0u, sgn = 0u;
       if (finisher) {
         if (cstart[c] + tid < cstart[c + 1]) {
           State st;
           uint32_t ent, x0[4];
           int G[4], Ac[Stage::NG][4];
           Stage::template load<NW>(stage + parity * SLOT, tid, st, ent, x0, G, Ac);
-          uint32_t F[B::NFEAT], Lw[Stage::NG];
+          uint32_t Lw[Stage::NG];
           B::template Pipe<PIPE>::late(sw.loader(ent), st, F, Lw);
 #pragma unroll
           for (int t = 0; t < 4; ++t)
 #pragma unroll
             for (int gi = 0; gi < Stage::NG; ++gi) G[t] += (int)((Lw[gi] >> (8 * t)) & 1u) * Ac[gi][t];
-          sw.finish_g(ent, st.own, F, G, x0, acc);
+          flip = sw.decide_store(ent, st.own, F, G, x0, acc, sgn);
         }
       } else {
         prepare(last ? 0 : c + 1, last ? pass_g + 1 : pass_g, stage + (parity ^ 1) * SLOT);
       }
       if (S > 1) {
         cluster_arrive_release();
+        if (finisher) sw.accumulate(F, flip, sgn, acc);
         cluster_wait_acquire();
       } else {
+        if (finisher) sw.accumulate(F, flip, sgn, acc);
         __syncthreads();
       }
       parity ^= 1;

@@ -118,3 +118,19 @@ def test_word_layout_full_size(gpu_lib):
     assert np.array_equal(bp.occupation(), bb.occupation())
     s = clex.accumulate(model, corr0, ow, mu, bw.n_sites)
     assert np.array_equal(bw.corr(), s.int_corr[-1])
+
+
+def test_autotune_keeps_results(gpu_lib):
+    """The autotuner times layouts and CTA counts on the batch's own chains but restores
+    them: a tuned batch continues exactly as an untuned one."""
+    L = (32, 32, 32)
+    model, occ, T, mu, seeds = _setup(L, 4, seed=9)
+    tuned = clex.ChainBatch(model, L, occ, T, mu, seeds)
+    plain = clex.ChainBatch(model, L, occ, T, mu, seeds)
+    o1, o2 = tuned.run(3), plain.run(3)
+    choice = tuned.autotune(probe_passes=2)
+    assert choice["layout"] in ("byte", "word", "word_pipelined", "word_specialised")
+    assert tuned.layout == choice["layout"] and tuned.ctas_per_chain == choice["ctas_per_chain"]
+    assert np.array_equal(tuned.occupation(), plain.occupation())
+    assert np.array_equal(tuned.run(4), plain.run(4))
+    assert np.array_equal(tuned.occupation(), plain.occupation())
