@@ -133,13 +133,21 @@ def cpu_baseline_sample(seconds_target: float = 10.0) -> dict:
             "sample": f"{n} random-site attempts on one 64^3 chain at T={T[3]:.0f} K (oracle restatement, g++ -O2)"}
 
 
-def _ref_worker(args):
-    chain, n_steps = args
-    from tests import oracle_lib
+_REF_STATE = {}
 
-    eci, occ, T, mu, seeds = make_inputs(0)
-    orc = oracle_lib.OracleCE((L, L, L), 2, eci)
-    _, _, t = orc.random_site_run(occ[chain].astype(np.int32), float(T[chain]), mu[chain], 100 + chain, n_steps)
+
+def _ref_worker(args):
+    """One bounded sample of the reference loop; the model and the chain's initial
+    occupation are built once per worker process and reused across steps."""
+    chain, n_steps, step = args
+    if chain not in _REF_STATE:
+        from tests import oracle_lib
+
+        eci, occ, T, mu, seeds = make_inputs(0)
+        _REF_STATE[chain] = (oracle_lib.OracleCE((L, L, L), 2, eci), occ[chain].astype(np.int32),
+                             float(T[chain]), mu[chain])
+    orc, o, t_k, mu_c = _REF_STATE[chain]
+    _, _, t = orc.random_site_run(o, t_k, mu_c, 100 + 1000 * step + chain, n_steps)
     return n_steps, t
 
 
@@ -148,20 +156,24 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    n_proc = min(cores, N_CHAINS)
-    steps_per_chain = int(args.ref_steps_per_sample)
+    n_proc = cores  # one independent chain per host core (chain c % 8 of the workload)
+    # each step is a bounded sample: about two minutes for the whole run at ~0.8 M
+    # attempts/s per process, at most --ref-steps-per-sample attempts per process
+    steps_per_chain = int(min(args.ref_steps_per_sample, max(2e4, 0.8e6 * 120.0 / (args.steps + args.warmup))))
     ctx = mp.get_context("spawn")
-    vals = []
+    vals, walls = [], []
     with ctx.Pool(n_proc) as pool:
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
-            res = pool.map(_ref_worker, [(c % N_CHAINS, steps_per_chain) for c in range(n_proc)])
+            res = pool.map(_ref_worker, [(c % N_CHAINS, steps_per_chain, i) for c in range(n_proc)], chunksize=1)
             wall = time.perf_counter() - t0
             if i >= args.warmup:
                 vals.append(sum(r[0] for r in res) / wall)
+                walls.append(wall)
     value = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "site-attempts/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(walls),
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "supercell": [L, L, L], "chains": N_CHAINS,
                        "sample_steps_per_process": steps_per_chain, "processes": n_proc},
