@@ -304,7 +304,9 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
 // ---- word layout (four sites per 32-bit word, binary basis)
 
 constexpr int NT_QUAD = 384;
-constexpr int NW_WS = 384;  // threads per role of the warp-specialised kernel
+// threads per role of the warp-specialised kernel: 11 warps, one word per thread (FCC
+// 64^3 in 12 row slabs proposes at most 344 words per CTA and colour)
+constexpr int NW_WS = 352;
 
 // padded words per row: Q + 2 * HALO, made odd so that consecutive rows start in
 // different shared-memory banks
@@ -312,9 +314,45 @@ inline int quad_row_stride(int Q) {
   const int r = Q + 2 * CE_HALO;
   return (r & 1) ? r : r + 1;
 }
+// Row slabs (row_slab) of one kind are valid when every word appears only in its own
+// CTA's window (once) and, through the flagged copies, in the previous and the next
+// CTA's windows at the offsets dkp and dkn: checked plane by plane over periodic images.
+inline bool row_slabs_ok(int L1, int L2, int S, int planes) {
+  if (S < 1 || S > L1 * L2 || (planes && S > L2)) return false;
+  std::vector<RowSlab> sl(S);
+  for (int r = 0; r < S; ++r) {
+    sl[r] = row_slab(L1, L2, S, r, planes);
+    if (sl[r].r1 <= sl[r].r0) return false;
+  }
+  for (int r = 0; r < S; ++r) {
+    const int prev = (r + S - 1) % S, next = (r + 1) % S;
+    const int offp = r == 0 ? L2 : 0, offn = r == S - 1 ? -L2 : 0;
+    for (int k = sl[r].kb; k < sl[r].kb + sl[r].nk; ++k)
+      for (int x = 0; x < S; ++x)
+        for (int off = -2 * L2; off <= 2 * L2; off += L2) {
+          const int kk = k + off;
+          if (kk < sl[x].kb - CE_HALO || kk > sl[x].kb + sl[x].nk - 1 + CE_HALO) continue;
+          const bool expected = (x == r && off == 0) || (x == prev && off == offp) || (x == next && off == offn);
+          if (!expected) return false;
+        }
+  }
+  return true;
+}
+// slab kind of the word layout: balanced rows where valid, else whole planes, else -1
+inline int word_slab_kind(int L1, int L2, int S) {
+  if (row_slabs_ok(L1, L2, S, 0)) return 0;
+  if (row_slabs_ok(L1, L2, S, 1)) return 1;
+  return -1;
+}
 inline size_t quad_smem(int L0, int L1, int L2, int S) {
+  const int kind = word_slab_kind(L1, L2, S);
   return sizeof(uint32_t) * (size_t)quad_row_stride(L0 / 4) * (L1 + 2 * CE_HALO) *
-         ((L2 + S - 1) / S + 2 * CE_HALO);
+         row_window_planes(L1, L2, S, CE_HALO, kind < 0 ? 1 : kind);
+}
+// slab decomposition of a layout: row slabs for the word layouts, whole planes (at least
+// HALO per CTA) for the byte layout
+inline bool slabs_ok(int layout, int L1, int L2, int S) {
+  return layout >= 1 ? word_slab_kind(L1, L2, S) >= 0 : (S >= 1 && L2 / S >= CE_HALO);
 }
 // warp-specialised kernel: the lattice (rounded to 16 bytes) and two stage slots
 static_assert(WsStage<FccBinary, 0>::NFIELD == WsStage<FccBinary, 1>::NFIELD, "one stage size for all pipelines");
@@ -322,7 +360,8 @@ static_assert(WsStage<FccBinary, 0>::NFIELD == WsStage<FccBinary, 1>::NFIELD, "o
 // site lists (entry and Philox counter word per word) and its colour starts
 inline size_t ws_smem(int L0, int L1, int L2, int S, int n_colors = CE_MAX_COLORS) {
   const size_t lattice = (quad_smem(L0, L1, L2, S) + 15) & ~(size_t)15;
-  const size_t words = (size_t)(L0 / 4) * L1 * ((L2 + S - 1) / S);
+  const int kind = word_slab_kind(L1, L2, S);
+  const size_t words = (size_t)(L0 / 4) * row_slab_max_rows(L1, L2, S, kind < 0 ? 1 : kind);
   return lattice + sizeof(uint32_t) * (2 * (size_t)WsStage<FccBinary, 0>::NFIELD * NW_WS + 2 * words) +
          sizeof(int) * (n_colors + 1);
 }
@@ -341,27 +380,33 @@ inline bool quad_eligible(int kind, int L0, int L1, int L2, const int32_t* col) 
   return true;
 }
 
-// Per-slab, per-colour word lists.  Within one (slab, colour) list the words are ordered
-// round-robin over the 32 banks (padded word index mod 32), so that the lanes of a warp
-// load from distinct banks at every constant neighbour offset.
-// Entry = padded word index | mirror flags << 24 (1: w < 2, 2: w >= Q-2, 4: j < 2,
-// 8: j >= L1-2, 16: kl < 2, 32: kl >= nk-2); site[e] = linear index of byte 0's site.
+// Per-slab, per-colour word lists of the row slabs (row_slab, kind word_slab_kind; the
+// caller has checked that one is valid).  Within one (slab,
+// colour) list the words are ordered round-robin over the 32 banks (padded word index mod
+// 32), so that the lanes of a warp load from distinct banks at every constant neighbour
+// offset.  Entry = padded word index in the slab's window | copy flags << 24 (1: w < 2,
+// 2: w >= Q-2, 4: j < 2, 8: j >= L1-2, 16: the word lies in the previous CTA's window,
+// 32: in the next CTA's); site[e] = linear index of byte 0's site.
 inline void build_word_lists(int L0, int L1, int L2, int S, const int32_t* col, int n_colors, int* cstart,
                              uint32_t* entries, uint32_t* site) {
   const int Q = L0 / 4, RS = quad_row_stride(Q), RY = L1 + 2 * CE_HALO;
   int count[CE_MAX_COLORS * 32], seen[CE_MAX_COLORS * 32];
   long long cbase[CE_MAX_COLORS + 1];
   long long pos = 0;
+  const int kind = word_slab_kind(L1, L2, S);
   for (int r = 0; r < S; ++r) {
-    const int nk = slab_planes(L2, S, r), k0 = slab_start(L2, S, r);
+    const RowSlab sl = row_slab(L1, L2, S, r, kind);
+    const RowSlab sp = row_slab(L1, L2, S, (r + S - 1) % S, kind), sn = row_slab(L1, L2, S, (r + 1) % S, kind);
+    const int offp = r == 0 ? L2 : 0, offn = r == S - 1 ? -L2 : 0;
+    auto prow_of = [&](int j, int k) { return (uint32_t)(CE_HALO + RS * ((j + CE_HALO) + RY * (k - sl.kb + CE_HALO))); };
     std::fill(count, count + n_colors * 32, 0);
     std::fill(seen, seen + n_colors * 32, 0);
-    for (int kl = 0; kl < nk; ++kl)
-      for (int j = 0; j < L1; ++j) {
-        const long long row = (long long)L0 * (j + (long long)L1 * (k0 + kl));
-        const uint32_t prow = (uint32_t)(CE_HALO + RS * ((j + CE_HALO) + RY * (kl + CE_HALO)));
-        for (int w = 0; w < Q; ++w) count[(size_t)col[row + w] * 32 + ((prow + w) & 31)]++;
-      }
+    for (int R = sl.r0; R < sl.r1; ++R) {
+      const int j = R % L1, k = R / L1;
+      const long long row = (long long)L0 * R;
+      const uint32_t prow = prow_of(j, k);
+      for (int w = 0; w < Q; ++w) count[(size_t)col[row + w] * 32 + ((prow + w) & 31)]++;
+    }
     cbase[0] = pos;
     for (int c = 0; c < n_colors; ++c) {
       long long b = cbase[c];
@@ -370,29 +415,32 @@ inline void build_word_lists(int L0, int L1, int L2, int S, const int32_t* col, 
       cstart[r * (n_colors + 1) + c] = (int)cbase[c];
     }
     cstart[r * (n_colors + 1) + n_colors] = (int)cbase[n_colors];
-    for (int kl = 0; kl < nk; ++kl)
-      for (int j = 0; j < L1; ++j) {
-        const long long row = (long long)L0 * (j + (long long)L1 * (k0 + kl));
-        const uint32_t prow = (uint32_t)(CE_HALO + RS * ((j + CE_HALO) + RY * (kl + CE_HALO)));
-        for (int w = 0; w < Q; ++w) {
-          const int c = col[row + w];
-          const uint32_t pw = prow + w;
-          const int q = pw & 31;
-          const int* cnt = &count[(size_t)c * 32];
-          const int t = seen[(size_t)c * 32 + q]++;
-          long long p = cbase[c];
-          for (int q2 = 0; q2 < 32; ++q2) p += std::min(cnt[q2], t) + ((q2 < q && cnt[q2] > t) ? 1 : 0);
-          uint32_t flags = 0;
-          if (w < CE_HALO) flags |= 1;
-          else if (w >= Q - CE_HALO) flags |= 2;
-          if (j < CE_HALO) flags |= 4;
-          else if (j >= L1 - CE_HALO) flags |= 8;
-          if (kl < CE_HALO) flags |= 16;
-          if (kl >= nk - CE_HALO) flags |= 32;
-          entries[p] = pw | (flags << 24);
-          site[p] = (uint32_t)(row + w);
-        }
+    for (int R = sl.r0; R < sl.r1; ++R) {
+      const int j = R % L1, k = R / L1;
+      const long long row = (long long)L0 * R;
+      const uint32_t prow = prow_of(j, k);
+      const int kp = k + offp, kn = k + offn;
+      const bool in_prev = kp >= sp.kb - CE_HALO && kp <= sp.kb + sp.nk - 1 + CE_HALO;
+      const bool in_next = kn >= sn.kb - CE_HALO && kn <= sn.kb + sn.nk - 1 + CE_HALO;
+      for (int w = 0; w < Q; ++w) {
+        const int c = col[row + w];
+        const uint32_t pw = prow + w;
+        const int q = pw & 31;
+        const int* cnt = &count[(size_t)c * 32];
+        const int t = seen[(size_t)c * 32 + q]++;
+        long long p = cbase[c];
+        for (int q2 = 0; q2 < 32; ++q2) p += std::min(cnt[q2], t) + ((q2 < q && cnt[q2] > t) ? 1 : 0);
+        uint32_t flags = 0;
+        if (w < CE_HALO) flags |= 1;
+        else if (w >= Q - CE_HALO) flags |= 2;
+        if (j < CE_HALO) flags |= 4;
+        else if (j >= L1 - CE_HALO) flags |= 8;
+        if (in_prev) flags |= 16;
+        if (in_next) flags |= 32;
+        entries[p] = pw | (flags << 24);
+        site[p] = (uint32_t)(row + w);
       }
+    }
     pos = cbase[n_colors];
   }
 }
@@ -490,7 +538,7 @@ inline int choose_ctas(int kind, int L0, int L1, int L2, int n_chains, int reque
   MG_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t budget = (size_t)max_smem - 1024;
   auto ok = [&](int S) {
-    return S >= 1 && S <= 16 && L2 / S >= CE_HALO && layout_smem(layout, L0, L1, L2, S) <= budget;
+    return S >= 1 && S <= 16 && slabs_ok(layout, L1, L2, S) && layout_smem(layout, L0, L1, L2, S) <= budget;
   };
   if (requested > 0) {
     if (!ok(requested)) {
@@ -589,6 +637,7 @@ inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L, int pip
   A.g.L2 = L.L2;
   A.g.Q = L.L0 / 4;
   A.g.S = L.S;
+  A.g.planes = word_slab_kind(L.L1, L.L2, L.S);
   A.g.RS = quad_row_stride(L.L0 / 4);
   A.g.RY = L.L1 + 2 * CE_HALO;
   A.g.n_colors = L.n_colors;
@@ -637,6 +686,7 @@ inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe)
   A.g.L2 = L.L2;
   A.g.Q = L.L0 / 4;
   A.g.S = L.S;
+  A.g.planes = word_slab_kind(L.L1, L.L2, L.S);
   A.g.RS = quad_row_stride(L.L0 / 4);
   A.g.RY = L.L1 + 2 * CE_HALO;
   A.g.n_colors = L.n_colors;

@@ -165,7 +165,7 @@ int shape_plan(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan** out) {
   auto fit = [&](int layout) {
     for (int c = 0; c < kClasses; ++c) {
       const int S = kClassS[c];
-      if (L2 / S >= mg::CE_HALO && layout_smem(layout, L0, L1, L2, S) <= (size_t)max_smem - 1024) return c;
+      if (slabs_ok(layout, L1, L2, S) && layout_smem(layout, L0, L1, L2, S) <= (size_t)max_smem - 1024) return c;
     }
     return -1;
   };
@@ -218,7 +218,8 @@ int geometry(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan& sp, int* ou
   MG_CUDA_TRY(cudaMemcpyAsync(g.dcstart, cstart.data(), sizeof(int) * cstart.size(), cudaMemcpyHostToDevice, p->stream));
   MG_CUDA_TRY(cudaMemcpyAsync(g.dentries, entries.data(), sizeof(uint32_t) * n_entries, cudaMemcpyHostToDevice, p->stream));
   MG_CUDA_TRY(cudaMemcpyAsync(g.dsite, site.data(), sizeof(uint32_t) * n_entries, cudaMemcpyHostToDevice, p->stream));
-  mg::PoolGeometry dg{L0, L1, L2, g.n_colors, g.dcstart, g.dentries, g.dsite};
+  const int planes = sp.layout == 1 ? word_slab_kind(L1, L2, S) : 1;
+  mg::PoolGeometry dg{L0, L1, L2, g.n_colors, planes, g.dcstart, g.dentries, g.dsite};
   const int gi = (int)p->geoms.size();
   MG_CUDA_TRY(cudaMemcpyAsync(p->dgeoms + gi, &dg, sizeof(dg), cudaMemcpyHostToDevice, p->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(p->stream));

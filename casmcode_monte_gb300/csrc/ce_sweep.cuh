@@ -502,9 +502,99 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
 // come out of one pass of byte-parallel integer code, the four decisions are taken one
 // by one (same random numbers, same arithmetic as the per-site kernel, so trajectories
 // are identical), and accepted flips are written back as one word.
+// Row slabs of the word layout.  With rows numbered R = j + L1 k, CTA r of S owns the
+// rows [R_r, R_r+1): balanced, R_r = floor(r L1 L2 / S), so that every CTA proposes the
+// same number of words (to within one row) whatever S divides; or, where balanced slabs
+// are too thin for the halo, whole planes (R_r = L1 (r floor(L2/S) + min(r, L2 mod S))).
+// A slab's shared-memory window holds the nk planes its rows touch, from plane kb, plus
+// HALO planes on each side; the rows of the window it does not own belong to the
+// previous or the next CTA, which write their updates into it.  A word at local offset pw
+// of CTA r lies at pw + dkp RSY in the previous CTA's window and at pw - dkn RSY in the
+// next CTA's (plane offsets with the periodic wrap of the first and the last CTA).
+struct RowSlab {
+  int r0, r1;    // owned rows [r0, r1)
+  int kb, nk;    // first plane touched, planes touched
+  int dkp, dkn;  // plane offsets of the copies in the previous / next CTA's window
+};
+__host__ __device__ __forceinline__ int slab_row(int L1, int L2, int S, int r, int planes) {
+  if (planes) return L1 * (r * (L2 / S) + (r < L2 % S ? r : L2 % S));
+  return (int)(((long long)r * L1 * L2) / S);
+}
+__host__ __device__ __forceinline__ RowSlab row_slab(int L1, int L2, int S, int r, int planes) {
+  RowSlab s;
+  s.r0 = slab_row(L1, L2, S, r, planes);
+  s.r1 = slab_row(L1, L2, S, r + 1, planes);
+  s.kb = s.r0 / L1;
+  s.nk = (s.r1 - 1) / L1 - s.kb + 1;
+  const int kbp = slab_row(L1, L2, S, (r + S - 1) % S, planes) / L1;
+  const int kbn = slab_row(L1, L2, S, (r + 1) % S, planes) / L1;
+  s.dkp = s.kb - kbp + (r == 0 ? L2 : 0);
+  s.dkn = kbn - s.kb + (r == S - 1 ? L2 : 0);
+  return s;
+}
+// planes of the largest window (touched planes + 2 halo) and rows of the largest slab
+__host__ __device__ __forceinline__ int row_window_planes(int L1, int L2, int S, int halo, int planes) {
+  int m = 0;
+  for (int r = 0; r < S; ++r) {
+    const int n = row_slab(L1, L2, S, r, planes).nk;
+    m = n > m ? n : m;
+  }
+  return m + 2 * halo;
+}
+__host__ __device__ __forceinline__ int row_slab_max_rows(int L1, int L2, int S, int planes) {
+  int m = 0;
+  for (int r = 0; r < S; ++r) {
+    const int n = slab_row(L1, L2, S, r + 1, planes) - slab_row(L1, L2, S, r, planes);
+    m = n > m ? n : m;
+  }
+  return m;
+}
+
+// Load the window of a row slab into shared memory: planes kb - HALO .. kb + nk - 1 +
+// HALO, each row with its periodic copies (words -HALO .. Q + HALO - 1 of a padded row of
+// RS; padding words beyond are zero and never read); word w holds sites w + tQ, t = 0..3.
+template <int HALO>
+__device__ __forceinline__ void load_word_window(uint32_t* sq, const int8_t* gocc, int L0, int L1, int L2, int Q,
+                                                 int RS, int RY, int kb, int nk, int tid, int nthreads) {
+  const int RSY = RS * RY;
+  for (int idx = tid; idx < RSY * (nk + 2 * HALO); idx += nthreads) {
+    const int wp = idx % RS, jp = (idx / RS) % RY, kp = idx / RSY;
+    const int w = wp - HALO;
+    uint32_t word = 0u;
+    if (w < Q + HALO) {
+      int j = jp - HALO, k = kb + kp - HALO;
+      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+      const int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        int i = w + t * Q;
+        i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+        word |= (uint32_t)(uint8_t)row[i] << (8 * t);
+      }
+    }
+    sq[idx] = word;
+  }
+}
+
+// Write the owned rows of a row slab back to the occupation array.
+template <int HALO>
+__device__ __forceinline__ void store_word_rows(const uint32_t* sq, int8_t* gocc, int L0, int L1, int Q, int RS,
+                                                int RY, const RowSlab& sl, int tid, int nthreads) {
+  for (int idx = tid; idx < Q * (sl.r1 - sl.r0); idx += nthreads) {
+    const int w = idx % Q, R = sl.r0 + idx / Q;
+    const int j = R % L1, k = R / L1;
+    const uint32_t word = sq[(w + HALO) + RS * ((j + HALO) + RY * (k - sl.kb + HALO))];
+    int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) row[w + t * Q] = (int8_t)((word >> (8 * t)) & 0xFFu);
+  }
+}
+
 struct QuadGeometry {
   int L0, L1, L2, Q;
   int S;
+  int planes;  // slab kind: 0 balanced rows, 1 whole planes (row_slab)
   int RS, RY;  // padded words per row (odd: rows start in different banks), rows per plane
   int n_colors;
   const int* color_start;   // [S][n_colors + 1]
@@ -773,33 +863,13 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_const
 
   const int Q = g.Q, RS = g.RS, RY = g.RY, RSY = RS * RY;
   const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
-  const int nkq = L2 / S, nkr = L2 % S;
-  const int nk = nkq + (rank < nkr ? 1 : 0);
-  const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+  const RowSlab sl = row_slab(L1, L2, S, rank, g.planes);
   const int rprev = (rank + S - 1) % S;
-  const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
   const long long N = (long long)L0 * L1 * L2;
   int8_t* gocc = A.occ + (size_t)chain * N;
 
-  // ---- load slab + borders (padding words beyond Q + 2 are zero and never read)
-  for (int idx = threadIdx.x; idx < RSY * (nk + 2 * B::HALO); idx += NT) {
-    const int wp = idx % RS, jp = (idx / RS) % RY, kp = idx / RSY;
-    const int w = wp - B::HALO;
-    uint32_t word = 0u;
-    if (w < Q + B::HALO) {
-      int j = jp - B::HALO, k = k0 + kp - B::HALO;
-      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
-      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
-      const int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        int i = w + t * Q;
-        i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
-        word |= (uint32_t)(uint8_t)row[i] << (8 * t);
-      }
-    }
-    sq[idx] = word;
-  }
+  // ---- load the slab's window
+  load_word_window<B::HALO>(sq, gocc, L0, L1, L2, Q, RS, RY, sl.kb, sl.nk, threadIdx.x, NT);
   if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
 
   const CeChainParams* cpg = A.cp + chain;
@@ -819,8 +889,8 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_const
   sw.RSY = RSY;
   sw.Q = Q;
   sw.dJ = L1 * RS;
-  sw.dKp = nk_prev * RSY;
-  sw.dKn = nk * RSY;
+  sw.dKp = sl.dkp * RSY;
+  sw.dKn = sl.dkn * RSY;
   sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
                               A.precision};
   const int lane = threadIdx.x & 31;
@@ -888,13 +958,7 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_quad_kernel(const __grid_const
                 (unsigned long long)(long long)v);
   }
   // ---- write back own words
-  for (int idx = threadIdx.x; idx < Q * L1 * nk; idx += NT) {
-    const int w = idx % Q, j = (idx / Q) % L1, kl = idx / (Q * L1);
-    const uint32_t word = sq[(w + B::HALO) + RS * ((j + B::HALO) + RY * (kl + B::HALO))];
-    int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * (k0 + kl));
-#pragma unroll
-    for (int t = 0; t < 4; ++t) row[w + t * Q] = (int8_t)((word >> (8 * t)) & 0xFFu);
-  }
+  store_word_rows<B::HALO>(sq, gocc, L0, L1, Q, RS, RY, sl, threadIdx.x, NT);
   barrier();
 }
 
@@ -1005,40 +1069,20 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
 
   const int Q = g.Q, RS = g.RS, RY = g.RY, RSY = RS * RY;
   const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
-  const int nkq = L2 / S, nkr = L2 % S;
-  const int nk = nkq + (rank < nkr ? 1 : 0);
-  const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+  const RowSlab sl = row_slab(L1, L2, S, rank, g.planes);
   const int rprev = (rank + S - 1) % S;
-  const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
   const long long N = (long long)L0 * L1 * L2;
   int8_t* gocc = A.occ + (size_t)chain * N;
-  const int lattice_words = RSY * (nkq + (nkr ? 1 : 0) + 2 * B::HALO);
+  const int lattice_words = RSY * row_window_planes(L1, L2, S, B::HALO, g.planes);
   uint32_t* stage = sq + ((lattice_words + 3) & ~3);  // [2][NFIELD][NW]
   // the CTA's site lists (entries, Philox counter words) and colour starts, copied once
-  const int max_words = Q * L1 * (nkq + (nkr ? 1 : 0));
+  const int max_words = Q * row_slab_max_rows(L1, L2, S, g.planes);
   uint32_t* ents = stage + 2 * Stage::NFIELD * NW;
   uint32_t* sites = ents + max_words;
   int* cst = reinterpret_cast<int*>(sites + max_words);
 
-  // ---- load slab + borders (as ce_sweep_quad_kernel)
-  for (int idx = threadIdx.x; idx < RSY * (nk + 2 * B::HALO); idx += 2 * NW) {
-    const int wp = idx % RS, jp = (idx / RS) % RY, kp = idx / RSY;
-    const int w = wp - B::HALO;
-    uint32_t word = 0u;
-    if (w < Q + B::HALO) {
-      int j = jp - B::HALO, k = k0 + kp - B::HALO;
-      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
-      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
-      const int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        int i = w + t * Q;
-        i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
-        word |= (uint32_t)(uint8_t)row[i] << (8 * t);
-      }
-    }
-    sq[idx] = word;
-  }
+  // ---- load the slab's window
+  load_word_window<B::HALO>(sq, gocc, L0, L1, L2, Q, RS, RY, sl.kb, sl.nk, threadIdx.x, 2 * NW);
   if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
 
   const CeChainParams* cpg = A.cp + chain;
@@ -1067,8 +1111,8 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
   sw.RSY = RSY;
   sw.Q = Q;
   sw.dJ = L1 * RS;
-  sw.dKp = nk_prev * RSY;
-  sw.dKn = nk * RSY;
+  sw.dKp = sl.dkp * RSY;
+  sw.dKn = sl.dkn * RSY;
   sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
                               A.precision};
   const int lane = threadIdx.x & 31;
@@ -1161,13 +1205,7 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
       atomicAdd(reinterpret_cast<unsigned long long*>(A.out + ((size_t)pl * A.n_chains + chain) * NSLOT + threadIdx.x),
                 (unsigned long long)(long long)v);
   }
-  for (int idx = threadIdx.x; idx < Q * L1 * nk; idx += 2 * NW) {
-    const int w = idx % Q, j = (idx / Q) % L1, kl = idx / (Q * L1);
-    const uint32_t word = sq[(w + B::HALO) + RS * ((j + B::HALO) + RY * (kl + B::HALO))];
-    int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * (k0 + kl));
-#pragma unroll
-    for (int t = 0; t < 4; ++t) row[w + t * Q] = (int8_t)((word >> (8 * t)) & 0xFFu);
-  }
+  store_word_rows<B::HALO>(sq, gocc, L0, L1, Q, RS, RY, sl, threadIdx.x, 2 * NW);
   barrier();
 }
 
@@ -1177,6 +1215,7 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
 struct PoolGeometry {
   int L0, L1, L2;
   int n_colors;
+  int planes;  // word layout: slab kind (row_slab)
   const int* color_start;   // [S][n_colors + 1]
   const uint32_t* entries;  // padded index | flags << 24
   const uint32_t* site_l;
@@ -1464,30 +1503,10 @@ __global__ void __launch_bounds__(NT, 1) ce_pool_quad_kernel(const __grid_consta
     const PoolGeometry g = A.geoms[item.geom];
     const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
     const int Q = L0 / 4, RS = (Q + 2 * B::HALO) | 1, RY = L1 + 2 * B::HALO, RSY = RS * RY;
-    const int nkq = L2 / S, nkr = L2 % S;
-    const int nk = nkq + (rank < nkr ? 1 : 0);
-    const int k0 = rank * nkq + (rank < nkr ? rank : nkr);
+    const RowSlab sl = row_slab(L1, L2, S, rank, g.planes);
     const int rprev = (rank + S - 1) % S;
-    const int nk_prev = nkq + (rprev < nkr ? 1 : 0);
     int8_t* gocc = A.occ + item.occ_offset;
-    for (int idx = threadIdx.x; idx < RSY * (nk + 2 * B::HALO); idx += NT) {
-      const int wp = idx % RS, jp = (idx / RS) % RY, kp = idx / RSY;
-      const int w = wp - B::HALO;
-      uint32_t word = 0u;
-      if (w < Q + B::HALO) {
-        int j = jp - B::HALO, k = k0 + kp - B::HALO;
-        j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
-        k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
-        const int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          int i = w + t * Q;
-          i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
-          word |= (uint32_t)(uint8_t)row[i] << (8 * t);
-        }
-      }
-      sq[idx] = word;
-    }
+    load_word_window<B::HALO>(sq, gocc, L0, L1, L2, Q, RS, RY, sl.kb, sl.nk, threadIdx.x, NT);
     if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
     const CeChainParams* cpg = A.cp + item.param;
     load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
@@ -1505,8 +1524,8 @@ __global__ void __launch_bounds__(NT, 1) ce_pool_quad_kernel(const __grid_consta
     sw.RSY = RSY;
     sw.Q = Q;
     sw.dJ = L1 * RS;
-    sw.dKp = nk_prev * RSY;
-    sw.dKn = nk * RSY;
+    sw.dKp = sl.dkp * RSY;
+    sw.dKn = sl.dkn * RSY;
     sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
                                 A.precision};
     int acc[NSLOT];
@@ -1557,13 +1576,7 @@ __global__ void __launch_bounds__(NT, 1) ce_pool_quad_kernel(const __grid_consta
         atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)pl * NSLOT + threadIdx.x),
                   (unsigned long long)(long long)v);
     }
-    for (int idx = threadIdx.x; idx < Q * L1 * nk; idx += NT) {
-      const int w = idx % Q, j = (idx / Q) % L1, kl = idx / (Q * L1);
-      const uint32_t word = sq[(w + B::HALO) + RS * ((j + B::HALO) + RY * (kl + B::HALO))];
-      int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * (k0 + kl));
-#pragma unroll
-      for (int t = 0; t < 4; ++t) row[w + t * Q] = (int8_t)((word >> (8 * t)) & 0xFFu);
-    }
+    store_word_rows<B::HALO>(sq, gocc, L0, L1, Q, RS, RY, sl, threadIdx.x, NT);
     sync_all();
   }
 }

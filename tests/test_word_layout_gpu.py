@@ -76,8 +76,10 @@ def test_word_equals_byte_layout(gpu_lib, L, S, precision):
         assert np.array_equal(b.corr(), batches[0].corr())
 
 
-@pytest.mark.parametrize("L,S", [((16, 16, 16), 4), ((20, 12, 10), 1)])
+@pytest.mark.parametrize("L,S", [((16, 16, 16), 4), ((20, 12, 10), 1), ((16, 16, 8), 3), ((16, 32, 16), 7)])
 def test_word_layout_matches_oracle(gpu_lib, L, S):
+    """Row slabs that split planes between CTAs (16 x 8 rows over 3 CTAs, 32 x 16 over 7)
+    and ones that do not give the oracle's trajectory."""
     n_chains = 2
     model, occ, T, mu, seeds = _setup(L, n_chains, seed=21)
     b = clex.ChainBatch(model, L, occ, T, mu, seeds, ctas_per_chain=S)
