@@ -7,7 +7,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/montegpu.h"
@@ -228,6 +231,26 @@ inline size_t slab_smem(int L0, int L1, int L2, int S) {
   return (size_t)(L0 + 2 * CE_HALO) * (L1 + 2 * CE_HALO) * ((L2 + S - 1) / S + 2 * CE_HALO);
 }
 
+// Round-robin placement over the 32 shared-memory banks.  Within a bucket of per-bank
+// counts cnt[32] the t-th item of bank q goes to offset R_t + #{q2 < q : cnt[q2] > t},
+// R_t = sum_q2 min(cnt[q2], t) (all first items of the banks, then all second items, ...):
+// a table of these offsets, built once per bucket.
+struct BankRoundRobin {
+  std::vector<long long> off;  // [t * 32 + q]
+  void build(const int* cnt) {
+    int tmax = 0;
+    for (int q = 0; q < 32; ++q) tmax = std::max(tmax, cnt[q]);
+    off.assign((size_t)tmax * 32, 0);
+    long long k = 0;
+    for (int t = 0; t < tmax; ++t)
+      for (int q = 0; q < 32; ++q) {
+        off[(size_t)t * 32 + q] = k;
+        if (cnt[q] > t) ++k;
+      }
+  }
+  long long at(int q, int t) const { return off[(size_t)t * 32 + q]; }
+};
+
 // Per-slab, per-colour site lists (two passes over the slab).  Within one (slab, colour)
 // list the sites are grouped
 // by (padded index mod 4) and, inside a group, ordered round-robin over the 32 word banks
@@ -246,6 +269,7 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
   // n_colors <= CE_MAX_COLORS, at most 2^31 sites per bucket)
   int count[CE_MAX_COLORS * 128], seen[CE_MAX_COLORS * 128];
   long long cbase[CE_MAX_COLORS + 1], gbase[CE_MAX_COLORS * 4];
+  std::vector<BankRoundRobin> rr((size_t)n_colors * 4);
   long long pos = 0;
   for (int r = 0; r < S; ++r) {
     const int nk = slab_planes(L2, S, r), k0 = slab_start(L2, S, r);
@@ -271,6 +295,7 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
       cstart[r * (n_colors + 1) + c] = (int)cbase[c];
     }
     cstart[r * (n_colors + 1) + n_colors] = (int)cbase[n_colors];
+    for (int b = 0; b < n_colors * 4; ++b) rr[b].build(&count[(size_t)b * 32]);
     for (int kl = 0; kl < nk; ++kl)
       for (int j = 0; j < L1; ++j) {
         const long long row = (long long)L0 * (j + (long long)L1 * (k0 + kl));
@@ -280,11 +305,9 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
           const int c = col[l];
           const uint32_t pidx = prow + i;
           const int g = pidx & 3, q = (pidx >> 2) & 31;
-          const int* cnt = &count[(size_t)c * 128 + g * 32];
           const int t = seen[(size_t)c * 128 + g * 32 + q]++;
           // round-robin position of the t-th site of bank q within (colour, group)
-          long long p = gbase[(size_t)c * 4 + g];
-          for (int q2 = 0; q2 < 32; ++q2) p += std::min(cnt[q2], t) + ((q2 < q && cnt[q2] > t) ? 1 : 0);
+          const long long p = gbase[(size_t)c * 4 + g] + rr[(size_t)c * 4 + g].at(q, t);
           uint32_t flags = 0;
           if (i < CE_HALO) flags |= 1;
           else if (i >= L0 - CE_HALO) flags |= 2;
@@ -392,6 +415,7 @@ inline void build_word_lists(int L0, int L1, int L2, int S, const int32_t* col, 
   const int Q = L0 / 4, RS = quad_row_stride(Q), RY = L1 + 2 * CE_HALO;
   int count[CE_MAX_COLORS * 32], seen[CE_MAX_COLORS * 32];
   long long cbase[CE_MAX_COLORS + 1];
+  std::vector<BankRoundRobin> rr(n_colors);
   long long pos = 0;
   const int kind = word_slab_kind(L1, L2, S);
   for (int r = 0; r < S; ++r) {
@@ -415,6 +439,7 @@ inline void build_word_lists(int L0, int L1, int L2, int S, const int32_t* col, 
       cstart[r * (n_colors + 1) + c] = (int)cbase[c];
     }
     cstart[r * (n_colors + 1) + n_colors] = (int)cbase[n_colors];
+    for (int c = 0; c < n_colors; ++c) rr[c].build(&count[(size_t)c * 32]);
     for (int R = sl.r0; R < sl.r1; ++R) {
       const int j = R % L1, k = R / L1;
       const long long row = (long long)L0 * R;
@@ -426,10 +451,8 @@ inline void build_word_lists(int L0, int L1, int L2, int S, const int32_t* col, 
         const int c = col[row + w];
         const uint32_t pw = prow + w;
         const int q = pw & 31;
-        const int* cnt = &count[(size_t)c * 32];
         const int t = seen[(size_t)c * 32 + q]++;
-        long long p = cbase[c];
-        for (int q2 = 0; q2 < 32; ++q2) p += std::min(cnt[q2], t) + ((q2 < q && cnt[q2] > t) ? 1 : 0);
+        const long long p = cbase[c] + rr[c].at(q, t);
         uint32_t flags = 0;
         if (w < CE_HALO) flags |= 1;
         else if (w >= Q - CE_HALO) flags |= 2;
@@ -484,7 +507,7 @@ inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* 
 }
 
 template <class Kern>
-int max_active_clusters_k(Kern kern, int NT, int S, size_t smem, int* out) {
+int max_active_clusters_query(Kern kern, int NT, int S, size_t smem, int* out) {
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   if (S == 1) {
@@ -510,6 +533,30 @@ int max_active_clusters_k(Kern kern, int NT, int S, size_t smem, int* out) {
   MG_CUDA_TRY(cudaOccupancyMaxActiveClusters(&n, (void*)kern, &cfg));
   *out = n;
   return MG_OK;
+}
+
+template <class Kern>
+int max_active_clusters_k(Kern kern, int NT, int S, size_t smem, int* out) {
+  // results per (device, kernel, threads, CTAs, shared memory): the query is made once
+  static std::mutex mu;
+  static std::map<std::tuple<int, const void*, int, int, size_t>, int> cache;
+  int dev0 = 0;
+  MG_CUDA_TRY(cudaGetDevice(&dev0));
+  const auto key = std::make_tuple(dev0, (const void*)kern, NT, S, smem);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    const auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second;
+      return MG_OK;
+    }
+  }
+  const int rc = max_active_clusters_query(kern, NT, S, smem, out);
+  if (rc == MG_OK) {
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = *out;
+  }
+  return rc;
 }
 
 // layout 0: one site per byte (ce_sweep_kernel); layout 1: four sites per word
