@@ -226,78 +226,51 @@ def default_write_status(mc_calculator, method_log: MethodLog) -> None:
     method_log.begin_lap()
 
 
-class SemiGrandCanonicalCalculator:
-    """Semi-grand canonical Monte Carlo calculator (basic_semigrand_canonical.hh:324-470)."""
+def _flat_occupation(cfg) -> np.ndarray:
+    """Occupation in linear-site-index order (column-major), int32, for either
+    configuration type (this package's 1-D one or the numpy 2-D one of ``ising_py``)."""
+    o = np.asarray(cfg.occupation())
+    if o.ndim == 2:
+        o = o.flatten(order="F")
+    return np.ascontiguousarray(o, dtype=np.int32)
 
-    def __init__(self, system: IsingSystem):
-        if system is None:
-            raise RuntimeError("Error constructing SemiGrandCanonicalCalculator: _system==nullptr")
-        self.system = system
-        self.state: Optional[IsingState] = None
-        self.conditions: Optional[SemiGrandCanonicalConditions] = None
-        self.potential = SemiGrandCanonicalPotential(system)
-        self.formation_energy_calculator = self.potential.formation_energy_calculator
-        self.param_composition_calculator = self.potential.param_composition_calculator
-        self.data: Optional[SemiGrandCanonicalData] = None
-        #: upper bound on passes per kernel launch
-        self.max_passes_per_launch = 4096
-        #: device time of the replay kernels in the last run (ms)
-        self.last_kernel_ms = 0.0
 
-    def default_sampling_functions(self) -> StateSamplingFunctionMap:
-        m = StateSamplingFunctionMap()
-        n = self.system.param_composition_calculator.n_independent_compositions()
-        m["param_composition"] = StateSamplingFunction(
-            "param_composition", "Parametric composition", [n], _DeviceSampled(self, "param_composition"))
-        m["formation_energy"] = StateSamplingFunction(
-            "formation_energy", "Intensive formation energy", [], _DeviceSampled(self, "formation_energy"))
-        m["potential_energy"] = StateSamplingFunction(
-            "potential_energy", "Intensive potential energy", [], _DeviceSampled(self, "potential_energy"))
-        return m
+def _set_flat_occupation(cfg, occ: np.ndarray) -> None:
+    if np.asarray(cfg.occupation()).ndim == 2:
+        cfg.set_occupation(occ.reshape(tuple(cfg.shape), order="F"))
+    else:
+        cfg.set_occupation(occ)
 
-    def default_json_sampling_functions(self) -> jsonStateSamplingFunctionMap:
-        m = jsonStateSamplingFunctionMap()
-        m["configuration"] = jsonStateSamplingFunction(
-            "configuration", "Configuration values", lambda: self.state.configuration.to_dict())
-        return m
 
-    def run(self, state: IsingState, sampling_functions, json_sampling_functions,
-            completion_check_params: CompletionCheckParams, event_generator: SemiGrandCanonicalEventGenerator,
-            sample_period: int = 1, method_log: Optional[MethodLog] = None,
-            random_engine: Optional[RandomNumberEngine] = None,
-            write_status_f: Optional[Callable] = None) -> SemiGrandCanonicalData:
-        """Run at one thermodynamic state; ``state`` is modified in place."""
-        if write_status_f is None:
-            write_status_f = default_write_status
-        self.state = state
-        self.conditions = SemiGrandCanonicalConditions.from_values(state.conditions)
-        if self.conditions.exchange_potential.size != 1:
-            raise RuntimeError("Error in SemiGrandCanonicalCalculator::run: exchange_potential must have size 1")
-        T = self.conditions.temperature
-        cfg = state.configuration
+class _ReplayDriver:
+    """The main loop of basic_occupation_metropolis.hh:354-425 for the random single-site
+    flip of a 2-D Ising model, executed as a serial replay on the GPU: the kernel consumes
+    the caller's mt19937_64 engine exactly as the reference does (site draw, acceptance
+    draw only for dE >= 0).  The host drives it in chunks of whole passes and reproduces,
+    call for call, the completion check evaluated before every step: samples and counts
+    change only at pass boundaries, so a chunk ends at the first pass boundary where that
+    check could finish the run or run a convergence check."""
+
+    #: upper bound on passes per kernel launch
+    max_passes_per_launch = 4096
+    #: device time of the replay kernels in the last run (ms)
+    last_kernel_ms = 0.0
+
+    def _replay(self, data, J: float, mu: float, T: float, use_nlist: bool, sample_period: int,
+                method_log: MethodLog, random_engine: RandomNumberEngine, write_status_f: Callable,
+                completion_check_params: CompletionCheckParams) -> None:
+        """Run ``self.state`` with ``dE = dE_f - mu (new - old) / 2`` until complete; the
+        occupation, the engine and the acceptance counts are synchronised at the end."""
+        cfg = self.state.configuration
         N = cfg.n_variable_sites
-        self.potential.set_state(state, self.conditions)
-        event_generator.set_state(state)
-        self.data = data = SemiGrandCanonicalData(sampling_functions, json_sampling_functions, N,
-                                                  completion_check_params)
-        if random_engine is None:
-            random_engine = RandomNumberEngine()
-        if method_log is None:
-            method_log = MethodLog(os.path.join(os.getcwd(), "status.json"), 600.0)
-        method_log.restart_clock()
-        method_log.begin_lap()
-
         rows, cols = int(cfg.shape[0]), int(cfg.shape[1])
-        J = self.system.formation_energy_calculator.J
-        use_nlist = self.system.formation_energy_calculator.use_nlist
-        mu = float(self.conditions.exchange_potential[0])
         L = _lib.lib()
         h = C.c_void_p()
-        occ = np.ascontiguousarray(cfg.occupation().astype(np.int32))
+        occ = _flat_occupation(cfg)
         states = (C.c_char_p * 1)(random_engine.dump().encode())
         _lib.check(L.mg_ising_replay_create(
-            rows, cols, 1, 1 if use_nlist else 0, _lib.ptr(np.array([J]), C.c_double),
-            _lib.ptr(np.array([T], dtype=float), C.c_double), _lib.ptr(np.array([mu]), C.c_double),
+            rows, cols, 1, 1 if use_nlist else 0, _lib.ptr(np.array([J], dtype=float), C.c_double),
+            _lib.ptr(np.array([T], dtype=float), C.c_double), _lib.ptr(np.array([mu], dtype=float), C.c_double),
             _lib.ptr(occ, C.c_int32), states, C.byref(h)))
         self.last_kernel_ms = 0.0
         try:
@@ -306,8 +279,6 @@ class SemiGrandCanonicalCalculator:
         finally:
             self._sync_state(h, random_engine, data)
             L.mg_ising_replay_destroy(h)
-        write_status_f(self, method_log)
-        return data
 
     # -- internals
     def _sync_state(self, h, random_engine, data) -> None:
@@ -319,7 +290,7 @@ class SemiGrandCanonicalCalculator:
         acc, rej = C.c_ulonglong(), C.c_ulonglong()
         _lib.check(L.mg_ising_replay_get_state(h, _lib.ptr(occ, C.c_int32), bufs, ENGINE_STATE_LEN,
                                                C.byref(acc), C.byref(rej)))
-        cfg.set_occupation(occ)
+        _set_flat_occupation(cfg, occ)
         random_engine.load(buf.value.decode())
         data.n_accept = int(acc.value)
         data.n_reject = int(rej.value)
@@ -404,7 +375,7 @@ class SemiGrandCanonicalCalculator:
             # custom functions read the host state: bring the occupation back first
             occ = np.zeros(N, dtype=np.int32)
             _lib.check(_lib.lib().mg_ising_replay_get_state(h, _lib.ptr(occ, C.c_int32), None, 0, None, None))
-            self.state.configuration.set_occupation(occ)
+            _set_flat_occupation(self.state.configuration, occ)
         for name in sorted(data.sampling_functions):
             f = data.sampling_functions[name]
             if isinstance(f.function, _DeviceSampled) and f.function.calc is self:
@@ -413,6 +384,72 @@ class SemiGrandCanonicalCalculator:
                 data.samplers[name].append(f())
         for name in sorted(data.json_sampling_functions):
             data.json_samplers[name].values.append(data.json_sampling_functions[name]())
+
+
+class SemiGrandCanonicalCalculator(_ReplayDriver):
+    """Semi-grand canonical Monte Carlo calculator (basic_semigrand_canonical.hh:324-470)."""
+
+    def __init__(self, system: IsingSystem):
+        if system is None:
+            raise RuntimeError("Error constructing SemiGrandCanonicalCalculator: _system==nullptr")
+        self.system = system
+        self.state: Optional[IsingState] = None
+        self.conditions: Optional[SemiGrandCanonicalConditions] = None
+        self.potential = SemiGrandCanonicalPotential(system)
+        self.formation_energy_calculator = self.potential.formation_energy_calculator
+        self.param_composition_calculator = self.potential.param_composition_calculator
+        self.data: Optional[SemiGrandCanonicalData] = None
+
+    def default_sampling_functions(self) -> StateSamplingFunctionMap:
+        m = StateSamplingFunctionMap()
+        n = self.system.param_composition_calculator.n_independent_compositions()
+        m["param_composition"] = StateSamplingFunction(
+            "param_composition", "Parametric composition", [n], _DeviceSampled(self, "param_composition"))
+        m["formation_energy"] = StateSamplingFunction(
+            "formation_energy", "Intensive formation energy", [], _DeviceSampled(self, "formation_energy"))
+        m["potential_energy"] = StateSamplingFunction(
+            "potential_energy", "Intensive potential energy", [], _DeviceSampled(self, "potential_energy"))
+        return m
+
+    def default_json_sampling_functions(self) -> jsonStateSamplingFunctionMap:
+        m = jsonStateSamplingFunctionMap()
+        m["configuration"] = jsonStateSamplingFunction(
+            "configuration", "Configuration values", lambda: self.state.configuration.to_dict())
+        return m
+
+    def run(self, state: IsingState, sampling_functions, json_sampling_functions,
+            completion_check_params: CompletionCheckParams, event_generator: SemiGrandCanonicalEventGenerator,
+            sample_period: int = 1, method_log: Optional[MethodLog] = None,
+            random_engine: Optional[RandomNumberEngine] = None,
+            write_status_f: Optional[Callable] = None) -> SemiGrandCanonicalData:
+        """Run at one thermodynamic state; ``state`` is modified in place."""
+        if write_status_f is None:
+            write_status_f = default_write_status
+        self.state = state
+        self.conditions = SemiGrandCanonicalConditions.from_values(state.conditions)
+        if self.conditions.exchange_potential.size != 1:
+            raise RuntimeError("Error in SemiGrandCanonicalCalculator::run: exchange_potential must have size 1")
+        T = self.conditions.temperature
+        cfg = state.configuration
+        N = cfg.n_variable_sites
+        self.potential.set_state(state, self.conditions)
+        event_generator.set_state(state)
+        self.data = data = SemiGrandCanonicalData(sampling_functions, json_sampling_functions, N,
+                                                  completion_check_params)
+        if random_engine is None:
+            random_engine = RandomNumberEngine()
+        if method_log is None:
+            method_log = MethodLog(os.path.join(os.getcwd(), "status.json"), 600.0)
+        method_log.restart_clock()
+        method_log.begin_lap()
+
+        J = self.system.formation_energy_calculator.J
+        use_nlist = self.system.formation_energy_calculator.use_nlist
+        mu = float(self.conditions.exchange_potential[0])
+        self._replay(data, J, mu, T, use_nlist, sample_period, method_log, random_engine, write_status_f,
+                     completion_check_params)
+        write_status_f(self, method_log)
+        return data
 
 
 __all__ = ["SemiGrandCanonicalCalculator", "SemiGrandCanonicalConditions", "SemiGrandCanonicalData",
