@@ -59,7 +59,7 @@ MG_BASIS_ADAPTER(FccTernary, fcc_ternary, )
 #undef MG_BASIS_ADAPTER
 
 constexpr int NT_BINARY = 512;
-constexpr int NT_TERNARY = 256;
+constexpr int NT_TERNARY = 384;
 constexpr int CE_HALO = 2;
 constexpr int CE_MAX_COLORS = 64;
 

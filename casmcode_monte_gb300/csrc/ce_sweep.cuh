@@ -355,7 +355,7 @@ template <class B, int NT>
 __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__ CeSweepArgs<B::NFEAT> A) {
   constexpr int NS = B::NSPECIES;
   constexpr int NSLOT = CeSlots<B::NCLASS>::N;
-  constexpr int PRE = (NS == 2) ? 3 : 2;
+  constexpr int PRE = (NS == 2) ? 3 : 1;
   extern __shared__ __align__(16) int8_t s[];
   __shared__ int acc_sm[2][NSLOT];
   __shared__ float dmu32_sm[NS * NS];
@@ -1248,7 +1248,7 @@ template <class B, int NT>
 __global__ void __launch_bounds__(NT, 1) ce_pool_kernel(const __grid_constant__ CePoolArgs<B::NFEAT> A) {
   constexpr int NS = B::NSPECIES;
   constexpr int NSLOT = CeSlots<B::NCLASS>::N;
-  constexpr int PRE = (NS == 2) ? 3 : 2;
+  constexpr int PRE = (NS == 2) ? 3 : 1;
   extern __shared__ __align__(16) int8_t s[];
   __shared__ int acc_sm[2][NSLOT];
   __shared__ float dmu32_sm[NS * NS];
@@ -1350,7 +1350,7 @@ template <class B, int NT>
 __global__ void __launch_bounds__(NT, 1) ce_pool_cluster_kernel(const __grid_constant__ CePoolArgs<B::NFEAT> A) {
   constexpr int NS = B::NSPECIES;
   constexpr int NSLOT = CeSlots<B::NCLASS>::N;
-  constexpr int PRE = (NS == 2) ? 3 : 2;
+  constexpr int PRE = (NS == 2) ? 3 : 1;
   extern __shared__ __align__(16) int8_t s[];
   __shared__ int acc_sm[2][NSLOT];
   __shared__ float dmu32_sm[NS * NS];
