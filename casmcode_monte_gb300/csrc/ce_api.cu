@@ -6,12 +6,32 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/montegpu.h"
 #include "ce_host.cuh"
 #include "mg_common.cuh"
+
+// Host geometry of one supercell shape, shared by every batch of that shape and built
+// once per process: the colouring (number of colours, pipeline colouring id, word-layout
+// eligibility) and, per CTA count and layout family (byte / word), the site lists.
+struct ShapeColouring {
+  std::vector<int32_t> color;
+  int n_colors = 0;
+  int pipe = -1;
+  bool word = false;  // eligible for the word layouts
+};
+struct ShapeLists {
+  std::vector<int> cstart;
+  std::vector<uint32_t> entries, site;
+  int max_words = 0;  // most words (word lists) or sites of one CTA and colour
+};
 
 struct mg_ce_batch {
   const mg_ce_model* model = nullptr;
@@ -23,7 +43,7 @@ struct mg_ce_batch {
   int ctas_requested = 0;  // 0: chosen by occupancy
   size_t smem = 0;
   long long pass = 0;
-  std::vector<int32_t> color;
+  std::shared_ptr<const ShapeColouring> col;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
@@ -41,6 +61,75 @@ namespace {
 
 using mg::set_error;
 using namespace mg::host;
+
+// Bounded first-in first-out caches of shape geometry (a shape used again after many
+// others is rebuilt).
+constexpr size_t kMaxCachedColourings = 32, kMaxCachedLists = 64;
+std::mutex g_shape_mu;
+std::map<std::tuple<int, int, int, int>, std::shared_ptr<const ShapeColouring>> g_colourings;
+std::deque<std::tuple<int, int, int, int>> g_colouring_order;
+std::map<std::tuple<int, int, int, int, int, int>, std::shared_ptr<const ShapeLists>> g_lists;
+std::deque<std::tuple<int, int, int, int, int, int>> g_lists_order;
+
+// the colouring of a shape; null when it needs more than CE_MAX_COLORS colours
+std::shared_ptr<const ShapeColouring> shape_colouring(int kind, int L0, int L1, int L2) {
+  const auto key = std::make_tuple(kind, L0, L1, L2);
+  {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    const auto it = g_colourings.find(key);
+    if (it != g_colourings.end()) return it->second;
+  }
+  auto c = std::make_shared<ShapeColouring>();
+  c->color.assign((size_t)L0 * L1 * L2, -1);
+  c->n_colors = color_supercell(L0, L1, L2, kind, c->color.data(), &c->pipe);
+  if (c->n_colors < 1) return nullptr;
+  c->word = quad_eligible(kind, L0, L1, L2, c->color.data());
+  std::lock_guard<std::mutex> lk(g_shape_mu);
+  if (g_colourings.emplace(key, c).second) {
+    g_colouring_order.push_back(key);
+    if (g_colouring_order.size() > kMaxCachedColourings) {
+      g_colourings.erase(g_colouring_order.front());
+      g_colouring_order.pop_front();
+    }
+  }
+  return g_colourings[key];
+}
+
+// site lists of a shape for S CTAs per chain, word (layout >= 1) or byte lists
+std::shared_ptr<const ShapeLists> shape_lists(int kind, int L0, int L1, int L2, int S, int layout,
+                                              const ShapeColouring& col) {
+  const int word = layout >= 1 ? 1 : 0;
+  const auto key = std::make_tuple(kind, L0, L1, L2, S, word);
+  {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    const auto it = g_lists.find(key);
+    if (it != g_lists.end()) return it->second;
+  }
+  auto l = std::make_shared<ShapeLists>();
+  const long long N = (long long)L0 * L1 * L2;
+  const long long n_entries = word ? N / 4 : N;
+  l->cstart.assign((size_t)S * (col.n_colors + 1), 0);
+  l->entries.resize(n_entries);
+  l->site.resize(n_entries);
+  if (word)
+    build_word_lists(L0, L1, L2, S, col.color.data(), col.n_colors, l->cstart.data(), l->entries.data(),
+                     l->site.data());
+  else
+    build_site_lists(L0, L1, L2, S, col.color.data(), col.n_colors, kind, l->cstart.data(), l->entries.data(),
+                     l->site.data());
+  for (int r = 0; r < S; ++r)
+    for (int c = 0; c < col.n_colors; ++c)
+      l->max_words = std::max(l->max_words, l->cstart[r * (col.n_colors + 1) + c + 1] - l->cstart[r * (col.n_colors + 1) + c]);
+  std::lock_guard<std::mutex> lk(g_shape_mu);
+  if (g_lists.emplace(key, l).second) {
+    g_lists_order.push_back(key);
+    if (g_lists_order.size() > kMaxCachedLists) {
+      g_lists.erase(g_lists_order.front());
+      g_lists_order.pop_front();
+    }
+  }
+  return g_lists[key];
+}
 
 bool make_model(int kind, const double* eci, int n, mg_ce_model* m, std::string& err) {
   m->kind = kind;
@@ -117,26 +206,16 @@ int setup_layout(mg_ce_batch* b, int layout) {
     set_error("Error in mg_ce_batch_create: slab too large for 24-bit shared-memory indices");
     return MG_ERR_INVALID;
   }
-  const long long n_entries = layout >= 1 ? b->N / 4 : b->N;
-  std::vector<int> cstart((size_t)S * (b->n_colors + 1), 0);
-  std::vector<uint32_t> entries(n_entries), site(n_entries);
-  if (layout == 3) {
+  const auto lists = shape_lists(m->kind, b->L0, b->L1, b->L2, S, layout, *b->col);
+  if (layout == 3 && lists->max_words > mg::host::NW_WS) {
     // the warp-specialised kernel stages at most NW_WS words per (CTA, colour)
-    build_word_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
-                     site.data());
-    for (int r = 0; r < S; ++r)
-      for (int c = 0; c < b->n_colors; ++c)
-        if (cstart[r * (b->n_colors + 1) + c + 1] - cstart[r * (b->n_colors + 1) + c] > mg::host::NW_WS) {
-          set_error("Error in mg_ce_batch_set_layout: more words per CTA and colour than the warp-specialised "
-                    "kernel stages");
-          return MG_ERR_INVALID;
-        }
-  } else if (layout >= 1)
-    build_word_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, cstart.data(), entries.data(),
-                     site.data());
-  else
-    build_site_lists(b->L0, b->L1, b->L2, S, b->color.data(), b->n_colors, b->model->kind, cstart.data(), entries.data(),
-                     site.data());
+    set_error("Error in mg_ce_batch_set_layout: more words per CTA and colour than the warp-specialised "
+              "kernel stages");
+    return MG_ERR_INVALID;
+  }
+  const std::vector<int>& cstart = lists->cstart;
+  const std::vector<uint32_t>& entries = lists->entries;
+  const std::vector<uint32_t>& site = lists->site;
   cudaFree(b->dcstart);
   cudaFree(b->dentries);
   cudaFree(b->dsite);
@@ -252,14 +331,15 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   b->ctas_requested = ctas_per_chain;
 
   // colouring, then the layout (word layout where the basis and colouring allow it)
-  b->color.assign(N, -1);
-  b->n_colors = color_supercell(L0, L1, L2, m->kind, b->color.data(), &b->pipe);
+  b->col = shape_colouring(m->kind, L0, L1, L2);
+  b->n_colors = b->col ? b->col->n_colors : 0;
+  b->pipe = b->col ? b->col->pipe : -1;
   if (b->n_colors < 1) {
     set_error("Error in mg_ce_batch_create: colouring needs more than 64 colours");
     delete b;
     return MG_ERR_INVALID;
   }
-  const int layout = !quad_eligible(m->kind, L0, L1, L2, b->color.data()) ? 0 : (b->pipe >= 0 ? 3 : 1);
+  const int layout = !b->col->word ? 0 : (b->pipe >= 0 ? 3 : 1);
   b->hcp.resize(n_chains);
   make_chain_params(m, n_chains, temperature, mu, seeds, chain_ids, b->hcp.data());
 
@@ -338,7 +418,7 @@ int mg_ce_batch_set_layout(mg_ce_batch* b, int layout) {
     set_error("Error in mg_ce_batch_set_layout: invalid argument");
     return MG_ERR_INVALID;
   }
-  if (layout >= 1 && !quad_eligible(b->model->kind, b->L0, b->L1, b->L2, b->color.data())) {
+  if (layout >= 1 && !b->col->word) {
     set_error("Error in mg_ce_batch_set_layout: the word layout needs the binary basis, L0 = 4Q with Q >= 4 "
               "and a colouring with colour(i + Q) = colour(i)");
     return MG_ERR_INVALID;
@@ -358,7 +438,7 @@ int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout_out, int*
     return MG_ERR_INVALID;
   }
   const mg_ce_model* m = b->model;
-  const bool word = quad_eligible(m->kind, b->L0, b->L1, b->L2, b->color.data());
+  const bool word = b->col->word;
   std::vector<int> layouts = {0};
   if (word) layouts.push_back(1);
   if (word && b->pipe >= 0) {
@@ -424,7 +504,7 @@ int mg_ce_batch_colors(const mg_ce_batch* b, int32_t* color) {
     set_error("Error in mg_ce_batch_colors: invalid argument");
     return MG_ERR_INVALID;
   }
-  std::memcpy(color, b->color.data(), sizeof(int32_t) * b->color.size());
+  std::memcpy(color, b->col->color.data(), sizeof(int32_t) * b->col->color.size());
   return MG_OK;
 }
 
