@@ -3,6 +3,10 @@
 * ``metropolis_acceptance`` (python/libcasm/monte/methods/_metropolis.py:6-48,
   include/casm/monte/methods/metropolis.hh:26-35): accept if dE < 0 without drawing,
   else accept if ``random_real(1.0) < exp(-dE * beta)``.
+* ``occupation_metropolis`` (include/casm/monte/methods/occupation_metropolis.hh:90-154):
+  the same loop over an ``OccLocation`` with a proposal function over possible swaps,
+  tracking the potential energy per unit cell in ``state.properties`` and sampling through
+  a ``run_management.RunManager`` (sampling fixtures, completion checks, results files).
 * ``BasicOccupationMetropolisData`` and ``basic_occupation_metropolis``
   (include/casm/monte/methods/basic_occupation_metropolis.hh:18-115, 354-425): the
   reference's generic Metropolis loop, parameterised by caller-supplied functions for the
@@ -19,12 +23,15 @@ import math
 import sys
 from typing import Callable, Optional
 
+import numpy as np
+
 from .. import MethodLog, RandomNumberEngine, RandomNumberGenerator
+from ..events import OccEvent
 from ..sampling import (CompletionCheck, CompletionCheckParams, Sampler, get_n_samples, jsonSampler,
                         jsonStateSamplingFunctionMap, StateSamplingFunctionMap)
 
 __all__ = ["KB", "BasicOccupationMetropolisData", "basic_occupation_metropolis", "default_write_status",
-           "metropolis_acceptance", "write_no_status"]
+           "metropolis_acceptance", "occupation_metropolis", "write_no_status"]
 
 KB = 8.6173303e-05  # eV/K (the reference's libcasm-global constant)
 
@@ -151,3 +158,55 @@ def basic_occupation_metropolis(data: BasicOccupationMetropolisData, temperature
             if freq is not None and method_log.lap_time() >= freq:
                 write_status_f(data, method_log)
     write_status_f(data, method_log)
+
+
+def _occupation_array(state) -> np.ndarray:
+    """The state's occupation as a writable array (the configurations of this package
+    keep it in ``_occ`` or ``_occupation``; a plain array is used as it is)."""
+    cfg = state.configuration
+    for attr in ("_occ", "_occupation"):
+        a = getattr(cfg, attr, None)
+        if isinstance(a, np.ndarray):
+            return a.reshape(-1, order="F") if a.ndim > 1 else a
+    return cfg.occupation()
+
+
+def occupation_metropolis(state, occ_location, potential, possible_swaps, propose_event_f: Callable,
+                          random_number_generator, run_manager) -> None:
+    """Occupation Metropolis Monte Carlo with run management (occupation_metropolis.hh:90-154).
+
+    Until ``run_manager.is_complete()``: write status if due; propose an event with
+    ``propose_event_f(event, occ_location, possible_swaps, random_number_generator)`` (an
+    exception ends the run); ``dE = potential.occ_delta_per_supercell(sites, new_occ)``;
+    Metropolis acceptance; an accepted event updates ``occ_location`` and the occupation
+    and adds dE / n_unitcells to ``state.properties.scalar_values["potential_energy"]``;
+    count the step; sample if due.  The run manager is initialized with
+    ``occ_location.mol_size()`` steps per pass and finalized with the final state.
+    """
+    if getattr(potential, "state", None) is not state:
+        raise RuntimeError("Error in monte::occupation_metropolis: potential not set to correct state")
+    n_unitcells = float(state.configuration.n_unitcells)
+    state.properties.scalar_values["potential_energy"] = potential.per_supercell() / n_unitcells
+    beta = 1.0 / (KB * state.conditions.scalar_values["temperature"])
+    occupation = _occupation_array(state)
+    event = OccEvent()
+    run_manager.initialize(occ_location.mol_size())
+    run_manager.sample_data_by_count_if_due(state)
+    while not run_manager.is_complete():
+        run_manager.write_status_if_due()
+        try:
+            propose_event_f(event, occ_location, possible_swaps, random_number_generator)
+        except Exception as e:  # the reference logs the error and ends the run
+            sys.stderr.write(f"\nError proposing event: {e}\n")
+            break
+        dE = potential.occ_delta_per_supercell(event.linear_site_index, event.new_occ)
+        if metropolis_acceptance(dE, beta, random_number_generator):
+            run_manager.increment_n_accept()
+            occ_location.apply(event, occupation)
+            state.properties.scalar_values["potential_energy"] += dE / n_unitcells
+        else:
+            run_manager.increment_n_reject()
+        run_manager.increment_step()
+        run_manager.sample_data_by_count_if_due(state)
+    run_manager.finalize(state)
+
