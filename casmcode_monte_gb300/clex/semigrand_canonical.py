@@ -499,6 +499,81 @@ class SemiGrandCanonicalCalculator:
                 if b < k - 1:
                     cc._repeat_calls(N - 1)
 
+    def run_fixtures(self, state: ClexState, run_manager) -> None:
+        """Run with the sampling fixtures of a ``run_management.RunManager`` (as
+        occupation_metropolis.hh:90-154 does on the host), sweeping on the GPU.
+
+        Fixtures must sample by pass.  Every pass counts N steps; the accepted flips of a
+        pass come from the device, and ``state.properties.scalar_values["potential_energy"]``
+        (per unit cell) follows the device's exact integer sums.  Chunks of passes end at
+        the next pass where a fixture samples or where its completion check could finish or
+        check convergence; before each sample the occupation is brought back to ``state``.
+        The fixtures are finalized (results written) with the final state.
+        """
+        from ..sampling import SAMPLE_MODE
+
+        for f in run_manager.sampling_fixtures:
+            if f.params().sampling_params.sample_mode != SAMPLE_MODE.BY_PASS:
+                raise RuntimeError("Error in SemiGrandCanonicalCalculator::run_fixtures: the GPU sweep proposes whole "
+                                   "passes; sampling fixtures must sample by pass")
+        self.state = state
+        self.conditions = SemiGrandCanonicalConditions.from_values(state.conditions)
+        self.potential.set_state(state, self.conditions)
+        model = self.system.model
+        N = state.configuration.n_variable_sites
+        mu = self.conditions.exchange_potential.reshape(1, -1)
+        seed = RandomNumberGenerator(run_manager.engine).random_int(2**63 - 1)
+        batch = ChainBatch(model, state.configuration.shape, state.configuration.occupation()[None, :],
+                           [self.conditions.temperature], mu, np.array([seed], dtype=np.uint64),
+                           precision=self.precision)
+        fixtures = run_manager.sampling_fixtures
+        self.last_kernel_ms = 0.0
+        try:
+            run_manager.initialize(N)
+            corr = batch.corr()
+            ef = float(model.formation_per_supercell(corr[0]))
+            nx = model.n_x(corr[0], N)
+            state.properties.scalar_values["potential_energy"] = (ef - float(np.dot(mu[0], nx))) / N
+            run_manager.sample_data_by_count_if_due(state)
+            while not run_manager.is_complete():
+                run_manager.write_status_if_due()
+                for f in fixtures:
+                    f._completion_check._repeat_calls(N - 1)
+                # plan the chunk
+                k = max(1, min(int(self.max_passes_per_launch), *[max(1, _fixture_passes_to_sample(f)) for f in fixtures]))
+                for p in range(1, k + 1):
+                    if any(f._completion_check._could_complete_at(
+                            get_n_samples(f.results().samplers) + (1 if f.next_sample_count() <= f.counter().count + p
+                                                                   else 0), f.counter().count + p) for f in fixtures):
+                        k = p
+                        break
+                out = batch.run(k)
+                self.last_kernel_ms += batch.last_kernel_ms()
+                s = accumulate(model, corr, out, mu, N)
+                corr = s.int_corr[-1]
+                for b in range(k):
+                    acc = int(out[b, 0, 0])
+                    for f in fixtures:
+                        c = f.counter()
+                        c.pass_ += 1
+                        c.count += 1
+                        c.n_accept += acc
+                        c.n_reject += N - acc
+                    state.properties.scalar_values["potential_energy"] = float(s.potential_energy[b, 0])
+                    if any(f.counter().count == f.next_sample_count() for f in fixtures):
+                        # a chunk ends at the first pass where a fixture samples
+                        state.configuration.set_occupation(batch.occupation()[0])
+                        run_manager.sample_data_by_count_if_due(state)
+                    if b < k - 1:
+                        if run_manager.is_complete():
+                            raise RuntimeError("internal error: completion inside a planned chunk")
+                        for f in fixtures:
+                            f._completion_check._repeat_calls(N - 1)
+        finally:
+            state.configuration.set_occupation(batch.occupation()[0])
+            batch.close()
+        run_manager.finalize(state)
+
     def _push_sample(self, batch, data, s, b, device_only) -> None:
         values = {
             "param_composition": np.asarray(s.param_composition[b, 0], dtype=float),
@@ -519,6 +594,10 @@ class SemiGrandCanonicalCalculator:
                 data.samplers[name].append(f())
         for name in sorted(data.json_sampling_functions):
             data.json_samplers[name].values.append(data.json_sampling_functions[name]())
+
+
+def _fixture_passes_to_sample(f) -> int:
+    return f.next_sample_count() - f.counter().count
 
 
 __all__ = ["ClexConfiguration", "ClexFormationEnergy", "ClexParamComposition", "ClexState", "ClexSystem",

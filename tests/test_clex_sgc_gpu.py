@@ -121,3 +121,45 @@ def test_ternary_run_and_state_queries(gpu_lib, tmp_path):
     cfg.set_occ(l1, n1)
     cfg.set_occ(l2, n2)
     assert abs((fe.per_supercell() - e0) - d2) <= 1e-10 * max(1.0, abs(e0))
+
+
+def test_run_fixtures_with_run_manager(gpu_lib, tmp_path):
+    """GPU sweeps driven by the reference's run management: a converging fixture with its
+    results files and a second fixture with a count cutoff (all fixtures must complete)."""
+    import json
+
+    import casmcode_monte_gb300.run_management as rm
+
+    model, calc, state, _ = _setup(T=1200.0)
+    fmap = calc.default_sampling_functions()
+    fmap["pe_tracked"] = sampling.StateSamplingFunction(
+        "pe_tracked", "tracked potential energy per unit cell", [],
+        lambda: np.array([state.properties.scalar_values["potential_energy"]]))
+    cc = _params()
+    sampling.converge(fmap, cc).set_precision("pe_tracked", abs=3e-4)
+    thermo = rm.SamplingFixtureParams(
+        "thermo", fmap, {}, {}, rm.SamplingParams(sampler_names=["pe_tracked", "potential_energy", "param_composition"]),
+        cc, results_io=rm.jsonResultsIO(str(tmp_path / "thermo"), write_observations=True))
+    cc2 = _params(max_count=150, min_sample=None)
+    traj = rm.SamplingFixtureParams(
+        "traj", fmap, {}, {}, rm.SamplingParams(sampler_names=["param_composition"], period=10.0, begin=10.0,
+                                               do_sample_trajectory=True),
+        cc2, results_io=rm.jsonResultsIO(str(tmp_path / "traj"), write_trajectory=True))
+    engine = monte.RandomNumberEngine()
+    engine.seed(8)
+    manager = rm.RunManager(engine, [thermo, traj], global_cutoff=False)
+    calc.run_fixtures(state, manager)
+    t, tr = manager.sampling_fixtures
+    assert t.completion_check_results().convergence_check_results.all_converged
+    assert tr.counter().count >= 150 and tr.results().sample_count[:3] == [10, 20, 30]
+    rt = t.results()
+    # the tracked energy is the device's exact sums; the default function recomputes it
+    assert np.allclose(rt.samplers["pe_tracked"].component(0), rt.samplers["potential_energy"].component(0),
+                       rtol=0, atol=1e-12)
+    assert rt.n_accept + rt.n_reject == 512 * t.counter().count
+    with open(tmp_path / "thermo" / "summary.json") as f:
+        summary = json.load(f)
+    assert summary["completion_check_results"]["all_converged"] == [True]
+    assert summary["statistics"]["pe_tracked"]["value"]["is_converged"] == [True]
+    with open(tmp_path / "traj" / "run.0" / "trajectory.json") as f:
+        assert len(json.load(f)) == len(tr.results().sample_count)
