@@ -184,6 +184,8 @@ class ChainBatch:
 
     def run(self, n_passes: int, want_output: bool = True) -> Optional[np.ndarray]:
         """Advance every chain by n_passes; returns [n_passes, n_chains, n_classes+2] int64."""
+        if int(n_passes) < 0:
+            raise RuntimeError("Error in mg_ce_batch_run: invalid argument")
         out = None
         if want_output:
             out = np.zeros((n_passes, self.n_chains, self.n_slots), dtype=np.int64)
@@ -293,6 +295,8 @@ class ChainPool:
 
     def run(self, slots, n_passes: int, want_output: bool = True) -> Optional[np.ndarray]:
         """Sweep the chains in ``slots``; returns [len(slots), n_passes, n_classes+2] int64."""
+        if int(n_passes) < 0:
+            raise RuntimeError("Error in mg_ce_pool_run: invalid argument")
         sl = np.ascontiguousarray(np.asarray(slots, dtype=np.int32).reshape(-1))
         out = np.zeros((sl.size, n_passes, self.n_slots), dtype=np.int64) if want_output else None
         _lib.check(_lib.lib().mg_ce_pool_run(self._h, _lib.ptr(sl, C.c_int32), sl.size, int(n_passes),

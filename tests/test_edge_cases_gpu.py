@@ -1,0 +1,58 @@
+"""Edge cases of the GPU path: the largest supercell the sweep kernels hold in shared
+memory, one too large (a clean error, the context stays usable), zero passes, and invalid
+arguments (each a RuntimeError with the library's message)."""
+import numpy as np
+import pytest
+
+from casmcode_monte_gb300 import clex
+
+pytestmark = pytest.mark.gpu
+
+
+def _model():
+    return clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 2))
+
+
+def test_largest_supercell_tracks_exact_correlations(gpu_lib):
+    model = _model()
+    L = (128, 128, 128)
+    n = L[0] * L[1] * L[2]
+    rng = np.random.default_rng(1)
+    occ = np.stack([clex.random_occupation(2, n, rng) for _ in range(2)])
+    b = clex.ChainBatch(model, L, occ, [800.0, 1600.0], np.zeros((2, 1)), [3, 4])
+    corr0 = b.corr()
+    out = b.run(3)
+    s = clex.accumulate(model, corr0, out, np.zeros((2, 1)), n)
+    assert np.array_equal(b.corr(), s.int_corr[-1])
+    assert np.array_equal(b.occupation().sum(axis=1, dtype=np.int64), s.int_corr[-1][:, 1])
+    assert np.all(out[:, :, 0] > 0)
+
+
+def test_too_large_supercell_is_refused_cleanly(gpu_lib):
+    model = _model()
+    L = (256, 256, 256)
+    occ = np.zeros((1, L[0] * L[1] * L[2]), dtype=np.int8)
+    with pytest.raises(RuntimeError, match="does not fit in shared memory"):
+        clex.ChainBatch(model, L, occ, [1000.0], np.zeros((1, 1)), [1])
+    # the context is still usable
+    small = clex.ChainBatch(model, (8, 8, 8), np.zeros((1, 512), dtype=np.int8), [1000.0], np.zeros((1, 1)), [1])
+    assert small.run(2).shape == (2, 1, model.n_classes + 2)
+
+
+def test_zero_passes_and_invalid_arguments(gpu_lib):
+    model = _model()
+    occ = clex.random_occupation(2, 512, np.random.default_rng(2))[None, :]
+    b = clex.ChainBatch(model, (8, 8, 8), occ, [1000.0], np.zeros((1, 1)), [5])
+    out = b.run(0)
+    assert out.shape == (0, 1, model.n_classes + 2)
+    assert np.array_equal(b.occupation(), occ)
+    with pytest.raises(RuntimeError, match="invalid argument"):
+        b.run(-1)
+    with pytest.raises(RuntimeError, match="temperature must be > 0"):
+        clex.ChainBatch(model, (8, 8, 8), occ, [0.0], np.zeros((1, 1)), [5])
+    bad = occ.copy()
+    bad[0, 7] = 2
+    with pytest.raises(RuntimeError, match="occupant index out of range"):
+        clex.ChainBatch(model, (8, 8, 8), bad, [1000.0], np.zeros((1, 1)), [5])
+    with pytest.raises(RuntimeError, match=">= 4"):
+        clex.ChainBatch(model, (3, 8, 8), occ[:, :192], [1000.0], np.zeros((1, 1)), [5])
