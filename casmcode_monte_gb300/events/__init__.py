@@ -38,7 +38,8 @@ from typing import Optional, Sequence
 import numpy as np
 
 __all__ = [
-    "Atom", "AtomInfo", "AtomLocation", "AtomTraj", "Conversions", "IntegralSiteCoordinate", "Mol",
+    "Atom", "AtomInfo", "AtomInfoMap", "AtomLocation", "AtomTraj", "AtomTrajVector", "AtomVector", "Conversions",
+    "IntVector", "IntegralSiteCoordinate", "LongVector", "Mol", "MolVector", "OccSwapCountMap", "OccTransformVector",
     "MultiOccSwap", "OccCandidate", "OccCandidateList", "OccEvent", "OccLocation", "OccSwap", "OccTransform",
     "Occupant", "Prim", "choose_canonical_swap", "choose_semigrand_canonical_multiswap",
     "choose_semigrand_canonical_swap", "is_allowed_canonical_swap", "is_allowed_semigrand_canonical_swap",
@@ -49,6 +50,46 @@ __all__ = [
 ]
 
 _TOL = 1e-5
+
+
+class _Vector(list):
+    """The reference's bound ``std::vector`` types (python/src/monte_events.cpp): a list
+    with the vector's ``push_back``."""
+
+    def push_back(self, value) -> None:
+        self.append(value)
+
+
+class IntVector(_Vector):
+    """std::vector<int>."""
+
+
+class LongVector(_Vector):
+    """std::vector<Index>."""
+
+
+class AtomVector(_Vector):
+    """std::vector<Atom>."""
+
+
+class MolVector(_Vector):
+    """std::vector<Mol>."""
+
+
+class OccTransformVector(_Vector):
+    """std::vector<OccTransform>."""
+
+
+class AtomTrajVector(_Vector):
+    """std::vector<AtomTraj>."""
+
+
+class OccSwapCountMap(dict):
+    """std::map<OccSwap, int>: swap counts of a multi-swap."""
+
+
+class AtomInfoMap(dict):
+    """std::map<std::string, std::vector<AtomInfo>>."""
 
 
 # ---------------------------------------------------------------- structure

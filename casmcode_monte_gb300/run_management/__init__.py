@@ -28,7 +28,7 @@ import numpy as np
 
 from .. import MethodLog, RandomNumberEngine, RandomNumberGenerator, ValueMap
 from ..sampling import (SAMPLE_METHOD, SAMPLE_MODE, CompletionCheck, CompletionCheckParams, Sampler,
-                        SamplerComponent, default_component_names, get_n_samples, jsonSampler)
+                        SamplerComponent, SamplingParams, default_component_names, get_n_samples, jsonSampler)
 
 __all__ = ["SamplingParams", "sample_at", "stochastic_count_step", "stochastic_time_step", "stochastic_sample_at",
            "MonteCounter", "ResultsAnalysisFunction", "make_analysis", "Results", "SamplingFixtureParams",
@@ -36,28 +36,6 @@ __all__ = ["SamplingParams", "sample_at", "stochastic_count_step", "stochastic_t
 
 
 # ---- sampling schedule (SamplingParams.hh)
-
-class SamplingParams:
-    """What to sample and when (SamplingParams.hh:14-153)."""
-
-    def __init__(self, sampler_names=None, json_sampler_names=None, sample_mode: SAMPLE_MODE = SAMPLE_MODE.BY_PASS,
-                 sample_method: SAMPLE_METHOD = SAMPLE_METHOD.LINEAR, period: float = 1.0, begin: float = 1.0,
-                 base: float = 10.0 ** (1.0 / 10.0), shift: float = 10.0,
-                 custom_sample_at: Optional[Callable[[float], float]] = None, stochastic_sample_period: bool = False,
-                 do_sample_trajectory: bool = False, do_sample_time: bool = False):
-        self.sampler_names = list(sampler_names or [])
-        self.json_sampler_names = list(json_sampler_names or [])
-        self.sample_mode = sample_mode
-        self.sample_method = sample_method
-        self.period = float(period)
-        self.begin = float(begin)
-        self.base = float(base)
-        self.shift = float(shift)
-        self.custom_sample_at = custom_sample_at
-        self.stochastic_sample_period = bool(stochastic_sample_period)
-        self.do_sample_trajectory = bool(do_sample_trajectory)
-        self.do_sample_time = bool(do_sample_time)
-
 
 def sample_at(sample_index: int, s: SamplingParams) -> float:
     """Count or time of the sample_index-th sample (SamplingParams.hh:164-181)."""

@@ -40,6 +40,28 @@ class SAMPLE_METHOD(enum.Enum):
     CUSTOM = 2
 
 
+class SamplingParams:
+    """What to sample and when (sampling/SamplingParams.hh:14-153)."""
+
+    def __init__(self, sampler_names=None, json_sampler_names=None, sample_mode: SAMPLE_MODE = SAMPLE_MODE.BY_PASS,
+                 sample_method: SAMPLE_METHOD = SAMPLE_METHOD.LINEAR, period: float = 1.0, begin: float = 1.0,
+                 base: float = 10.0 ** (1.0 / 10.0), shift: float = 10.0,
+                 custom_sample_at: Optional[Callable[[float], float]] = None, stochastic_sample_period: bool = False,
+                 do_sample_trajectory: bool = False, do_sample_time: bool = False):
+        self.sampler_names = list(sampler_names or [])
+        self.json_sampler_names = list(json_sampler_names or [])
+        self.sample_mode = sample_mode
+        self.sample_method = sample_method
+        self.period = float(period)
+        self.begin = float(begin)
+        self.base = float(base)
+        self.shift = float(shift)
+        self.custom_sample_at = custom_sample_at
+        self.stochastic_sample_period = bool(stochastic_sample_period)
+        self.do_sample_trajectory = bool(do_sample_trajectory)
+        self.do_sample_time = bool(do_sample_time)
+
+
 def default_component_names(shape: list[int]) -> list[str]:
     """Sampler.hh:333-349: [] -> ["0"]; [n] -> ["0".."n-1"]; [m,n] -> column-major "i,j"."""
     if len(shape) == 0:
@@ -700,7 +722,7 @@ def converge(sampling_functions: dict, completion_check_params: CompletionCheckP
 
 
 __all__ = [
-    "SAMPLE_MODE", "SAMPLE_METHOD", "BasicStatistics", "BasicStatisticsCalculator", "CompletionCheck",
+    "SAMPLE_MODE", "SAMPLE_METHOD", "SamplingParams", "BasicStatistics", "BasicStatisticsCalculator", "CompletionCheck",
     "CompletionCheckParams", "CompletionCheckResults", "ConvergenceCheckResults", "ConvergenceResultMap",
     "CutoffCheckParams", "EquilibrationCheckResults", "EquilibrationResultMap", "IndividualConvergenceResult",
     "IndividualEquilibrationResult", "RequestedPrecision", "RequestedPrecisionMap", "Sampler",
