@@ -10,6 +10,7 @@ Semantics follow:
 * convergence                    include/casm/monte/checks/ConvergenceCheck.hh:74-184
 * ``BasicStatisticsCalculator``  src/casm/monte/BasicStatistics.cc:24-188
 * ``converge``                   python/libcasm/monte/sampling/_requested_precision_constructor.py
+* selected-event data and histograms: ``_selected_event`` (SelectedEventFunctions.hh/.cc)
 
 The per-component numerics (equilibration scan, autocorrelation, precision of the
 mean) run natively in libmontegpu (the same functions the device convergence kernel
@@ -716,6 +717,10 @@ class RequestedPrecisionConstructor:
         return self
 
 
+from . import _selected_event  # noqa: E402
+from ._selected_event import *  # noqa: E402,F401,F403
+
+
 def converge(sampling_functions: dict, completion_check_params: CompletionCheckParams
              ) -> RequestedPrecisionConstructor:
     return RequestedPrecisionConstructor(sampling_functions, completion_check_params)
@@ -732,4 +737,4 @@ __all__ = [
     "get_n_samples", "jsonSampler", "jsonSamplerMap", "jsonStateSamplingFunction",
     "jsonStateSamplingFunctionMap", "matrix_as_vector", "scalar_as_vector", "RequestedPrecisionConstructor",
     "converge",
-]
+] + _selected_event.__all__
