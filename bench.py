@@ -7,8 +7,10 @@ occupation basis; ECI N(0, 0.03 eV)/size^2 from seed 1), 64^3 primitive-cell sup
 temperatures linspace(300, 2000, 8) K, mu = 0.  The 8 chains are independent; with
 N GPUs every rank runs its own 8 chains (weak scaling, no collective).
 
-value   device throughput of the sweep kernel: attempts / sum of CUDA-event kernel times,
-        inputs resident in HBM, L2 flushed between launches (outside the events).
+value   device throughput of the sweep: attempts / sum over runs of the CUDA-event time of
+        each run (first launch to last; a rotated run is several launches on the batch's
+        streams, seven chains on 16-CTA clusters and one in turn on a 12-CTA cluster), inputs
+        resident in HBM, L2 flushed between runs (outside the events).
 e2e     the same job through the public C-ABI with host buffers: create the batch
         (H2D of occupations and parameters), run the passes returning per-pass samples to
         the host (D2H), read the final occupations (D2H); wall clock.
@@ -239,7 +241,7 @@ def run_gpu(args) -> None:
         torch.cuda.synchronize()
         batch.run(n, want_output=False)
         kernel_ms += batch.last_kernel_ms()
-        launches += 1
+        launches += batch.last_launches()
         left -= n
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -286,6 +288,7 @@ def run_gpu(args) -> None:
         with open(tp) as f:
             tj = json.load(f)
         traffic = tj["dram_bytes_per_pass"] * ppl
+    rotation = batch.rotation()
     if rank == 0:
         cpu = cpu_baseline_sample(args.cpu_seconds) if args.cpu_seconds > 0 else None
         line = {
@@ -295,7 +298,7 @@ def run_gpu(args) -> None:
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "supercell": [L, L, L], "chains_per_gpu": N_CHAINS,
                        "temperatures_K": T.tolist(), "passes_per_launch": ppl,
-                       "ctas_per_chain": batch.ctas_per_chain, "colors": batch.n_colors,
+                       "ctas_per_chain": batch.ctas_per_chain, "rotation": rotation, "colors": batch.n_colors,
                        "threads_per_cta": batch.threads, "l2": "flushed between launches (256 MB write)",
                        "attempts_per_step": attempts_per_step},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -62,6 +62,10 @@ SIGNATURES = {
     "mg_ce_batch_autotune": (C.c_int, [vp, C.c_int, c_int_p, c_int_p, C.POINTER(C.c_float)]),
     "mg_ce_batch_run": (C.c_int, [vp, C.c_int, c_ll_p]),
     "mg_ce_batch_last_kernel_ms": (C.c_int, [vp, c_float_p]),
+    "mg_ce_batch_rotation": (C.c_int, [vp, c_int_p, c_double_p]),
+    "mg_ce_batch_set_rotation": (C.c_int, [vp, C.c_int]),
+    "mg_ce_batch_last_launches": (C.c_int, [vp, c_int_p]),
+    "mg_ce_batch_rotation_timeline": (C.c_int, [vp, c_float_p]),
     "mg_ce_batch_get_occ": (C.c_int, [vp, c_int8_p]),
     "mg_ce_batch_set_occ": (C.c_int, [vp, c_int8_p]),
     "mg_ce_batch_corr": (C.c_int, [vp, c_ll_p]),

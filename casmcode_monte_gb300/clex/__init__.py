@@ -199,6 +199,31 @@ class ChainBatch:
         _lib.check(_lib.lib().mg_ce_batch_last_kernel_ms(self._h, C.byref(ms)))
         return float(ms.value)
 
+    def last_launches(self) -> int:
+        """Sweep kernels launched by the last run (1 unless it rotated)."""
+        n = C.c_int()
+        _lib.check(_lib.lib().mg_ce_batch_last_launches(self._h, C.byref(n)))
+        return int(n.value)
+
+    def rotation_timeline(self) -> np.ndarray:
+        """After a rotated run: [n_chains, 6] ms from the run's start to each chain's first
+        fast sweep start/end, slow-slot sweep start/end and second fast sweep start/end."""
+        ms = np.zeros((self.n_chains, 6), dtype=np.float32)
+        _lib.check(_lib.lib().mg_ce_batch_rotation_timeline(self._h, _lib.ptr(ms, C.c_float)))
+        return ms
+
+    def rotation(self) -> dict:
+        """Rotation over two cluster sizes: {"ctas_fast": 0} when the batch does not rotate,
+        else the fast clusters' CTA count and the measured time ratio per pass."""
+        S, r = C.c_int(), C.c_double()
+        _lib.check(_lib.lib().mg_ce_batch_rotation(self._h, C.byref(S), C.byref(r)))
+        return {"ctas_fast": S.value, "ratio": float(r.value)}
+
+    def set_rotation(self, allowed: bool) -> None:
+        """Allow (re-plan) or forbid rotation over two cluster sizes; trajectories are the
+        same either way."""
+        _lib.check(_lib.lib().mg_ce_batch_set_rotation(self._h, 1 if allowed else 0))
+
     def occupation(self) -> np.ndarray:
         occ = np.zeros((self.n_chains, self.n_sites), dtype=np.int8)
         _lib.check(_lib.lib().mg_ce_batch_get_occ(self._h, _lib.ptr(occ, C.c_int8)))

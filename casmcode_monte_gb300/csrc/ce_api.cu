@@ -47,6 +47,7 @@ struct mg_ce_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
+  int last_launches = 0;  // sweep kernels launched by the last run
   int8_t* docc = nullptr;
   mg::CeChainParams* dcp = nullptr;
   std::vector<mg::CeChainParams> hcp;
@@ -55,6 +56,26 @@ struct mg_ce_batch {
   uint32_t* dsite = nullptr;
   long long* dout = nullptr;
   size_t out_cap = 0;
+  // Rotation over two cluster sizes (warp-specialised layout with the CTA count chosen by
+  // occupancy).  When n_chains - 1 clusters of S_fast > S CTAs fit on the GPU at once but
+  // n_chains do not, the chains take turns on one cluster of S CTAs (the slow slot) while
+  // the others sweep on clusters of S_fast CTAs, each chain with the call's passes (see
+  // rotation_plan).
+  int S_fast = 0;  // 0: no rotation
+  bool rotation_allowed = true;
+  int* dcstart_f = nullptr;
+  uint32_t* dentries_f = nullptr;
+  uint32_t* dsite_f = nullptr;
+  int max_words = 0, max_words_f = 0;
+  double ratio = 1.0;  // time per pass on S_fast CTAs over that on S CTAs (re-measured by rotated calls)
+  std::vector<cudaStream_t> stream_fast;  // n_chains - 1 fast lanes, high priority (the batch's
+                                          // stream is the slow lane)
+  std::vector<cudaEvent_t> rev;            // six per chain (launch_rotated) and a join
+};
+
+// Pass counts of one rotated call (rotation_plan)
+struct RotationPlan {
+  std::vector<int> a, g, b;  // chain c: passes on a fast cluster, in the slow slot, fast again
 };
 
 namespace {
@@ -188,10 +209,226 @@ void free_batch(mg_ce_batch* b) {
   cudaFree(b->dentries);
   cudaFree(b->dsite);
   cudaFree(b->dout);
+  cudaFree(b->dcstart_f);
+  cudaFree(b->dentries_f);
+  cudaFree(b->dsite_f);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
+  for (cudaEvent_t e : b->rev) cudaEventDestroy(e);
   if (b->stream) cudaStreamDestroy(b->stream);
+  for (cudaStream_t s : b->stream_fast) cudaStreamDestroy(s);
   delete b;
+}
+
+// Fixed part of a colour phase of the warp-specialised kernel (cluster barrier, loop,
+// staging), in words of work per CTA: a phase at S CTAs per chain takes time proportional
+// to (most words of one CTA and colour + this).  Fitted on GB300 to 100-pass launches of
+// FCC 64^3 at 12 CTAs per chain (342 words, 3.04 ms) and 16 (256 words, 2.62 ms).
+constexpr double kWsPhaseFixedWords = 288.0;
+
+// Rotation plan of a warp-specialised batch whose CTA count was chosen by occupancy (the
+// fields after out_cap in mg_ce_batch): S_fast is the largest CTA count above S at which
+// n_chains - 1 clusters fit at once, kept when the modelled throughput gain,
+// ((n_chains - 1) / ratio + 1) / n_chains, is at least 3%.  The slow chain's S-CTA cluster
+// runs beside them: on GB300 seven 16-CTA clusters leave a group of 12 SMs that holds one
+// 12-CTA cluster (measured: both launches keep their own speed when run together).
+int setup_rotation(mg_ce_batch* b) {
+  cudaFree(b->dcstart_f);
+  cudaFree(b->dentries_f);
+  cudaFree(b->dsite_f);
+  b->dcstart_f = nullptr;
+  b->dentries_f = nullptr;
+  b->dsite_f = nullptr;
+  b->S_fast = 0;
+  const int C = b->n_chains;
+  if (b->layout != 3 || b->ctas_requested != 0 || !b->rotation_allowed || C < 2 || C - 1 > mg::CE_MAX_MAP)
+    return MG_OK;
+  const mg_ce_model* m = b->model;
+  int dev = 0, max_smem = 0;
+  MG_CUDA_TRY(cudaGetDevice(&dev));
+  MG_CUDA_TRY(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  for (int s = 16; s > b->S; --s) {
+    if (!slabs_ok(3, b->L1, b->L2, s)) continue;
+    const size_t smem = ws_smem(b->L0, b->L1, b->L2, s);
+    if (smem > (size_t)max_smem - 1024) continue;
+    int n_active = 0;
+    const int rc = max_active_chains(m->kind, s, smem, &n_active, 3);
+    if (rc != MG_OK) return rc;
+    if (n_active < C - 1) continue;
+    const auto lists = shape_lists(m->kind, b->L0, b->L1, b->L2, s, 3, *b->col);
+    if (lists->max_words > mg::host::NW_WS) continue;
+    const double r = (lists->max_words + kWsPhaseFixedWords) / (b->max_words + kWsPhaseFixedWords);
+    if (((C - 1) / r + 1.0) / C < 1.03) break;
+    MG_CUDA_TRY(cudaMalloc(&b->dcstart_f, sizeof(int) * lists->cstart.size()));
+    MG_CUDA_TRY(cudaMalloc(&b->dentries_f, sizeof(uint32_t) * lists->entries.size()));
+    MG_CUDA_TRY(cudaMalloc(&b->dsite_f, sizeof(uint32_t) * lists->site.size()));
+    MG_CUDA_TRY(cudaMemcpyAsync(b->dcstart_f, lists->cstart.data(), sizeof(int) * lists->cstart.size(),
+                                cudaMemcpyHostToDevice, b->stream));
+    MG_CUDA_TRY(cudaMemcpyAsync(b->dentries_f, lists->entries.data(), sizeof(uint32_t) * lists->entries.size(),
+                                cudaMemcpyHostToDevice, b->stream));
+    MG_CUDA_TRY(cudaMemcpyAsync(b->dsite_f, lists->site.data(), sizeof(uint32_t) * lists->site.size(),
+                                cudaMemcpyHostToDevice, b->stream));
+    MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    int least = 0, greatest = 0;
+    MG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    while (b->stream_fast.size() < (size_t)C - 1) {
+      cudaStream_t st = nullptr;
+      MG_CUDA_TRY(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, greatest));
+      b->stream_fast.push_back(st);
+    }
+    while (b->rev.size() < 6 * (size_t)C + 1) {
+      cudaEvent_t e = nullptr;
+      MG_CUDA_TRY(cudaEventCreate(&e));
+      b->rev.push_back(e);
+    }
+    b->S_fast = s;
+    b->max_words_f = lists->max_words;
+    b->ratio = r;
+    break;
+  }
+  return MG_OK;
+}
+
+// Fixed cost of one launch of the warp-specialised kernel (prologue, epilogue, launch
+// latency) in passes of a chain on the slow cluster: about 23 us against 31 us per pass of
+// FCC 64^3 at 12 CTAs on GB300.
+constexpr double kLaunchFixedPasses = 0.75;
+
+// Pass counts of a rotated call of P passes over C chains and C - 1 fast lanes.  Chain c
+// sweeps a_c passes on a fast cluster (lane c; a_0 = 0), then g_c passes in the slow slot
+// (chains in order), then b_c passes on a fast cluster again (lane c + 1, after that lane's
+// first sweep); the last chain ends in the slow slot (g_{C-1} = P - a_{C-1}).  With r the
+// time per pass on a fast cluster over that on the slow one, a_c = round(c g / r) brings
+// chain c to the slot as chain c - 1 leaves it; g (every chain but the last) is the value
+// whose simulated schedule, with a fixed cost per launch, ends first.  False when the call
+// is too short to rotate (it then runs unrotated).
+bool rotation_plan(const mg_ce_batch* b, int P, RotationPlan* plan) {
+  const int C = b->n_chains;
+  if (b->S_fast <= 0 || P < 2 * C) return false;
+  const double r = b->ratio, phi = kLaunchFixedPasses;
+  double best = 1e300;
+  for (int g = 1; g <= P; ++g) {
+    std::vector<int> a(C), gg(C), bb(C);
+    bool ok = true;
+    for (int c = 0; c < C && ok; ++c) {
+      a[c] = (int)std::lround(c * (double)g / r);
+      gg[c] = c < C - 1 ? g : P - a[c];
+      bb[c] = P - a[c] - gg[c];
+      ok = a[c] >= 0 && gg[c] >= 1 && bb[c] >= 0;
+    }
+    if (!ok) continue;
+    // simulated schedule in units of a slow-slot pass
+    std::vector<double> f1(C, 0.0);
+    for (int c = 1; c < C; ++c) f1[c] = a[c] > 0 ? a[c] * r + phi : 0.0;
+    double slot = 0.0, end = 0.0;
+    for (int c = 0; c < C; ++c) {
+      slot = std::max(slot, f1[c]) + gg[c] + phi;
+      if (c < C - 1) {
+        const double start2 = std::max(slot, f1[c + 1]);
+        end = std::max(end, start2 + (bb[c] > 0 ? bb[c] * r + phi : 0.0));
+      }
+    }
+    end = std::max(end, slot);
+    if (end < best) {
+      best = end;
+      plan->a = a;
+      plan->g = gg;
+      plan->b = bb;
+    }
+  }
+  return best < 1e299;
+}
+
+// One chain's sweep of n passes from pass offset `off` of this call, on a cluster of S CTAs
+// with the given lists.
+int launch_one_chain(mg_ce_batch* b, int chain, int off, int n, int S, const int* cstart, const uint32_t* entries,
+                     const uint32_t* site, cudaStream_t st) {
+  SweepLaunch L{b->L0, b->L1, b->L2, S, b->n_colors, b->n_chains, b->precision, cstart, entries, site, b->dcp,
+                b->docc, b->pass, n, b->dout, st};
+  L.n_map = 1;
+  L.map_chain = &chain;
+  L.map_pass = &off;
+  return launch_sweep_ws(b->model, L, b->pipe);
+}
+
+// Queue a rotated call (after the output was cleared on b->stream).  Streams: the batch's
+// own stream is the slow lane (chains in order); fast lane c (high priority) runs chain c's
+// first sweep, then chain c - 1's second sweep.  Every stream receives its commands in the
+// planned time order, so that a wait at the head of a hardware queue shared with another
+// stream delays only work planned for later; when a fast and a slow sweep become ready
+// together the fast cluster, which fits only in a full GPC, is placed first.  Events per
+// chain: first fast sweep start/end, slow sweep start/end, second fast sweep start/end.
+int launch_rotated(mg_ce_batch* b, const RotationPlan& p) {
+  const int C = b->n_chains;
+  cudaEvent_t join = b->rev[6 * (size_t)C];
+  auto E = [&](int c, int k) { return b->rev[6 * (size_t)c + k]; };
+  auto lane = [&](int c) { return b->stream_fast[c - 1]; };
+  MG_CUDA_TRY(cudaEventRecord(join, b->stream));
+  for (int c = 1; c < C; ++c) {
+    MG_CUDA_TRY(cudaStreamWaitEvent(lane(c), join, 0));
+    MG_CUDA_TRY(cudaEventRecord(E(c, 0), lane(c)));
+    if (p.a[c] > 0) {
+      const int rc = launch_one_chain(b, c, 0, p.a[c], b->S_fast, b->dcstart_f, b->dentries_f, b->dsite_f, lane(c));
+      if (rc != MG_OK) return rc;
+    }
+    MG_CUDA_TRY(cudaEventRecord(E(c, 1), lane(c)));
+  }
+  MG_CUDA_TRY(cudaEventRecord(E(0, 0), b->stream));
+  MG_CUDA_TRY(cudaEventRecord(E(0, 1), b->stream));
+  for (int c = 0; c < C; ++c) {
+    if (c > 0) {
+      // chain c - 1's second sweep on lane c, after chain c's first sweep there
+      MG_CUDA_TRY(cudaStreamWaitEvent(lane(c), E(c - 1, 3), 0));
+      MG_CUDA_TRY(cudaEventRecord(E(c - 1, 4), lane(c)));
+      if (p.b[c - 1] > 0) {
+        const int rc = launch_one_chain(b, c - 1, p.a[c - 1] + p.g[c - 1], p.b[c - 1], b->S_fast, b->dcstart_f,
+                                        b->dentries_f, b->dsite_f, lane(c));
+        if (rc != MG_OK) return rc;
+      }
+      MG_CUDA_TRY(cudaEventRecord(E(c - 1, 5), lane(c)));
+      MG_CUDA_TRY(cudaStreamWaitEvent(b->stream, E(c, 1), 0));
+    }
+    MG_CUDA_TRY(cudaEventRecord(E(c, 2), b->stream));
+    const int rc = launch_one_chain(b, c, p.a[c], p.g[c], b->S, b->dcstart, b->dentries, b->dsite, b->stream);
+    if (rc != MG_OK) return rc;
+    MG_CUDA_TRY(cudaEventRecord(E(c, 3), b->stream));
+  }
+  MG_CUDA_TRY(cudaEventRecord(E(C - 1, 4), b->stream));
+  MG_CUDA_TRY(cudaEventRecord(E(C - 1, 5), b->stream));
+  for (int c = 0; c < C - 1; ++c) MG_CUDA_TRY(cudaStreamWaitEvent(b->stream, E(c, 5), 0));
+  return MG_OK;
+}
+
+// After a rotated call has completed: the time ratio per pass of the two cluster sizes, from
+// the first fast sweeps (they start together, before any chain waits for the slow slot)
+// and the slow sweeps.  Rotation stops for the batch when it gains nothing (ratio above 1)
+// or when the slow cluster evidently did not run beside the fast ones (ratio below 0.6; the
+// occupancy model gives 0.86 for FCC 64^3 on GB300).
+constexpr int kMinRatioPasses = 8;
+void update_ratio(mg_ce_batch* b, const RotationPlan& p) {
+  const int C = b->n_chains;
+  double tf = 0.0, ts = 0.0;
+  long nf = 0, ns = 0;
+  for (int c = 0; c < C; ++c) {
+    const cudaEvent_t* e = &b->rev[6 * (size_t)c];
+    float ms = 0.f;
+    // launches of a few passes are dominated by their fixed start-up cost: not counted
+    if (c > 0 && p.a[c] >= kMinRatioPasses && cudaEventElapsedTime(&ms, e[0], e[1]) == cudaSuccess) {
+      tf += ms;
+      nf += p.a[c];
+    }
+    if (p.g[c] >= kMinRatioPasses && cudaEventElapsedTime(&ms, e[2], e[3]) == cudaSuccess) {
+      ts += ms;
+      ns += p.g[c];
+    }
+  }
+  if (nf > 0 && ns > 0 && tf > 0.0 && ts > 0.0) {
+    const double r = (tf / nf) / (ts / ns);
+    if (r > 1.0 || r < 0.6)
+      b->S_fast = 0;
+    else
+      b->ratio = r;
+  }
 }
 
 // CTA count, shared-memory size and site (or word) lists of the batch's layout, uploaded
@@ -235,7 +472,8 @@ int setup_layout(mg_ce_batch* b, int layout) {
   b->PZ = (b->L2 + S - 1) / S + 2 * mg::CE_HALO;
   b->threads = layout == 3 ? 2 * mg::host::NW_WS
                            : (layout >= 1 ? mg::host::NT_QUAD : (m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY));
-  return MG_OK;
+  b->max_words = lists->max_words;
+  return setup_rotation(b);
 }
 
 }  // namespace
@@ -527,7 +765,11 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   SweepLaunch L{b->L0, b->L1, b->L2, b->S, b->n_colors, b->n_chains, b->precision, b->dcstart, b->dentries,
                 b->dsite, b->dcp, b->docc, b->pass, n_passes, b->dout, b->stream};
   int rc;
-  if (b->layout == 3)
+  RotationPlan plan;
+  const bool rotated = b->layout == 3 && rotation_plan(b, n_passes, &plan);
+  if (rotated)
+    rc = launch_rotated(b, plan);
+  else if (b->layout == 3)
     rc = launch_sweep_ws(b->model, L, b->pipe);
   else if (b->layout >= 1)
     rc = launch_sweep_quad(b->model, L, b->layout == 2 ? b->pipe : -1);
@@ -538,8 +780,55 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, b->dout, sizeof(long long) * need, cudaMemcpyDeviceToHost, b->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
   MG_CUDA_TRY(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+  b->last_launches = 1;
+  if (rotated) {
+    b->last_launches = b->n_chains;
+    for (int c = 0; c < b->n_chains; ++c) b->last_launches += (c > 0 && plan.a[c] > 0) + (plan.b[c] > 0);
+    update_ratio(b, plan);
+  }
   b->pass += n_passes;
   return MG_OK;
+}
+
+int mg_ce_batch_rotation(const mg_ce_batch* b, int* ctas_fast, double* ratio) {
+  if (!b) {
+    set_error("Error in mg_ce_batch_rotation: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  if (ctas_fast) *ctas_fast = b->S_fast;
+  if (ratio) *ratio = b->S_fast > 0 ? b->ratio : 0.0;
+  return MG_OK;
+}
+
+int mg_ce_batch_rotation_timeline(const mg_ce_batch* b, float* ms) {
+  if (!b || !ms) {
+    set_error("Error in mg_ce_batch_rotation_timeline: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  if (b->last_launches <= 1 || b->rev.size() < 6 * (size_t)b->n_chains + 1) {
+    set_error("Error in mg_ce_batch_rotation_timeline: the last run did not rotate");
+    return MG_ERR_INVALID;
+  }
+  for (int i = 0; i < 6 * b->n_chains; ++i) MG_CUDA_TRY(cudaEventElapsedTime(&ms[i], b->ev0, b->rev[i]));
+  return MG_OK;
+}
+
+int mg_ce_batch_last_launches(const mg_ce_batch* b, int* launches) {
+  if (!b || !launches) {
+    set_error("Error in mg_ce_batch_last_launches: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  *launches = b->last_launches;
+  return MG_OK;
+}
+
+int mg_ce_batch_set_rotation(mg_ce_batch* b, int allowed) {
+  if (!b) {
+    set_error("Error in mg_ce_batch_set_rotation: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  b->rotation_allowed = allowed != 0;
+  return setup_rotation(b);
 }
 
 int mg_ce_batch_last_kernel_ms(const mg_ce_batch* b, float* ms) {

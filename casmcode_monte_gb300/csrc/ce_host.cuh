@@ -362,10 +362,20 @@ inline bool row_slabs_ok(int L1, int L2, int S, int planes) {
   return true;
 }
 // slab kind of the word layout: balanced rows where valid, else whole planes, else -1
+// (memoised: the check walks every periodic image and launches ask for it each time)
 inline int word_slab_kind(int L1, int L2, int S) {
-  if (row_slabs_ok(L1, L2, S, 0)) return 0;
-  if (row_slabs_ok(L1, L2, S, 1)) return 1;
-  return -1;
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int>, int> memo;
+  const auto key = std::make_tuple(L1, L2, S);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    const auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+  }
+  const int kind = row_slabs_ok(L1, L2, S, 0) ? 0 : (row_slabs_ok(L1, L2, S, 1) ? 1 : -1);
+  std::lock_guard<std::mutex> lk(mu);
+  memo[key] = kind;
+  return kind;
 }
 inline size_t quad_smem(int L0, int L1, int L2, int S) {
   const int kind = word_slab_kind(L1, L2, S);
@@ -506,9 +516,26 @@ inline void make_chain_params(const mg_ce_model* m, int n_chains, const double* 
   }
 }
 
+// Raise a kernel's dynamic shared-memory limit to the most the device allows it (the
+// opt-in maximum per CTA less the kernel's static shared memory)
+template <class Kern>
+int raise_smem_limit(Kern kern) {
+  int dev = 0, optin = 0;
+  MG_CUDA_TRY(cudaGetDevice(&dev));
+  MG_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  MG_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
+  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  return MG_OK;
+}
+
 template <class Kern>
 int max_active_clusters_query(Kern kern, int NT, int S, size_t smem, int* out) {
-  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // the limit is raised to the device maximum, never lowered: the occupancy answer depends
+  // only on the launch's own shared memory, and a launcher that set the limit once
+  // (launch_sweep_ws) keeps a valid limit
+  const int rc0 = raise_smem_limit(kern);
+  if (rc0 != MG_OK) return rc0;
   if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   if (S == 1) {
     int nb = 0, dev = 0, sms = 0;
@@ -628,6 +655,12 @@ struct SweepLaunch {
   int n_passes;
   long long* out;
   cudaStream_t stream;
+  // warp-specialised launches only: launch slot i sweeps chain map_chain[i] from pass
+  // pass0 + map_pass[i] (n_map slots, n_map <= CE_MAX_MAP); n_chains stays the batch's
+  // chain count (the output stride).  n_map == 0: slot i is chain i, n_chains slots.
+  int n_map = 0;
+  const int* map_chain = nullptr;
+  const int* map_pass = nullptr;
 };
 
 template <class B, int NT>
@@ -685,6 +718,8 @@ inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L, int pip
   A.g.Q = L.L0 / 4;
   A.g.S = L.S;
   A.g.planes = word_slab_kind(L.L1, L.L2, L.S);
+  A.g.window_planes = row_window_planes(L.L1, L.L2, L.S, B::HALO, A.g.planes);
+  A.g.max_rows = row_slab_max_rows(L.L1, L.L2, L.S, A.g.planes);
   A.g.RS = quad_row_stride(L.L0 / 4);
   A.g.RY = L.L1 + 2 * CE_HALO;
   A.g.n_colors = L.n_colors;
@@ -699,6 +734,7 @@ inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L, int pip
   A.n_chains = L.n_chains;
   A.precision = L.precision;
   A.out = L.out;
+  A.n_map = 0;
   const size_t smem = quad_smem(L.L0, L.L1, L.L2, L.S);
   static_assert(fcc_binary::NPIPE == 2, "one kernel instance per pipeline colouring");
   auto kern = pipe == 0 ? ce_sweep_quad_kernel<B, NT_QUAD, 0>
@@ -734,6 +770,8 @@ inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe)
   A.g.Q = L.L0 / 4;
   A.g.S = L.S;
   A.g.planes = word_slab_kind(L.L1, L.L2, L.S);
+  A.g.window_planes = row_window_planes(L.L1, L.L2, L.S, B::HALO, A.g.planes);
+  A.g.max_rows = row_slab_max_rows(L.L1, L.L2, L.S, A.g.planes);
   A.g.RS = quad_row_stride(L.L0 / 4);
   A.g.RY = L.L1 + 2 * CE_HALO;
   A.g.n_colors = L.n_colors;
@@ -748,18 +786,48 @@ inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe)
   A.n_chains = L.n_chains;
   A.precision = L.precision;
   A.out = L.out;
+  if (L.n_map < 0 || L.n_map > CE_MAX_MAP || (L.n_map > 0 && (!L.map_chain || !L.map_pass))) {
+    set_error("Error in ce sweep: invalid chain map");
+    return MG_ERR_INVALID;
+  }
+  for (int i = 0; i < L.n_map; ++i)
+    if (L.map_chain[i] < 0 || L.map_chain[i] >= L.n_chains || L.map_pass[i] < 0) {
+      set_error("Error in ce sweep: invalid chain map");
+      return MG_ERR_INVALID;
+    }
+  A.n_map = L.n_map;
+  for (int i = 0; i < CE_MAX_MAP; ++i) {
+    A.map_chain[i] = i < L.n_map ? L.map_chain[i] : 0;
+    A.map_pass[i] = i < L.n_map ? L.map_pass[i] : 0;
+  }
+  const int n_slots = L.n_map > 0 ? L.n_map : L.n_chains;
   const size_t smem = ws_smem(L.L0, L.L1, L.L2, L.S, L.n_colors);
   static_assert(fcc_binary::NPIPE == 2, "one kernel instance per pipeline colouring");
   auto kern = pipe == 0 ? ce_sweep_ws_kernel<B, NW_WS, 0> : ce_sweep_ws_kernel<B, NW_WS, 1>;
-  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  {
+    // attributes set once per (device, kernel): the device's maximum shared memory (which
+    // max_active_clusters_query also sets, never less) and non-portable cluster sizes; a
+    // rotated run launches this kernel many times and each call costs host time
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, bool> ready;
+    int dev = 0;
+    MG_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    bool& done = ready[std::make_pair(dev, (const void*)kern)];
+    if (!done) {
+      const int rc0 = raise_smem_limit(kern);
+      if (rc0 != MG_OK) return rc0;
+      MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      done = true;
+    }
+  }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);
+  cfg.gridDim = dim3((unsigned)(n_slots * L.S), 1, 1);
   cfg.blockDim = dim3(2 * NW_WS, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = L.stream;
   cudaLaunchAttribute attr[1];
   if (L.S > 1) {
-    if (L.S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)L.S;
     attr[0].val.clusterDim.y = 1;

@@ -41,6 +41,7 @@ namespace mg {
 namespace cg = cooperative_groups;
 
 constexpr int CE_MAX_SPECIES = 3;
+constexpr int CE_MAX_MAP = 16;  // chains of one mapped launch of the warp-specialised kernel
 
 struct CeChainParams {
   double beta;
@@ -518,7 +519,9 @@ struct RowSlab {
 };
 __host__ __device__ __forceinline__ int slab_row(int L1, int L2, int S, int r, int planes) {
   if (planes) return L1 * (r * (L2 / S) + (r < L2 % S ? r : L2 % S));
-  return (int)(((long long)r * L1 * L2) / S);
+  const long long num = (long long)r * L1 * L2;
+  if (num <= 0x7fffffffll) return (int)num / S;  // 32-bit division where the product fits
+  return (int)(num / S);
 }
 __host__ __device__ __forceinline__ RowSlab row_slab(int L1, int L2, int S, int r, int planes) {
   RowSlab s;
@@ -550,12 +553,77 @@ __host__ __device__ __forceinline__ int row_slab_max_rows(int L1, int L2, int S,
   return m;
 }
 
+// 4 x 4 byte transpose: byte t of out[m] = byte m of in[t] (its own inverse)
+__device__ __forceinline__ void transpose4x4(const uint32_t in[4], uint32_t out[4]) {
+  const uint32_t a = __byte_perm(in[0], in[1], 0x5140), b = __byte_perm(in[2], in[3], 0x5140);
+  const uint32_t c = __byte_perm(in[0], in[1], 0x7362), d = __byte_perm(in[2], in[3], 0x7362);
+  out[0] = __byte_perm(a, b, 0x5410);
+  out[1] = __byte_perm(a, b, 0x7632);
+  out[2] = __byte_perm(c, d, 0x5410);
+  out[3] = __byte_perm(c, d, 0x7632);
+}
+
+// Window load when Q is a multiple of 4 and the chain's occupation is 4-byte aligned:
+// word group k4 of a row (words 4 k4 .. 4 k4 + 3) is the byte transpose of the row's 32-bit
+// words k4 + t Q/4, t = 0..3; the loads of U groups are issued before any is used.  Writes
+// the same shared words as the byte loop below, halo copies (rotated one byte) and the
+// zero padding word included.
+template <int HALO>
+__device__ __forceinline__ void load_word_window_x4(uint32_t* sq, const int8_t* gocc, int L1, int L2, int Q, int RS,
+                                                    int RY, int kb, int nk, int tid, int nthreads) {
+  constexpr int U = 4;
+  const int G = Q >> 2;
+  const int total = G * RY * (nk + 2 * HALO);
+  const uint32_t* g32 = reinterpret_cast<const uint32_t*>(gocc);
+  for (int base = tid; base < total; base += U * nthreads) {
+    uint32_t v[U][4];
+    int dst[U], k4s[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int idx = base + u * nthreads;
+      dst[u] = -1;
+      k4s[u] = 0;
+      if (idx < total) {
+        const int k4 = idx % G, pr = idx / G;
+        const int jp = pr % RY, kp = pr / RY;
+        int j = jp - HALO, k = kb + kp - HALO;
+        j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+        k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+        const uint32_t* row = g32 + (long long)Q * (j + (long long)L1 * k);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) v[u][t] = __ldg(row + k4 + t * G);
+        dst[u] = pr * RS + HALO + 4 * k4;
+        k4s[u] = k4;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (dst[u] < 0) continue;
+      uint32_t w[4];
+      transpose4x4(v[u], w);
+      uint32_t* d = sq + dst[u];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        d[m] = w[m];
+        const int wi = 4 * k4s[u] + m;
+        if (wi < HALO) d[m + Q] = __funnelshift_r(w[m], w[m], 8);         // word Q + wi
+        if (wi >= Q - HALO) d[m - Q] = __funnelshift_l(w[m], w[m], 8);    // word wi - Q
+      }
+      if (k4s[u] == G - 1 && RS > Q + 2 * HALO) d[4 + HALO] = 0u;  // padding word (w = Q + HALO)
+    }
+  }
+}
+
 // Load the window of a row slab into shared memory: planes kb - HALO .. kb + nk - 1 +
 // HALO, each row with its periodic copies (words -HALO .. Q + HALO - 1 of a padded row of
 // RS; padding words beyond are zero and never read); word w holds sites w + tQ, t = 0..3.
 template <int HALO>
 __device__ __forceinline__ void load_word_window(uint32_t* sq, const int8_t* gocc, int L0, int L1, int L2, int Q,
                                                  int RS, int RY, int kb, int nk, int tid, int nthreads) {
+  if ((Q & 3) == 0 && HALO <= 4 && RS <= Q + 2 * HALO + 1 && (reinterpret_cast<uintptr_t>(gocc) & 3u) == 0) {
+    load_word_window_x4<HALO>(sq, gocc, L1, L2, Q, RS, RY, kb, nk, tid, nthreads);
+    return;
+  }
   const int RSY = RS * RY;
   for (int idx = tid; idx < RSY * (nk + 2 * HALO); idx += nthreads) {
     const int wp = idx % RS, jp = (idx / RS) % RY, kp = idx / RSY;
@@ -581,6 +649,23 @@ __device__ __forceinline__ void load_word_window(uint32_t* sq, const int8_t* goc
 template <int HALO>
 __device__ __forceinline__ void store_word_rows(const uint32_t* sq, int8_t* gocc, int L0, int L1, int Q, int RS,
                                                 int RY, const RowSlab& sl, int tid, int nthreads) {
+  if ((Q & 3) == 0 && (reinterpret_cast<uintptr_t>(gocc) & 3u) == 0) {
+    // word group k4 of a row back to the row's 32-bit words k4 + t Q/4 (the same transpose)
+    const int G = Q >> 2;
+    uint32_t* g32 = reinterpret_cast<uint32_t*>(gocc);
+    for (int idx = tid; idx < G * (sl.r1 - sl.r0); idx += nthreads) {
+      const int k4 = idx % G, R = sl.r0 + idx / G;
+      const int j = R % L1, k = R / L1;
+      const uint32_t* s = sq + (4 * k4 + HALO) + RS * ((j + HALO) + RY * (k - sl.kb + HALO));
+      const uint32_t w[4] = {s[0], s[1], s[2], s[3]};
+      uint32_t v[4];
+      transpose4x4(w, v);
+      uint32_t* row = g32 + (long long)Q * (j + (long long)L1 * k);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) row[k4 + t * G] = v[t];
+    }
+    return;
+  }
   for (int idx = tid; idx < Q * (sl.r1 - sl.r0); idx += nthreads) {
     const int w = idx % Q, R = sl.r0 + idx / Q;
     const int j = R % L1, k = R / L1;
@@ -600,6 +685,9 @@ struct QuadGeometry {
   const int* color_start;   // [S][n_colors + 1]
   const uint32_t* entries;  // padded word index | flags << 24
   const uint32_t* site_l;   // linear index of the word's byte-0 site
+  // computed once on the host: planes of the largest window (row_window_planes with the
+  // basis halo) and rows of the largest slab (row_slab_max_rows)
+  int window_planes, max_rows;
 };
 
 template <int NFEAT>
@@ -610,9 +698,16 @@ struct CeQuadArgs {
   int8_t* occ;
   long long pass0;
   int n_passes;
-  int n_chains;
+  int n_chains;  // chains of the batch: the output's chain stride
   int precision;
   long long* out;
+  // Chain map (warp-specialised kernel).  n_map == 0: the CTAs [i S, (i+1) S) sweep chain i
+  // from pass pass0.  n_map > 0: they sweep chain map_chain[i], which has already advanced
+  // map_pass[i] passes beyond pass0 in this call (its Philox passes and output rows start
+  // there), so a call's passes can be split over launches of different cluster sizes.
+  int n_map;
+  int map_chain[CE_MAX_MAP];
+  int map_pass[CE_MAX_MAP];
 };
 
 struct WordLoader {
@@ -1054,7 +1149,10 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
 
   const QuadGeometry& g = A.g;
   const int S = g.S;
-  const int chain = blockIdx.x / S;
+  const int slot_i = blockIdx.x / S;
+  const int chain = A.n_map > 0 ? A.map_chain[slot_i] : slot_i;
+  const long long pbase = A.n_map > 0 ? (long long)A.map_pass[slot_i] : 0ll;  // output row of pass 0
+  const long long pass0 = A.pass0 + pbase;
   int rank = 0;
   cg::cluster_group cluster = cg::this_cluster();
   if (S > 1) rank = (int)cluster.block_rank();
@@ -1073,10 +1171,10 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
   const int rprev = (rank + S - 1) % S;
   const long long N = (long long)L0 * L1 * L2;
   int8_t* gocc = A.occ + (size_t)chain * N;
-  const int lattice_words = RSY * row_window_planes(L1, L2, S, B::HALO, g.planes);
+  const int lattice_words = RSY * g.window_planes;
   uint32_t* stage = sq + ((lattice_words + 3) & ~3);  // [2][NFIELD][NW]
   // the CTA's site lists (entries, Philox counter words) and colour starts, copied once
-  const int max_words = Q * row_slab_max_rows(L1, L2, S, g.planes);
+  const int max_words = Q * g.max_rows;
   uint32_t* ents = stage + 2 * Stage::NFIELD * NW;
   uint32_t* sites = ents + max_words;
   int* cst = reinterpret_cast<int*>(sites + max_words);
@@ -1092,9 +1190,25 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
     const int* cg0 = g.color_start + rank * (g.n_colors + 1);
     const int base = cg0[0], n = cg0[g.n_colors] - base;
     for (int i = threadIdx.x; i <= g.n_colors; i += 2 * NW) cst[i] = cg0[i] - base;
-    for (int i = threadIdx.x; i < n; i += 2 * NW) {
-      ents[i] = __ldg(g.entries + base + i);
-      sites[i] = __ldg(g.site_l + base + i);
+    constexpr int UL = 4;  // loads of UL entries in flight per thread
+    for (int i0 = threadIdx.x; i0 < n; i0 += UL * 2 * NW) {
+      uint32_t e[UL], t[UL];
+#pragma unroll
+      for (int u = 0; u < UL; ++u) {
+        const int i = i0 + u * 2 * NW;
+        if (i < n) {
+          e[u] = __ldg(g.entries + base + i);
+          t[u] = __ldg(g.site_l + base + i);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UL; ++u) {
+        const int i = i0 + u * 2 * NW;
+        if (i < n) {
+          ents[i] = e[u];
+          sites[i] = t[u];
+        }
+      }
     }
   }
   const int* cstart = cst;
@@ -1138,13 +1252,13 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
   constexpr int SLOT = Stage::NFIELD * NW;
 
   barrier();  // slab loaded
-  if (!finisher) prepare(0, (uint32_t)A.pass0, stage);
+  if (!finisher) prepare(0, (uint32_t)pass0, stage);
   barrier();  // stage 0 ready
 
   int parity = 0;
 #pragma unroll 1
   for (int pass = 0; pass < A.n_passes; ++pass) {
-    const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
+    const uint32_t pass_g = (uint32_t)(pass0 + pass);
 #pragma unroll 1
     for (int c = 0; c < g.n_colors; ++c) {
       const bool last = (c + 1 == g.n_colors);
@@ -1183,7 +1297,7 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
         buf[threadIdx.x] = 0;
         if (v)
           atomicAdd(reinterpret_cast<unsigned long long*>(
-                        A.out + ((size_t)(pass - 1) * A.n_chains + chain) * NSLOT + threadIdx.x),
+                        A.out + ((size_t)(pbase + pass - 1) * A.n_chains + chain) * NSLOT + threadIdx.x),
                     (unsigned long long)(long long)v);
       }
     }
@@ -1202,7 +1316,8 @@ __global__ void __launch_bounds__(2 * NW, 1) ce_sweep_ws_kernel(const __grid_con
     int* buf = acc_sm[pl & 1];
     const int v = buf[threadIdx.x];
     if (v)
-      atomicAdd(reinterpret_cast<unsigned long long*>(A.out + ((size_t)pl * A.n_chains + chain) * NSLOT + threadIdx.x),
+      atomicAdd(reinterpret_cast<unsigned long long*>(A.out + ((size_t)(pbase + pl) * A.n_chains + chain) * NSLOT +
+                                                      threadIdx.x),
                 (unsigned long long)(long long)v);
   }
   store_word_rows<B::HALO>(sq, gocc, L0, L1, Q, RS, RY, sl, threadIdx.x, 2 * NW);

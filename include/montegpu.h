@@ -137,6 +137,25 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out);
 /* device time of the sweep kernel(s) of the last run, from CUDA events on the batch's
  * stream */
 int mg_ce_batch_last_kernel_ms(const mg_ce_batch* b, float* ms);
+/* Rotation over two cluster sizes (layout 3 with the CTA count chosen by occupancy; no
+ * counterpart in the reference, whose loop runs one chain on one host thread).  When
+ * n_chains - 1 chains fit on the GPU at once on clusters of ctas_fast > ctas_per_chain CTAs
+ * but n_chains do not, a run of at least 2 n_chains passes lets the chains take turns on one
+ * cluster of ctas_per_chain CTAs (the slow slot) while the others sweep on clusters of
+ * ctas_fast CTAs: chain c sweeps a_c passes fast, g passes in the slow slot (chains in
+ * order) and the rest fast, with a_c and g set from the measured time ratio so that the slow
+ * slot stays busy and every chain gets the run's passes.  Outputs and occupations are
+ * identical to unrotated runs.  ctas_fast receives 0 when the batch does not rotate; ratio
+ * the measured time per pass on ctas_fast CTAs over that on ctas_per_chain CTAs.
+ * set_rotation(b, 0) turns it off for the batch, set_rotation(b, 1) re-plans it.
+ * last_launches: sweep kernels launched by the last run (1 unless it rotated). */
+int mg_ce_batch_rotation(const mg_ce_batch* b, int* ctas_fast, double* ratio);
+int mg_ce_batch_set_rotation(mg_ce_batch* b, int allowed);
+int mg_ce_batch_last_launches(const mg_ce_batch* b, int* launches);
+/* After a rotated run: ms[n_chains][6] = milliseconds from the run's start to each chain's
+ * first fast sweep start and end, slow-slot sweep start and end, second fast sweep start and
+ * end (a sweep of no passes starts and ends together). */
+int mg_ce_batch_rotation_timeline(const mg_ce_batch* b, float* ms);
 int mg_ce_batch_get_occ(mg_ce_batch* b, int8_t* occ);
 int mg_ce_batch_set_occ(mg_ce_batch* b, const int8_t* occ);
 /* full recompute of the integer correlation sums [n_chains][n_classes] */
