@@ -66,6 +66,15 @@ SIGNATURES = {
     "mg_ce_batch_set_rotation": (C.c_int, [vp, C.c_int]),
     "mg_ce_batch_last_launches": (C.c_int, [vp, c_int_p]),
     "mg_ce_batch_rotation_timeline": (C.c_int, [vp, c_float_p]),
+    "mg_ce_canon_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p, c_uint64_p, c_uint32_p,
+                                     c_int8_p, C.c_int, vpp]),
+    "mg_ce_canon_info": (C.c_int, [vp, c_int_p, c_int_p, c_int_p, c_size_p]),
+    "mg_ce_canon_colors": (C.c_int, [vp, C.c_int, c_int32_p]),
+    "mg_ce_canon_run": (C.c_int, [vp, C.c_int, c_ll_p]),
+    "mg_ce_canon_last_kernel_ms": (C.c_int, [vp, c_float_p]),
+    "mg_ce_canon_get_occ": (C.c_int, [vp, c_int8_p]),
+    "mg_ce_canon_corr": (C.c_int, [vp, c_ll_p]),
+    "mg_ce_canon_destroy": (C.c_int, [vp]),
     "mg_ce_batch_get_occ": (C.c_int, [vp, c_int8_p]),
     "mg_ce_batch_set_occ": (C.c_int, [vp, c_int8_p]),
     "mg_ce_batch_corr": (C.c_int, [vp, c_ll_p]),

@@ -255,6 +255,92 @@ class ChainBatch:
         return out
 
 
+class CanonicalBatch:
+    """Chains of one L0 x L1 x L2 supercell swept at fixed composition on the GPU (handle to
+    mg_ce_canon): the canonical swap of the reference (events.propose_canonical_event with
+    Metropolis acceptance) made parallel by exchanging the occupants of matched same-colour
+    sites, passes alternating between two colourings whose classes connect every site.
+
+    occ: [n_chains, N] occupant indices; temperature [n_chains]; seeds [n_chains] (Philox
+    keys).  One CTA per chain: the supercell must fit in shared memory (up to 56^3).
+    """
+
+    def __init__(self, model: ClexModel, shape: Sequence[int], occ, temperature, seeds, chain_ids=None,
+                 precision: str = "fp64"):
+        self.model = model
+        self.shape = tuple(int(x) for x in shape)
+        L0, L1, L2 = self.shape
+        self.n_sites = L0 * L1 * L2
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int8).reshape(-1, self.n_sites))
+        self.n_chains = occ.shape[0]
+        T = np.ascontiguousarray(np.asarray(temperature, dtype=np.float64).reshape(self.n_chains))
+        seeds = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(self.n_chains))
+        ids = None
+        if chain_ids is not None:
+            ids = np.ascontiguousarray(np.asarray(chain_ids, dtype=np.uint32).reshape(self.n_chains))
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.temperature, self.seeds, self.precision = T, seeds, precision
+        h = C.c_void_p()
+        _lib.check(_lib.lib().mg_ce_canon_create(
+            model._h, L0, L1, L2, self.n_chains, _lib.ptr(T, C.c_double), _lib.ptr(seeds, C.c_uint64),
+            _lib.ptr(ids, C.c_uint32) if ids is not None else None, _lib.ptr(occ, C.c_int8),
+            0 if precision == "fp64" else 1, C.byref(h)))
+        self._h = h
+        na, nb, nt, sm = C.c_int(), C.c_int(), C.c_int(), C.c_size_t()
+        _lib.check(_lib.lib().mg_ce_canon_info(self._h, C.byref(na), C.byref(nb), C.byref(nt), C.byref(sm)))
+        self.n_colors = (na.value, nb.value)
+        self.threads, self.smem_bytes = nt.value, sm.value
+        self.pass_count = 0
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.mg_ce_canon_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def n_slots(self) -> int:
+        return self.model.n_classes + 2
+
+    def run(self, n_passes: int, want_output: bool = True) -> Optional[np.ndarray]:
+        """Advance every chain by n_passes; returns [n_passes, n_chains, n_classes+2] int64
+        (slot 0 accepted swaps, then the batch's layout)."""
+        if int(n_passes) < 0:
+            raise RuntimeError("Error in mg_ce_canon_run: invalid argument")
+        out = None
+        if want_output:
+            out = np.zeros((n_passes, self.n_chains, self.n_slots), dtype=np.int64)
+        _lib.check(_lib.lib().mg_ce_canon_run(self._h, int(n_passes),
+                                              _lib.ptr(out, C.c_longlong) if out is not None else None))
+        self.pass_count += n_passes
+        return out
+
+    def last_kernel_ms(self) -> float:
+        ms = C.c_float()
+        _lib.check(_lib.lib().mg_ce_canon_last_kernel_ms(self._h, C.byref(ms)))
+        return float(ms.value)
+
+    def occupation(self) -> np.ndarray:
+        occ = np.zeros((self.n_chains, self.n_sites), dtype=np.int8)
+        _lib.check(_lib.lib().mg_ce_canon_get_occ(self._h, _lib.ptr(occ, C.c_int8)))
+        return occ
+
+    def corr(self) -> np.ndarray:
+        out = np.zeros((self.n_chains, self.model.n_classes), dtype=np.int64)
+        _lib.check(_lib.lib().mg_ce_canon_corr(self._h, _lib.ptr(out, C.c_longlong)))
+        return out
+
+    def colors(self, which: int) -> np.ndarray:
+        """Colouring `which` (0: passes with even index, 1: odd), [N] int32."""
+        col = np.zeros(self.n_sites, dtype=np.int32)
+        _lib.check(_lib.lib().mg_ce_canon_colors(self._h, int(which), _lib.ptr(col, C.c_int32)))
+        return col
+
+
 class PoolFull(RuntimeError):
     """Admission refused: no free chain slot or not enough arena memory."""
 

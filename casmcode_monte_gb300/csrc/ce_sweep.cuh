@@ -247,8 +247,6 @@ struct SiteSweeper {
   // site and its copies and add the changes of the integer correlation sums to acc.
   __device__ __forceinline__ void decide(uint32_t ent, uint32_t x0, uint32_t x1, int o, const int (&F)[NF],
                                          int (&acc)[NSLOT]) const {
-    const int pidx = (int)(ent & 0xFFFFFFu);
-    const uint32_t flags = ent >> 24;
     int o2;
     if (NS == 2)
       o2 = 1 - o;
@@ -260,30 +258,37 @@ struct SiteSweeper {
     const MetropolisRule<B> rule{dmu32, dmu64, w, beta, beta_log2e, dtol, eps, precision};
     const bool accept = rule(o, o2, dpsi, [&](int k) { return F[k]; }, x0, acc);
     if (accept) {
-      const int8_t c2 = B::code_of_occ(o2);
-      const int oi = (flags & 1u) ? dI : ((flags & 2u) ? -dI : 0);
-      const int oj = (flags & 4u) ? dJ : ((flags & 8u) ? -dJ : 0);
-      s[pidx] = c2;
-      if (oi) s[pidx + oi] = c2;
-      if (oj) s[pidx + oj] = c2;
-      if (oi && oj) s[pidx + oi + oj] = c2;
-      if (flags & 16u) {
-        int8_t* r = s_prev + pidx + dKp;
-        r[0] = c2;
-        if (oi) r[oi] = c2;
-        if (oj) r[oj] = c2;
-        if (oi && oj) r[oi + oj] = c2;
-      }
-      if (flags & 32u) {
-        int8_t* r = s_next + pidx - dKn;
-        r[0] = c2;
-        if (oi) r[oi] = c2;
-        if (oj) r[oj] = c2;
-        if (oi && oj) r[oi + oj] = c2;
-      }
+      store(ent, B::code_of_occ(o2));
       acc[0] += 1;
 #pragma unroll
       for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += dpsi[B::feat_b(k)] * F[k];
+    }
+  }
+
+  // write code c2 at the entry's site and at its periodic copies (own padding and, through
+  // distributed shared memory, the halo planes of the neighbouring CTAs)
+  __device__ __forceinline__ void store(uint32_t ent, int8_t c2) const {
+    const int pidx = (int)(ent & 0xFFFFFFu);
+    const uint32_t flags = ent >> 24;
+    const int oi = (flags & 1u) ? dI : ((flags & 2u) ? -dI : 0);
+    const int oj = (flags & 4u) ? dJ : ((flags & 8u) ? -dJ : 0);
+    s[pidx] = c2;
+    if (oi) s[pidx + oi] = c2;
+    if (oj) s[pidx + oj] = c2;
+    if (oi && oj) s[pidx + oi + oj] = c2;
+    if (flags & 16u) {
+      int8_t* r = s_prev + pidx + dKp;
+      r[0] = c2;
+      if (oi) r[oi] = c2;
+      if (oj) r[oj] = c2;
+      if (oi && oj) r[oi + oj] = c2;
+    }
+    if (flags & 32u) {
+      int8_t* r = s_next + pidx - dKn;
+      r[0] = c2;
+      if (oi) r[oi] = c2;
+      if (oj) r[oj] = c2;
+      if (oi && oj) r[oi + oj] = c2;
     }
   }
 };

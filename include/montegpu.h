@@ -156,6 +156,33 @@ int mg_ce_batch_last_launches(const mg_ce_batch* b, int* launches);
  * first fast sweep start and end, slow-slot sweep start and end, second fast sweep start and
  * end (a sweep of no passes starts and ends together). */
 int mg_ce_batch_rotation_timeline(const mg_ce_batch* b, float* ms);
+
+/* ---- FCC cluster expansion: canonical (fixed-composition) sweep ----
+ * Replaces the canonical swap of include/casm/monte/events/OccEventProposal.hh:108-237
+ * (propose_canonical_event) accepted by methods/metropolis.hh:26-35 inside the loop of
+ * methods/occupation_metropolis.hh:114-150.  n_chains chains of an L0 x L1 x L2 supercell,
+ * one CTA per chain (the supercell with a 2-site border must fit in one CTA's shared
+ * memory: up to 56^3).  A pass proposes, colour by colour, a perfect matching of each colour
+ * class (positions k and (d - k) mod n, d random per phase) and exchanges the occupants of
+ * each pair by Metropolis; passes alternate between two colourings whose classes connect
+ * every site, so atoms reach any site.  Composition is conserved exactly.  Same occupant,
+ * temperature, seed, chain-id and precision conventions as mg_ce_batch_create; run's out has
+ * the batch's layout with slot 0 = accepted swaps. */
+typedef struct mg_ce_canon mg_ce_canon;
+int mg_ce_canon_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chains,
+                       const double* temperature, const uint64_t* seeds, const uint32_t* chain_ids,
+                       const int8_t* occ, int precision, mg_ce_canon** out);
+/* colours of the two colourings, threads per CTA, dynamic shared bytes */
+int mg_ce_canon_info(const mg_ce_canon* h, int* n_colors_a, int* n_colors_b, int* threads,
+                     size_t* smem_bytes);
+/* colouring `which` (0: passes with even index, 1: odd) as color[N] */
+int mg_ce_canon_colors(const mg_ce_canon* h, int which, int32_t* color);
+int mg_ce_canon_run(mg_ce_canon* h, int n_passes, long long* out);
+int mg_ce_canon_last_kernel_ms(const mg_ce_canon* h, float* ms);
+int mg_ce_canon_get_occ(mg_ce_canon* h, int8_t* occ);
+/* integer correlation sums [n_chains][n_classes] from a full recompute */
+int mg_ce_canon_corr(mg_ce_canon* h, long long* corr);
+int mg_ce_canon_destroy(mg_ce_canon* h);
 int mg_ce_batch_get_occ(mg_ce_batch* b, int8_t* occ);
 int mg_ce_batch_set_occ(mg_ce_batch* b, const int8_t* occ);
 /* full recompute of the integer correlation sums [n_chains][n_classes] */

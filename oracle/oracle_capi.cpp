@@ -424,4 +424,78 @@ long long orc_ce_sgc_samples(void* h, int* occ, double T, const double* mu, int 
   return nacc;
 }
 
+int orc_ce_canonical_sweep(void* h, int* occ, double T, unsigned long long seed, unsigned int chain,
+                           const int* color_a, int n_a, const int* color_b, int n_b, long pass0, long n_passes,
+                           long long* corr_out, long long* nacc_out) {
+  auto* S = static_cast<CESupercell*>(h);
+  std::vector<int> ca(color_a, color_a + S->n()), cb(color_b, color_b + S->n());
+  auto R = colored_canonical_sweep(*S, occ, T, seed, chain, ca, n_a, cb, n_b, pass0, n_passes);
+  const long nc = (long)S->classes.size();
+  for (long p = 0; p < n_passes; ++p) {
+    for (long c = 0; c < nc; ++c) corr_out[p * nc + c] = R.corr[p][c];
+    nacc_out[p] = R.n_accept[p];
+  }
+  return 0;
+}
+
+// The reference's canonical dynamics: N steps per pass, each the canonical event of
+// OccEventProposal.hh:108-237 (swap type (a, b), a < b, chosen with weight n_a n_b by
+// random_real; then an atom of each species by random_int over the occupant lists, as
+// OccLocation::choose_mol) accepted by metropolis.hh:26-35 with the exact formation-energy
+// change of the swap (the second site's change evaluated after the first is applied, so
+// pairs sharing a cluster are exact).  Per pass: formation energy per site (tracked by
+// accepted changes).  Returns the accepted count.
+long long orc_ce_canonical_samples(void* h, int* occ, double T, unsigned long long seed, long n_passes,
+                                   double* e_out) {
+  auto* S = static_cast<CESupercell*>(h);
+  const int ns = S->basis.n_species;
+  std::mt19937_64 e(seed);
+  RNG rng{&e};
+  const double beta = 1.0 / (KB * T);
+  const long N = S->n();
+  std::vector<std::vector<long>> loc(ns);
+  std::vector<long> mol_loc(N);
+  for (long l = 0; l < N; ++l) {
+    if (occ[l] < 0 || occ[l] >= ns) return -1;
+    mol_loc[l] = (long)loc[occ[l]].size();
+    loc[occ[l]].push_back(l);
+  }
+  std::vector<std::pair<int, int>> swaps;
+  for (int a = 0; a < ns; ++a)
+    for (int b = a + 1; b < ns; ++b) swaps.push_back({a, b});
+  std::vector<double> tsum(swaps.size() + 1);
+  long long nacc = 0;
+  double Ef = S->formation_per_supercell(occ);
+  for (long p = 0; p < n_passes; ++p) {
+    for (long t = 0; t < N; ++t) {
+      tsum[0] = 0.0;
+      for (size_t i = 0; i < swaps.size(); ++i)
+        tsum[i + 1] = tsum[i] + (double)loc[swaps[i].first].size() * (double)loc[swaps[i].second].size();
+      if (tsum.back() == 0.0) break;
+      const double r = rng.random_real(tsum.back());
+      size_t k = 0;
+      while (k + 1 < swaps.size() && !(r < tsum[k + 1])) ++k;
+      const int a = swaps[k].first, b = swaps[k].second;
+      const long la = loc[a][rng.random_int((long)loc[a].size() - 1)];
+      const long lb = loc[b][rng.random_int((long)loc[b].size() - 1)];
+      const double dEa = S->delta_formation(occ, la, b);
+      occ[la] = b;
+      const double dEb = S->delta_formation(occ, lb, a);
+      occ[la] = a;
+      const double dE = dEa + dEb;
+      if (metropolis_acceptance(dE, beta, rng)) {
+        ++nacc;
+        Ef += dE;
+        occ[la] = b;
+        occ[lb] = a;
+        loc[a][mol_loc[la]] = lb;
+        loc[b][mol_loc[lb]] = la;
+        std::swap(mol_loc[la], mol_loc[lb]);
+      }
+    }
+    e_out[p] = Ef / (double)N;
+  }
+  return nacc;
+}
+
 }  // extern "C"

@@ -443,4 +443,66 @@ inline ColoredRun colored_sweep(const CESupercell& S, int* occ, double T,
   return R;
 }
 
+constexpr uint32_t CANON_TAG = 0x4D434343u;    // acceptance draws of the canonical sweep
+constexpr uint32_t CANON_D_TAG = 0x4D434344u;  // matching offsets of the canonical sweep
+
+// Coloured canonical sweep: pass p uses colouring A (p even) or B (p odd); colour c = 0..n-1
+// of it; the class's sites in ascending order s_0 < s_1 < ... < s_{n-1}; matching offset
+// d = (x * n) >> 32 with x word 0 of Philox(c, p, chain, CANON_D_TAG); positions k and
+// k2 = (d - k) mod n with k < k2 form a pair (i, j) = (s_k, s_k2); a pair of different
+// occupants is exchanged by Metropolis (metropolis.hh:26-35) with u = word 0 of
+// Philox(i, p, chain, CANON_TAG) * 2^-32 and dE the formation-energy change of the swap
+// (the two sites share no cluster, so dE = dE_i + dE_j).  The swap is the canonical event of
+// OccEventProposal.hh:108-237 with its pair chosen by the matching instead of at random.
+inline ColoredRun colored_canonical_sweep(const CESupercell& S, int* occ, double T, uint64_t seed, uint32_t chain,
+                                          const std::vector<int>& colA, int nA, const std::vector<int>& colB,
+                                          int nB, long pass0, long n_passes) {
+  ColoredRun R;
+  const double beta = 1.0 / (KB * T);
+  std::vector<std::vector<long>> cls[2];
+  cls[0].resize(nA);
+  cls[1].resize(nB);
+  for (long l = 0; l < S.n(); ++l) {
+    cls[0][colA[l]].push_back(l);
+    cls[1][colB[l]].push_back(l);
+  }
+  std::array<uint32_t, 2> key{(uint32_t)seed, (uint32_t)(seed >> 32)};
+  for (long p = pass0; p < pass0 + n_passes; ++p) {
+    long long nacc = 0;
+    const auto& by_color = cls[p & 1];
+    for (int c = 0; c < (int)by_color.size(); ++c) {
+      const auto& site = by_color[c];
+      const long n = (long)site.size();
+      if (n < 2) continue;
+      const auto xd = philox4x32_10({(uint32_t)c, (uint32_t)p, chain, CANON_D_TAG}, key);
+      const long d = (long)(((uint64_t)xd[0] * (uint64_t)n) >> 32);
+      for (long k = 0; k < n; ++k) {
+        long k2 = d - k;
+        if (k2 < 0) k2 += n;
+        if (!(k < k2)) continue;
+        const long i = site[k], j = site[k2];
+        const int oi = occ[i], oj = occ[j];
+        if (oi == oj) continue;
+        const auto x = philox4x32_10({(uint32_t)i, (uint32_t)p, chain, CANON_TAG}, key);
+        const double dE = S.delta_formation(occ, i, oj) + S.delta_formation(occ, j, oi);
+        bool acc;
+        if (dE < 0.0) {
+          acc = true;
+        } else {
+          const double u = (double)x[0] * (1.0 / 4294967296.0);
+          acc = u < std::exp(-dE * beta);
+        }
+        if (acc) {
+          occ[i] = oj;
+          occ[j] = oi;
+          ++nacc;
+        }
+      }
+    }
+    R.corr.push_back(S.int_corr(occ));
+    R.n_accept.push_back(nacc);
+  }
+  return R;
+}
+
 }  // namespace oracle

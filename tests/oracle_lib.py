@@ -74,6 +74,12 @@ def load():
         L.orc_ce_colored_sweep.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int,
                                            C.c_ulonglong, C.c_uint, C.POINTER(C.c_int), C.c_int, C.c_long, C.c_long,
                                            C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        L.orc_ce_canonical_sweep.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.c_ulonglong, C.c_uint,
+                                             C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int, C.c_long,
+                                             C.c_long, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        L.orc_ce_canonical_samples.restype = C.c_longlong
+        L.orc_ce_canonical_samples.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.c_ulonglong, C.c_long,
+                                               C.POINTER(C.c_double)]
         L.orc_ce_random_site_run.restype = C.c_longlong
         L.orc_ce_random_site_run.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int,
                                              C.c_ulonglong, C.c_longlong, C.POINTER(C.c_double)]
@@ -175,6 +181,29 @@ class OracleCE:
                                     C.c_uint(chain), p(colors, C.c_int), n_colors, pass0, n_passes,
                                     p(corr, C.c_longlong), p(nacc, C.c_longlong))
         return occ, corr, nacc
+
+    def canonical_sweep(self, occ, T, seed, chain, colors_a, n_a, colors_b, n_b, pass0, n_passes, n_classes):
+        """Coloured canonical sweep (matched same-colour pairs, colourings alternating by
+        pass): final occupation, correlations after each pass, accepted swaps per pass."""
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
+        ca = np.ascontiguousarray(np.asarray(colors_a, dtype=np.int32))
+        cb = np.ascontiguousarray(np.asarray(colors_b, dtype=np.int32))
+        corr = np.zeros((n_passes, n_classes), dtype=np.int64)
+        nacc = np.zeros(n_passes, dtype=np.int64)
+        load().orc_ce_canonical_sweep(self.h, p(occ, C.c_int), T, C.c_ulonglong(seed), C.c_uint(chain),
+                                      p(ca, C.c_int), n_a, p(cb, C.c_int), n_b, pass0, n_passes,
+                                      p(corr, C.c_longlong), p(nacc, C.c_longlong))
+        return occ, corr, nacc
+
+    def canonical_samples(self, occ, T, seed, n_passes):
+        """Reference-dynamics canonical run (random swaps of two different occupants): formation
+        energy per site after each pass [n_passes], accepted count."""
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
+        e = np.zeros(n_passes, dtype=np.float64)
+        nacc = load().orc_ce_canonical_samples(self.h, p(occ, C.c_int), T, C.c_ulonglong(seed), n_passes,
+                                               p(e, C.c_double))
+        assert nacc >= 0
+        return e, nacc
 
     def sgc_samples(self, occ, T, mu, seed, n_passes):
         """Reference-dynamics SGC run: per-pass potential energy per site [n_passes] and
