@@ -319,6 +319,91 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+CANON_L = 48
+CANON_METRIC = "canonical Metropolis site-attempts/s (FCC 48^3 CE, fixed composition)"
+
+
+def run_canonical(args) -> None:
+    """Canonical (fixed-composition) sweep: one chain per SM of binary FCC 48^3 (110,592
+    sites, exactly 50 % B by a seeded shuffle), T linspace(300, 2000), exchanges of matched
+    same-colour pairs.  A site-attempt is one site of a proposed pair (every site of a pass is
+    in one pair or a fixed point: N per chain and pass); the reference's step proposes one
+    pair (2 site-attempts).  value: attempts / CUDA-event time, L2 flushed between runs;
+    cpu_baseline: the reference's canonical dynamics (random pairs of different occupants)
+    restated in the oracle, on one host core."""
+    import torch
+
+    from casmcode_monte_gb300 import clex
+
+    rank, world, local = _env_rank()
+    torch.cuda.set_device(local)
+    n_chains = torch.cuda.get_device_properties(local).multi_processor_count
+    eci = clex.make_eci("fcc_binary", 1)
+    model = clex.ClexModel("fcc_binary", eci)
+    rng = np.random.default_rng(2000 + rank)
+    n = CANON_L**3
+    occ = np.stack([clex.random_occupation(2, n, rng) for _ in range(n_chains)])
+    T = np.linspace(300.0, 2000.0, n_chains)
+    seeds = np.arange(1, n_chains + 1, dtype=np.uint64) * np.uint64(0x9E3779B1) + np.uint64(rank)
+    batch = clex.CanonicalBatch(model, (CANON_L,) * 3, occ, T, seeds)
+    ppl = max(1, int(args.passes_per_launch))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    left = args.warmup
+    while left > 0:
+        m = min(ppl, left)
+        batch.run(m, want_output=False)
+        left -= m
+    torch.cuda.synchronize()
+    kernel_ms, launches, left = 0.0, 0, args.steps
+    while left > 0:
+        m = min(ppl, left)
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        batch.run(m, want_output=False)
+        kernel_ms += batch.last_kernel_ms()
+        launches += 1
+        left -= m
+    attempts = n_chains * n * args.steps
+    value = attempts / (kernel_ms * 1e-3)
+    # end to end: create (H2D), run with per-pass outputs (D2H), read the occupations
+    t1 = time.perf_counter()
+    b2 = clex.CanonicalBatch(model, (CANON_L,) * 3, occ, T, seeds)
+    left = args.steps
+    while left > 0:
+        m = min(ppl, left)
+        b2.run(m)
+        left -= m
+    final = b2.occupation()
+    e2e_s = time.perf_counter() - t1
+    assert np.array_equal(np.bincount(final[0], minlength=2), np.bincount(occ[0], minlength=2))
+    line = {"metric": CANON_METRIC, "value": value, "unit": "site-attempts/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": kernel_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "i8/i32+f32 (f64 exact decisions)", "data": "synthetic",
+            "config": {"workload": "fcc48_binary_ce_canonical", "supercell": [CANON_L] * 3, "chains": n_chains,
+                       "composition_B": 0.5, "passes_per_launch": ppl, "colors": list(batch.n_colors),
+                       "threads_per_cta": batch.threads, "l2": "flushed between launches (256 MB write)"},
+            "e2e": {"value": attempts / e2e_s, "unit": "site-attempts/s", "h2d_bytes_per_step": occ.nbytes / args.steps,
+                    "d2h_bytes_per_step": n_chains * batch.n_slots * 8 + occ.nbytes / args.steps},
+            "gpu_launches": launches}
+    if rank == 0 and args.cpu_seconds > 0:
+        from tests import oracle_lib
+
+        orc = oracle_lib.OracleCE((CANON_L,) * 3, 2, eci)
+        o = occ[0].astype(np.int32)
+        t0 = time.perf_counter()
+        orc.canonical_samples(o, float(T[n_chains // 2]), 5, 1)
+        per_pass = time.perf_counter() - t0
+        passes = max(1, int(args.cpu_seconds / max(per_pass, 1e-9)))
+        t0 = time.perf_counter()
+        orc.canonical_samples(o, float(T[n_chains // 2]), 6, passes)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 2.0 * n * passes / dt, "unit": "site-attempts/s", "cores": 1, "kind": "port",
+                                "sample": f"{passes} passes of {n} random canonical swaps on one 48^3 chain at "
+                                          f"T={T[n_chains // 2]:.0f} K (oracle restatement, g++ -O2)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -329,11 +414,16 @@ def main():
     ap.add_argument("--ctas-per-chain", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-steps-per-sample", type=float, default=2e6)
+    ap.add_argument("--workload", default="fcc64_sgc", choices=["fcc64_sgc", "canonical"],
+                    help="fcc64_sgc: the headline semi-grand canonical pass; canonical: fixed-composition "
+                         "sweeps of 48^3 chains")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "canonical":
+        run_canonical(args)
     else:
         run_gpu(args)
 

@@ -504,5 +504,5 @@ def random_occupation(n_species: int, n_sites: int, rng: np.random.Generator,
     return occ
 
 
-__all__ = ["ClexModel", "ChainBatch", "ChainPool", "PoolFull", "SweepSamples", "accumulate", "basis_description", "make_eci",
+__all__ = ["ClexModel", "ChainBatch", "CanonicalBatch", "ChainPool", "PoolFull", "SweepSamples", "accumulate", "basis_description", "make_eci",
            "random_occupation", "KB"]
