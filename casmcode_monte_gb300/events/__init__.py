@@ -814,6 +814,33 @@ class OccLocation:
     def atom_size(self) -> int:
         return len(self._atoms)
 
+    def atom_positions_cart(self) -> np.ndarray:
+        """Current atom positions, shape (3, n_atoms), following atoms across periodic
+        boundaries: site basis position + the atom's position in its molecule + lattice
+        translation of the atom (OccLocation.cc:385-405).  Needs ``update_atoms``."""
+        conv = self._convert
+        L = conv.lat_column_mat()
+        R = np.zeros((3, len(self._atoms)))
+        for mol in self._mol:
+            basis = conv.l_to_basis_cart(mol.l)
+            molecule = conv.species_to_mol(mol.species_index)
+            for k, atom_id in enumerate(mol.component):
+                R[:, atom_id] = basis + np.asarray(molecule.atoms[k][1], dtype=float) + \
+                    L @ np.asarray(self._atoms[atom_id].translation, dtype=float)
+        return R
+
+    def atom_positions_cart_within(self) -> np.ndarray:
+        """Current atom positions, shape (3, n_atoms), within the periodic supercell: site
+        position + the atom's position in its molecule (OccLocation.cc:412-429)."""
+        conv = self._convert
+        R = np.zeros((3, len(self._atoms)))
+        for mol in self._mol:
+            site = conv.l_to_cart(mol.l)
+            molecule = conv.species_to_mol(mol.species_index)
+            for k, atom_id in enumerate(mol.component):
+                R[:, atom_id] = site + np.asarray(molecule.atoms[k][1], dtype=float)
+        return R
+
     def atom(self, atom_id: int) -> Atom:
         return self._atoms[atom_id]
 

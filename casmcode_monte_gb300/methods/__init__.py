@@ -31,7 +31,8 @@ from ..sampling import (CompletionCheck, CompletionCheckParams, Sampler, get_n_s
                         jsonStateSamplingFunctionMap, StateSamplingFunctionMap)
 
 __all__ = ["KB", "BasicOccupationMetropolisData", "basic_occupation_metropolis", "default_write_status",
-           "metropolis_acceptance", "occupation_metropolis", "write_no_status"]
+           "metropolis_acceptance", "occupation_metropolis", "write_no_status", "NfoldData", "nfold", "KMCData",
+           "kinetic_monte_carlo"]
 
 KB = 8.6173303e-05  # eV/K (the reference's libcasm-global constant)
 
@@ -210,3 +211,136 @@ def occupation_metropolis(state, occ_location, potential, possible_swaps, propos
         run_manager.sample_data_by_count_if_due(state)
     run_manager.finalize(state)
 
+
+
+# ---- rejection-free and kinetic loops (methods/nfold.hh, methods/kinetic_monte_carlo.hh)
+
+class NfoldData:
+    """Data sampling functions can use during an N-fold way run (nfold.hh:24-44)."""
+
+    def __init__(self, n_events_possible: float = 0.0):
+        #: set to the current sampling fixture's label before it samples
+        self.sampling_fixture_label = ""
+        #: set to the sampling fixture before it samples
+        self.sampling_fixture = None
+        #: total number of events that could be selected at any time (set before running)
+        self.n_events_possible = float(n_events_possible)
+        #: total_rate / n_events_possible: the Metropolis acceptance rate the current
+        #: event acceptance probabilities imply
+        self.expected_acceptance_rate = 0.0
+
+
+def _sample_mode_is_time(fixture) -> bool:
+    from ..sampling import SAMPLE_MODE
+
+    return fixture.params().sampling_params.sample_mode == SAMPLE_MODE.BY_TIME
+
+
+def nfold(state, occ_location, nfold_data: NfoldData, event_selector, get_event_f: Callable, run_manager) -> None:
+    """N-fold way occupation Monte Carlo with run management (nfold.hh:48-149).
+
+    ``event_selector.total_rate()`` and ``event_selector.select_event() -> (event_id,
+    time_increment)`` choose the next event without rejection (the selector updates the rates
+    the last event changed); ``get_event_f(event_id) -> OccEvent`` gives the event to apply.
+    Each step: write status if due; total rate, then selection; sample if due by count and by
+    time (the samples' weight is the time increment, or 1.0 for fixtures that sample by
+    time, whose time is then set to the sample time); apply the event (every selected event
+    is accepted); advance time; count the step.  The run manager is initialized with
+    ``occ_location.mol_size()`` steps per pass and finalized with the final state.
+    """
+    loop = {"total_rate": 0.0, "time": 0.0, "time_increment": 0.0}
+
+    def pre_sample_action(fixture, state_):
+        nfold_data.sampling_fixture_label = fixture.label()
+        nfold_data.sampling_fixture = fixture
+        nfold_data.expected_acceptance_rate = loop["total_rate"] / nfold_data.n_events_possible
+        if _sample_mode_is_time(fixture):
+            fixture.push_back_sample_weight(1.0)
+            loop["time"] = fixture.next_sample_time()
+        else:
+            fixture.push_back_sample_weight(loop["time_increment"])
+
+    occupation = _occupation_array(state)
+    run_manager.initialize(occ_location.mol_size())
+    run_manager.update_next_sampling_fixture()
+    while not run_manager.is_complete():
+        run_manager.write_status_if_due()
+        loop["total_rate"] = event_selector.total_rate()
+        selected_event_id, loop["time_increment"] = event_selector.select_event()
+        event_time = loop["time"] + loop["time_increment"]
+        run_manager.sample_data_by_count_if_due(state, pre_sample_action, None)
+        run_manager.sample_data_by_time_if_due(event_time, state, pre_sample_action, None)
+        run_manager.increment_n_accept()
+        occ_location.apply(get_event_f(selected_event_id), occupation)
+        loop["time"] = event_time
+        run_manager.set_time(event_time)
+        run_manager.increment_step()
+    run_manager.finalize(state)
+
+
+class KMCData:
+    """Data sampling functions can use during a kinetic Monte Carlo run
+    (kinetic_monte_carlo.hh:25-98): the total rate and time at sampling, the previous sample
+    time per fixture, and atom positions now and at each fixture's previous sample (shape
+    (3, n_atoms), Cartesian, following atoms across periodic boundaries)."""
+
+    def __init__(self):
+        self.sampling_fixture_label = ""
+        self.sampling_fixture = None
+        self.total_rate = 0.0
+        self.time = 0.0
+        self.prev_time: dict = {}
+        self.unique_atom_id: list = []
+        self.prev_unique_atom_id: dict = {}
+        #: atom name index of each column of the position matrices (set by the caller)
+        self.atom_name_index_list: list = []
+        self.atom_positions_cart = np.zeros((3, 0))
+        self.prev_atom_positions_cart: dict = {}
+
+
+def kinetic_monte_carlo(state, occ_location, kmc_data: KMCData, event_selector, get_event_f: Callable,
+                        run_manager) -> None:
+    """Kinetic Monte Carlo with run management (kinetic_monte_carlo.hh:108-224).
+
+    As ``nfold`` but the event is selected before the total rate is read (the selector
+    updates rates after the last event, then chooses), and sampling functions see
+    ``kmc_data``: before a sample its label, fixture, current atom positions, total rate and,
+    for fixtures that sample by time, the sample time; after it the fixture's previous time
+    and positions.  ``occ_location`` must track atoms (``update_atoms=True``).
+    """
+    kmc_data.time = 0.0
+    kmc_data.atom_positions_cart = occ_location.atom_positions_cart()
+    kmc_data.prev_atom_positions_cart = {}
+    for fixture in run_manager.sampling_fixtures:
+        kmc_data.prev_time.setdefault(fixture.label(), kmc_data.time)
+        kmc_data.prev_atom_positions_cart.setdefault(fixture.label(), kmc_data.atom_positions_cart.copy())
+    loop = {"total_rate": 0.0}
+
+    def pre_sample_action(fixture, state_):
+        kmc_data.sampling_fixture_label = fixture.label()
+        kmc_data.sampling_fixture = fixture
+        kmc_data.atom_positions_cart = occ_location.atom_positions_cart()
+        kmc_data.total_rate = loop["total_rate"]
+        if _sample_mode_is_time(fixture):
+            kmc_data.time = fixture.next_sample_time()
+
+    def post_sample_action(fixture, state_):
+        kmc_data.prev_time[fixture.label()] = kmc_data.time
+        kmc_data.prev_atom_positions_cart[fixture.label()] = kmc_data.atom_positions_cart.copy()
+
+    occupation = _occupation_array(state)
+    run_manager.initialize(occ_location.mol_size())
+    run_manager.update_next_sampling_fixture()
+    while not run_manager.is_complete():
+        run_manager.write_status_if_due()
+        selected_event_id, time_increment = event_selector.select_event()
+        loop["total_rate"] = event_selector.total_rate()
+        event_time = kmc_data.time + time_increment
+        run_manager.sample_data_by_count_if_due(state, pre_sample_action, post_sample_action)
+        run_manager.sample_data_by_time_if_due(event_time, state, pre_sample_action, post_sample_action)
+        run_manager.increment_n_accept()
+        occ_location.apply(get_event_f(selected_event_id), occupation)
+        kmc_data.time = event_time
+        run_manager.set_time(event_time)
+        run_manager.increment_step()
+    run_manager.finalize(state)
