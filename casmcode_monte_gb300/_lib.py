@@ -70,6 +70,7 @@ SIGNATURES = {
                                      c_int8_p, C.c_int, vpp]),
     "mg_ce_canon_info": (C.c_int, [vp, c_int_p, c_int_p, c_int_p, c_size_p]),
     "mg_ce_canon_colors": (C.c_int, [vp, C.c_int, c_int32_p]),
+    "mg_ce_canon_class_order": (C.c_int, [vp, C.c_int, c_int32_p]),
     "mg_ce_canon_run": (C.c_int, [vp, C.c_int, c_ll_p]),
     "mg_ce_canon_last_kernel_ms": (C.c_int, [vp, c_float_p]),
     "mg_ce_canon_get_occ": (C.c_int, [vp, c_int8_p]),

@@ -340,6 +340,13 @@ class CanonicalBatch:
         _lib.check(_lib.lib().mg_ce_canon_colors(self._h, int(which), _lib.ptr(col, C.c_int32)))
         return col
 
+    def class_order(self, which: int) -> np.ndarray:
+        """The sites of colouring `which`'s per-colour lists, colour by colour ([N] int32): a
+        phase's matching pairs positions k and (d - k) mod n of its colour's list."""
+        order = np.zeros(self.n_sites, dtype=np.int32)
+        _lib.check(_lib.lib().mg_ce_canon_class_order(self._h, int(which), _lib.ptr(order, C.c_int32)))
+        return order
+
 
 class PoolFull(RuntimeError):
     """Admission refused: no free chain slot or not enough arena memory."""

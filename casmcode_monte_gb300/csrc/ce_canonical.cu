@@ -22,6 +22,7 @@ struct mg_ce_canon {
   size_t smem = 0;
   int n_colors[2] = {0, 0};
   std::vector<int32_t> color[2];
+  std::vector<int32_t> order[2];  // list sites of each colouring, colour by colour
   int* dcstart[2] = {nullptr, nullptr};
   uint32_t* dentries[2] = {nullptr, nullptr};
   uint32_t* dsite[2] = {nullptr, nullptr};
@@ -173,33 +174,56 @@ bool canonical_colourings(int kind, int L0, int L1, int L2, mg_ce_canon* h) {
   return false;
 }
 
-// Per-colour lists of one colouring for one CTA holding the whole lattice, ascending site
-// index within a colour: entry = padded index | flags << 24 (flags: the site's periodic
-// copies, as SiteSweeper::store reads them), site = linear index.
+// Per-colour lists of one colouring for one CTA holding the whole lattice: entry = padded
+// index | flags << 24 (flags: the site's periodic copies, as SiteSweeper::store reads them),
+// site = linear index.  Within a colour the sites are ordered for shared-memory banks, as the
+// sweep's byte lists are: by residue g = padded index & 3, then round-robin over the 32 banks
+// (bank q = (padded index >> 2) & 31): the first site of every bank, then the second, ... (in
+// ascending site order within a bank), so that consecutive list positions, which adjacent
+// lanes take, fall in different banks.  The matching pairs list positions, so the order is
+// part of the trajectory (mg_ce_canon_class_order returns it).
 void canonical_lists(int L0, int L1, int L2, const int32_t* col, int nc, std::vector<int>& cstart,
                      std::vector<uint32_t>& entries, std::vector<uint32_t>& site) {
   const long long N = (long long)L0 * L1 * L2;
-  const int PX = L0 + 2 * mg::CE_HALO, PY = L1 + 2 * mg::CE_HALO;
-  cstart.assign(nc + 1, 0);
-  for (long long l = 0; l < N; ++l) cstart[col[l] + 1]++;
-  for (int c = 0; c < nc; ++c) cstart[c + 1] += cstart[c];
-  std::vector<int> pos(cstart.begin(), cstart.end() - 1);
-  entries.assign(N, 0u);
-  site.assign(N, 0u);
+  const int H = mg::CE_HALO;
+  const int PX = L0 + 2 * H, PY = L1 + 2 * H;
+  std::vector<std::vector<std::vector<long long>>> bucket((size_t)nc, std::vector<std::vector<long long>>(128));
+  std::vector<uint32_t> pidx_of(N);
   for (long long l = 0; l < N; ++l) {
     const int i = (int)(l % L0), j = (int)((l / L0) % L1), k = (int)(l / ((long long)L0 * L1));
-    uint32_t flags = 0;
-    if (i < mg::CE_HALO) flags |= 1;
-    else if (i >= L0 - mg::CE_HALO) flags |= 2;
-    if (j < mg::CE_HALO) flags |= 4;
-    else if (j >= L1 - mg::CE_HALO) flags |= 8;
-    if (k < mg::CE_HALO) flags |= 16;
-    if (k >= L2 - mg::CE_HALO) flags |= 32;
-    const uint32_t pidx = (uint32_t)((i + mg::CE_HALO) + PX * ((j + mg::CE_HALO) + PY * (k + mg::CE_HALO)));
-    const int p = pos[col[l]]++;
-    entries[p] = pidx | (flags << 24);
-    site[p] = (uint32_t)l;
+    const uint32_t pidx = (uint32_t)((i + H) + PX * ((j + H) + PY * (k + H)));
+    pidx_of[l] = pidx;
+    bucket[col[l]][(pidx & 3u) * 32u + ((pidx >> 2) & 31u)].push_back(l);
   }
+  cstart.assign(nc + 1, 0);
+  entries.assign(N, 0u);
+  site.assign(N, 0u);
+  long long p = 0;
+  for (int c = 0; c < nc; ++c) {
+    cstart[c] = (int)p;
+    for (int g = 0; g < 4; ++g) {
+      size_t rounds = 0;
+      for (int q = 0; q < 32; ++q) rounds = std::max(rounds, bucket[c][g * 32 + q].size());
+      for (size_t t = 0; t < rounds; ++t)
+        for (int q = 0; q < 32; ++q) {
+          const auto& b = bucket[c][g * 32 + q];
+          if (t >= b.size()) continue;
+          const long long l = b[t];
+          const int i = (int)(l % L0), j = (int)((l / L0) % L1), k = (int)(l / ((long long)L0 * L1));
+          uint32_t flags = 0;
+          if (i < H) flags |= 1;
+          else if (i >= L0 - H) flags |= 2;
+          if (j < H) flags |= 4;
+          else if (j >= L1 - H) flags |= 8;
+          if (k < H) flags |= 16;
+          if (k >= L2 - H) flags |= 32;
+          entries[p] = pidx_of[l] | (flags << 24);
+          site[p] = (uint32_t)l;
+          ++p;
+        }
+    }
+  }
+  cstart[nc] = (int)p;
 }
 
 template <class B, int NT>
@@ -316,6 +340,7 @@ int mg_ce_canon_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
     std::vector<int> cstart;
     std::vector<uint32_t> entries, site;
     canonical_lists(L0, L1, L2, h->color[t].data(), h->n_colors[t], cstart, entries, site);
+    h->order[t].assign(site.begin(), site.end());
     MGX(cudaMalloc(&h->dcstart[t], sizeof(int) * cstart.size()), "malloc lists");
     MGX(cudaMalloc(&h->dentries[t], sizeof(uint32_t) * entries.size()), "malloc lists");
     MGX(cudaMalloc(&h->dsite[t], sizeof(uint32_t) * site.size()), "malloc lists");
@@ -351,6 +376,15 @@ int mg_ce_canon_colors(const mg_ce_canon* h, int which, int32_t* color) {
     return MG_ERR_INVALID;
   }
   std::memcpy(color, h->color[which].data(), sizeof(int32_t) * (size_t)h->N);
+  return MG_OK;
+}
+
+int mg_ce_canon_class_order(const mg_ce_canon* h, int which, int32_t* site_order) {
+  if (!h || !site_order || which < 0 || which > 1) {
+    set_error("Error in mg_ce_canon_class_order: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  std::memcpy(site_order, h->order[which].data(), sizeof(int32_t) * (size_t)h->N);
   return MG_OK;
 }
 

@@ -185,13 +185,28 @@ __global__ void __launch_bounds__(NT, 1) ce_canonical_kernel(const __grid_consta
       if (n >= 2) {
         const U32x4 xd = philox4x32_10(U32x4{(uint32_t)c, pass_g, chain_id, CANON_D_TAG}, key0, key1);
         const int d = (int)(((unsigned long long)xd.x * (unsigned long long)n) >> 32);
-#pragma unroll 1
-        for (int k = threadIdx.x; k < n; k += NT) {
+        // list entries of position k's pair (k < k2 only), fetched one pair ahead of its use
+        auto fetch = [&](int k, uint32_t& ei, uint32_t& ej, uint32_t& li) -> bool {
+          if (k >= n) return false;
           int k2 = d - k;
           if (k2 < 0) k2 += n;
-          if (k < k2)
-            canonical_swap<B>(sw, __ldg(cc.entries + base + k), __ldg(cc.entries + base + k2),
-                              __ldg(cc.site_l + base + k), pass_g, chain_id, key0, key1, acc);
+          if (!(k < k2)) return false;
+          ei = __ldg(cc.entries + base + k);
+          ej = __ldg(cc.entries + base + k2);
+          li = __ldg(cc.site_l + base + k);
+          return true;
+        };
+        uint32_t ei = 0u, ej = 0u, li = 0u;
+        bool cur = fetch(threadIdx.x, ei, ej, li);
+#pragma unroll 1
+        for (int k = threadIdx.x; k < n; k += NT) {
+          uint32_t ei2 = 0u, ej2 = 0u, li2 = 0u;
+          const bool nxt = fetch(k + NT, ei2, ej2, li2);
+          if (cur) canonical_swap<B>(sw, ei, ej, li, pass_g, chain_id, key0, key1, acc);
+          ei = ei2;
+          ej = ej2;
+          li = li2;
+          cur = nxt;
         }
       }
       __syncthreads();

@@ -177,6 +177,9 @@ int mg_ce_canon_info(const mg_ce_canon* h, int* n_colors_a, int* n_colors_b, int
                      size_t* smem_bytes);
 /* colouring `which` (0: passes with even index, 1: odd) as color[N] */
 int mg_ce_canon_colors(const mg_ce_canon* h, int which, int32_t* color);
+/* the order of colouring `which`'s per-colour site lists (site_order[N], colour by colour):
+ * the matching of a phase pairs positions k and (d - k) mod n of its colour's list */
+int mg_ce_canon_class_order(const mg_ce_canon* h, int which, int32_t* site_order);
 int mg_ce_canon_run(mg_ce_canon* h, int n_passes, long long* out);
 int mg_ce_canon_last_kernel_ms(const mg_ce_canon* h, float* ms);
 int mg_ce_canon_get_occ(mg_ce_canon* h, int8_t* occ);

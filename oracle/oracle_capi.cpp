@@ -425,11 +425,14 @@ long long orc_ce_sgc_samples(void* h, int* occ, double T, const double* mu, int 
 }
 
 int orc_ce_canonical_sweep(void* h, int* occ, double T, unsigned long long seed, unsigned int chain,
-                           const int* color_a, int n_a, const int* color_b, int n_b, long pass0, long n_passes,
-                           long long* corr_out, long long* nacc_out) {
+                           const int* color_a, int n_a, const int* color_b, int n_b, const int* order_a,
+                           const int* order_b, long pass0, long n_passes, long long* corr_out, long long* nacc_out) {
   auto* S = static_cast<CESupercell*>(h);
   std::vector<int> ca(color_a, color_a + S->n()), cb(color_b, color_b + S->n());
-  auto R = colored_canonical_sweep(*S, occ, T, seed, chain, ca, n_a, cb, n_b, pass0, n_passes);
+  std::vector<long> oa, ob;
+  if (order_a) oa.assign(order_a, order_a + S->n());
+  if (order_b) ob.assign(order_b, order_b + S->n());
+  auto R = colored_canonical_sweep(*S, occ, T, seed, chain, ca, n_a, cb, n_b, pass0, n_passes, oa, ob);
   const long nc = (long)S->classes.size();
   for (long p = 0; p < n_passes; ++p) {
     for (long c = 0; c < nc; ++c) corr_out[p * nc + c] = R.corr[p][c];

@@ -447,24 +447,28 @@ constexpr uint32_t CANON_TAG = 0x4D434343u;    // acceptance draws of the canoni
 constexpr uint32_t CANON_D_TAG = 0x4D434344u;  // matching offsets of the canonical sweep
 
 // Coloured canonical sweep: pass p uses colouring A (p even) or B (p odd); colour c = 0..n-1
-// of it; the class's sites in ascending order s_0 < s_1 < ... < s_{n-1}; matching offset
+// of it; the class's sites s_0, s_1, ..., s_{n-1} in list order; matching offset
 // d = (x * n) >> 32 with x word 0 of Philox(c, p, chain, CANON_D_TAG); positions k and
 // k2 = (d - k) mod n with k < k2 form a pair (i, j) = (s_k, s_k2); a pair of different
 // occupants is exchanged by Metropolis (metropolis.hh:26-35) with u = word 0 of
 // Philox(i, p, chain, CANON_TAG) * 2^-32 and dE the formation-energy change of the swap
 // (the two sites share no cluster, so dE = dE_i + dE_j).  The swap is the canonical event of
 // OccEventProposal.hh:108-237 with its pair chosen by the matching instead of at random.
+// orderA / orderB: the sites in the order of the GPU's class lists (empty: ascending); a
+// colour's class is its sites in that order.
 inline ColoredRun colored_canonical_sweep(const CESupercell& S, int* occ, double T, uint64_t seed, uint32_t chain,
                                           const std::vector<int>& colA, int nA, const std::vector<int>& colB,
-                                          int nB, long pass0, long n_passes) {
+                                          int nB, long pass0, long n_passes, const std::vector<long>& orderA = {},
+                                          const std::vector<long>& orderB = {}) {
   ColoredRun R;
   const double beta = 1.0 / (KB * T);
   std::vector<std::vector<long>> cls[2];
   cls[0].resize(nA);
   cls[1].resize(nB);
-  for (long l = 0; l < S.n(); ++l) {
-    cls[0][colA[l]].push_back(l);
-    cls[1][colB[l]].push_back(l);
+  for (long p = 0; p < S.n(); ++p) {
+    const long la = orderA.empty() ? p : orderA[p], lb = orderB.empty() ? p : orderB[p];
+    cls[0][colA[la]].push_back(la);
+    cls[1][colB[lb]].push_back(lb);
   }
   std::array<uint32_t, 2> key{(uint32_t)seed, (uint32_t)(seed >> 32)};
   for (long p = pass0; p < pass0 + n_passes; ++p) {

@@ -75,8 +75,9 @@ def load():
                                            C.c_ulonglong, C.c_uint, C.POINTER(C.c_int), C.c_int, C.c_long, C.c_long,
                                            C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
         L.orc_ce_canonical_sweep.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.c_ulonglong, C.c_uint,
-                                             C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int, C.c_long,
-                                             C.c_long, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+                                             C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.c_int,
+                                             C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_long, C.c_long,
+                                             C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
         L.orc_ce_canonical_samples.restype = C.c_longlong
         L.orc_ce_canonical_samples.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.c_ulonglong, C.c_long,
                                                C.POINTER(C.c_double)]
@@ -182,16 +183,22 @@ class OracleCE:
                                     p(corr, C.c_longlong), p(nacc, C.c_longlong))
         return occ, corr, nacc
 
-    def canonical_sweep(self, occ, T, seed, chain, colors_a, n_a, colors_b, n_b, pass0, n_passes, n_classes):
+    def canonical_sweep(self, occ, T, seed, chain, colors_a, n_a, colors_b, n_b, pass0, n_passes, n_classes,
+                        order_a=None, order_b=None):
         """Coloured canonical sweep (matched same-colour pairs, colourings alternating by
-        pass): final occupation, correlations after each pass, accepted swaps per pass."""
+        pass; classes in the given list orders, else ascending): final occupation,
+        correlations after each pass, accepted swaps per pass."""
         occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
         ca = np.ascontiguousarray(np.asarray(colors_a, dtype=np.int32))
         cb = np.ascontiguousarray(np.asarray(colors_b, dtype=np.int32))
+        oa = None if order_a is None else np.ascontiguousarray(np.asarray(order_a, dtype=np.int32))
+        ob = None if order_b is None else np.ascontiguousarray(np.asarray(order_b, dtype=np.int32))
         corr = np.zeros((n_passes, n_classes), dtype=np.int64)
         nacc = np.zeros(n_passes, dtype=np.int64)
         load().orc_ce_canonical_sweep(self.h, p(occ, C.c_int), T, C.c_ulonglong(seed), C.c_uint(chain),
-                                      p(ca, C.c_int), n_a, p(cb, C.c_int), n_b, pass0, n_passes,
+                                      p(ca, C.c_int), n_a, p(cb, C.c_int), n_b,
+                                      p(oa, C.c_int) if oa is not None else None,
+                                      p(ob, C.c_int) if ob is not None else None, pass0, n_passes,
                                       p(corr, C.c_longlong), p(nacc, C.c_longlong))
         return occ, corr, nacc
 

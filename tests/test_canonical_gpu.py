@@ -44,6 +44,9 @@ def test_canonical_sweep_equals_oracle(gpu_lib, kind, L, n_chains):
     model, occ, T, seeds, ns = _setup(kind, L, n_chains, seed=L[0] + n_chains)
     b = clex.CanonicalBatch(model, L, occ, T, seeds)
     col_a, col_b = b.colors(0), b.colors(1)
+    for col, order in ((col_a, b.class_order(0)), (col_b, b.class_order(1))):
+        assert np.array_equal(np.sort(order), np.arange(order.size))  # a permutation of the sites
+        assert (np.diff(col[order]) >= 0).all()                        # grouped colour by colour
     corr0 = b.corr()
     nc = model.n_classes
     outs = [b.run(3), b.run(4)]  # pass 0..2, then 3..6: both colourings, two launches
@@ -52,7 +55,8 @@ def test_canonical_sweep_equals_oracle(gpu_lib, kind, L, n_chains):
     orc = OracleCE(L, ns, model.eci)
     for c in range(n_chains):
         occ_ref, corr_ref, nacc_ref = orc.canonical_sweep(occ[c], T[c], int(seeds[c]), c, col_a, b.n_colors[0],
-                                                          col_b, b.n_colors[1], 0, 7, nc)
+                                                          col_b, b.n_colors[1], 0, 7, nc, b.class_order(0),
+                                                          b.class_order(1))
         assert np.array_equal(got[c], occ_ref.astype(np.int8)), c
         d = out[:, c, :nc].copy()
         d[:, 0] = 0
