@@ -725,8 +725,34 @@ int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout_out, int*
       }
     }
   }
+  // the occupancy choice of the warp-specialised layout with rotation over two cluster sizes,
+  // timed per pass on runs long enough to rotate (at least 4 n_chains passes)
+  bool best_rot = false;
+  if (rc == MG_OK && word && b->pipe >= 0 && b->rotation_allowed) {
+    b->ctas_requested = 0;
+    if (setup_layout(b, 3) == MG_OK && b->S_fast > 0) {
+      const int np = std::max(probe_passes, 4 * b->n_chains);
+      rc = mg_ce_batch_run(b, np, nullptr);  // warm; measures the time ratio
+      if (rc == MG_OK) rc = mg_ce_batch_run(b, np, nullptr);
+      if (rc == MG_OK) {
+        const float ms = b->last_ms * (float)probe_passes / (float)np;
+        b->pass = pass_keep;
+        e = cudaMemcpyAsync(b->docc, saved, occ_bytes, cudaMemcpyDeviceToDevice, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) {
+          rc = MG_ERR_CUDA;
+          set_error(std::string("CUDA error in mg_ce_batch_autotune: ") + cudaGetErrorString(e));
+        } else if (ms < best) {
+          best = ms;
+          best_layout = 3;
+          best_S = b->S;
+          best_rot = true;
+        }
+      }
+    }
+  }
   cudaFree(saved);
-  b->ctas_requested = best_S;
+  b->ctas_requested = best_rot ? 0 : best_S;
   const int rc2 = setup_layout(b, best_layout);
   if (rc != MG_OK) return rc;
   if (rc2 != MG_OK) return rc2;

@@ -125,9 +125,12 @@ int mg_ce_batch_layout(const mg_ce_batch* b, int* layout);
 int mg_ce_color_supercell(int basis_kind, int L0, int L1, int L2, int32_t* color, int* word_layout);
 int mg_ce_batch_set_layout(mg_ce_batch* b, int layout);
 /* Autotuner: times probe_passes passes of every layout that applies at every CTA count it
- * accepts (on the batch's own chains, whose occupations and pass counters are restored
- * after each trial, so results do not change) and keeps the fastest.  Reports the chosen
- * layout, CTA count and milliseconds per pass (each may be NULL). */
+ * accepts, and the occupancy choice with rotation over two cluster sizes where the batch
+ * has a rotation plan (runs of at least 4 n_chains passes, compared per pass), on the
+ * batch's own chains, whose occupations and pass counters are restored after each trial, so
+ * results do not change; keeps the fastest.  Reports the chosen layout, CTA count (the slow
+ * slot's when rotating: mg_ce_batch_rotation tells) and milliseconds per pass (each may be
+ * NULL). */
 int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout, int* ctas_per_chain, float* ms_per_pass);
 /* Run n_passes passes.  out (host, may be NULL) receives [n_passes][n_chains][n_classes+2]
  * int64: slot 0 accepted proposals, slot f (1..n_classes-1) change of the integer

@@ -137,10 +137,73 @@ class CeBatch {
     check(mg_ce_batch_last_kernel_ms(h_.get(), &ms));
     return ms;
   }
+  /* rotation over two cluster sizes: {CTAs of the fast clusters (0: no rotation), measured
+   * time ratio per pass fast / slow}; allow or forbid it; kernels launched by the last run */
+  std::pair<int, double> rotation() const {
+    int s = 0;
+    double r = 0.0;
+    check(mg_ce_batch_rotation(h_.get(), &s, &r));
+    return {s, r};
+  }
+  void set_rotation(bool allowed) { check(mg_ce_batch_set_rotation(h_.get(), allowed ? 1 : 0)); }
+  int last_launches() const {
+    int n = 0;
+    check(mg_ce_batch_last_launches(h_.get(), &n));
+    return n;
+  }
   mg_ce_batch* get() const { return h_.get(); }
 
  private:
   using H = Handle<mg_ce_batch, mg_ce_batch_destroy>;
+  H h_;
+  int n_chains_;
+  long long n_sites_;
+  int n_slots_;
+};
+
+/* Chains of one supercell swept at fixed composition (mg_ce_canon_*): exchanges of matched
+ * same-colour sites, the canonical event of the reference made parallel. */
+class CeCanon {
+ public:
+  CeCanon(const CeModel& m, int L0, int L1, int L2, const std::vector<double>& temperature,
+          const std::vector<uint64_t>& seeds, const std::vector<int8_t>& occ, bool fp32_decisions = false)
+      : n_chains_((int)temperature.size()), n_sites_((long long)L0 * L1 * L2), n_slots_(m.n_classes() + 2) {
+    mg_ce_canon* h = nullptr;
+    check(mg_ce_canon_create(m.get(), L0, L1, L2, n_chains_, temperature.data(), seeds.data(), nullptr, occ.data(),
+                             fp32_decisions ? 1 : 0, &h));
+    h_ = H(h);
+  }
+  /* per-pass outputs [n_passes][n_chains][n_classes + 2], slot 0 accepted swaps */
+  std::vector<long long> run(int n_passes) {
+    std::vector<long long> out((size_t)n_passes * n_chains_ * n_slots_);
+    check(mg_ce_canon_run(h_.get(), n_passes, out.data()));
+    return out;
+  }
+  std::vector<int8_t> occupation() {
+    std::vector<int8_t> occ((size_t)n_sites_ * n_chains_);
+    check(mg_ce_canon_get_occ(h_.get(), occ.data()));
+    return occ;
+  }
+  /* colouring `which` (0: even passes, 1: odd) and its list order */
+  std::vector<int32_t> colors(int which) const {
+    std::vector<int32_t> c((size_t)n_sites_);
+    check(mg_ce_canon_colors(h_.get(), which, c.data()));
+    return c;
+  }
+  std::vector<int32_t> class_order(int which) const {
+    std::vector<int32_t> o((size_t)n_sites_);
+    check(mg_ce_canon_class_order(h_.get(), which, o.data()));
+    return o;
+  }
+  float last_kernel_ms() const {
+    float ms = 0.f;
+    check(mg_ce_canon_last_kernel_ms(h_.get(), &ms));
+    return ms;
+  }
+  mg_ce_canon* get() const { return h_.get(); }
+
+ private:
+  using H = Handle<mg_ce_canon, mg_ce_canon_destroy>;
   H h_;
   int n_chains_;
   long long n_sites_;

@@ -66,3 +66,25 @@ def test_rotation_off_and_on_again():
     assert c.rotation()["ctas_fast"] == 0
     b.close()
     c.close()
+
+
+def test_autotune_with_rotation_keeps_results():
+    """The autotuner also times the rotated occupancy choice; whatever it keeps, the batch
+    continues exactly as an untuned, unrotated one."""
+    torch = pytest.importorskip("torch")
+    model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 6))
+    occ, T, mu, seeds = _inputs(seed=33)
+    tuned = clex.ChainBatch(model, (64, 64, 64), occ, T, mu, seeds)
+    plain = clex.ChainBatch(model, (64, 64, 64), occ, T, mu, seeds)
+    plain.set_rotation(False)
+    assert np.array_equal(tuned.run(3), plain.run(3))
+    choice = tuned.autotune(probe_passes=3)
+    assert choice["ms_per_pass"] > 0.0 and tuned.ctas_per_chain == choice["ctas_per_chain"]
+    rot = tuned.rotation()
+    if rot["ctas_fast"] > 0:
+        assert choice["layout"] == "word_specialised"
+    assert np.array_equal(tuned.occupation(), plain.occupation())
+    assert np.array_equal(tuned.run(40), plain.run(40))
+    assert np.array_equal(tuned.occupation(), plain.occupation())
+    tuned.close()
+    plain.close()
