@@ -381,6 +381,18 @@ class SemiGrandCanonicalCalculator:
         #: device time of the sweep kernels in the last run (ms)
         self.last_kernel_ms = 0.0
 
+    # construction steps a calculator of another ensemble replaces (clex.canonical)
+    def _conditions_from(self, values: ValueMap) -> SemiGrandCanonicalConditions:
+        return SemiGrandCanonicalConditions.from_values(values)
+
+    def _default_event_generator(self):
+        return SemiGrandCanonicalEventGenerator()
+
+    def _make_batch(self, state: ClexState, mu: np.ndarray, seed: int):
+        return ChainBatch(self.system.model, state.configuration.shape, state.configuration.occupation()[None, :],
+                          [self.conditions.temperature], mu, np.array([seed], dtype=np.uint64),
+                          precision=self.precision)
+
     def default_sampling_functions(self) -> StateSamplingFunctionMap:
         m = StateSamplingFunctionMap()
         model = self.system.model
@@ -417,10 +429,10 @@ class SemiGrandCanonicalCalculator:
         if sample_period < 1:
             raise RuntimeError("Error in SemiGrandCanonicalCalculator::run: sample_period must be >= 1")
         self.state = state
-        self.conditions = SemiGrandCanonicalConditions.from_values(state.conditions)
+        self.conditions = self._conditions_from(state.conditions)
         self.potential.set_state(state, self.conditions)
         if event_generator is None:
-            event_generator = SemiGrandCanonicalEventGenerator()
+            event_generator = self._default_event_generator()
         event_generator.set_state(state)
         N = state.configuration.n_variable_sites
         self.data = data = SemiGrandCanonicalData(sampling_functions, json_sampling_functions, N,
@@ -435,9 +447,7 @@ class SemiGrandCanonicalCalculator:
         seed = RandomNumberGenerator(random_engine).random_int(2**63 - 1)
         model = self.system.model
         mu = self.conditions.exchange_potential.reshape(1, -1)
-        batch = ChainBatch(model, state.configuration.shape, state.configuration.occupation()[None, :],
-                           [self.conditions.temperature], mu, np.array([seed], dtype=np.uint64),
-                           precision=self.precision)
+        batch = self._make_batch(state, mu, seed)
         self.last_kernel_ms = 0.0
         try:
             self._main_loop(batch, data, N, mu, sample_period, method_log, write_status_f, completion_check_params)
@@ -517,15 +527,13 @@ class SemiGrandCanonicalCalculator:
                 raise RuntimeError("Error in SemiGrandCanonicalCalculator::run_fixtures: the GPU sweep proposes whole "
                                    "passes; sampling fixtures must sample by pass")
         self.state = state
-        self.conditions = SemiGrandCanonicalConditions.from_values(state.conditions)
+        self.conditions = self._conditions_from(state.conditions)
         self.potential.set_state(state, self.conditions)
         model = self.system.model
         N = state.configuration.n_variable_sites
         mu = self.conditions.exchange_potential.reshape(1, -1)
         seed = RandomNumberGenerator(run_manager.engine).random_int(2**63 - 1)
-        batch = ChainBatch(model, state.configuration.shape, state.configuration.occupation()[None, :],
-                           [self.conditions.temperature], mu, np.array([seed], dtype=np.uint64),
-                           precision=self.precision)
+        batch = self._make_batch(state, mu, seed)
         fixtures = run_manager.sampling_fixtures
         self.last_kernel_ms = 0.0
         try:

@@ -31,3 +31,15 @@ def test_conditions_and_composition():
     assert x.n_independent_compositions() == 2
     assert np.array_equal(x.per_supercell(), [3.0, 2.0])
     assert np.array_equal(x.occ_delta_per_supercell([0, 2], [2, 1]), [1.0, 0.0])
+
+
+def test_canonical_conditions_and_calculator_construction():
+    import casmcode_monte_gb300.clex.canonical as can
+
+    c = can.CanonicalConditions.from_values(monte.ValueMap.from_dict({"temperature": 900.0, "other": 1.0}))
+    assert c.temperature == 900.0 and c.to_dict() == {"temperature": 900.0}
+    assert can.CanonicalConditions.from_dict({"temperature": 5.0}).temperature == 5.0
+    with pytest.raises(RuntimeError, match="temperature"):
+        can.CanonicalConditions.from_values(monte.ValueMap())
+    with pytest.raises(RuntimeError):
+        can.CanonicalCalculator(None)
