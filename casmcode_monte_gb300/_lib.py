@@ -76,6 +76,13 @@ SIGNATURES = {
     "mg_ce_canon_get_occ": (C.c_int, [vp, c_int8_p]),
     "mg_ce_canon_corr": (C.c_int, [vp, c_ll_p]),
     "mg_ce_canon_destroy": (C.c_int, [vp]),
+    "mg_ce_nfold_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p, c_double_p, c_uint64_p,
+                                     c_uint32_p, c_int8_p, vpp]),
+    "mg_ce_nfold_run": (C.c_int, [vp, C.c_int, c_double_p]),
+    "mg_ce_nfold_last_kernel_ms": (C.c_int, [vp, c_float_p]),
+    "mg_ce_nfold_get_occ": (C.c_int, [vp, c_int8_p]),
+    "mg_ce_nfold_corr": (C.c_int, [vp, C.c_int, c_ll_p]),
+    "mg_ce_nfold_destroy": (C.c_int, [vp]),
     "mg_ce_batch_get_occ": (C.c_int, [vp, c_int8_p]),
     "mg_ce_batch_set_occ": (C.c_int, [vp, c_int8_p]),
     "mg_ce_batch_corr": (C.c_int, [vp, c_ll_p]),

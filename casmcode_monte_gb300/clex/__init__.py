@@ -348,6 +348,69 @@ class CanonicalBatch:
         return order
 
 
+class NfoldBatch:
+    """Chains of one binary L0 x L1 x L2 supercell run by rejection-free (N-fold way)
+    semi-grand canonical dynamics on the GPU (handle to mg_ce_nfold): an event selector for
+    the loop of methods.nfold, every event a single-site flip chosen with probability
+    proportional to its Metropolis rate, residence times -ln(u) / R.  At most 32768 sites.
+
+    ``run(n)`` returns [n, n_chains, n_classes + 2] float64: per pass (N events) its time,
+    the total rate at its end, and the time-weighted integer correlation sums.
+    """
+
+    def __init__(self, model: ClexModel, shape: Sequence[int], occ, temperature, mu, seeds, chain_ids=None):
+        self.model = model
+        self.shape = tuple(int(x) for x in shape)
+        L0, L1, L2 = self.shape
+        self.n_sites = L0 * L1 * L2
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int8).reshape(-1, self.n_sites))
+        self.n_chains = occ.shape[0]
+        T = np.ascontiguousarray(np.asarray(temperature, dtype=np.float64).reshape(self.n_chains))
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64).reshape(self.n_chains, model.n_species - 1))
+        seeds = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(self.n_chains))
+        ids = None
+        if chain_ids is not None:
+            ids = np.ascontiguousarray(np.asarray(chain_ids, dtype=np.uint32).reshape(self.n_chains))
+        self.temperature, self.mu, self.seeds = T, mu, seeds
+        h = C.c_void_p()
+        _lib.check(_lib.lib().mg_ce_nfold_create(
+            model._h, L0, L1, L2, self.n_chains, _lib.ptr(T, C.c_double), _lib.ptr(mu, C.c_double),
+            _lib.ptr(seeds, C.c_uint64), _lib.ptr(ids, C.c_uint32) if ids is not None else None,
+            _lib.ptr(occ, C.c_int8), C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.mg_ce_nfold_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, n_passes: int) -> np.ndarray:
+        if int(n_passes) < 0:
+            raise RuntimeError("Error in mg_ce_nfold_run: invalid argument")
+        out = np.zeros((n_passes, self.n_chains, self.model.n_classes + 2), dtype=np.float64)
+        _lib.check(_lib.lib().mg_ce_nfold_run(self._h, int(n_passes), _lib.ptr(out, C.c_double)))
+        return out
+
+    def last_kernel_ms(self) -> float:
+        ms = C.c_float()
+        _lib.check(_lib.lib().mg_ce_nfold_last_kernel_ms(self._h, C.byref(ms)))
+        return float(ms.value)
+
+    def occupation(self) -> np.ndarray:
+        occ = np.zeros((self.n_chains, self.n_sites), dtype=np.int8)
+        _lib.check(_lib.lib().mg_ce_nfold_get_occ(self._h, _lib.ptr(occ, C.c_int8)))
+        return occ
+
+    def corr(self, recompute: bool = False) -> np.ndarray:
+        out = np.zeros((self.n_chains, self.model.n_classes), dtype=np.int64)
+        _lib.check(_lib.lib().mg_ce_nfold_corr(self._h, 1 if recompute else 0, _lib.ptr(out, C.c_longlong)))
+        return out
+
+
 class PoolFull(RuntimeError):
     """Admission refused: no free chain slot or not enough arena memory."""
 
@@ -511,5 +574,5 @@ def random_occupation(n_species: int, n_sites: int, rng: np.random.Generator,
     return occ
 
 
-__all__ = ["ClexModel", "ChainBatch", "CanonicalBatch", "ChainPool", "PoolFull", "SweepSamples", "accumulate", "basis_description", "make_eci",
+__all__ = ["ClexModel", "ChainBatch", "CanonicalBatch", "NfoldBatch", "ChainPool", "PoolFull", "SweepSamples", "accumulate", "basis_description", "make_eci",
            "random_occupation", "KB"]

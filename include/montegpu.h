@@ -189,6 +189,26 @@ int mg_ce_canon_get_occ(mg_ce_canon* h, int8_t* occ);
 /* integer correlation sums [n_chains][n_classes] from a full recompute */
 int mg_ce_canon_corr(mg_ce_canon* h, long long* corr);
 int mg_ce_canon_destroy(mg_ce_canon* h);
+
+/* ---- FCC cluster expansion (binary basis): rejection-free (N-fold way) dynamics ----
+ * An event selector for the loop of include/casm/monte/methods/nfold.hh:48-149 (which takes
+ * the selector from the caller) run on the GPU for semi-grand canonical single-site flips:
+ * rate of flipping site l = min(1, exp(-beta dE_l)), an event chosen with probability
+ * rate / R, the residence time -ln(u) / R.  One CTA per chain (at most 32768 sites: the
+ * rates and their sums live in shared memory).  A pass is N events; out receives per pass
+ * and chain [2 + n_classes] doubles: the pass's time, the total rate at its end, and the
+ * time-weighted sums of the integer correlation sums (time averages are these over the
+ * time).  Same conventions as mg_ce_batch_create otherwise. */
+typedef struct mg_ce_nfold mg_ce_nfold;
+int mg_ce_nfold_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chains,
+                       const double* temperature, const double* mu, const uint64_t* seeds,
+                       const uint32_t* chain_ids, const int8_t* occ, mg_ce_nfold** out);
+int mg_ce_nfold_run(mg_ce_nfold* h, int n_passes, double* out);
+int mg_ce_nfold_last_kernel_ms(const mg_ce_nfold* h, float* ms);
+int mg_ce_nfold_get_occ(mg_ce_nfold* h, int8_t* occ);
+/* integer correlation sums [n_chains][n_classes]: tracked (recompute 0) or recomputed */
+int mg_ce_nfold_corr(mg_ce_nfold* h, int recompute, long long* corr);
+int mg_ce_nfold_destroy(mg_ce_nfold* h);
 int mg_ce_batch_get_occ(mg_ce_batch* b, int8_t* occ);
 int mg_ce_batch_set_occ(mg_ce_batch* b, const int8_t* occ);
 /* full recompute of the integer correlation sums [n_chains][n_classes] */

@@ -501,4 +501,57 @@ long long orc_ce_canonical_samples(void* h, int* occ, double T, unsigned long lo
   return nacc;
 }
 
+// Rejection-free (N-fold way) semi-grand canonical dynamics on the CPU: the loop of
+// methods/nfold.hh:48-149 with an event selector over single-site flips of Metropolis rate
+// min(1, exp(-beta dE)) (FP64, delta_formation), chosen by a Fenwick tree of the rates;
+// after a flip the rates of the sites sharing a cluster with it (and its own) are
+// recomputed.  Used as the timed CPU baseline of the GPU selector.  Returns the events run;
+// *seconds = wall time, *time_out = the simulated time.
+long long orc_ce_nfold_run(void* h, int* occ, double T, const double* mu, int n_mu, unsigned long long seed,
+                           long long n_events, double* seconds, double* time_out) {
+  auto* S = static_cast<CESupercell*>(h);
+  if (S->basis.n_species != 2 || n_mu != 1) return -1;
+  std::vector<double> m(mu, mu + n_mu);
+  const double beta = 1.0 / (KB * T);
+  const long N = S->n();
+  const long ns = (long)S->slots.size();
+  std::mt19937_64 e(seed);
+  RNG rng{&e};
+  std::vector<double> rate(N), tree(N + 1, 0.0);
+  auto set_rate = [&](long l, double r) {
+    const double d = r - rate[l];
+    rate[l] = r;
+    for (long x = l + 1; x <= N; x += x & -x) tree[x] += d;
+  };
+  auto site_rate = [&](long l) {
+    const double dE = S->delta_formation(occ, l, 1 - occ[l]) - S->mu_dot_Ndx(m, occ[l], 1 - occ[l]);
+    return dE <= 0.0 ? 1.0 : std::exp(-beta * dE);
+  };
+  for (long l = 0; l < N; ++l) set_rate(l, site_rate(l));
+  long top = 1;
+  while (top * 2 <= N) top *= 2;
+  const auto t0 = std::chrono::steady_clock::now();
+  double time = 0.0;
+  for (long long ev = 0; ev < n_events; ++ev) {
+    double R = 0.0;
+    for (long x = N; x > 0; x -= x & -x) R += tree[x];
+    double target = rng.random_real(R);
+    long pos = 0;
+    for (long step = top; step > 0; step >>= 1)
+      if (pos + step <= N && tree[pos + step] <= target) {
+        pos += step;
+        target -= tree[pos];
+      }
+    const long l = std::min(pos, N - 1);
+    time += -std::log(1.0 - rng.random_real(1.0)) / R;
+    occ[l] = 1 - occ[l];
+    set_rate(l, site_rate(l));
+    const int32_t* nb = S->nbr.data() + l * ns;
+    for (long q = 0; q < ns; ++q) set_rate(nb[q], site_rate(nb[q]));
+  }
+  *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  *time_out = time;
+  return n_events;
+}
+
 }  // extern "C"

@@ -81,6 +81,9 @@ def load():
         L.orc_ce_canonical_samples.restype = C.c_longlong
         L.orc_ce_canonical_samples.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.c_ulonglong, C.c_long,
                                                C.POINTER(C.c_double)]
+        L.orc_ce_nfold_run.restype = C.c_longlong
+        L.orc_ce_nfold_run.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int,
+                                       C.c_ulonglong, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_ce_random_site_run.restype = C.c_longlong
         L.orc_ce_random_site_run.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int,
                                              C.c_ulonglong, C.c_longlong, C.POINTER(C.c_double)]
@@ -223,6 +226,16 @@ class OracleCE:
                                          n_passes, p(e, C.c_double), p(x, C.c_double))
         assert nacc >= 0
         return e, x, nacc
+
+    def nfold_run(self, occ, T, mu, seed, n_events):
+        """The N-fold way on the CPU (binary): final occupation, wall seconds, simulated time."""
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64))
+        secs, t = C.c_double(), C.c_double()
+        n = load().orc_ce_nfold_run(self.h, p(occ, C.c_int), T, p(mu, C.c_double), mu.size, C.c_ulonglong(seed),
+                                    C.c_longlong(n_events), C.byref(secs), C.byref(t))
+        assert n == n_events
+        return occ, secs.value, t.value
 
     def random_site_run(self, occ, T, mu, seed, n_steps):
         occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
