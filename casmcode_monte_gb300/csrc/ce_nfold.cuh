@@ -223,18 +223,19 @@ __global__ void __launch_bounds__(NT, 1) ce_nfold_kernel(const __grid_constant__
         }
       }
       __syncthreads();
-      // 2. the residence time of the current state, and the sites the flip affects
+      // 2. thread 0: the residence time of the current state weights its correlation sums,
+      // then the flip and its exact correlation change; the other threads: the sites the flip
+      // affects (itself and the sites sharing a cluster with it)
       const int l = sel_sm;
-      if (threadIdx.x < NC) tw_sm[threadIdx.x] += (double)dt_sm * (double)corr_sm[threadIdx.x];
-      if (threadIdx.x == NC) time_sm += (double)dt_sm;
-      if (threadIdx.x < NAFF)
-        aff[threadIdx.x] = threadIdx.x == 0 ? l
-                                            : site.neighbour(l, A.offs[3 * (threadIdx.x - 1)],
-                                                             A.offs[3 * (threadIdx.x - 1) + 1],
-                                                             A.offs[3 * (threadIdx.x - 1) + 2]);
-      __syncthreads();
-      // 3. the flip and its exact correlation change (one thread)
+      if (threadIdx.x > 0 && threadIdx.x <= NFOLD_NOFF)
+        aff[threadIdx.x] = site.neighbour(l, A.offs[3 * (threadIdx.x - 1)], A.offs[3 * (threadIdx.x - 1) + 1],
+                                          A.offs[3 * (threadIdx.x - 1) + 2]);
       if (threadIdx.x == 0) {
+        aff[0] = l;
+        const double dt = (double)dt_sm;
+        time_sm += dt;
+#pragma unroll
+        for (int f = 0; f < NC; ++f) tw_sm[f] += dt * (double)corr_sm[f];
         const uint32_t ent = site.entry(l);
         int o;
         int F[B::NFEAT];
@@ -248,17 +249,17 @@ __global__ void __launch_bounds__(NT, 1) ce_nfold_kernel(const __grid_constant__
         sw.store(ent, B::code_of_occ(o2));
       }
       __syncthreads();
-      // 4. new rates of the affected sites
+      // 3. new rates of the affected sites
       if (threadIdx.x < NAFF) rate[aff[threadIdx.x]] = site.rate(aff[threadIdx.x]);
       __syncthreads();
-      // 5. their blocks' sums (a block met twice gets the same value twice)
+      // 4. their blocks' sums (a block met twice gets the same value twice)
       for (int a = warp; a < NAFF; a += NW) {
         const int bidx = aff[a] >> 5;
         const float v = warp_sum_f(rate[bidx * 32 + lane]);
         if (lane == 0) block_sum[bidx] = v;
       }
       __syncthreads();
-      // 6. their superblocks' sums
+      // 5. their superblocks' sums
       for (int a = warp; a < NAFF; a += NW) {
         const int q = aff[a] >> 10;
         const float v = warp_sum_f(block_sum[q * 32 + lane]);
