@@ -404,14 +404,14 @@ def run_canonical(args) -> None:
         print(json.dumps(line), flush=True)
 
 
-NFOLD_L = 32
-NFOLD_METRIC = "rejection-free (N-fold way) events/s (FCC 32^3 binary CE)"
+NFOLD_METRIC = "rejection-free (N-fold way) events/s (FCC binary CE)"
 
 
 def run_nfold(args) -> None:
-    """Rejection-free semi-grand canonical dynamics: one chain per SM of binary FCC 32^3
-    (32,768 sites, 50 % B by a seeded shuffle), T linspace(300, 2000), mu = 0; a step is one
-    event (a selected flip with its rate updates) of every chain.  value: events / CUDA-event
+    """Rejection-free semi-grand canonical dynamics of binary FCC L^3 chains (--nfold-size L,
+    default 32: 32,768 sites, one chain per SM; up to 8192 sites four chains per SM), 50 % B
+    by a seeded shuffle, T linspace(300, 2000), mu = 0; a step is one event (a selected flip
+    with its rate updates) of every chain.  value: events / CUDA-event
     time; cpu_baseline: the same dynamics on the CPU (oracle: FP64 rates, Fenwick selection)
     on one host core."""
     import torch
@@ -420,16 +420,20 @@ def run_nfold(args) -> None:
 
     rank, world, local = _env_rank()
     torch.cuda.set_device(local)
-    n_chains = torch.cuda.get_device_properties(local).multi_processor_count
+    L_n = int(args.nfold_size)
+    n = L_n**3
     eci = clex.make_eci("fcc_binary", 1)
     model = clex.ClexModel("fcc_binary", eci)
+    # chains resident per SM for this size (4 up to 8192 sites), one chain per resident slot
+    probe = clex.NfoldBatch(model, (L_n,) * 3, np.zeros((1, n), dtype=np.int8), [1000.0], [[0.0]], [1])
+    n_chains = torch.cuda.get_device_properties(local).multi_processor_count * probe.chains_per_sm
+    probe.close()
     rng = np.random.default_rng(3000 + rank)
-    n = NFOLD_L**3
     occ = np.stack([clex.random_occupation(2, n, rng) for _ in range(n_chains)])
     T = np.linspace(300.0, 2000.0, n_chains)
     mu = np.zeros((n_chains, 1))
     seeds = np.arange(1, n_chains + 1, dtype=np.uint64) * np.uint64(0x2545F491) + np.uint64(rank)
-    batch = clex.NfoldBatch(model, (NFOLD_L,) * 3, occ, T, mu, seeds)
+    batch = clex.NfoldBatch(model, (L_n,) * 3, occ, T, mu, seeds)
     warm = max(1, args.warmup // n)  # passes of N events
     batch.run(warm)
     passes = max(1, args.steps // n)
@@ -443,19 +447,20 @@ def run_nfold(args) -> None:
             "steps": passes * n, "warmup": warm * n, "ms_per_step": kernel_ms / (passes * n),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 rates, i64 correlations",
             "data": "synthetic",
-            "config": {"workload": "fcc32_binary_ce_nfold", "supercell": [NFOLD_L] * 3, "chains": n_chains,
+            "config": {"workload": f"fcc{L_n}_binary_ce_nfold", "supercell": [L_n] * 3, "chains": n_chains,
+                       "chains_per_sm": batch.chains_per_sm, "threads_per_cta": batch.threads,
                        "events_per_pass": n, "passes": passes},
             "gpu_launches": passes}
     if rank == 0 and args.cpu_seconds > 0:
         from tests import oracle_lib
 
-        orc = oracle_lib.OracleCE((NFOLD_L,) * 3, 2, eci)
+        orc = oracle_lib.OracleCE((L_n,) * 3, 2, eci)
         o = occ[0].astype(np.int32)
         _, secs, _ = orc.nfold_run(o, float(T[n_chains // 2]), mu[0], 5, 2000)
         n_ev = int(max(2000, 2000 * args.cpu_seconds / max(secs, 1e-9)))
         _, secs, _ = orc.nfold_run(o, float(T[n_chains // 2]), mu[0], 6, n_ev)
         line["cpu_baseline"] = {"value": n_ev / secs, "unit": "events/s", "cores": 1, "kind": "port",
-                                "sample": f"{n_ev} events on one 32^3 chain at T={T[n_chains // 2]:.0f} K "
+                                "sample": f"{n_ev} events on one {L_n}^3 chain at T={T[n_chains // 2]:.0f} K "
                                           "(oracle: FP64 rates, Fenwick selection, g++ -O2)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -471,6 +476,7 @@ def main():
     ap.add_argument("--ctas-per-chain", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-steps-per-sample", type=float, default=2e6)
+    ap.add_argument("--nfold-size", type=int, default=32, help="supercell edge of the nfold workload")
     ap.add_argument("--workload", default="fcc64_sgc", choices=["fcc64_sgc", "canonical", "nfold"],
                     help="fcc64_sgc: the headline semi-grand canonical pass; canonical: fixed-composition "
                          "sweeps of 48^3 chains; nfold: rejection-free dynamics of 32^3 chains")

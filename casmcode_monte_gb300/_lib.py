@@ -79,6 +79,7 @@ SIGNATURES = {
     "mg_ce_nfold_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p, c_double_p, c_uint64_p,
                                      c_uint32_p, c_int8_p, vpp]),
     "mg_ce_nfold_run": (C.c_int, [vp, C.c_int, c_double_p]),
+    "mg_ce_nfold_info": (C.c_int, [vp, c_int_p, c_int_p, c_size_p]),
     "mg_ce_nfold_last_kernel_ms": (C.c_int, [vp, c_float_p]),
     "mg_ce_nfold_get_occ": (C.c_int, [vp, c_int8_p]),
     "mg_ce_nfold_corr": (C.c_int, [vp, C.c_int, c_ll_p]),

@@ -378,6 +378,9 @@ class NfoldBatch:
             _lib.ptr(seeds, C.c_uint64), _lib.ptr(ids, C.c_uint32) if ids is not None else None,
             _lib.ptr(occ, C.c_int8), C.byref(h)))
         self._h = h
+        nt, cps, sm = C.c_int(), C.c_int(), C.c_size_t()
+        _lib.check(_lib.lib().mg_ce_nfold_info(self._h, C.byref(nt), C.byref(cps), C.byref(sm)))
+        self.threads, self.chains_per_sm, self.smem_bytes = nt.value, cps.value, sm.value
 
     def close(self) -> None:
         h = getattr(self, "_h", None)

@@ -16,6 +16,7 @@ struct mg_ce_nfold {
   int L0 = 0, L1 = 0, L2 = 0, n_chains = 0, n_super = 0;
   long long N = 0, events = 0;
   size_t smem = 0;
+  bool small = false;  // the 128-thread instance
   mg::CeChainParams* dcp = nullptr;
   int8_t* docc = nullptr;
   long long* dcorr = nullptr;
@@ -31,7 +32,11 @@ namespace {
 using mg::set_error;
 using namespace mg::host;
 
+// Instances: 512 threads and one chain per SM; for supercells of at most kSmallSites sites,
+// 128 threads and four chains per SM (at most 128 registers a thread, a quarter of the SM's
+// shared memory each)
 constexpr int kNtNfold = 512;
+constexpr int kNtNfoldSmall = 128, kChainsPerSmSmall = 4, kSmallSites = 8192;
 
 void free_nfold(mg_ce_nfold* h) {
   if (!h) return;
@@ -116,6 +121,7 @@ int mg_ce_nfold_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   h->n_chains = n_chains;
   h->n_super = n_super;
   h->smem = smem;
+  h->small = N <= kSmallSites && kChainsPerSmSmall * (smem + 1024) <= (size_t)max_smem;
   std::vector<mg::CeChainParams> cp(n_chains);
   make_chain_params(m, n_chains, temperature, mu, seeds, chain_ids, cp.data());
   auto fail = [&](cudaError_t e, const char* what) {
@@ -182,16 +188,29 @@ int mg_ce_nfold_run(mg_ce_nfold* h, int n_passes, double* out) {
     return MG_ERR_INVALID;
   }
   std::memcpy(A.offs, off, sizeof(int) * 3 * noff);
-  auto kern = mg::ce_nfold_kernel<mg::FccBinary, kNtNfold>;
+  auto kern = h->small ? mg::ce_nfold_kernel<mg::FccBinary, kNtNfoldSmall, kChainsPerSmSmall>
+                       : mg::ce_nfold_kernel<mg::FccBinary, kNtNfold, 1>;
+  const int nt = h->small ? kNtNfoldSmall : kNtNfold;
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
   MG_CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
-  kern<<<h->n_chains, kNtNfold, h->smem, h->stream>>>(A);
+  kern<<<h->n_chains, nt, h->smem, h->stream>>>(A);
   MG_CUDA_TRY(cudaGetLastError());
   MG_CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, h->dout, sizeof(double) * need, cudaMemcpyDeviceToHost, h->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(h->stream));
   MG_CUDA_TRY(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
   h->events += (long long)n_passes * h->N;
+  return MG_OK;
+}
+
+int mg_ce_nfold_info(const mg_ce_nfold* h, int* threads, int* chains_per_sm, size_t* smem_bytes) {
+  if (!h) {
+    set_error("Error in mg_ce_nfold_info: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  if (threads) *threads = h->small ? kNtNfoldSmall : kNtNfold;
+  if (chains_per_sm) *chains_per_sm = h->small ? kChainsPerSmSmall : 1;
+  if (smem_bytes) *smem_bytes = h->smem;
   return MG_OK;
 }
 

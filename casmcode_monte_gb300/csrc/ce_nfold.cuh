@@ -119,8 +119,10 @@ struct NfoldSite {
   }
 };
 
-template <class B, int NT>
-__global__ void __launch_bounds__(NT, 1) ce_nfold_kernel(const __grid_constant__ CeNfoldArgs<B::NFEAT> A) {
+// NT threads per chain, MINB chains resident per SM (the small instance keeps several chains
+// of a small supercell on one SM, so that their sequential events overlap)
+template <class B, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) ce_nfold_kernel(const __grid_constant__ CeNfoldArgs<B::NFEAT> A) {
   static_assert(B::NSPECIES == 2, "the rejection-free sweep flips binary sites");
   constexpr int NC = B::NCLASS;
   constexpr int NW = NT / 32;

@@ -195,7 +195,7 @@ int mg_ce_canon_destroy(mg_ce_canon* h);
  * the selector from the caller) run on the GPU for semi-grand canonical single-site flips:
  * rate of flipping site l = min(1, exp(-beta dE_l)), an event chosen with probability
  * rate / R, the residence time -ln(u) / R.  One CTA per chain (at most 32768 sites: the
- * rates and their sums live in shared memory).  A pass is N events; out receives per pass
+ * rates and their sums live in shared memory; four chains share an SM up to 8192 sites).  A pass is N events; out receives per pass
  * and chain [2 + n_classes] doubles: the pass's time, the total rate at its end, and the
  * time-weighted sums of the integer correlation sums (time averages are these over the
  * time).  Same conventions as mg_ce_batch_create otherwise. */
@@ -204,6 +204,9 @@ int mg_ce_nfold_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
                        const double* temperature, const double* mu, const uint64_t* seeds,
                        const uint32_t* chain_ids, const int8_t* occ, mg_ce_nfold** out);
 int mg_ce_nfold_run(mg_ce_nfold* h, int n_passes, double* out);
+/* threads per chain, chains resident per SM (4 for supercells of at most 8192 sites, else 1),
+ * dynamic shared bytes per chain */
+int mg_ce_nfold_info(const mg_ce_nfold* h, int* threads, int* chains_per_sm, size_t* smem_bytes);
 int mg_ce_nfold_last_kernel_ms(const mg_ce_nfold* h, float* ms);
 int mg_ce_nfold_get_occ(mg_ce_nfold* h, int8_t* occ);
 /* integer correlation sums [n_chains][n_classes]: tracked (recompute 0) or recomputed */

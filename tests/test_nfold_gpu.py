@@ -21,17 +21,18 @@ pytestmark = pytest.mark.gpu
 KB = 8.6173303e-05
 
 
-def test_nfold_tracks_correlations_and_total_rate(gpu_lib):
-    L = (8, 8, 12)
-    N = 8 * 8 * 12
+@pytest.mark.parametrize("L,small", [((8, 8, 12), True), ((24, 24, 24), False)])
+def test_nfold_tracks_correlations_and_total_rate(gpu_lib, L, small):
+    N = L[0] * L[1] * L[2]
     model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 2))
     rng = np.random.default_rng(4)
     occ = np.stack([clex.random_occupation(2, N, rng) for _ in range(2)])
     T = np.array([900.0, 1600.0])
     mu = np.array([[0.0], [0.03]])
     b = clex.NfoldBatch(model, L, occ, T, mu, [11, 12])
+    assert (b.chains_per_sm, b.threads) == ((4, 128) if small else (1, 512))
     assert np.array_equal(b.corr(), b.corr(recompute=True))
-    out = b.run(6)
+    out = b.run(6 if small else 1)
     assert (out[:, :, 0] > 0).all()
     assert np.array_equal(b.corr(), b.corr(recompute=True))
     final = b.occupation()
