@@ -210,6 +210,51 @@ class CeCanon {
   int n_slots_;
 };
 
+/* Rejection-free (N-fold way) dynamics of binary chains (mg_ce_nfold_*): per pass of N
+ * events the pass's time, the total rate at its end and the time-weighted correlation sums. */
+class CeNfold {
+ public:
+  CeNfold(const CeModel& m, int L0, int L1, int L2, const std::vector<double>& temperature,
+          const std::vector<double>& mu, const std::vector<uint64_t>& seeds, const std::vector<int8_t>& occ)
+      : n_chains_((int)temperature.size()), n_sites_((long long)L0 * L1 * L2), n_slots_(m.n_classes() + 2),
+        n_classes_(m.n_classes()) {
+    mg_ce_nfold* h = nullptr;
+    check(mg_ce_nfold_create(m.get(), L0, L1, L2, n_chains_, temperature.data(), mu.data(), seeds.data(), nullptr,
+                             occ.data(), &h));
+    h_ = H(h);
+  }
+  /* [n_passes][n_chains][n_classes + 2] */
+  std::vector<double> run(int n_passes) {
+    std::vector<double> out((size_t)n_passes * n_chains_ * n_slots_);
+    check(mg_ce_nfold_run(h_.get(), n_passes, out.data()));
+    return out;
+  }
+  std::vector<int8_t> occupation() {
+    std::vector<int8_t> occ((size_t)n_sites_ * n_chains_);
+    check(mg_ce_nfold_get_occ(h_.get(), occ.data()));
+    return occ;
+  }
+  /* integer correlation sums [n_chains][n_classes], tracked or recomputed */
+  std::vector<long long> corr(bool recompute = false) {
+    std::vector<long long> c((size_t)n_chains_ * n_classes_);
+    check(mg_ce_nfold_corr(h_.get(), recompute ? 1 : 0, c.data()));
+    return c;
+  }
+  float last_kernel_ms() const {
+    float ms = 0.f;
+    check(mg_ce_nfold_last_kernel_ms(h_.get(), &ms));
+    return ms;
+  }
+  mg_ce_nfold* get() const { return h_.get(); }
+
+ private:
+  using H = Handle<mg_ce_nfold, mg_ce_nfold_destroy>;
+  H h_;
+  int n_chains_;
+  long long n_sites_;
+  int n_slots_, n_classes_;
+};
+
 /* The sweep's colouring of a supercell (host only): colours per site, number of
  * colours, layout (0 byte, 1 word, 2 pipelined word). */
 struct Colouring {
