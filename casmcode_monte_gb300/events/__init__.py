@@ -31,6 +31,7 @@ sweeps of ``casmcode_monte_gb300.clex`` do not need them.
 """
 from __future__ import annotations
 
+import copy
 import itertools
 from dataclasses import dataclass, field
 from typing import Optional, Sequence
@@ -729,7 +730,12 @@ class OccLocation:
     """Occupant locations by candidate type (OccLocation.hh:44-385): ``mol(i)`` per
     variable site, ``mol_id(cand, loc)`` lists per candidate, swap-remove updates."""
 
-    def __init__(self, convert: Conversions, candidate_list: OccCandidateList, update_atoms: bool = False):
+    def __init__(self, convert: Conversions, candidate_list: OccCandidateList, update_atoms: bool = False,
+                 track_unique_atoms: bool = False, save_atom_info: bool = False):
+        """OccLocation.cc:14-29: ``update_atoms`` tracks atom trajectories through
+        ``apply``; ``track_unique_atoms`` gives every atom that enters the supercell a
+        unique id (atoms may come from or go to a reservoir); ``save_atom_info`` keeps the
+        initial and final position, species and time of atoms added and removed."""
         self._convert = convert
         self._cand_list = candidate_list
         self._loc = [[] for _ in range(len(candidate_list))]
@@ -737,13 +743,30 @@ class OccLocation:
         self._l_to_mol: list = []
         self._atoms: list = []
         self._update_atoms = bool(update_atoms)
+        self._track_unique_atoms = bool(track_unique_atoms)
+        self._save_atom_info = bool(save_atom_info)
+        self._initial_atom_species_index: list = []
+        self._initial_atom_position_index: list = []
+        self._available_atom_id: set = set()
+        self._next_unique_atom_id = 0
+        self._unique_atom_id: list = []
+        self._atom_info_initial: dict = {}
+        self._atom_info_final: dict = {}
 
-    def initialize(self, occupation) -> None:
-        """OccLocation.cc:37-108."""
+    def initialize(self, occupation, time: Optional[float] = None) -> None:
+        """OccLocation.cc:37-108 (with ``save_atom_info`` and a time, the initial atom
+        info of every atom is stored with that time)."""
         occupation = np.asarray(occupation)
         conv, cl = self._convert, self._cand_list
         self._mol, self._atoms = [], []
+        self._initial_atom_species_index, self._initial_atom_position_index = [], []
         self._loc = [[] for _ in range(len(cl))]
+        if self._update_atoms and self._track_unique_atoms:
+            self._available_atom_id = set()
+            self._next_unique_atom_id = 0
+            self._unique_atom_id = []
+            if self._save_atom_info:
+                self._atom_info_initial, self._atom_info_final = {}, {}
         n = occupation.size
         variable = [conv.occ_size(conv.l_to_asym(l)) > 1 for l in range(n)]
         n_mut = sum(variable)
@@ -757,21 +780,45 @@ class OccLocation:
             ci = cl.index(asym, sp)
             mol = Mol(id=len(self._mol), l=l, asym=asym, species_index=sp, loc=len(self._loc[ci]))
             if self._update_atoms:
-                for _ in range(conv.components_size(sp)):
+                for atom_index in range(conv.components_size(sp)):
                     mol.component.append(len(self._atoms))
-                    self._atoms.append(Atom(translation=conv.l_to_ijk(l), n_jumps=0))
+                    atom = Atom(translation=conv.l_to_ijk(l), n_jumps=0)
+                    self._atoms.append(atom)
+                    if self._track_unique_atoms:
+                        self._unique_atom_id.append(self._next_unique_atom_id)
+                        if self._save_atom_info and time is not None:
+                            self._atom_info_initial.setdefault(
+                                self._next_unique_atom_id, AtomInfo(copy.deepcopy(atom), sp, atom_index, float(time)))
+                        self._next_unique_atom_id += 1
+                    self._initial_atom_species_index.append(sp)
+                    self._initial_atom_position_index.append(atom_index)
             self._loc[ci].append(mol.id)
             self._l_to_mol.append(mol.id)
             self._mol.append(mol)
 
-    def apply(self, e: OccEvent, occupation: np.ndarray) -> None:
-        """Update the occupation vector (in place) and the lists for event e
-        (OccLocation.cc:212-283, occupant part; atoms move with their molecules)."""
+    def apply(self, e: OccEvent, occupation: np.ndarray, time: Optional[float] = None) -> None:
+        """Update the occupation vector (in place), the lists and the atoms for event e
+        (OccLocation.cc:212-366).  An atom trajectory from or to position l == -1 is a move
+        from or to the reservoir (whose mol_id is the species index); with
+        ``track_unique_atoms`` an atom leaving frees its atom id (the smallest free id is
+        reused first) and an entering atom gets the next unique id, its species index taken
+        from ``to.mol_id`` as the reference does; with ``save_atom_info`` and a time the
+        final (leaving) and initial (entering) atom info is stored."""
         conv, cl = self._convert, self._cand_list
         moving = []
         if self._update_atoms:
             for t in e.atom_traj:
-                moving.append(self._mol[t.from_.mol_id].component[t.from_.mol_comp])
+                if t.from_.l == -1:
+                    moving.append(-1)  # from the reservoir: a new atom
+                    continue
+                mol = self._mol[t.from_.mol_id]
+                atom_id = mol.component[t.from_.mol_comp]
+                if self._track_unique_atoms and t.to.l == -1 and self._save_atom_info and time is not None:
+                    self._atom_info_final.setdefault(
+                        self._unique_atom_id[atom_id],
+                        AtomInfo(copy.deepcopy(self._atoms[atom_id]), mol.species_index, t.from_.mol_comp,
+                                 float(time)))
+                moving.append(atom_id)
         for t in e.occ_transform:
             mol = self._mol[t.mol_id]
             if mol.species_index != t.from_species:
@@ -789,8 +836,43 @@ class OccLocation:
             ci = cl.index(mol.asym, mol.species_index)
             mol.loc = len(self._loc[ci])
             self._loc[ci].append(mol.id)
-        if self._update_atoms:
+        if not self._update_atoms:
+            return
+        if self._track_unique_atoms:
+            lmin = np.iinfo(np.int64).min
             for atom_id, t in zip(moving, e.atom_traj):
+                if t.to.l == -1 and t.from_.l != -1:  # to the reservoir
+                    self._atoms[atom_id].translation = np.array([lmin, lmin, lmin], dtype=np.int64)
+                    self._atoms[atom_id].n_jumps = lmin
+                    self._unique_atom_id[atom_id] = -1
+                    self._initial_atom_species_index[atom_id] = -1
+                    self._initial_atom_position_index[atom_id] = -1
+                    self._available_atom_id.add(atom_id)
+            for t in e.atom_traj:
+                if t.to.l != -1 and t.from_.l == -1:  # from the reservoir
+                    atom = Atom(translation=conv.l_to_ijk(t.to.l), n_jumps=0)
+                    species_index, position_index = t.to.mol_id, t.to.mol_comp
+                    if self._available_atom_id:
+                        atom_id = min(self._available_atom_id)
+                        self._available_atom_id.remove(atom_id)
+                        self._atoms[atom_id] = atom
+                        self._unique_atom_id[atom_id] = self._next_unique_atom_id
+                        self._initial_atom_species_index[atom_id] = species_index
+                        self._initial_atom_position_index[atom_id] = position_index
+                    else:
+                        atom_id = len(self._atoms)
+                        self._atoms.append(atom)
+                        self._unique_atom_id.append(self._next_unique_atom_id)
+                        self._initial_atom_species_index.append(species_index)
+                        self._initial_atom_position_index.append(position_index)
+                    if self._save_atom_info and time is not None:
+                        self._atom_info_initial.setdefault(
+                            self._next_unique_atom_id,
+                            AtomInfo(copy.deepcopy(atom), species_index, position_index, float(time)))
+                    self._mol[t.to.mol_id].component[t.to.mol_comp] = atom_id
+                    self._next_unique_atom_id += 1
+        for atom_id, t in zip(moving, e.atom_traj):
+            if t.to.l != -1 and t.from_.l != -1:  # within the supercell
                 self._mol[t.to.mol_id].component[t.to.mol_comp] = atom_id
                 self._atoms[atom_id].translation = self._atoms[atom_id].translation + np.asarray(t.delta_ijk)
                 self._atoms[atom_id].n_jumps += 1
@@ -813,6 +895,76 @@ class OccLocation:
 
     def atom_size(self) -> int:
         return len(self._atoms)
+
+    def initial_atom_species_index(self) -> list:
+        """Initial species index of each atom (-1 for an atom id freed by a move to the
+        reservoir)."""
+        return self._initial_atom_species_index
+
+    def initial_atom_position_index(self) -> list:
+        return self._initial_atom_position_index
+
+    def current_atom_names(self) -> list:
+        """Current atom name of each atom ("UK" when it is no longer in the supercell)."""
+        names = ["UK"] * len(self._atoms)
+        for mol in self._mol:
+            molecule = self._convert.species_to_mol(mol.species_index)
+            for k, atom_id in enumerate(mol.component):
+                names[atom_id] = molecule.atoms[k][0]
+        return names
+
+    def current_atom_species_index(self) -> list:
+        out = [-1] * len(self._atoms)
+        for mol in self._mol:
+            for atom_id in mol.component:
+                out[atom_id] = mol.species_index
+        return out
+
+    def current_atom_position_index(self) -> list:
+        out = [-1] * len(self._atoms)
+        for mol in self._mol:
+            for k, atom_id in enumerate(mol.component):
+                out[atom_id] = k
+        return out
+
+    def current_atom_n_jumps(self) -> list:
+        return [a.n_jumps for a in self._atoms]
+
+    def unique_atom_id(self) -> list:
+        return self._unique_atom_id
+
+    def atom_info_initial(self) -> dict:
+        """unique atom id -> AtomInfo when the atom entered the supercell (save_atom_info)."""
+        return self._atom_info_initial
+
+    def atom_info_final(self) -> dict:
+        """unique atom id -> AtomInfo when the atom left the supercell (save_atom_info)."""
+        return self._atom_info_final
+
+    def clear_atom_info_final(self) -> None:
+        self._atom_info_final = {}
+
+    def replace_mol(self, l: int, occ: int, atom_id, atom) -> None:
+        """Put occupant ``occ`` on site l with the given atom ids and atoms, for restoring a
+        saved state (OccLocation.cc:506-548); not with unique atom tracking."""
+        if self._track_unique_atoms:
+            raise RuntimeError("Error in OccLocation::replace_mol: `replace_mol` is not supported when tracking "
+                               "unique atoms")
+        conv, cl = self._convert, self._cand_list
+        mol = self._mol[self.l_to_mol_id(l)]
+        ci = cl.index(mol.asym, mol.species_index)
+        back = self._loc[ci][-1]
+        self._loc[ci][mol.loc] = back
+        self._mol[back].loc = mol.loc
+        self._loc[ci].pop()
+        mol.species_index = conv.species_index(mol.asym, int(occ))
+        ci = cl.index(mol.asym, mol.species_index)
+        mol.loc = len(self._loc[ci])
+        self._loc[ci].append(mol.id)
+        mol.component = []
+        for aid, a in zip(atom_id, atom):
+            mol.component.append(int(aid))
+            self._atoms[int(aid)] = a
 
     def atom_positions_cart(self) -> np.ndarray:
         """Current atom positions, shape (3, n_atoms), following atoms across periodic

@@ -10,6 +10,9 @@
   OccEventProposal.hh:168-247 with std::mt19937_64 and libstdc++'s distributions.
 * basic_occupation_metropolis driving the Ising model through user functions: the same
   trajectory, counters and samples as the oracle's Ising semi-grand canonical run.
+* OccLocation with atoms moving to and from a reservoir (vacancies as occupants with no
+  atoms): atom ids freed and reused, unique atom ids, initial and final atom info with
+  times; ``replace_mol``.
 """
 import numpy as np
 import pytest
@@ -246,3 +249,96 @@ def test_basic_occupation_metropolis_matches_oracle(oracle):
     pe = data.samplers["potential_energy"].component(0)
     assert [float.hex(float(x)) for x in pe] == [float.hex(float(x)) for x in ref["potential_energy"]]
     assert engine.dump() == ref["engine"]
+
+
+def _reservoir_setup(**kw):
+    prim = ev.Prim(np.eye(3), np.zeros((3, 1)), [["A", "B", "Va"]], occupants={"Va": ev.Occupant("Va", [])})
+    convert = ev.Conversions(prim, np.eye(3, dtype=int) * 2)
+    occ = np.array([0, 1, 2, 0, 1, 2, 0, 0], dtype=np.int32)
+    loc = ev.OccLocation(convert, ev.OccCandidateList(convert), update_atoms=True, **kw)
+    return convert, occ, loc
+
+
+def _flip(loc, l, to_species):
+    mol = loc.mol(loc.l_to_mol_id(l))
+    return ev.OccTransform(l=l, mol_id=mol.id, asym=mol.asym, from_species=mol.species_index, to_species=to_species)
+
+
+def test_occ_location_reservoir_moves_and_unique_atoms():
+    """Atoms to and from a reservoir (OccLocation.cc:216-366): a leaving atom frees its atom
+    id (translation and n_jumps set to LONG_MIN, unique id -1), an entering atom takes the
+    smallest free id with the next unique id, final and initial atom info carry the time."""
+    convert, occ, loc = _reservoir_setup(track_unique_atoms=True, save_atom_info=True)
+    A, B, Va = (convert.species_index(0, i) for i in range(3))
+    loc.initialize(occ, time=0.0)
+    assert loc.atom_size() == 6 and loc.unique_atom_id() == list(range(6))
+    assert loc.current_atom_names() == ["A", "B", "A", "B", "A", "A"]
+    assert sorted(loc.atom_info_initial()) == list(range(6))
+    assert all(i.time == 0.0 for i in loc.atom_info_initial().values())
+
+    # site 3 (atom id 2) leaves to the reservoir at t = 1.5
+    e = ev.OccEvent()
+    e.occ_transform = [_flip(loc, 3, Va)]
+    e.atom_traj = [ev.AtomTraj(ev.AtomLocation(3, loc.l_to_mol_id(3), 0), ev.AtomLocation(-1, A, 0))]
+    loc.apply(e, occ, time=1.5)
+    lmin = np.iinfo(np.int64).min
+    assert occ[3] == 2 and loc.cand_size(loc.candidate_list().index(0, Va)) == 3
+    assert loc.atom(2).n_jumps == lmin and list(loc.atom(2).translation) == [lmin] * 3
+    assert loc.unique_atom_id()[2] == -1 and loc.initial_atom_species_index()[2] == -1
+    assert loc.current_atom_names()[2] == "UK" and loc.current_atom_species_index()[2] == -1
+    info = loc.atom_info_final()[2]
+    assert (info.species_index, info.position_index, info.time) == (A, 0, 1.5)
+
+    # a B atom enters on site 2 at t = 2.5: it reuses atom id 2 with unique id 6; its
+    # species index is recorded from the trajectory's to.mol_id, as the reference does
+    m2 = loc.l_to_mol_id(2)
+    e.occ_transform = [_flip(loc, 2, B)]
+    e.atom_traj = [ev.AtomTraj(ev.AtomLocation(-1, B, 0), ev.AtomLocation(2, m2, 0))]
+    loc.apply(e, occ, time=2.5)
+    assert occ[2] == 1 and loc.atom_size() == 6 and loc.unique_atom_id()[2] == 6
+    assert loc.mol(m2).component == [2] and loc.atom(2).n_jumps == 0
+    assert list(loc.atom(2).translation) == list(convert.l_to_ijk(2))
+    assert loc.initial_atom_species_index()[2] == m2
+    assert loc.current_atom_names()[2] == "B" and loc.current_atom_species_index()[2] == B
+    assert loc.atom_info_initial()[6].time == 2.5
+
+    # another enters with no free id: appended as atom id 6, unique id 7
+    e.occ_transform = [_flip(loc, 5, A)]
+    e.atom_traj = [ev.AtomTraj(ev.AtomLocation(-1, A, 0), ev.AtomLocation(5, loc.l_to_mol_id(5), 0))]
+    loc.apply(e, occ, time=3.0)
+    assert loc.atom_size() == 7 and loc.unique_atom_id()[6] == 7
+    # a jump within the supercell: site 0 -> site 3 (vacant), one lattice translation
+    e.occ_transform = [_flip(loc, 0, Va), _flip(loc, 3, A)]
+    e.atom_traj = [ev.AtomTraj(ev.AtomLocation(0, loc.l_to_mol_id(0), 0), ev.AtomLocation(3, loc.l_to_mol_id(3), 0),
+                               np.array([1, 0, 0]))]
+    loc.apply(e, occ, time=4.0)
+    assert loc.mol(loc.l_to_mol_id(3)).component == [0] and loc.current_atom_n_jumps()[0] == 1
+    assert list(loc.atom(0).translation) == [1, 0, 0] and loc.unique_atom_id()[0] == 0
+    assert sorted(loc.atom_info_final()) == [2]
+    loc.clear_atom_info_final()
+    assert loc.atom_info_final() == {}
+    # re-initialising (one atom left, two entered) renumbers and resets the records
+    loc.initialize(occ, time=5.0)
+    assert loc.unique_atom_id() == list(range(7)) and loc.atom_info_final() == {}
+    assert len(loc.initial_atom_species_index()) == 7 and sorted(loc.atom_info_initial()) == list(range(7))
+
+
+def test_occ_location_replace_mol():
+    """replace_mol puts an occupant with given atoms on a site (OccLocation.cc:506-548);
+    refused while tracking unique atoms."""
+    convert, occ, loc = _reservoir_setup()
+    A, B, Va = (convert.species_index(0, i) for i in range(3))
+    loc.initialize(occ)
+    a = ev.Atom(translation=np.array([0, 1, 0]), n_jumps=4)
+    loc.replace_mol(2, 1, [5], [a])  # site 2 (vacant) gets a B atom as atom id 5
+    m = loc.mol(loc.l_to_mol_id(2))
+    assert m.species_index == B and m.component == [5] and loc.atom(5).n_jumps == 4
+    assert loc.cand_size(loc.candidate_list().index(0, Va)) == 1
+    assert loc.cand_size(loc.candidate_list().index(0, B)) == 3
+    for cand in range(3):
+        for i in range(loc.cand_size(cand)):
+            assert loc.mol(loc.mol_id(cand, i)).loc == i
+    _, occ2, tracked = _reservoir_setup(track_unique_atoms=True)
+    tracked.initialize(occ2)
+    with pytest.raises(RuntimeError, match="tracking unique atoms"):
+        tracked.replace_mol(2, 1, [5], [a])
