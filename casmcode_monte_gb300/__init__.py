@@ -90,17 +90,98 @@ class RandomNumberGenerator:
         return float(out.value)
 
 
+class _TypedValueMap(dict):
+    """A str-keyed dict that converts each value it stores (the bound std::map types of
+    monte.cpp:106-109)."""
+
+    def __init__(self, data=None):
+        super().__init__()
+        if data is not None:
+            self.update(data)
+
+    @staticmethod
+    def _convert(value):
+        return value
+
+    def __setitem__(self, key: str, value) -> None:
+        super().__setitem__(str(key), self._convert(value))
+
+    def update(self, other=(), **kw) -> None:
+        for k, v in dict(other, **kw).items():
+            self[k] = v
+
+    def setdefault(self, key: str, default=None):
+        if key not in self:
+            self[key] = default
+        return self[key]
+
+    def __deepcopy__(self, memo):
+        return type(self)({k: copy.deepcopy(v, memo) for k, v in self.items()})
+
+
+class BooleanValueMap(_TypedValueMap):
+    """std::map<std::string, bool>."""
+
+    @staticmethod
+    def _convert(value):
+        return bool(value)
+
+
+class ScalarValueMap(_TypedValueMap):
+    """std::map<std::string, double>."""
+
+    @staticmethod
+    def _convert(value):
+        return float(value)
+
+
+class VectorValueMap(_TypedValueMap):
+    """std::map<std::string, Eigen::VectorXd>: values are 1-d float64 arrays."""
+
+    @staticmethod
+    def _convert(value):
+        a = np.array(value, dtype=np.float64)
+        if a.ndim == 2 and 1 in a.shape:
+            a = a.reshape(-1)
+        if a.ndim != 1:
+            raise ValueError(f"VectorValueMap: expected a vector, got shape {a.shape}")
+        return a
+
+
+class MatrixValueMap(_TypedValueMap):
+    """std::map<std::string, Eigen::MatrixXd>: values are 2-d float64 arrays."""
+
+    @staticmethod
+    def _convert(value):
+        a = np.array(value, dtype=np.float64)
+        if a.ndim != 2:
+            raise ValueError(f"MatrixValueMap: expected a matrix, got shape {a.shape}")
+        return a
+
+
 class ValueMap:
-    """Named boolean, scalar, vector and matrix values (ValueMap.hh:14-19)."""
+    """Named boolean, scalar, vector and matrix values (ValueMap.hh:14-19).  The four
+    attributes are the typed maps above; assigning a plain dict converts it, as the
+    reference's read-write members do (monte.cpp:411-426)."""
 
     def __init__(self, data: Optional[dict] = None):
-        self.boolean_values: dict[str, bool] = {}
-        self.scalar_values: dict[str, float] = {}
-        self.vector_values: dict[str, np.ndarray] = {}
-        self.matrix_values: dict[str, np.ndarray] = {}
+        self.boolean_values = BooleanValueMap()
+        self.scalar_values = ScalarValueMap()
+        self.vector_values = VectorValueMap()
+        self.matrix_values = MatrixValueMap()
         if data is not None:
             v = ValueMap.from_dict(data)
             self.__dict__.update(v.__dict__)
+
+    def _get(name):
+        return property(lambda self: self.__dict__[name],
+                        lambda self, value: self.__dict__.__setitem__(name, _MAP_TYPES[name](value)))
+
+    boolean_values = _get("boolean_values")
+    scalar_values = _get("scalar_values")
+    vector_values = _get("vector_values")
+    matrix_values = _get("matrix_values")
+    del _get
 
     @staticmethod
     def from_dict(data: dict) -> "ValueMap":
@@ -158,11 +239,15 @@ class ValueMap:
 
     def __deepcopy__(self, memo):
         v = ValueMap()
-        v.boolean_values = dict(self.boolean_values)
-        v.scalar_values = dict(self.scalar_values)
-        v.vector_values = {k: np.array(x) for k, x in self.vector_values.items()}
-        v.matrix_values = {k: np.array(x) for k, x in self.matrix_values.items()}
+        v.boolean_values = self.boolean_values
+        v.scalar_values = self.scalar_values
+        v.vector_values = self.vector_values
+        v.matrix_values = self.matrix_values
         return v
+
+
+_MAP_TYPES = {"boolean_values": BooleanValueMap, "scalar_values": ScalarValueMap, "vector_values": VectorValueMap,
+              "matrix_values": MatrixValueMap}
 
 
 class MethodLog:
@@ -212,4 +297,7 @@ class MethodLog:
         self.print(json.dumps(data, indent=2) + "\n")
 
 
-__all__ = ["MethodLog", "RandomNumberEngine", "RandomNumberGenerator", "ValueMap"]
+__all__ = ["BooleanValueMap", "MatrixValueMap", "MethodLog", "RandomNumberEngine", "RandomNumberGenerator",
+           "ScalarValueMap", "ValueMap", "VectorValueMap"]
+
+from . import _monte  # noqa: E402,F401  (the names at libcasm.monte._monte)

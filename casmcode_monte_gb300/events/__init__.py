@@ -12,8 +12,9 @@ Mirrors python/libcasm/monte/events/__init__.py:3-39 and the C++ it binds:
 * ``Mol``, ``Atom``, ``OccTransform``, ``AtomLocation``, ``AtomTraj``, ``OccEvent``
   (include/casm/monte/events/OccEvent.hh:10-73).
 * ``OccLocation`` (include/casm/monte/events/OccLocation.hh:44-385,
-  src/casm/monte/events/OccLocation.cc:14-283): per variable site a Mol, per candidate
-  the list of Mol ids, O(1) updates by swap-remove.
+  src/casm/monte/events/OccLocation.cc:14-548): per variable site a Mol, per candidate
+  the list of Mol ids, O(1) updates by swap-remove; atoms (optionally with unique ids and
+  initial/final records) moving within the supercell and to or from a reservoir.
 * the proposal functions of include/casm/monte/events/OccEventProposal.hh:74-484: a swap
   type is chosen with probability proportional to its number of possible events
   (``random_real(total)`` against the running sums), then the site(s) with
@@ -37,6 +38,8 @@ from dataclasses import dataclass, field
 from typing import Optional, Sequence
 
 import numpy as np
+
+from .. import __version__  # noqa: F401  (the module version, as each bound module has)
 
 __all__ = [
     "Atom", "AtomInfo", "AtomInfoMap", "AtomLocation", "AtomTraj", "AtomTrajVector", "AtomVector", "Conversions",
@@ -332,6 +335,23 @@ def _as_bijk(x) -> IntegralSiteCoordinate:
     return x if isinstance(x, IntegralSiteCoordinate) else IntegralSiteCoordinate.from_list(list(x))
 
 
+class UnitCellIndexConverter:
+    """Unit cell (i, j, k) <-> linear unit cell index within a supercell (the unit cell
+    part of the site index conversion)."""
+
+    def __init__(self, transformation_matrix_to_super):
+        self._c = UnitCellCoordIndexConverter(transformation_matrix_to_super, 1)
+
+    def total_unitcells(self) -> int:
+        return self._c.n_uc
+
+    def linear_unitcell_index(self, unitcell) -> int:
+        return self._c.unitcell_index(unitcell)
+
+    def unitcell(self, unitcell_index: int) -> np.ndarray:
+        return self._c.unitcell(unitcell_index)
+
+
 class UnitCellCoordIndexConverter:
     """Linear site index <-> (b, i, j, k) within a supercell, b-major."""
 
@@ -386,26 +406,60 @@ class Conversions:
     ``xtal_prim`` (Conversions.hh:44-137)."""
 
     def __init__(self, xtal_prim: Prim, transformation_matrix_to_super, b_to_asym: Optional[Sequence[int]] = None):
-        self.prim = xtal_prim
-        self._T = np.asarray(transformation_matrix_to_super, dtype=np.int64).reshape(3, 3)
-        self._conv = UnitCellCoordIndexConverter(self._T, xtal_prim.n_basis)
-        self._unit_conv = UnitCellCoordIndexConverter(np.eye(3, dtype=np.int64), xtal_prim.n_basis)
-        self._species_names, self._species = _species_list(xtal_prim)
+        names, species = _species_list(xtal_prim)
         if b_to_asym is None:
-            b_to_asym = _b_to_asym(xtal_prim, self._species_names)
-        self._b_to_asym = [int(x) for x in b_to_asym]
-        if len(self._b_to_asym) != xtal_prim.n_basis:
+            b_to_asym = _b_to_asym(xtal_prim, names)
+        if len(b_to_asym) != xtal_prim.n_basis:
             raise ValueError("Error in Conversions: b_to_asym must have one entry per basis site")
-        self._n_asym = max(self._b_to_asym) + 1
+        self._setup(xtal_prim, names, species, transformation_matrix_to_super, np.eye(3, dtype=np.int64), b_to_asym)
+
+    @staticmethod
+    def make_with_custom_asym(xtal_prim: Prim, transformation_matrix_to_super, b_to_asym) -> "Conversions":
+        """An asymmetric unit of lower symmetry than the prim's factor group, one index per
+        basis site (Conversions.cc:79-84)."""
+        return Conversions(xtal_prim, transformation_matrix_to_super, b_to_asym)
+
+    @staticmethod
+    def make_with_custom_unitcell(xtal_prim: Prim, species_list: Sequence[Occupant], transformation_matrix_to_super,
+                                  unit_transformation_matrix_to_super, unitl_to_asym) -> "Conversions":
+        """An asymmetric unit that does not fit in the primitive cell: ``unitl_to_asym``
+        gives the asymmetric unit index of every site of the sub-supercell U = P T_unit,
+        which must tile the supercell (Conversions.cc:114-174).  ``species_list`` lists
+        every distinct occupant (each orientation its own)."""
+        T = np.asarray(transformation_matrix_to_super, dtype=np.int64).reshape(3, 3)
+        Tu = np.asarray(unit_transformation_matrix_to_super, dtype=np.int64).reshape(3, 3)
+        tiling = np.linalg.solve(Tu.astype(float), T.astype(float))
+        if np.abs(tiling - np.round(tiling)).max() > 1e-9:
+            raise ValueError("Error in Conversions: the unit supercell does not tile the supercell")
+        n_unitl = int(round(abs(np.linalg.det(Tu)))) * xtal_prim.n_basis
+        if len(unitl_to_asym) != n_unitl:
+            raise ValueError("Error in Conversions: unitl_to_asym must have one entry per unit supercell site")
+        c = Conversions.__new__(Conversions)
+        c._setup(xtal_prim, [o.name for o in species_list], list(species_list), T, Tu, unitl_to_asym)
+        return c
+
+    def _setup(self, xtal_prim, names, species, T, T_unit, unitl_to_asym) -> None:
+        self.prim = xtal_prim
+        self._T = np.asarray(T, dtype=np.int64).reshape(3, 3)
+        self._T_unit = np.asarray(T_unit, dtype=np.int64).reshape(3, 3)
+        self._conv = UnitCellCoordIndexConverter(self._T, xtal_prim.n_basis)
+        self._unit_conv = UnitCellCoordIndexConverter(self._T_unit, xtal_prim.n_basis)
+        self._unit_is_prim = bool(np.array_equal(self._T_unit, np.eye(3, dtype=np.int64)))
+        self._species_names, self._species = list(names), list(species)
+        self._unitl_to_asym = [int(x) for x in unitl_to_asym]
+        self._b_to_asym = self._unitl_to_asym if self._unit_is_prim else None
+        self._n_asym = max(self._unitl_to_asym) + 1
+        self._asym_to_unitl = [set() for _ in range(self._n_asym)]
         self._asym_to_b = [set() for _ in range(self._n_asym)]
-        for b, a in enumerate(self._b_to_asym):
-            self._asym_to_b[a].add(b)
+        for unitl, a in enumerate(self._unitl_to_asym):
+            self._asym_to_unitl[a].add(unitl)
+            self._asym_to_b[a].add(self.unitl_to_b(unitl))
+        skeys = [(o.key(), n.split(".")[0]) for n, o in zip(self._species_names, self._species)]
         ns = len(self._species_names)
         self._occ_to_species, self._species_to_occ = [], []
         for a in range(self._n_asym):
             b = min(self._asym_to_b[a])
-            o2s = [self._species_names.index(_canonical_name(xtal_prim, n, self._species_names))
-                   for n in xtal_prim.occ_dof[b]]
+            o2s = [skeys.index((xtal_prim.occupants[n].key(), n.split(".")[0])) for n in xtal_prim.occ_dof[b]]
             s2o = [len(o2s)] * ns
             for o, s in enumerate(o2s):
                 s2o[s] = o
@@ -435,22 +489,43 @@ class Conversions:
         return self._conv.linear_site_index(bijk)
 
     def l_to_asym(self, l: int) -> int:
-        return self._b_to_asym[self.l_to_b(l)]
+        if self._unit_is_prim:
+            return self._b_to_asym[self.l_to_b(l)]
+        return self._unitl_to_asym[self.l_to_unitl(l)]
 
     def bijk_to_asym(self, bijk) -> int:
-        return self._b_to_asym[_as_bijk(bijk).sublattice()]
+        if self._unit_is_prim:
+            return self._b_to_asym[_as_bijk(bijk).sublattice()]
+        return self._unitl_to_asym[self.bijk_to_unitl(bijk)]
 
     def l_to_unitl(self, l: int) -> int:
-        return self.l_to_b(l)
+        if self._unit_is_prim:
+            return self.l_to_b(l)
+        return self._unit_conv.linear_site_index(self.l_to_bijk(l))
+
+    def bijk_to_unitl(self, bijk) -> int:
+        """Site index within the (possibly non-primitive) unit cell."""
+        return self._unit_conv.linear_site_index(bijk)
 
     def unitl_size(self) -> int:
-        return self.prim.n_basis
+        return self._unit_conv.total_sites()
 
     def unitl_to_b(self, unitl: int) -> int:
-        return int(unitl)
+        return int(unitl) // self._unit_conv.n_uc
+
+    def unitl_to_bijk(self, unitl: int) -> IntegralSiteCoordinate:
+        """(b, i, j, k) of a unit-cell site (the reference's binding of this name returns
+        unitl_to_b; this returns what its documentation states)."""
+        return self._unit_conv.bijk(int(unitl))
 
     def unitl_to_asym(self, unitl: int) -> int:
-        return self._b_to_asym[int(unitl)]
+        return self._unitl_to_asym[int(unitl)]
+
+    def unit_transformation_matrix_to_super(self) -> np.ndarray:
+        return self._T_unit.copy()
+
+    def unitcell_index_converter(self) -> "UnitCellIndexConverter":
+        return UnitCellIndexConverter(self._T)
 
     def l_to_frac(self, l: int) -> np.ndarray:
         bijk = self.l_to_bijk(l)
@@ -482,7 +557,7 @@ class Conversions:
         return set(self._asym_to_b[asym])
 
     def asym_to_unitl(self, asym: int) -> set:
-        return set(self._asym_to_b[asym])
+        return set(self._asym_to_unitl[asym])
 
     # -- occupants and species
     def occ_size(self, asym: int) -> int:
@@ -514,6 +589,27 @@ class Conversions:
     def species_to_mol(self, species_index: int) -> Occupant:
         return self._species[species_index]
 
+    # -- names of the reference's Python binding (python/src/monte_events.cpp:360-433)
+    def occ_to_species_index(self, asym: int, occ_index: int) -> int:
+        return self.species_index(asym, occ_index)
+
+    def species_to_occ_index(self, asym: int, species_index: int) -> int:
+        return self.occ_index(asym, species_index)
+
+    def species_name_to_index(self, species_name: str) -> int:
+        return self.species_index(species_name)
+
+    def species_index_to_occupant(self, species_index: int) -> Occupant:
+        return self.species_to_mol(species_index)
+
+    def species_index_to_name(self, species_index: int) -> str:
+        return self.species_name(species_index)
+
+    def species_index_to_atoms_size(self, species_index: int) -> int:
+        """Number of atoms of the occupant (the reference's binding of this name returns the
+        species name; this returns what its documentation states)."""
+        return self.components_size(species_index)
+
     def components_size(self, species_index: int) -> int:
         return len(self._species[species_index].atoms)
 
@@ -528,6 +624,35 @@ class OccCandidate:
     asym: int
     species_index: int
 
+    asymmetric_unit_index = property(lambda self: self.asym,
+                                     lambda self, v: object.__setattr__(self, "asym", int(v)))
+
+    def is_valid(self, convert: "Conversions") -> bool:
+        """Indices in range and the species allowed on the asymmetric unit."""
+        return _is_valid(convert, self)
+
+    def __copy__(self) -> "OccCandidate":
+        return OccCandidate(self.asym, self.species_index)
+
+    def __deepcopy__(self, memo) -> "OccCandidate":
+        return self.__copy__()
+
+    def to_dict(self, convert: "Conversions") -> dict:
+        """{"asym": a, "spec": species name} (OccCandidate_json_io.cc:40-46)."""
+        return {"asym": int(self.asym), "spec": convert.species_name(self.species_index)}
+
+    @staticmethod
+    def from_dict(data: dict, convert: "Conversions") -> "OccCandidate":
+        try:
+            asym, name = int(data["asym"]), data["spec"]
+        except (KeyError, TypeError, ValueError):
+            raise RuntimeError("Error: Invalid monte::OccCandidate object")
+        species_index = convert.species_index(name)
+        if species_index == convert.species_size():
+            raise RuntimeError(f"Error: Invalid monte::OccCandidate object: species name '{name}' is not a valid "
+                               "option")
+        return OccCandidate(asym, species_index)
+
 
 @dataclass(frozen=True, order=True)
 class OccSwap:
@@ -536,12 +661,46 @@ class OccSwap:
     cand_a: OccCandidate
     cand_b: OccCandidate
 
+    first = property(lambda self: self.cand_a, lambda self, v: object.__setattr__(self, "cand_a", v))
+    second = property(lambda self: self.cand_b, lambda self, v: object.__setattr__(self, "cand_b", v))
+
     def reversed(self) -> "OccSwap":
         return OccSwap(self.cand_b, self.cand_a)
 
     def sorted(self) -> "OccSwap":
         r = self.reversed()
         return r if r < self else self
+
+    def reverse(self) -> None:
+        """Exchange first and second in place (a swap used as a dict key is copied into
+        the dict, so changing this object leaves the dict intact)."""
+        a, b = self.cand_a, self.cand_b
+        object.__setattr__(self, "cand_a", b)
+        object.__setattr__(self, "cand_b", a)
+
+    def sort(self) -> None:
+        """Make (first, second) <= (second, first) in place."""
+        if self.reversed() < self:
+            self.reverse()
+
+    def is_valid(self, convert: "Conversions") -> bool:
+        return _is_valid(convert, self.cand_a) and _is_valid(convert, self.cand_b)
+
+    def __copy__(self) -> "OccSwap":
+        return OccSwap(copy.copy(self.cand_a), copy.copy(self.cand_b))
+
+    def __deepcopy__(self, memo) -> "OccSwap":
+        return self.__copy__()
+
+    def to_dict(self, convert: "Conversions") -> list:
+        """[first.to_dict(), second.to_dict()] (OccCandidate_json_io.cc:73-80)."""
+        return [self.cand_a.to_dict(convert), self.cand_b.to_dict(convert)]
+
+    @staticmethod
+    def from_dict(data, convert: "Conversions") -> "OccSwap":
+        if not isinstance(data, (list, tuple)) or len(data) != 2:
+            raise RuntimeError("Error: Invalid monte::OccSwap object")
+        return OccSwap(OccCandidate.from_dict(data[0], convert), OccCandidate.from_dict(data[1], convert))
 
 
 class MultiOccSwap:
@@ -550,7 +709,7 @@ class MultiOccSwap:
     def __init__(self, swaps: dict):
         if not swaps:
             raise ValueError("Error constructing MultiOccSwap: Empty multi-occ swap.")
-        self.swaps = dict(sorted(swaps.items()))
+        self.swaps = OccSwapCountMap(sorted((copy.copy(k), int(v)) for k, v in swaps.items()))
         self.total_count = sum(self.swaps.values())
 
     def _key(self):
@@ -571,6 +730,33 @@ class MultiOccSwap:
     def sorted(self) -> "MultiOccSwap":
         r = self.reversed()
         return r if r < self else self
+
+    def reverse(self) -> None:
+        """Reverse every swap in place."""
+        self.swaps = self.reversed().swaps
+
+    def sort(self) -> None:
+        """Make self <= its reverse in place."""
+        self.swaps = self.sorted().swaps
+
+    def __copy__(self) -> "MultiOccSwap":
+        return MultiOccSwap(self.swaps)
+
+    def __deepcopy__(self, memo) -> "MultiOccSwap":
+        return self.__copy__()
+
+    def to_dict(self, convert: "Conversions") -> list:
+        """[{"swap": swap.to_dict(), "count": n}, ...] (OccCandidate_json_io.cc:122-131)."""
+        return [{"swap": s.to_dict(convert), "count": int(n)} for s, n in self.swaps.items()]
+
+    @staticmethod
+    def from_dict(data, convert: "Conversions") -> "MultiOccSwap":
+        if not isinstance(data, (list, tuple)):
+            raise RuntimeError("Error: Invalid monte::MultiOccSwap object: not an array")
+        try:
+            return MultiOccSwap({OccSwap.from_dict(x["swap"], convert): int(x["count"]) for x in data})
+        except (KeyError, TypeError, ValueError):
+            raise RuntimeError("Error: Invalid monte::MultiOccSwap object")
 
 
 class OccCandidateList:
@@ -607,6 +793,28 @@ class OccCandidateList:
 
     def size(self) -> int:
         return self._end
+
+    def matching_index(self, asymmetric_unit_index: int, species_index: int) -> int:
+        """Index of the candidate (asym, species), len(self) if not in the list."""
+        return self._index[asymmetric_unit_index][species_index]
+
+    def to_dict(self, convert: "Conversions") -> dict:
+        """The candidates and the canonical and semi-grand canonical swaps made from them
+        (OccCandidate_json_io.cc:187-209)."""
+        return {"candidate": [c.to_dict(convert) for c in self._cand],
+                "canonical_swaps": [x.to_dict(convert) for x in make_canonical_swaps(convert, self)],
+                "grand_canonical_swaps": [x.to_dict(convert) for x in make_semigrand_canonical_swaps(convert, self)]}
+
+    @staticmethod
+    def from_dict(data, convert: "Conversions") -> "OccCandidateList":
+        """From a list of candidates or a dict with a "candidate" list
+        (OccCandidate_json_io.cc:134-184)."""
+        if isinstance(data, dict) and isinstance(data.get("candidate"), list):
+            data = data["candidate"]
+        if not isinstance(data, list):
+            raise RuntimeError('Error: Invalid monte::OccCandidateList object: not an array or an object with a '
+                               '"candidate" array.')
+        return OccCandidateList(convert, [OccCandidate.from_dict(x, convert) for x in data])
 
 
 def _is_valid(convert: Conversions, cand: OccCandidate) -> bool:
@@ -693,6 +901,12 @@ class Mol:
     loc: int = 0
 
 
+Mol.component_id = property(lambda self: self.component, lambda self, v: setattr(self, "component", list(v)))
+Mol.linear_site_index = property(lambda self: self.l, lambda self, v: setattr(self, "l", int(v)))
+Mol.asymmetric_unit_index = property(lambda self: self.asym, lambda self, v: setattr(self, "asym", int(v)))
+Mol.mol_location_index = property(lambda self: self.loc, lambda self, v: setattr(self, "loc", int(v)))
+
+
 @dataclass
 class OccTransform:
     l: int = 0
@@ -716,6 +930,12 @@ class AtomTraj:
     delta_ijk: np.ndarray = field(default_factory=lambda: np.zeros(3, dtype=np.int64))
 
 
+OccTransform.linear_site_index = property(lambda self: self.l, lambda self, v: setattr(self, "l", int(v)))
+AtomLocation.linear_site_index = property(lambda self: self.l, lambda self, v: setattr(self, "l", int(v)))
+# ``from`` is a Python keyword: reached as getattr(traj, "from"), as with the reference's binding
+setattr(AtomTraj, "from", property(lambda self: self.from_, lambda self, v: setattr(self, "from_", v)))
+
+
 @dataclass
 class OccEvent:
     """Sites, new occupant indices, occupant transforms, atom trajectories (OccEvent.hh:55-71)."""
@@ -724,6 +944,14 @@ class OccEvent:
     new_occ: list = field(default_factory=list)
     occ_transform: list = field(default_factory=list)
     atom_traj: list = field(default_factory=list)
+
+    def __copy__(self) -> "OccEvent":
+        return copy.deepcopy(self)
+
+    def __deepcopy__(self, memo) -> "OccEvent":
+        return OccEvent(list(self.linear_site_index), list(self.new_occ),
+                        [copy.copy(t) for t in self.occ_transform],
+                        [AtomTraj(copy.copy(t.from_), copy.copy(t.to), np.array(t.delta_ijk)) for t in self.atom_traj])
 
 
 class OccLocation:
@@ -1006,6 +1234,18 @@ class OccLocation:
     def mol_id(self, cand, loc: int) -> int:
         ci = cand if isinstance(cand, (int, np.integer)) else self._cand_list.index(cand)
         return self._loc[ci][loc]
+
+    def cand_size_by_candidate_index(self, candidate_index: int) -> int:
+        return len(self._loc[candidate_index])
+
+    def mol_id_by_candidate_index(self, candidate_index: int, location_index: int) -> int:
+        return self._loc[candidate_index][location_index]
+
+    def choose_mol_by_candidate_index(self, candidate_index: int, random_number_generator) -> Mol:
+        return self.choose_mol(int(candidate_index), random_number_generator)
+
+    def linear_site_index_to_mol_id(self, linear_site_index: int) -> int:
+        return self.l_to_mol_id(linear_site_index)
 
     def l_to_mol_id(self, l: int) -> int:
         return self._l_to_mol[l]

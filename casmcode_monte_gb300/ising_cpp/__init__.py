@@ -19,7 +19,7 @@ from typing import Optional
 
 import numpy as np
 
-from .. import ValueMap
+from .. import ValueMap, __version__  # noqa: F401
 
 
 class IsingConfiguration:

@@ -23,7 +23,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from ... import MethodLog, RandomNumberEngine, ValueMap
+from ... import MethodLog, RandomNumberEngine, ValueMap, __version__  # noqa: F401
 from ... import _lib
 from ...sampling import (CompletionCheck, CompletionCheckParams, Sampler, StateSamplingFunction,
                          StateSamplingFunctionMap, jsonSampler, jsonSamplerMap, jsonStateSamplingFunction,

@@ -25,7 +25,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from .. import MethodLog, RandomNumberEngine, RandomNumberGenerator
+from .. import MethodLog, RandomNumberEngine, RandomNumberGenerator, __version__  # noqa: F401
 from ..events import OccEvent
 from ..sampling import (CompletionCheck, CompletionCheckParams, Sampler, get_n_samples, jsonSampler,
                         jsonStateSamplingFunctionMap, StateSamplingFunctionMap)

@@ -26,7 +26,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from .. import _lib
+from .. import __version__, _lib  # noqa: F401
 
 
 class SAMPLE_MODE(enum.Enum):

@@ -342,3 +342,79 @@ def test_occ_location_replace_mol():
     tracked.initialize(occ2)
     with pytest.raises(RuntimeError, match="tracking unique atoms"):
         tracked.replace_mol(2, 1, [5], [a])
+
+
+def test_reference_binding_names_and_dict_forms():
+    """Methods and fields under the names of the reference's binding
+    (python/src/monte_events.cpp) and the dict forms of OccCandidate_json_io.cc:40-209."""
+    convert = ev.Conversions(ev.Prim.fcc(4.0, ["A", "B", "C"]), np.eye(3, dtype=int) * 2)
+    assert convert.species_name_to_index("B") == 1 and convert.species_index_to_name(2) == "C"
+    assert convert.occ_to_species_index(0, 1) == 1 and convert.species_to_occ_index(0, 2) == 2
+    assert convert.species_index_to_occupant(0).name == "A" and convert.species_index_to_atoms_size(0) == 1
+    assert np.array_equal(convert.unit_transformation_matrix_to_super(), np.eye(3))
+    assert convert.unitcell_index_converter().total_unitcells() == 8
+    assert convert.bijk_to_unitl(bijk(0, 1, 1, 0)) == 0 and convert.unitl_to_bijk(0) == bijk(0, 0, 0, 0)
+
+    cand = ev.OccCandidate(0, 2)
+    assert cand.asymmetric_unit_index == 0 and cand.is_valid(convert) and not ev.OccCandidate(1, 0).is_valid(convert)
+    assert cand.to_dict(convert) == {"asym": 0, "spec": "C"}
+    assert ev.OccCandidate.from_dict({"asym": 0, "spec": "C"}, convert) == cand
+    with pytest.raises(RuntimeError, match="not a valid option"):
+        ev.OccCandidate.from_dict({"asym": 0, "spec": "Q"}, convert)
+    swap = ev.OccSwap(ev.OccCandidate(0, 2), ev.OccCandidate(0, 1))
+    assert swap.first == ev.OccCandidate(0, 2) and swap.is_valid(convert)
+    assert ev.OccSwap.from_dict(swap.to_dict(convert), convert) == swap
+    m = ev.MultiOccSwap({swap: 2})
+    swap.sort()  # in place; the multi-swap holds its own copy
+    assert swap.first == ev.OccCandidate(0, 1) and list(m.swaps) == [ev.OccSwap(ev.OccCandidate(0, 2),
+                                                                                 ev.OccCandidate(0, 1))]
+    swap.reverse()
+    assert swap.second == ev.OccCandidate(0, 1)
+    assert ev.MultiOccSwap.from_dict(m.to_dict(convert), convert) == m
+    m2 = m.__copy__()
+    m2.reverse()
+    assert m2 == m.reversed() and m2 != m
+    assert m.to_dict(convert) == [{"swap": [{"asym": 0, "spec": "C"}, {"asym": 0, "spec": "B"}], "count": 2}]
+
+    cl = ev.OccCandidateList(convert)
+    d = cl.to_dict(convert)
+    assert len(d["candidate"]) == 3 and len(d["canonical_swaps"]) == 3 and len(d["grand_canonical_swaps"]) == 6
+    cl2 = ev.OccCandidateList.from_dict(d, convert)
+    assert list(cl2) == list(cl) and cl2.matching_index(0, 1) == cl.index(ev.OccCandidate(0, 1))
+    assert list(ev.OccCandidateList.from_dict(d["candidate"], convert)) == list(cl)
+
+    occ = np.array([0, 1, 2, 0, 1, 2, 0, 1], dtype=np.int32)
+    loc = ev.OccLocation(convert, cl)
+    loc.initialize(occ)
+    ci = cl.index(ev.OccCandidate(0, 1))
+    assert loc.cand_size_by_candidate_index(ci) == 3 == loc.cand_size(ev.OccCandidate(0, 1))
+    mol = loc.mol(loc.mol_id_by_candidate_index(ci, 0))
+    assert mol.species_index == 1 and loc.linear_site_index_to_mol_id(mol.linear_site_index) == mol.id
+    assert (mol.asymmetric_unit_index, mol.mol_location_index, mol.component_id) == (0, 0, [])
+    g = monte.RandomNumberGenerator()
+    assert loc.choose_mol_by_candidate_index(ci, g).species_index == 1
+    traj = ev.AtomTraj(ev.AtomLocation(3, 3, 0), ev.AtomLocation(5, 5, 0))
+    assert getattr(traj, "from").linear_site_index == 3
+    e = ev.OccEvent([3], [1], [ev.OccTransform(3, 3, 0, 0, 1)], [traj])
+    e2 = e.__copy__()
+    e2.occ_transform[0].linear_site_index = 4
+    assert e.occ_transform[0].l == 3 and e2.occ_transform[0].l == 4
+
+
+def test_conversions_with_a_custom_unit_cell():
+    """An asymmetric unit on a 2x1x1 unit supercell of a one-site cubic prim (two
+    sublattices of alternating planes), Conversions.cc:114-174."""
+    prim = ev.Prim.cubic(1.0, ["A", "B"])
+    species = [prim.occupants["A"], prim.occupants["B"]]
+    T = np.diag([4, 2, 2])
+    convert = ev.Conversions.make_with_custom_unitcell(prim, species, T, np.diag([2, 1, 1]), [0, 1])
+    assert convert.unitl_size() == 2 and convert.asym_size() == 2
+    for l in range(convert.l_size()):
+        i = int(convert.l_to_ijk(l)[0])
+        assert convert.l_to_unitl(l) == i % 2 and convert.l_to_asym(l) == i % 2
+    assert convert.asym_to_unitl(1) == {1} and convert.asym_to_b(1) == {0}
+    assert convert.occ_size(1) == 2 and convert.species_index(1, 1) == 1
+    with pytest.raises(ValueError, match="tile"):
+        ev.Conversions.make_with_custom_unitcell(prim, species, T, np.diag([3, 1, 1]), [0, 1, 0])
+    lower = ev.Conversions.make_with_custom_asym(prim, T, [0])
+    assert lower.asym_size() == 1
