@@ -63,6 +63,27 @@ class SamplingParams:
         self.do_sample_time = bool(do_sample_time)
 
 
+def _list_helpers(attr: str):
+    def append(self, name: str) -> None:
+        getattr(self, attr).append(name)
+
+    def remove(self, name: str) -> None:
+        names = getattr(self, attr)
+        if name in names:
+            names.remove(name)
+
+    def extend(self, names) -> None:
+        getattr(self, attr).extend(names)
+    return append, remove, extend
+
+
+# monte_sampling.cpp:652-720: the first occurrence is removed; a missing name is ignored
+(SamplingParams.append_to_sampler_names, SamplingParams.remove_from_sampler_names,
+ SamplingParams.extend_sampler_names) = _list_helpers("sampler_names")
+(SamplingParams.append_to_json_sampler_names, SamplingParams.remove_from_json_sampler_names,
+ SamplingParams.extend_json_sampler_names) = _list_helpers("json_sampler_names")
+
+
 def default_component_names(shape: list[int]) -> list[str]:
     """Sampler.hh:333-349: [] -> ["0"]; [n] -> ["0".."n-1"]; [m,n] -> column-major "i,j"."""
     if len(shape) == 0:
@@ -207,12 +228,21 @@ class RequestedPrecision:
         self.rel_precision = float(rel) if rel is not None else 0.0
 
     def to_dict(self) -> dict:
+        """Sampler_json_io.cc:39-52."""
         d = {}
         if self.abs_convergence_is_required:
-            d["abs"] = self.abs_precision
+            d["abs_precision"] = self.abs_precision
         if self.rel_convergence_is_required:
-            d["rel"] = self.rel_precision
+            d["rel_precision"] = self.rel_precision
         return d
+
+    @staticmethod
+    def from_dict(data: dict) -> "RequestedPrecision":
+        """"abs_precision" (or the older "precision") and "rel_precision", each optional
+        (Sampler_json_io.cc:70-95)."""
+        a = data.get("abs_precision", data.get("precision"))
+        r = data.get("rel_precision")
+        return RequestedPrecision(abs=None if a is None else float(a), rel=None if r is None else float(r))
 
 
 class RequestedPrecisionMap(dict):
@@ -253,9 +283,55 @@ class jsonStateSamplingFunctionMap(dict):
     pass
 
 
+class _SampleList(list):
+    """The samples of a jsonSampler: a list that, called, returns them as a new list (the
+    binding's ``values()``)."""
+
+    def __call__(self) -> list:
+        return list(self)
+
+
 class jsonSampler:
+    """Sampled dict-like data for JSON output (monte_sampling.cpp:900-1010)."""
+
     def __init__(self):
-        self.values: list = []
+        self.values = _SampleList()
+        self._capacity = 0
+
+    values = property(lambda self: self.__dict__["_values"],
+                      lambda self, v: self.__dict__.__setitem__("_values", _SampleList(v)))
+
+    def append(self, data) -> None:
+        self.values.append(data)
+
+    def set_values(self, values) -> None:
+        self.values = values
+
+    def clear(self) -> None:
+        self.values.clear()
+
+    def set_sample_capacity(self, sample_capacity: int) -> None:
+        self._capacity = max(self._capacity, int(sample_capacity))
+
+    def n_samples(self) -> int:
+        return len(self.values)
+
+    def sample_capacity(self) -> int:
+        return max(self._capacity, len(self.values))
+
+    def sample(self, sample_index: int):
+        if not 0 <= int(sample_index) < len(self.values):
+            raise IndexError(f"jsonSampler.sample: index {sample_index} out of range")
+        return self.values[int(sample_index)]
+
+    def __len__(self) -> int:
+        return len(self.values)
+
+    def __iter__(self):
+        return iter(self.values)
+
+    def to_list(self) -> list:
+        return list(self.values)
 
 
 class jsonSamplerMap(dict):
@@ -274,6 +350,28 @@ class CutoffCheckParams:
     max_time: Optional[float] = None
     max_sample: Optional[int] = None
     max_clocktime: Optional[float] = None
+
+    _KINDS = (("count", int), ("time", float), ("sample", int), ("clocktime", float))
+
+    def to_dict(self) -> dict:
+        """{"count": {"min": .., "max": ..}, "time": .., "sample": .., "clocktime": ..}, set
+        values only (CutoffCheck_json_io.cc:9-48)."""
+        d = {}
+        for kind, _ in self._KINDS:
+            sub = {k: getattr(self, f"{k}_{kind}") for k in ("min", "max") if getattr(self, f"{k}_{kind}") is not None}
+            if sub:
+                d[kind] = sub
+        return d
+
+    @staticmethod
+    def from_dict(data: dict) -> "CutoffCheckParams":
+        p = CutoffCheckParams()
+        for kind, typ in CutoffCheckParams._KINDS:
+            for k, v in (data.get(kind) or {}).items():
+                if k not in ("min", "max"):
+                    raise RuntimeError(f"Error in CutoffCheckParams.from_dict: unknown option '{kind}/{k}'")
+                setattr(p, f"{k}_{kind}", None if v is None else typ(v))
+        return p
 
 
 def all_minimums_met(cutoff_params: CutoffCheckParams, count: Optional[int], time: Optional[float],
@@ -312,6 +410,11 @@ class BasicStatistics:
     def to_dict(self) -> dict:
         return {"mean": self.mean, "calculated_precision": self.calculated_precision}
 
+    def relative_precision(self) -> float:
+        """|calculated_precision / mean| (BasicStatistics.hh:42-44)."""
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return float(abs(np.float64(self.calculated_precision) / np.float64(self.mean)))
+
 
 def _f64(a) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
@@ -324,6 +427,21 @@ class BasicStatisticsCalculator:
         self.confidence = float(confidence)
         self.method = int(method)
         self.n_resamples = int(n_resamples)
+
+    weighted_observations_method = property(lambda self: self.method,
+                                            lambda self, v: setattr(self, "method", int(v)))
+
+    def calculate(self, observations, sample_weight) -> "BasicStatistics":
+        return self(observations, sample_weight)
+
+    def to_dict(self) -> dict:
+        return {"confidence": self.confidence, "weighted_observations_method": self.method,
+                "n_resamples": self.n_resamples}
+
+    @staticmethod
+    def from_dict(data: dict) -> "BasicStatisticsCalculator":
+        return BasicStatisticsCalculator(data.get("confidence", 0.95), data.get("weighted_observations_method", 1),
+                                         data.get("n_resamples", 10000))
 
     def __call__(self, observations, sample_weight=None) -> BasicStatistics:
         x = _f64(observations)
@@ -513,6 +631,83 @@ class CompletionCheckParams:
     def sample_check_linear(self, n: int) -> int:
         return self.check_begin + self.check_period * n
 
+    def to_dict(self) -> dict:
+        """CompletionCheck_json_io.hh:388-420 (statistics parameters not written, as there)."""
+        conv = []
+        for key, rp in sorted(self.requested_precision.items()):
+            conv.append({"quantity": key.sampler_name, "component_index": [key.component_index],
+                         "component_name": [key.component_name], **rp.to_dict()})
+        d = {"cutoff": self.cutoff_params.to_dict(), "convergence": conv}
+        if not self.log_spacing:
+            d.update(spacing="linear", begin=self.check_begin, period=self.check_period)
+        else:
+            d.update(spacing="log", begin=self.check_begin, base=self.check_base, shift=self.check_shift,
+                     period_max=self.check_period_max)
+        return d
+
+    @staticmethod
+    def from_dict(data: dict, sampling_functions: dict) -> "CompletionCheckParams":
+        """CompletionCheck_json_io.hh:295-386: "cutoff", "convergence" (per entry a
+        "quantity" naming a sampling function, its precision, and "component_index" and/or
+        "component_name", else every component), "spacing" ("linear": begin 100, period
+        100; "log": begin 0, base 10, shift 2, period_max 10000), overrides "begin",
+        "period", "base", "shift", "period_max"; "confidence",
+        "weighted_observations_method", "n_resamples" for the statistics."""
+        errors = []
+        p = CompletionCheckParams()
+        p.calc_statistics_f = BasicStatisticsCalculator.from_dict(data)
+        p.cutoff_params = CutoffCheckParams.from_dict(data.get("cutoff") or {})
+        conv = data.get("convergence", [])
+        if not isinstance(conv, list):
+            errors.append('"convergence" must be an array')
+            conv = []
+        for i, c in enumerate(conv):
+            q = c.get("quantity")
+            if q is None:
+                errors.append(f"convergence/{i}/quantity is required")
+                continue
+            f = next((g for g in sampling_functions.values() if g.name == q), None) if q not in sampling_functions \
+                else sampling_functions[q]
+            if f is None:
+                errors.append(f'"{q}" is not a sampling option.')
+                continue
+            rp = RequestedPrecision.from_dict(c)
+            names = list(f.component_names)
+            has_i, has_n = "component_index" in c, "component_name" in c
+            for index in c.get("component_index", []):
+                if not 0 <= int(index) < len(names):
+                    errors.append(f'For "{f.name}", component index {index} is out of range. Valid range is '
+                                  f'[0,{len(names)}).')
+                    continue
+                p.requested_precision.setdefault(SamplerComponent(f.name, int(index), names[int(index)]), rp)
+            for name in c.get("component_name", []):
+                if name not in names:
+                    errors.append(f'For "{f.name}", component name {name} is not valid.')
+                    continue
+                p.requested_precision.setdefault(SamplerComponent(f.name, names.index(name), name), rp)
+            if not has_i and not has_n:
+                for index, name in enumerate(names):
+                    p.requested_precision.setdefault(SamplerComponent(f.name, index, name), rp)
+        spacing = data.get("spacing", "linear")
+        if spacing == "linear":
+            p.log_spacing, p.check_begin, p.check_period = False, 100, 100
+        elif spacing == "log":
+            p.log_spacing, p.check_begin, p.check_base, p.check_shift, p.check_period_max = True, 0, 10.0, 2.0, 10000
+        else:
+            errors.append('"spacing" must be one of "linear", "log".')
+        p.check_begin = int(data.get("begin", p.check_begin))
+        p.check_period = int(data.get("period", p.check_period))
+        if p.check_period <= 1:  # the reference's own bound
+            errors.append('"period" must > 0.')
+        p.check_base = float(data.get("base", p.check_base))
+        p.check_shift = float(data.get("shift", p.check_shift))
+        p.check_period_max = int(data.get("period_max", p.check_period_max))
+        if p.check_base <= 1.0:
+            errors.append('"base" must > 1.0')
+        if errors:
+            raise RuntimeError("Error in libcasm.monte.sampling.CompletionCheckParams.from_dict: " + "; ".join(errors))
+        return p
+
     def _sample_check_log(self, n: int) -> int:
         return self.check_begin + int(_round_half_away(math.pow(self.check_base, n + self.check_shift)))
 
@@ -606,6 +801,10 @@ class CompletionCheck:
     # -- public variants (monte_sampling.cpp:2993-3080)
     def is_complete(self, samplers, sample_weight, method_log) -> bool:
         return self._is_complete(samplers, sample_weight, None, None, method_log)
+
+    def check(self, samplers, sample_weight, method_log) -> bool:
+        """The completion check without count or time cutoffs (monte_sampling.cpp:3235-3242)."""
+        return self.is_complete(samplers, sample_weight, method_log)
 
     def count_check(self, samplers, sample_weight, count, method_log) -> bool:
         return self._is_complete(samplers, sample_weight, int(count), None, method_log)

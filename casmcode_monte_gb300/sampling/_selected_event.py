@@ -53,10 +53,14 @@ class CorrelationsDataParams:
         self.stop_run_when_complete = bool(stop_run_when_complete)
 
     def copy(self) -> "CorrelationsDataParams":
-        return copy.copy(self)
+        return self.__copy__()
+
+    def __copy__(self) -> "CorrelationsDataParams":
+        return CorrelationsDataParams(self.jumps_per_position_sample, self.max_n_position_samples,
+                                      self.output_incomplete_samples, self.stop_run_when_complete)
 
     def __deepcopy__(self, memo):
-        return copy.copy(self)
+        return self.__copy__()
 
     def to_dict(self) -> dict:
         """SelectedEventFunctions_json_io.cc: to_json(CorrelationsDataParams)."""
@@ -588,7 +592,7 @@ class _VectorHistogramFunction:
         self.function = function
         self.has_value_function = has_value_function if has_value_function is not None else _always_true
         self.max_size = int(max_size)
-        self.value_labels = None
+        self._value_labels = None
 
     def __call__(self):
         return self.function()
@@ -596,8 +600,12 @@ class _VectorHistogramFunction:
     def has_value(self) -> bool:
         return bool(self.has_value_function())
 
+    def value_labels(self):
+        """Optional list of (value, label) (monte_sampling.cpp:1415-1430)."""
+        return self._value_labels
+
     def set_value_labels(self, value_labels) -> None:
-        self.value_labels = None if value_labels is None else [(np.asarray(v), str(s)) for v, s in value_labels]
+        self._value_labels = None if value_labels is None else [(np.asarray(v), str(s)) for v, s in value_labels]
 
 
 class VectorIntHistogramFunction(_VectorHistogramFunction):
@@ -728,6 +736,18 @@ class SelectedEventFunctionParams:
     @property
     def correlations_data_params(self) -> Optional[CorrelationsDataParams]:
         return self._correlations_data_params
+
+    def __copy__(self) -> "SelectedEventFunctionParams":
+        return copy.deepcopy(self)
+
+    def __deepcopy__(self, memo) -> "SelectedEventFunctionParams":
+        c = SelectedEventFunctionParams()
+        c._correlations_data_params = (None if self._correlations_data_params is None
+                                       else self._correlations_data_params.__copy__())
+        c._function_names = list(self._function_names)
+        for k in ("order", "tol", "bin_width", "initial_begin", "is_log", "max_size"):
+            setattr(c, k, dict(getattr(self, k)))
+        return c
 
     @property
     def function_names(self) -> list[str]:
@@ -910,7 +930,7 @@ class SelectedEventDataCollector:
                 if name in params.max_size:
                     f.max_size = params.max_size[name]
                 h = data.discrete_vector_int_histograms.setdefault(
-                    name, DiscreteVectorIntHistogram(f.component_names, f.shape, f.max_size, f.value_labels))
+                    name, DiscreteVectorIntHistogram(f.component_names, f.shape, f.max_size, f.value_labels()))
                 self.discrete_vector_int_f.append(f)
                 self.discrete_vector_int_hist.append(h)
             elif name in functions.discrete_vector_float_functions:
@@ -922,7 +942,7 @@ class SelectedEventDataCollector:
                     f.max_size = params.max_size[name]
                 h = data.discrete_vector_float_histograms.setdefault(
                     name, DiscreteVectorFloatHistogram(f.component_names, f.shape, f.tol, f.max_size,
-                                                       f.value_labels))
+                                                       f.value_labels()))
                 self.discrete_vector_float_f.append(f)
                 self.discrete_vector_float_hist.append(h)
             elif name in functions.continuous_1d_functions:

@@ -126,3 +126,65 @@ def test_repeat_calls_catch_up_matches_literal_calls():
             b._repeat_calls(steps_per_pass - 1)
             assert ra == rb
             assert a._n_checks == b._n_checks
+
+
+def test_sampling_binding_names_and_dict_forms():
+    """Methods under the reference binding's names (python/src/monte_sampling.cpp) and the
+    dict forms of Sampler_json_io.cc:39-95, CutoffCheck_json_io.cc:9-48 and
+    CompletionCheck_json_io.hh:295-420."""
+    import casmcode_monte_gb300.sampling as sp
+    js = sp.jsonSampler()
+    js.append({"a": 1})
+    js.set_values([{"a": 2}, {"b": 3}])
+    assert js.n_samples() == 2 == len(js) and js.values() == [{"a": 2}, {"b": 3}] and js.sample(1) == {"b": 3}
+    assert js.values[-1] == {"b": 3} and js.to_list() == list(js)
+    js.set_sample_capacity(10)
+    assert js.sample_capacity() == 10
+    js.clear()
+    assert js.n_samples() == 0
+
+    rp = sp.RequestedPrecision(abs=0.1, rel=0.2)
+    assert rp.to_dict() == {"abs_precision": 0.1, "rel_precision": 0.2}
+    old = sp.RequestedPrecision.from_dict({"precision": 0.5})
+    assert old.abs_convergence_is_required and old.abs_precision == 0.5 and not old.rel_convergence_is_required
+
+    st = sp.BasicStatistics(mean=-2.0, calculated_precision=0.5)
+    assert st.relative_precision() == 0.25
+    calc = sp.BasicStatisticsCalculator(0.9, 1, 500)
+    assert sp.BasicStatisticsCalculator.from_dict(calc.to_dict()).to_dict() == calc.to_dict()
+    assert calc.weighted_observations_method == 1
+    x = np.random.default_rng(1).normal(size=400)
+    assert calc.calculate(x, np.zeros(0)).mean == calc(x).mean
+
+    cut = sp.CutoffCheckParams(min_sample=10, max_count=100, max_clocktime=5.0)
+    assert cut.to_dict() == {"count": {"max": 100}, "sample": {"min": 10}, "clocktime": {"max": 5.0}}
+    assert sp.CutoffCheckParams.from_dict(cut.to_dict()) == cut
+
+    f = sp.StateSamplingFunction("comp", "composition", [2], lambda: np.zeros(2), ["x0", "x1"])
+    g = sp.StateSamplingFunction("energy", "energy", [], lambda: np.zeros(1))
+    fmap = sp.StateSamplingFunctionMap({"comp": f, "energy": g})
+    d = {"cutoff": {"sample": {"max": 1000}}, "spacing": "log", "period_max": 500,
+         "convergence": [{"quantity": "energy", "abs_precision": 0.001},
+                         {"quantity": "comp", "component_name": ["x1"], "rel_precision": 0.01}],
+         "confidence": 0.9}
+    p = sp.CompletionCheckParams.from_dict(d, fmap)
+    assert p.log_spacing and (p.check_begin, p.check_base, p.check_shift, p.check_period_max) == (0, 10.0, 2.0, 500)
+    assert p.cutoff_params.max_sample == 1000 and p.calc_statistics_f.confidence == 0.9
+    keys = sorted(p.requested_precision)
+    assert [(k.sampler_name, k.component_index) for k in keys] == [("comp", 1), ("energy", 0)]
+    assert p.requested_precision[keys[0]].rel_precision == 0.01
+    p2 = sp.CompletionCheckParams.from_dict(p.to_dict(), fmap)
+    assert p2.to_dict() == p.to_dict()
+    with pytest.raises(RuntimeError, match="not a sampling option"):
+        sp.CompletionCheckParams.from_dict({"convergence": [{"quantity": "nope", "abs_precision": 1.0}]}, fmap)
+    with pytest.raises(RuntimeError, match="out of range"):
+        sp.CompletionCheckParams.from_dict({"convergence": [{"quantity": "comp", "component_index": [2],
+                                                             "abs_precision": 1.0}]}, fmap)
+
+    s = sp.SamplingParams()
+    s.extend_sampler_names(["a", "b", "a"])
+    s.append_to_sampler_names("c")
+    s.remove_from_sampler_names("a")
+    s.remove_from_sampler_names("zz")
+    s.append_to_json_sampler_names("config")
+    assert s.sampler_names == ["b", "a", "c"] and s.json_sampler_names == ["config"]
