@@ -75,18 +75,22 @@ class RandomNumberGenerator:
     """Uniform integers/reals from a shared RandomNumberEngine (RandomNumberGenerator.hh:15-42)."""
 
     def __init__(self, engine: Optional[RandomNumberEngine] = None):
-        self.engine = engine if engine is not None else RandomNumberEngine()
+        self._engine = engine if engine is not None else RandomNumberEngine()
+
+    def engine(self) -> RandomNumberEngine:
+        """The shared engine the draws come from."""
+        return self._engine
 
     def random_int(self, maximum_value: int) -> int:
         """Uniformly distributed integer in [0, maximum_value]."""
         out = C.c_uint64()
-        _lib.check(_lib.lib().mg_engine_random_int(self.engine._h, C.c_uint64(int(maximum_value)), C.byref(out)))
+        _lib.check(_lib.lib().mg_engine_random_int(self._engine._h, C.c_uint64(int(maximum_value)), C.byref(out)))
         return int(out.value)
 
     def random_real(self, maximum_value: float) -> float:
         """Uniformly distributed float in [0, maximum_value)."""
         out = C.c_double()
-        _lib.check(_lib.lib().mg_engine_random_real(self.engine._h, float(maximum_value), C.byref(out)))
+        _lib.check(_lib.lib().mg_engine_random_real(self._engine._h, float(maximum_value), C.byref(out)))
         return float(out.value)
 
 
@@ -287,14 +291,142 @@ class MethodLog:
         self._logfile_path = None
 
     def print(self, text: str) -> None:
-        if self._logfile_path:
-            with open(self._logfile_path, "a") as f:
-                f.write(text)
-        else:
-            sys.stdout.write(text)
+        self._emit(text)
 
     def write_json(self, data) -> None:
         self.print(json.dumps(data, indent=2) + "\n")
+
+    # -- verbosity, sections and formatted text (monte.cpp:150-384; the Log of
+    # libcasm-global, restated): a section begun at a level prints only while the
+    # verbosity is at least that level; text outside sections always prints.
+    _LEVELS = {"quiet": 0, "standard": 1, "verbose": 2, "debug": 3}
+
+    def _fmt_state(self) -> dict:
+        st = self.__dict__.get("_fmt")
+        if st is None:
+            st = self.__dict__["_fmt"] = {"verbosity": 1, "sections": [], "indent": 0, "indent_space": 2,
+                                          "initial_indent": 0, "clock": False, "width": 100,
+                                          "justification": "left"}
+        return st
+
+    def _printing(self) -> bool:
+        st = self._fmt_state()
+        return not st["sections"] or st["sections"][-1] <= st["verbosity"]
+
+    def _emit(self, text: str) -> None:
+        if self._printing():
+            if self._logfile_path:
+                with open(self._logfile_path, "a") as f:
+                    f.write(text)
+            else:
+                sys.stdout.write(text)
+
+    def set_quiet(self) -> None:
+        self._fmt_state()["verbosity"] = 0
+
+    def set_standard(self) -> None:
+        self._fmt_state()["verbosity"] = 1
+
+    def set_verbose(self) -> None:
+        self._fmt_state()["verbosity"] = 2
+
+    def set_debug(self) -> None:
+        self._fmt_state()["verbosity"] = 3
+
+    def _begin(self, level: int) -> None:
+        self._fmt_state()["sections"].append(level)
+
+    def begin_section_print_always(self) -> None:
+        self._begin(-1)
+
+    def begin_section_print_if_quiet(self) -> None:
+        self._begin(0)
+
+    def begin_section_print_if_standard(self) -> None:
+        self._begin(1)
+
+    def begin_section_print_if_verbose(self) -> None:
+        self._begin(2)
+
+    def begin_section_print_if_debug(self) -> None:
+        self._begin(3)
+
+    def end_section(self) -> None:
+        st = self._fmt_state()
+        if st["sections"]:
+            st["sections"].pop()
+
+    def show_clock(self) -> None:
+        self._fmt_state()["clock"] = True
+
+    def hide_clock(self) -> None:
+        self._fmt_state()["clock"] = False
+
+    def increase_indent(self) -> None:
+        self._fmt_state()["indent"] += 1
+
+    def decrease_indent(self) -> None:
+        st = self._fmt_state()
+        st["indent"] = max(0, st["indent"] - 1)
+
+    def set_indent_space(self, indent_space: int) -> None:
+        self._fmt_state()["indent_space"] = int(indent_space)
+
+    def set_initial_indent_space(self, initial_indent_space: int) -> None:
+        self._fmt_state()["initial_indent"] = int(initial_indent_space)
+
+    def indent_str(self) -> str:
+        st = self._fmt_state()
+        return " " * (st["initial_indent"] + st["indent"] * st["indent_space"])
+
+    def set_paragraph_width(self, width: int) -> None:
+        self._fmt_state()["width"] = int(width)
+
+    def paragraph_width(self) -> int:
+        return self._fmt_state()["width"]
+
+    def set_paragraph_justification(self, justification_type: str) -> None:
+        if justification_type not in ("left", "right", "center", "full"):
+            raise ValueError(f"Error in MethodLog.set_paragraph_justification: invalid '{justification_type}'")
+        self._fmt_state()["justification"] = justification_type
+
+    def paragraph_justification(self) -> str:
+        return self._fmt_state()["justification"]
+
+    def section(self, what: str, show_clock: bool = False) -> None:
+        """A heading "-- what -- ", with the elapsed time when asked or when the clock is shown."""
+        text = self.indent_str() + "-- " + what + " -- "
+        if show_clock or self._fmt_state()["clock"]:
+            text += f"Time: {self.time_s()} (s)"
+        self._emit(text + "\n")
+
+    def paragraph(self, text: str) -> None:
+        """Indented, wrapped to the paragraph width and justified."""
+        import textwrap
+        st = self._fmt_state()
+        ind = self.indent_str()
+        width = max(1, st["width"] - len(ind))
+        lines = textwrap.wrap(" ".join(text.split()), width) or [""]
+        out = []
+        for i, line in enumerate(lines):
+            j = st["justification"]
+            if j == "right":
+                line = line.rjust(width)
+            elif j == "center":
+                line = line.center(width).rstrip()
+            elif j == "full" and i < len(lines) - 1 and " " in line:
+                words, gaps = line.split(" "), line.count(" ")
+                extra = width - len(line)
+                q, r = divmod(extra, gaps)
+                line = "".join(w + (" " * (1 + q + (k < r)) if k < gaps else "") for k, w in enumerate(words))
+            out.append(ind + line)
+        self._emit("\n".join(out) + "\n")
+
+    def verbatim(self, text: str, indent_first_line: bool = True) -> None:
+        """Each line indented, not re-wrapped or justified."""
+        ind = self.indent_str()
+        lines = text.split("\n")
+        self._emit("\n".join((ind if (k or indent_first_line) else "") + line for k, line in enumerate(lines)) + "\n")
 
 
 __all__ = ["BooleanValueMap", "MatrixValueMap", "MethodLog", "RandomNumberEngine", "RandomNumberGenerator",

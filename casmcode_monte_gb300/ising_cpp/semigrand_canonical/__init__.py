@@ -16,6 +16,7 @@ the run or run a convergence check.
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 import os
 import sys
@@ -101,6 +102,14 @@ class SemiGrandCanonicalPotential:
         dEf = self.formation_energy_calculator.occ_delta_per_supercell(linear_site_index, new_occ)
         Ndx = self.param_composition_calculator.occ_delta_per_supercell(linear_site_index, new_occ)
         return dEf - _dot(self.conditions.exchange_potential, Ndx)
+
+
+def _occ_event_delta_per_supercell(self, occ_event) -> float:
+    """The change of E_sgc for an OccEvent (its linear_site_index and new_occ)."""
+    return self.occ_delta_per_supercell(occ_event.linear_site_index, occ_event.new_occ)
+
+
+SemiGrandCanonicalPotential.occ_event_delta_per_supercell = _occ_event_delta_per_supercell
 
 
 def _dot(a, b) -> float:
@@ -384,6 +393,27 @@ class _ReplayDriver:
                 data.samplers[name].append(f())
         for name in sorted(data.json_sampling_functions):
             data.json_samplers[name].values.append(data.json_sampling_functions[name]())
+
+
+def _member_copy(self):
+    """A copy whose members are the same objects (system, state, samplers), as the
+    reference's copy constructors copy shared pointers."""
+    c = object.__new__(type(self))
+    c.__dict__.update(self.__dict__)
+    return c
+
+
+def _value_copy(self, memo=None):
+    c = object.__new__(type(self))
+    c.__dict__.update(copy.deepcopy(self.__dict__, memo))
+    return c
+
+
+SemiGrandCanonicalConditions.__copy__ = _value_copy
+SemiGrandCanonicalConditions.__deepcopy__ = _value_copy
+for _cls in (SemiGrandCanonicalPotential, SemiGrandCanonicalEventGenerator, SemiGrandCanonicalData):
+    _cls.__copy__ = _member_copy
+    _cls.__deepcopy__ = lambda self, memo=None: _member_copy(self)
 
 
 class SemiGrandCanonicalCalculator(_ReplayDriver):

@@ -215,6 +215,18 @@ def occupation_metropolis(state, occ_location, potential, possible_swaps, propos
 
 # ---- rejection-free and kinetic loops (methods/nfold.hh, methods/kinetic_monte_carlo.hh)
 
+def _member_copy(self, memo=None):
+    """A copy whose members are the same objects (samplers, functions), as the reference's
+    copy constructor copies shared pointers."""
+    c = object.__new__(type(self))
+    c.__dict__.update(self.__dict__)
+    return c
+
+
+BasicOccupationMetropolisData.__copy__ = _member_copy
+BasicOccupationMetropolisData.__deepcopy__ = _member_copy
+
+
 class NfoldData:
     """Data sampling functions can use during an N-fold way run (nfold.hh:24-44)."""
 
