@@ -152,7 +152,8 @@ class Sampler:
         self._n = v.shape[0]
 
     def clear(self) -> None:
-        self._data = np.zeros((self._data.shape[0], self._inc), dtype=np.float64)
+        """n_samples = 0; the buffer and its capacity are kept, so ``sample(i)`` still
+        reads what was stored there, as the reference's Sampler::clear leaves it."""
         self._n = 0
 
     def set_sample_capacity(self, capacity: int) -> None:
