@@ -14,9 +14,19 @@ value   device throughput of the sweep: attempts / sum over runs of the CUDA-eve
 e2e     the same job through the public C-ABI with host buffers: create the batch
         (H2D of occupations and parameters), run the passes returning per-pass samples to
         the host (D2H), read the final occupations (D2H); wall clock.
+batched the batched-chains workload (4096 binary FCC chains, L uniform in {8,12,16,24,32,48},
+        T in [300,2000] K, mu in [-0.3,0.3] eV, 500 passes, one persistent launch per CTA
+        class and layout) as converged-or-finished jobs/s, beside the same jobs one launch per
+        job on a sample; chains shard by rank.
+serving a Poisson stream of binary/ternary FCC jobs (L uniform in 16..128, pass budget
+        100..5000, stop at 1e-4 eV/site by the reference's rule) served with continuous
+        batching: converged jobs/s and p50/p99 latency, beside the same kind of jobs one at a
+        time; jobs shard by rank (job i on rank i mod N).
 --impl reference: the reference's CPU path (random-site SGC Metropolis, mt19937_64,
         FP64 cluster-expansion dE; the oracle restatement) on all host cores, one chain
         per process, each step a bounded sample.
+--gpus N without a torchrun environment starts its own N ranks (one process per GPU,
+        127.0.0.1 rendezvous) and prints rank 0's line.
 """
 from __future__ import annotations
 
@@ -41,6 +51,24 @@ N_CHAINS = 8
 BYTES_PER_ATTEMPT = 56  # (1 own read + 54 neighbour reads + 1 write) x int8
 METRIC = "Metropolis site-attempts/s (FCC 64^3 CE)"
 WORKLOAD = "fcc64_binary_ce_sgc_8T"
+
+
+def launch_ranks(n: int, argv: list) -> int:
+    """Start ``n`` ranks of this script (one process per GPU, RANK/LOCAL_RANK/WORLD_SIZE and a
+    127.0.0.1 rendezvous in their environment), forward rank 0's output and return the
+    largest exit code: ``--gpus N`` outside torchrun never silently runs one rank."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__), *argv], env=env,
+                                      stdout=None if r == 0 else subprocess.DEVNULL))
+    return max(p.wait() for p in procs)
 
 
 def _env_rank():
@@ -154,18 +182,25 @@ def cpu_baseline_sample(seconds_target: float = 10.0) -> dict:
 _REF_STATE = {}
 
 
-def _ref_worker(args):
-    """One bounded sample of the reference loop; the model and the chain's initial
-    occupation are built once per worker process and reused across steps."""
-    chain, n_steps, step = args
-    if chain not in _REF_STATE:
+def _ref_init():
+    """Worker set-up (pool initializer): the model and the chains' initial occupations."""
+    if "model" not in _REF_STATE:
         from tests import oracle_lib
 
         eci, occ, T, mu, seeds = make_inputs(0)
-        _REF_STATE[chain] = (oracle_lib.OracleCE((L, L, L), 2, eci), occ[chain].astype(np.int32),
-                             float(T[chain]), mu[chain])
-    orc, o, t_k, mu_c = _REF_STATE[chain]
-    _, _, t = orc.random_site_run(o, t_k, mu_c, 100 + 1000 * step + chain, n_steps)
+        _REF_STATE["model"] = oracle_lib.OracleCE((L, L, L), 2, eci)
+        _REF_STATE["inputs"] = (occ.astype(np.int32), T, mu)
+
+
+def _ref_worker(args):
+    """One bounded sample of the reference loop.  The model (the same cluster expansion for
+    every chain) and the chains' initial occupations are built once per worker process and
+    reused across steps, whichever chain a step hands the worker."""
+    chain, n_steps, step = args
+    _ref_init()
+    orc = _REF_STATE["model"]
+    occ, T, mu = _REF_STATE["inputs"]
+    _, _, t = orc.random_site_run(occ[chain], float(T[chain]), mu[chain], 100 + 1000 * step + chain, n_steps)
     return n_steps, t
 
 
@@ -180,7 +215,7 @@ def run_reference(args) -> None:
     steps_per_chain = int(min(args.ref_steps_per_sample, max(2e4, 0.8e6 * 120.0 / (args.steps + args.warmup))))
     ctx = mp.get_context("spawn")
     vals, walls = [], []
-    with ctx.Pool(n_proc) as pool:
+    with ctx.Pool(n_proc, initializer=_ref_init) as pool:
         for i in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             res = pool.map(_ref_worker, [(c % N_CHAINS, steps_per_chain, i) for c in range(n_proc)], chunksize=1)
@@ -199,6 +234,109 @@ def run_reference(args) -> None:
                              "sample": f"{steps_per_chain} random-site attempts per process, {n_proc} processes"},
             "e2e": {"value": value, "unit": "site-attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _gather(obj, dist_mod):
+    """Every rank's ``obj`` as a list (just [obj] on one rank)."""
+    if dist_mod is None:
+        return [obj]
+    out = [None] * dist_mod.get_world_size()
+    dist_mod.all_gather_object(out, obj)
+    return out
+
+
+def run_batched_extra(rank: int, world: int, dist_mod, n_chains: int = 4096, n_passes: int = 500,
+                      plain_sample: int = 48) -> dict:
+    """Batched chains (this rank's share: chain c on rank c mod N) in one persistent launch per
+    CTA class and layout, end to end through the pool API (admission H2D, the run, the
+    per-pass outputs and final occupations back to the host), against the same jobs one
+    ChainBatch per job (create, run, read back) on a sample."""
+    import torch
+
+    from casmcode_monte_gb300 import clex, workloads
+
+    model, jobs = workloads.batched_jobs(n_chains, seed=0)
+    mine = [j for j in jobs if j["id"] % world == rank]
+    total_sites = sum(j["L"] ** 3 for j in mine)
+    pool = clex.ChainPool(model, arena_bytes=total_sites + 16 * len(mine), max_chains=len(mine))
+    for L in workloads.BATCHED_L:  # geometry of every shape built once, as a long-lived pool has it
+        pool.prepare((L, L, L))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    slots = [pool.add((j["L"],) * 3, j["occ"], j["T"], j["mu"], j["seed"], j["id"]) for j in mine]
+    out = pool.run(slots, n_passes, want_output=True)
+    finals = [pool.occupation(s) for s in slots[:: max(1, len(slots) // 64)]]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    kernel_ms = pool.last_kernel_ms()
+    launches = pool.last_launches() if hasattr(pool, "last_launches") else None
+    pool.close()
+    rng = np.random.default_rng(1)
+    sample = [mine[int(i)] for i in rng.choice(len(mine), size=min(plain_sample, len(mine)), replace=False)]
+    for L in workloads.BATCHED_L:  # per-shape host geometry cached before the clock, as for the pool
+        clex.color_supercell("fcc_binary", (L, L, L))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for j in sample:
+        b = clex.ChainBatch(model, (j["L"],) * 3, j["occ"][None, :], [j["T"]], j["mu"][None, :], [j["seed"]],
+                            chain_ids=[j["id"]])
+        b.run(n_passes, want_output=True)
+        b.occupation()
+        b.close()
+    torch.cuda.synchronize()
+    plain_wall = time.perf_counter() - t1
+    per = _gather({"wall": wall, "kernel_ms": kernel_ms, "sites": total_sites, "n": len(mine),
+                   "plain_wall": plain_wall, "plain_n": len(sample),
+                   "accept": float(out[:, :, 0].sum())}, dist_mod)
+    wall_max = max(p["wall"] for p in per)
+    kms = max(p["kernel_ms"] for p in per)
+    n_all = sum(p["n"] for p in per)
+    sites_all = sum(p["sites"] for p in per)
+    plain_rate = sum(p["plain_n"] for p in per) / max(p["plain_wall"] for p in per)
+    jobs_per_s = n_all / wall_max
+    return {"workload": f"batched_fcc_binary_{n_chains}_chains", "chains": n_all, "passes": n_passes,
+            "jobs_per_s": jobs_per_s, "unit": "jobs/s",
+            "timed": "end to end: admission (H2D of every chain), one run of all passes with per-pass outputs "
+                     "back to the host, final occupations of a sample read back",
+            "kernel_ms": kms, "site_attempts_per_s_kernel": sites_all * n_passes / (kms * 1e-3),
+            "launches": launches,
+            "plain_jobs_per_s": plain_rate, "plain_sample_jobs": sum(p["plain_n"] for p in per),
+            "plain": "one ChainBatch per job: create (H2D), run with per-pass outputs, read the occupation",
+            "speedup_vs_plain": jobs_per_s / plain_rate,
+            "mean_acceptance": sum(p["accept"] for p in per) / (sites_all * n_passes)}
+
+
+def run_serving_extra(rank: int, world: int, dist_mod, n_jobs: int = 2000, rate: float = 200.0,
+                      plain_sample: int = 24) -> dict:
+    """A Poisson stream of jobs served with continuous batching (this rank's share: job i on
+    rank i mod N, arrival times kept), against the same kind of jobs run one at a time."""
+    from casmcode_monte_gb300 import clex, serving
+
+    models = {k: clex.ClexModel(k, clex.make_eci(k, 1)) for k in ("fcc_binary", "fcc_ternary")}
+    jobs = serving.poisson_jobs(n_jobs, rate, models, seed=0)
+    mine = [j for j in jobs if j.id % world == rank]
+    eng = serving.ServingEngine(models, arena_bytes=16 << 30, max_chains=4096, precision="fp32")
+    t_prep = eng.prepare(sorted({j.L for j in mine}))
+    st = eng.run(mine, realtime=True)
+    plain_jobs = [j for j in serving.poisson_jobs(plain_sample * world, rate, models, seed=1) if j.id % world == rank]
+    pst = serving.run_plain(plain_jobs, models, precision="fp32", prepare=True)
+    per = _gather({"lat": [j.latency for j in st.jobs], "conv": sum(1 for j in st.jobs if j.converged),
+                   "n": len(st.jobs), "wall": st.wall_s, "gpu_s": st.gpu_ms * 1e-3,
+                   "plain_conv": sum(1 for j in pst.jobs if j.converged), "plain_wall": pst.wall_s,
+                   "plain_n": len(pst.jobs), "prep": t_prep}, dist_mod)
+    lat = np.concatenate([np.asarray(p["lat"], dtype=np.float64) for p in per])
+    wall = max(p["wall"] for p in per)
+    conv = sum(p["conv"] for p in per)
+    plain_rate = sum(p["plain_conv"] for p in per) / max(p["plain_wall"] for p in per)
+    return {"workload": "serving_fcc_ce_poisson", "jobs": sum(p["n"] for p in per), "rate_per_s": rate,
+            "precision": "fp32 decisions (fp64 energies)", "converged_jobs": conv,
+            "converged_jobs_per_s": conv / wall, "unit": "converged jobs/s",
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "wall_s": wall, "gpu_busy_s": max(p["gpu_s"] for p in per),
+            "geometry_prepare_s": max(p["prep"] for p in per),
+            "plain_converged_jobs_per_s": plain_rate, "plain_sample_jobs": sum(p["plain_n"] for p in per),
+            "plain": "the same kind of jobs one at a time, one launch per 100-pass chunk per job",
+            "speedup_vs_plain": (conv / wall) / max(plain_rate, 1e-12)}
 
 
 def run_gpu(args) -> None:
@@ -280,15 +418,23 @@ def run_gpu(args) -> None:
         with open(peaks_path) as f:
             peak = float(json.load(f)["hbm_gbs"])
         peak_src = "measured"
-    per_launch_attempts = attempts_per_step * ppl
     achieved = BYTES_PER_ATTEMPT * attempts_per_step * args.steps / (kernel_ms * 1e-3) / 1e9
-    traffic = None
+    traffic, traffic_source = None, None
     tp = os.path.join(ROOT, "profiles", "ce_sweep_fcc64_binary_traffic.json")
-    if os.path.exists(tp):
+    last_launch_passes = min(ppl, args.steps)
+    if os.path.exists(tp) and launches > 0:
         with open(tp) as f:
             tj = json.load(f)
-        traffic = tj["dram_bytes_per_pass"] * ppl
+        # DRAM bytes per pass from an ncu capture of the same kernel and workload, scaled to
+        # the passes of one launch of this run (traffic per launch grows with its passes:
+        # the lattice stays in shared memory for the launch, so per pass it is nearly flat)
+        traffic = tj["dram_bytes_per_pass"] * args.steps / launches
+        traffic_source = f"{os.path.relpath(tp, ROOT)}: {tj['source']}; scaled to {args.steps / launches:g} passes per launch"
     rotation = batch.rotation()
+    extras = {}
+    if not args.no_extras:
+        extras["batched"] = run_batched_extra(rank, world, dist, n_chains=args.batched_chains)
+        extras["serving"] = run_serving_extra(rank, world, dist, n_jobs=args.serving_jobs)
     if rank == 0:
         cpu = cpu_baseline_sample(args.cpu_seconds) if args.cpu_seconds > 0 else None
         line = {
@@ -298,12 +444,14 @@ def run_gpu(args) -> None:
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "supercell": [L, L, L], "chains_per_gpu": N_CHAINS,
                        "temperatures_K": T.tolist(), "passes_per_launch": ppl,
-                       "ctas_per_chain": batch.ctas_per_chain, "rotation": rotation, "colors": batch.n_colors,
+                       "ctas_per_chain": batch.ctas_per_chain, "rotation": rotation,
+                       "rotated_launches": launches > (args.steps + ppl - 1) // ppl, "colors": batch.n_colors,
                        "threads_per_cta": batch.threads, "l2": "flushed between launches (256 MB write)",
                        "attempts_per_step": attempts_per_step},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                         "bytes_per_attempt": BYTES_PER_ATTEMPT, "attempts_per_launch": per_launch_attempts},
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_source,
+                         "peak_source": peak_src, "bytes_per_attempt": BYTES_PER_ATTEMPT,
+                         "attempts_per_launch": attempts_per_step * args.steps / max(launches, 1)},
             "e2e": {"value": e2e_value, "unit": "site-attempts/s", "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h_per_step + occ.nbytes / args.steps, "ms": e2e_best_ms},
             "gpu_launches": launches,
@@ -314,6 +462,7 @@ def run_gpu(args) -> None:
         }
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -477,12 +626,19 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-steps-per-sample", type=float, default=2e6)
     ap.add_argument("--nfold-size", type=int, default=32, help="supercell edge of the nfold workload")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving workloads")
+    ap.add_argument("--batched-chains", type=int, default=4096)
+    ap.add_argument("--serving-jobs", type=int, default=2000)
     ap.add_argument("--workload", default="fcc64_sgc", choices=["fcc64_sgc", "canonical", "nfold"],
                     help="fcc64_sgc: the headline semi-grand canonical pass; canonical: fixed-composition "
                          "sweeps of 48^3 chains; nfold: rejection-free dynamics of 32^3 chains")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args.gpus, sys.argv[1:]))
+    if args.gpus != int(os.environ.get("WORLD_SIZE", "1")):
+        ap.error(f"--gpus {args.gpus} but WORLD_SIZE={os.environ.get('WORLD_SIZE', '1')}")
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "canonical":

@@ -219,10 +219,12 @@ class ChainBatch:
         _lib.check(_lib.lib().mg_ce_batch_rotation(self._h, C.byref(S), C.byref(r)))
         return {"ctas_fast": S.value, "ratio": float(r.value)}
 
-    def set_rotation(self, allowed: bool) -> None:
+    def set_rotation(self, allowed) -> None:
         """Allow (re-plan) or forbid rotation over two cluster sizes; trajectories are the
-        same either way."""
-        _lib.check(_lib.lib().mg_ce_batch_set_rotation(self._h, 1 if allowed else 0))
+        same either way.  ``allowed="always"`` rotates every run long enough to have a plan
+        (at least 2 n_chains passes), also where one unrotated launch would be faster."""
+        mode = 2 if allowed == "always" else (1 if allowed else 0)
+        _lib.check(_lib.lib().mg_ce_batch_set_rotation(self._h, mode))
 
     def occupation(self) -> np.ndarray:
         occ = np.zeros((self.n_chains, self.n_sites), dtype=np.int8)

@@ -62,7 +62,8 @@ struct mg_ce_batch {
   // the others sweep on clusters of S_fast CTAs, each chain with the call's passes (see
   // rotation_plan).
   int S_fast = 0;  // 0: no rotation
-  bool rotation_allowed = true;
+  int rotation_mode = 1;  // 0: never; 1: when the plan beats one unrotated launch; 2: whenever a plan exists
+  double launch_passes = 0.0;  // fixed cost of one launch in slow-slot passes (0: not yet measured)
   int* dcstart_f = nullptr;
   uint32_t* dentries_f = nullptr;
   uint32_t* dsite_f = nullptr;
@@ -76,6 +77,7 @@ struct mg_ce_batch {
 // Pass counts of one rotated call (rotation_plan)
 struct RotationPlan {
   std::vector<int> a, g, b;  // chain c: passes on a fast cluster, in the slow slot, fast again
+  double makespan = 0.0, unrotated = 0.0;  // simulated, in slow-slot passes
 };
 
 namespace {
@@ -241,7 +243,7 @@ int setup_rotation(mg_ce_batch* b) {
   b->dsite_f = nullptr;
   b->S_fast = 0;
   const int C = b->n_chains;
-  if (b->layout != 3 || b->ctas_requested != 0 || !b->rotation_allowed || C < 2 || C - 1 > mg::CE_MAX_MAP)
+  if (b->layout != 3 || b->ctas_requested != 0 || b->rotation_mode == 0 || C < 2 || C - 1 > mg::CE_MAX_MAP)
     return MG_OK;
   const mg_ce_model* m = b->model;
   int dev = 0, max_smem = 0;
@@ -290,8 +292,8 @@ int setup_rotation(mg_ce_batch* b) {
 }
 
 // Fixed cost of one launch of the warp-specialised kernel (prologue, epilogue, launch
-// latency) in passes of a chain on the slow cluster: about 23 us against 31 us per pass of
-// FCC 64^3 at 12 CTAs on GB300.
+// latency) in passes of a chain on the slow cluster, until a rotated call has measured it:
+// about 23 us against 31 us per pass of FCC 64^3 at 12 CTAs on GB300.
 constexpr double kLaunchFixedPasses = 0.75;
 
 // Pass counts of a rotated call of P passes over C chains and C - 1 fast lanes.  Chain c
@@ -300,12 +302,14 @@ constexpr double kLaunchFixedPasses = 0.75;
 // first sweep); the last chain ends in the slow slot (g_{C-1} = P - a_{C-1}).  With r the
 // time per pass on a fast cluster over that on the slow one, a_c = round(c g / r) brings
 // chain c to the slot as chain c - 1 leaves it; g (every chain but the last) is the value
-// whose simulated schedule, with a fixed cost per launch, ends first.  False when the call
-// is too short to rotate (it then runs unrotated).
+// whose simulated schedule, with a fixed cost per launch, ends first.  False when no plan
+// exists, or (rotation mode 1) when the best plan does not end before one unrotated launch
+// of the P passes (P slow passes and one fixed cost): a short call loses more to the extra
+// launches than the faster clusters win back.
 bool rotation_plan(const mg_ce_batch* b, int P, RotationPlan* plan) {
   const int C = b->n_chains;
   if (b->S_fast <= 0 || P < 2 * C) return false;
-  const double r = b->ratio, phi = kLaunchFixedPasses;
+  const double r = b->ratio, phi = b->launch_passes > 0.0 ? b->launch_passes : kLaunchFixedPasses;
   double best = 1e300;
   for (int g = 1; g <= P; ++g) {
     std::vector<int> a(C), gg(C), bb(C);
@@ -336,7 +340,10 @@ bool rotation_plan(const mg_ce_batch* b, int P, RotationPlan* plan) {
       plan->b = bb;
     }
   }
-  return best < 1e299;
+  if (best >= 1e299) return false;
+  plan->makespan = best;
+  plan->unrotated = P + phi;
+  return b->rotation_mode == 2 || best < P + phi;
 }
 
 // One chain's sweep of n passes from pass offset `off` of this call, on a cluster of S CTAs
@@ -403,24 +410,44 @@ int launch_rotated(mg_ce_batch* b, const RotationPlan& p) {
 // the first fast sweeps (they start together, before any chain waits for the slow slot)
 // and the slow sweeps.  Rotation stops for the batch when it gains nothing (ratio above 1)
 // or when the slow cluster evidently did not run beside the fast ones (ratio below 0.6; the
-// occupancy model gives 0.86 for FCC 64^3 on GB300).
+// occupancy model gives 0.86 for FCC 64^3 on GB300).  The fixed cost of a launch comes from
+// a least-squares fit of every sweep of the call, t = n t_fast + t0 (fast clusters) or
+// n t_slow + t0 (slow slot), expressed in slow-slot passes (t0 / t_slow).
 constexpr int kMinRatioPasses = 8;
 void update_ratio(mg_ce_batch* b, const RotationPlan& p) {
   const int C = b->n_chains;
   double tf = 0.0, ts = 0.0;
   long nf = 0, ns = 0;
+  // normal equations of the fit over unknowns (t_fast, t_slow, t0)
+  double A[3][3] = {}, y[3] = {};
+  int n_fit = 0;
+  auto add = [&](double nfast, double nslow, double t) {
+    const double x[3] = {nfast, nslow, 1.0};
+    for (int i = 0; i < 3; ++i) {
+      for (int j = 0; j < 3; ++j) A[i][j] += x[i] * x[j];
+      y[i] += x[i] * t;
+    }
+    ++n_fit;
+  };
   for (int c = 0; c < C; ++c) {
     const cudaEvent_t* e = &b->rev[6 * (size_t)c];
     float ms = 0.f;
-    // launches of a few passes are dominated by their fixed start-up cost: not counted
-    if (c > 0 && p.a[c] >= kMinRatioPasses && cudaEventElapsedTime(&ms, e[0], e[1]) == cudaSuccess) {
-      tf += ms;
-      nf += p.a[c];
+    if (c > 0 && p.a[c] > 0 && cudaEventElapsedTime(&ms, e[0], e[1]) == cudaSuccess) {
+      add(p.a[c], 0.0, ms);
+      // launches of a few passes are dominated by their fixed start-up cost: not in the ratio
+      if (p.a[c] >= kMinRatioPasses) {
+        tf += ms;
+        nf += p.a[c];
+      }
     }
-    if (p.g[c] >= kMinRatioPasses && cudaEventElapsedTime(&ms, e[2], e[3]) == cudaSuccess) {
-      ts += ms;
-      ns += p.g[c];
+    if (cudaEventElapsedTime(&ms, e[2], e[3]) == cudaSuccess) {
+      add(0.0, p.g[c], ms);
+      if (p.g[c] >= kMinRatioPasses) {
+        ts += ms;
+        ns += p.g[c];
+      }
     }
+    if (c < C - 1 && p.b[c] > 0 && cudaEventElapsedTime(&ms, e[4], e[5]) == cudaSuccess) add(p.b[c], 0.0, ms);
   }
   if (nf > 0 && ns > 0 && tf > 0.0 && ts > 0.0) {
     const double r = (tf / nf) / (ts / ns);
@@ -428,6 +455,25 @@ void update_ratio(mg_ce_batch* b, const RotationPlan& p) {
       b->S_fast = 0;
     else
       b->ratio = r;
+  }
+  if (n_fit >= 4) {
+    // Cramer's rule on the 3 x 3 system; kept only when well conditioned and plausible
+    auto det3 = [](const double M[3][3]) {
+      return M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+             M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+    };
+    const double d = det3(A);
+    if (std::fabs(d) > 1e-9) {
+      double M[3][3];
+      double sol[3];
+      for (int k = 0; k < 3; ++k) {
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) M[i][j] = j == k ? y[i] : A[i][j];
+        sol[k] = det3(M) / d;
+      }
+      const double t_slow = sol[1], t0 = sol[2];
+      if (t_slow > 0.0 && t0 >= 0.0) b->launch_passes = std::min(std::max(t0 / t_slow, 0.05), 3.0);
+    }
   }
 }
 
@@ -728,7 +774,7 @@ int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout_out, int*
   // the occupancy choice of the warp-specialised layout with rotation over two cluster sizes,
   // timed per pass on runs long enough to rotate (at least 4 n_chains passes)
   bool best_rot = false;
-  if (rc == MG_OK && word && b->pipe >= 0 && b->rotation_allowed) {
+  if (rc == MG_OK && word && b->pipe >= 0 && b->rotation_mode != 0) {
     b->ctas_requested = 0;
     if (setup_layout(b, 3) == MG_OK && b->S_fast > 0) {
       const int np = std::max(probe_passes, 4 * b->n_chains);
@@ -853,7 +899,11 @@ int mg_ce_batch_set_rotation(mg_ce_batch* b, int allowed) {
     set_error("Error in mg_ce_batch_set_rotation: invalid argument");
     return MG_ERR_INVALID;
   }
-  b->rotation_allowed = allowed != 0;
+  if (allowed < 0 || allowed > 2) {
+    set_error("Error in mg_ce_batch_set_rotation: mode must be 0, 1 or 2");
+    return MG_ERR_INVALID;
+  }
+  b->rotation_mode = allowed;
   return setup_rotation(b);
 }
 

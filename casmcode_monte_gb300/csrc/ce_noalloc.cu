@@ -4,9 +4,20 @@
 // framework's memory pool or allocator hooks, a process whose device memory is fully
 // reserved up front, or a plugin host that forbids allocation during a run.  They own
 // the occupation and output buffers; everything else the sweep needs (per-colour site
-// lists and per-chain parameters) lives here in a fixed file-scope device array, so
-// this entry point calls no cudaMalloc, cudaFree or other allocating routine (host
-// staging uses static arrays as well).
+// lists, per-chain parameters and the occupant-check counter) lives here in a fixed
+// file-scope device array, so this entry point calls no cudaMalloc, cudaFree or other
+// allocating device routine.  Host staging of the lists and parameters uses static
+// arrays; the colouring and site-list helpers still use a little host heap (bank tables,
+// the per-device occupancy cache).  Where the CUDA runtime loads modules lazily, the
+// first call on a device is when the driver sets up the array's device memory.
+//
+// The sweep is the byte-layout kernel (one site per byte, any shape), the slowest of the
+// library's layouts; the batch API picks faster word layouts where the shape allows.
+//
+// The caller's occupations are checked on the device before the sweep: a code outside
+// [0, n_species) would index outside the kernel's per-species tables.  The check kernel
+// counts such codes into the array, the call waits for that count (one synchronisation
+// of `stream` per call) and returns an error without sweeping when it is not zero.
 //
 // Limits: at most MG_NOALLOC_MAX_SITES sites per chain and MG_NOALLOC_MAX_CHAINS chains
 // per call; the scratch array (MG_NOALLOC_SCRATCH_BYTES) stays resident on every device
@@ -16,6 +27,9 @@
 // share the one array and it keeps the last call's contents; calls that overlap on the
 // GPU (for example on two streams) race on it, and host calls must not run concurrently.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
 
 #include "../../include/montegpu.h"
 #include "ce_host.cuh"
@@ -33,7 +47,8 @@ constexpr size_t kOffCp = 0;
 constexpr size_t kOffCstart = align256(kOffCp + sizeof(mg::CeChainParams) * kMaxChains);
 constexpr size_t kOffEntries = align256(kOffCstart + sizeof(int) * kMaxCtas * (mg::CE_MAX_COLORS + 1));
 constexpr size_t kOffSite = align256(kOffEntries + sizeof(uint32_t) * kMaxSites);
-constexpr size_t kScratchBytes = align256(kOffSite + sizeof(uint32_t) * kMaxSites);
+constexpr size_t kOffBad = align256(kOffSite + sizeof(uint32_t) * kMaxSites);
+constexpr size_t kScratchBytes = align256(kOffBad + sizeof(unsigned int));
 static_assert(kScratchBytes <= MG_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the declared size");
 
 // The scratch array.  Host code must not use its name as an address (it is a host-side
@@ -49,6 +64,19 @@ static int h_cstart[kMaxCtas * (mg::CE_MAX_COLORS + 1)];
 static uint32_t h_entries[kMaxSites];
 static uint32_t h_site[kMaxSites];
 static int32_t h_color[kMaxSites];
+static unsigned int h_bad = 0;
+
+// Counts occupant codes outside [0, n_species) in occ[0, n) into *bad.  Reads only.
+__global__ void occupant_check_kernel(const int8_t* __restrict__ occ, long long n, int n_species,
+                                      unsigned int* __restrict__ bad) {
+  unsigned int count = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int o = occ[i];
+    count += (o < 0 || o >= n_species) ? 1u : 0u;
+  }
+  count = __reduce_add_sync(0xffffffffu, count);
+  if ((threadIdx.x & 31) == 0 && count) atomicAdd(bad, count);
+}
 
 int scratch_address(unsigned char** out) {
   int dev = 0;
@@ -111,6 +139,20 @@ extern "C" int mg_ce_sweep_noalloc(const mg_ce_model* m, int L0, int L1, int L2,
   make_chain_params(m, n_chains, temperature, mu, seeds, nullptr, h_cp);
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // occupant codes first: nothing is swept unless every code is in range
+  unsigned int* d_bad = reinterpret_cast<unsigned int*>(scratch + kOffBad);
+  MG_CUDA_TRY(cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), st));
+  const long long n_occ = N * n_chains;
+  const int check_blocks = (int)std::min<long long>((n_occ + 255) / 256, 1184);
+  occupant_check_kernel<<<check_blocks, 256, 0, st>>>(d_occ, n_occ, m->n_species, d_bad);
+  MG_CUDA_TRY(cudaGetLastError());
+  MG_CUDA_TRY(cudaMemcpyAsync(&h_bad, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+  MG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (h_bad != 0) {
+    mg::set_error("Error in mg_ce_sweep_noalloc: occupant index out of range (" + std::to_string(h_bad) +
+                  " codes outside [0, n_species))");
+    return MG_ERR_INVALID;
+  }
   mg::CeChainParams* d_cp = reinterpret_cast<mg::CeChainParams*>(scratch + kOffCp);
   int* d_cstart = reinterpret_cast<int*>(scratch + kOffCstart);
   uint32_t* d_entries = reinterpret_cast<uint32_t*>(scratch + kOffEntries);

@@ -147,11 +147,14 @@ def run_precision(L: int = 96, n_passes: int = 5000, T: float = 600.0, recompute
         xb = np.concatenate(x_b)[discard:]
         xc = np.concatenate(x_c)[discard:]
         kB = clex.KB
-        # heat capacity per site in units of kB: N * Var(e) / (kB T)^2
+        # heat capacity per site in units of kB: N * Var(e) / (kB T)^2, with the precision of
+        # the mean of its per-pass terms N (e - <e>)^2 / (kB T)^2
         cv = n * float(np.var(e)) / (kB * T) ** 2
+        cv_terms = _stats(n * (e - e.mean()) ** 2 / (kB * T) ** 2)
         series[prec] = e
         result[prec] = {
             "E_per_site": _stats(e), "x_B": _stats(xb), "x_C": _stats(xc), "Cv_per_site_kB": cv,
+            "Cv_precision": cv_terms["precision"],
             "acceptance": n_acc / (n * n_passes), "fp64_redecisions": n_exact,
             "fp32_flipped_decisions": n_flip, "recompute_mismatches": mismatches,
             "kernel_s": kernel_ms * 1e-3, "site_attempts_per_s": n * n_passes / (kernel_ms * 1e-3),
@@ -164,6 +167,8 @@ def run_precision(L: int = 96, n_passes: int = 5000, T: float = 600.0, recompute
             "combined_error_bar": (d32[k]["precision"] ** 2 + d64[k]["precision"] ** 2) ** 0.5}
         for k in ("E_per_site", "x_B", "x_C")}
     result["fp32_minus_fp64"]["Cv_rel"] = d32["Cv_per_site_kB"] / d64["Cv_per_site_kB"] - 1.0
+    result["fp32_minus_fp64"]["Cv"] = {"diff": d32["Cv_per_site_kB"] - d64["Cv_per_site_kB"],
+                                       "combined_error_bar": (d32["Cv_precision"] ** 2 + d64["Cv_precision"] ** 2) ** 0.5}
     return result
 
 

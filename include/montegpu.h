@@ -147,10 +147,14 @@ int mg_ce_batch_last_kernel_ms(const mg_ce_batch* b, float* ms);
  * cluster of ctas_per_chain CTAs (the slow slot) while the others sweep on clusters of
  * ctas_fast CTAs: chain c sweeps a_c passes fast, g passes in the slow slot (chains in
  * order) and the rest fast, with a_c and g set from the measured time ratio so that the slow
- * slot stays busy and every chain gets the run's passes.  Outputs and occupations are
- * identical to unrotated runs.  ctas_fast receives 0 when the batch does not rotate; ratio
- * the measured time per pass on ctas_fast CTAs over that on ctas_per_chain CTAs.
- * set_rotation(b, 0) turns it off for the batch, set_rotation(b, 1) re-plans it.
+ * slot stays busy and every chain gets the run's passes.  A run rotates only when the
+ * simulated rotated schedule (with the launch fixed cost measured by earlier rotated runs)
+ * ends before one unrotated launch of the same passes; short runs stay unrotated.  Outputs
+ * and occupations are identical to unrotated runs.  ctas_fast receives 0 when the batch does
+ * not rotate; ratio the measured time per pass on ctas_fast CTAs over that on ctas_per_chain
+ * CTAs.  set_rotation(b, mode): 0 turns it off for the batch, 1 re-plans it (the default),
+ * 2 rotates every run of at least 2 n_chains passes even where it does not pay (to test
+ * the rotated schedule).
  * last_launches: sweep kernels launched by the last run (1 unless it rotated). */
 int mg_ce_batch_rotation(const mg_ce_batch* b, int* ctas_fast, double* ratio);
 int mg_ce_batch_set_rotation(mg_ce_batch* b, int allowed);
@@ -267,17 +271,22 @@ int mg_ce_pool_destroy(mg_ce_pool* p);
 /* ---- allocation-free coloured sweep (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc (an embedding framework owns all device
  * memory, allocation is forbidden during a run, or the device is fully reserved): the
- * caller passes device pointers to the occupations d_occ[n_chains][N] (in/out) and the
- * per-pass outputs d_out[n_passes][n_chains][n_classes+2] (same meaning as
- * mg_ce_batch_run), plus host arrays of temperatures, exchange potentials and seeds.
- * The site lists and chain parameters go to a fixed file-scope device array of
- * MG_NOALLOC_SCRATCH_BYTES, resident on every device that loads the library until exit;
- * nothing is allocated.  Sizes beyond MG_NOALLOC_MAX_SITES sites per chain or
- * MG_NOALLOC_MAX_CHAINS chains are rejected.  The first call on a device looks up the
- * array's address (do it before any stream capture).  Calls share the array: calls that
- * overlap on the GPU race, and host calls must not run concurrently.  Work is enqueued
- * on `stream` (a cudaStream_t, NULL = legacy default stream) and not synchronised;
- * pass0 continues the Philox pass counter. */
+ * caller passes device pointers to the occupations d_occ[n_chains][N] (in/out; every code
+ * in [0, n_species)) and the per-pass outputs d_out[n_passes][n_chains][n_classes+2]
+ * (same meaning as mg_ce_batch_run), plus host arrays of temperatures, exchange
+ * potentials and seeds.  The site lists, chain parameters and an occupant-check counter
+ * go to a fixed file-scope device array of MG_NOALLOC_SCRATCH_BYTES, resident on every
+ * device that loads the library until exit; no device memory is allocated after the
+ * first call on a device (the colouring and site-list helpers use some host heap).
+ * Sizes beyond MG_NOALLOC_MAX_SITES sites per chain or MG_NOALLOC_MAX_CHAINS chains are
+ * rejected.  Occupant codes are checked on the device first; the call waits for that
+ * check (it synchronises `stream`) and returns MG_ERR_INVALID, sweeping nothing, when a
+ * code is out of range.  The sweep itself runs the byte-layout kernel (one site per byte),
+ * the slowest layout of the batch API.  The first call on a device looks up the array's
+ * address (do it before any stream capture).  Calls share the array: calls that overlap
+ * on the GPU race, and host calls must not run concurrently.  The sweep is enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) after the check and not
+ * synchronised; pass0 continues the Philox pass counter. */
 #define MG_NOALLOC_MAX_SITES 262144
 #define MG_NOALLOC_MAX_CHAINS 64
 #define MG_NOALLOC_SCRATCH_BYTES 2162688

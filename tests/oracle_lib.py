@@ -255,3 +255,33 @@ def sgc_proposals(occ, n_species, seed, n_steps, apply=True):
                                   p(l_out, C.c_long), p(o_out, C.c_int))
     assert rc == 0, rc
     return l_out, o_out
+
+
+def _colored_sweep_job(args):
+    """Process-pool job: the oracle's coloured sweep of one chain (see OracleCE.colored_sweep)."""
+    L, n_species, eci, occ, T, mu, seed, chain, colors, n_colors, pass0, n_passes, n_classes = args
+    orc = OracleCE(L, n_species, eci)
+    return orc.colored_sweep(occ, T, mu, seed, chain, colors, n_colors, pass0, n_passes, n_classes)
+
+
+def _sgc_samples_job(args):
+    """Process-pool job: the oracle's reference-dynamics semi-grand canonical run."""
+    L, n_species, eci, occ, T, mu, seed, n_passes = args
+    return OracleCE(L, n_species, eci).sgc_samples(occ, T, mu, seed, n_passes)
+
+
+def oracle_pool(n_workers: int):
+    """A process pool for oracle jobs, started with ``spawn`` (safe after CUDA is initialised)."""
+    import multiprocessing as mp
+    import os
+
+    return mp.get_context("spawn").Pool(max(1, min(n_workers, os.cpu_count() or 1)))
+
+
+def colored_sweeps(pool, jobs):
+    """Run coloured-sweep jobs (argument tuples of _colored_sweep_job) asynchronously."""
+    return pool.map_async(_colored_sweep_job, jobs, chunksize=1)
+
+
+def sgc_samples_async(pool, jobs):
+    return pool.map_async(_sgc_samples_job, jobs, chunksize=1)

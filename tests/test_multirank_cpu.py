@@ -73,3 +73,34 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     args = argparse.Namespace(gpus=2, steps=3, warmup=1, ref_steps_per_sample=1e4)
     bench.run_reference(args)  # returns at once, prints nothing
     assert capsys.readouterr().out == ""
+
+
+def test_gpus_flag_starts_its_own_ranks():
+    """``bench.py --gpus 2`` outside torchrun starts two ranks itself (RANK/WORLD_SIZE set per
+    process, 127.0.0.1 rendezvous): here through the reference arm, which needs no GPU; rank 0
+    prints the one line and rank 1 exits 0 without work."""
+    import json
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "3", "--warmup", "3", "--ref-steps-per-sample", "2000"],
+                       capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2
+
+
+def test_gpus_flag_must_match_world_size():
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "3", "--warmup", "3"], capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode != 0 and "WORLD_SIZE" in r.stderr

@@ -28,6 +28,7 @@ def test_rotated_runs_equal_unrotated():
     model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 5))
     occ, T, mu, seeds = _inputs()
     rot = clex.ChainBatch(model, (64, 64, 64), occ, T, mu, seeds)
+    rot.set_rotation("always")  # rotate every run that has a plan, also where it does not pay
     plain = clex.ChainBatch(model, (64, 64, 64), occ, T, mu, seeds)
     plain.set_rotation(False)
     assert plain.rotation()["ctas_fast"] == 0
@@ -48,6 +49,30 @@ def test_rotated_runs_equal_unrotated():
     assert rot.rotation()["ctas_fast"] == 16 or torch.cuda.get_device_properties(0).multi_processor_count != 152
     assert np.array_equal(rot.corr(), plain.corr())
     rot.close()
+    plain.close()
+
+
+def test_short_runs_stay_unrotated():
+    """A run too short for the rotated schedule to beat one unrotated launch (20 passes of 8
+    chains: the extra launches cost more than the faster clusters gain) runs unrotated; a long
+    one (200 passes) rotates.  Both give the unrotated trajectory."""
+    torch = pytest.importorskip("torch")
+    model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 5))
+    occ, T, mu, seeds = _inputs(seed=34)
+    auto = clex.ChainBatch(model, (64, 64, 64), occ, T, mu, seeds)
+    if auto.rotation()["ctas_fast"] == 0:
+        pytest.skip("this GPU has no rotation plan for 8 chains of 64^3")
+    plain = clex.ChainBatch(model, (64, 64, 64), occ, T, mu, seeds)
+    plain.set_rotation(False)
+    assert np.array_equal(auto.run(20), plain.run(20))
+    assert auto.last_launches() == 1
+    assert np.array_equal(auto.run(200), plain.run(200))
+    if torch.cuda.get_device_properties(0).multi_processor_count == 152:
+        assert auto.last_launches() > 8
+    assert np.array_equal(auto.run(20), plain.run(20))
+    assert auto.last_launches() == 1
+    assert np.array_equal(auto.occupation(), plain.occupation())
+    auto.close()
     plain.close()
 
 
