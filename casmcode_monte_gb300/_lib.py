@@ -105,6 +105,15 @@ SIGNATURES = {
     "mg_ce_pool_series": (C.c_int, [vp, C.c_int, c_double_p, C.c_int, c_int_p]),
     "mg_ce_pool_check": (C.c_int, [vp, c_int32_p, C.c_int, C.c_double, C.c_double, c_double_p]),
     "mg_ce_pool_destroy": (C.c_int, [vp]),
+    "mg_ce_replay_create": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p, c_double_p, c_int8_p,
+                                      C.POINTER(C.c_char_p), vpp]),
+    "mg_ce_replay_run": (C.c_int, [vp, C.c_int, c_ll_p]),
+    "mg_ce_replay_get_occ": (C.c_int, [vp, c_int8_p]),
+    "mg_ce_replay_engine_state": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int]),
+    "mg_ce_replay_candidates": (C.c_int, [vp, C.c_int, c_int32_p, c_int32_p]),
+    "mg_ce_replay_counts": (C.c_int, [vp, c_ull_p, c_ull_p]),
+    "mg_ce_replay_last_kernel_ms": (C.c_int, [vp, c_float_p]),
+    "mg_ce_replay_destroy": (C.c_int, [vp]),
     "mg_ce_sweep_noalloc": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p, c_double_p, c_uint64_p,
                                       vp, C.c_longlong, C.c_int, vp, C.c_int, vp]),
     "mg_equilibration_check": (C.c_int, [c_double_p, C.c_long, C.c_double, c_int_p, c_long_p]),

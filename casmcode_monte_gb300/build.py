@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIBNAME = "libmontegpu.so"
-SOURCES = ["mg_api.cu", "ising_replay.cu", "ce_api.cu", "ce_noalloc.cu", "ce_pool.cu", "ce_canonical.cu", "ce_nfold.cu"]
+SOURCES = ["mg_api.cu", "ising_replay.cu", "ce_api.cu", "ce_noalloc.cu", "ce_pool.cu", "ce_canonical.cu", "ce_nfold.cu", "ce_replay.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code keeps a*b+c unfused (-ffp-contract=off) so results match the reference's
 # un-contracted FP64 arithmetic on aarch64 as on x86-64

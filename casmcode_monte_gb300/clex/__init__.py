@@ -416,6 +416,90 @@ class NfoldBatch:
         return out
 
 
+class ReplayBatch:
+    """Chains of one supercell replaying the reference's semi-grand canonical dynamics on the
+    GPU (handle to mg_ce_replay): per step a swap type chosen by random_real over the occupant
+    counts, a site by random_int over the chosen species' occupant list, Metropolis acceptance
+    with random_real(1.0), occupant lists kept as OccLocation keeps them; each chain consumes
+    its std::mt19937_64 exactly as the reference's RandomNumberGenerator would.
+
+    occ: [n_chains, N] occupant indices; temperature [n_chains]; mu [n_chains, n_species-1];
+    engine_states: per chain, the engine's text form (``RandomNumberEngine.dump()``).
+    """
+
+    def __init__(self, model: ClexModel, shape: Sequence[int], occ, temperature, mu, engine_states):
+        self.model = model
+        self.shape = tuple(int(x) for x in shape)
+        L0, L1, L2 = self.shape
+        self.n_sites = L0 * L1 * L2
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int8).reshape(-1, self.n_sites))
+        self.n_chains = occ.shape[0]
+        T = np.ascontiguousarray(np.asarray(temperature, dtype=np.float64).reshape(self.n_chains))
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64).reshape(self.n_chains, model.n_species - 1))
+        if len(engine_states) != self.n_chains:
+            raise ValueError("one engine state per chain")
+        states = (C.c_char_p * self.n_chains)(*[s.encode() if isinstance(s, str) else s for s in engine_states])
+        h = C.c_void_p()
+        _lib.check(_lib.lib().mg_ce_replay_create(model._h, L0, L1, L2, self.n_chains, _lib.ptr(T, C.c_double),
+                                                  _lib.ptr(mu, C.c_double), _lib.ptr(occ, C.c_int8), states,
+                                                  C.byref(h)))
+        self._h = h
+        self.temperature, self.mu = T, mu
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.mg_ce_replay_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, n_passes: int, want_output: bool = True) -> Optional[np.ndarray]:
+        """n_passes passes of N steps; returns [n_passes, n_chains, n_classes+2] int64: accepted
+        steps, the change of each integer correlation sum (classes 1..), rejected steps, 0."""
+        if int(n_passes) < 0:
+            raise RuntimeError("Error in mg_ce_replay_run: invalid argument")
+        out = np.zeros((n_passes, self.n_chains, self.model.n_classes + 2), dtype=np.int64) if want_output else None
+        _lib.check(_lib.lib().mg_ce_replay_run(self._h, int(n_passes),
+                                               _lib.ptr(out, C.c_longlong) if out is not None else None))
+        return out
+
+    def occupation(self) -> np.ndarray:
+        occ = np.zeros((self.n_chains, self.n_sites), dtype=np.int8)
+        _lib.check(_lib.lib().mg_ce_replay_get_occ(self._h, _lib.ptr(occ, C.c_int8)))
+        return occ
+
+    def engine_state(self, chain: int) -> str:
+        buf = C.create_string_buffer(16384)
+        _lib.check(_lib.lib().mg_ce_replay_engine_state(self._h, int(chain), buf, len(buf)))
+        return buf.value.decode()
+
+    def candidates(self, chain: int) -> list:
+        """The chain's occupant lists (one per species, list order), as OccLocation holds them."""
+        sizes = np.zeros(self.model.n_species, dtype=np.int32)
+        sites = np.zeros(self.n_sites, dtype=np.int32)
+        _lib.check(_lib.lib().mg_ce_replay_candidates(self._h, int(chain), _lib.ptr(sizes, C.c_int32),
+                                                      _lib.ptr(sites, C.c_int32)))
+        out, off = [], 0
+        for n in sizes:
+            out.append(sites[off:off + n].copy())
+            off += int(n)
+        return out
+
+    def counts(self) -> tuple[np.ndarray, np.ndarray]:
+        """Accepted and rejected steps per chain since creation."""
+        a = np.zeros(self.n_chains, dtype=np.uint64)
+        r = np.zeros(self.n_chains, dtype=np.uint64)
+        _lib.check(_lib.lib().mg_ce_replay_counts(self._h, _lib.ptr(a, C.c_ulonglong), _lib.ptr(r, C.c_ulonglong)))
+        return a, r
+
+    def last_kernel_ms(self) -> float:
+        ms = C.c_float()
+        _lib.check(_lib.lib().mg_ce_replay_last_kernel_ms(self._h, C.byref(ms)))
+        return float(ms.value)
+
+
 class PoolFull(RuntimeError):
     """Admission refused: no free chain slot or not enough arena memory."""
 

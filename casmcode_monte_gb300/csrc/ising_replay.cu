@@ -215,23 +215,6 @@ void free_replay(mg_ising_replay* h) {
   delete h;
 }
 
-int parse_mt_state(const char* text, uint64_t* out313) {
-  std::istringstream ss(text);
-  for (int i = 0; i < mg::MT_N + 1; ++i) {
-    unsigned long long v;
-    if (!(ss >> v)) return -1;
-    out313[i] = v;
-  }
-  return 0;
-}
-
-std::string format_mt_state(const uint64_t* s313) {
-  std::ostringstream ss;
-  for (int i = 0; i < mg::MT_N; ++i) ss << (unsigned long long)s313[i] << ' ';
-  ss << (unsigned long long)s313[mg::MT_N];
-  return ss.str();
-}
-
 }  // namespace
 
 extern "C" {
@@ -262,7 +245,7 @@ int mg_ising_replay_create(int rows, int cols, int n_chains, int use_nlist, cons
   h->use_nlist = use_nlist ? 1 : 0;
   std::vector<uint64_t> mt((size_t)n_chains * (mg::MT_N + 1));
   for (int c = 0; c < n_chains; ++c) {
-    if (!engine_states[c] || parse_mt_state(engine_states[c], mt.data() + (size_t)c * (mg::MT_N + 1))) {
+    if (!engine_states[c] || mg::parse_mt_state(engine_states[c], mt.data() + (size_t)c * (mg::MT_N + 1))) {
       free_replay(h);
       mg::set_error("Error in mg_ising_replay_create: malformed engine state");
       return MG_ERR_INVALID;
@@ -412,7 +395,7 @@ int mg_ising_replay_get_state(mg_ising_replay* h, int32_t* occ, char** engine_st
     for (size_t i = 0; i < o8.size(); ++i) occ[i] = o8[i];
   for (int c = 0; c < h->n_chains; ++c) {
     if (engine_states && engine_states[c]) {
-      std::string s = format_mt_state(mt.data() + (size_t)c * (mg::MT_N + 1));
+      std::string s = mg::format_mt_state(mt.data() + (size_t)c * (mg::MT_N + 1));
       if (s.size() + 1 > state_len) {
         mg::set_error("Error in mg_ising_replay_get_state: engine state buffer too small");
         return MG_ERR_INVALID;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <sstream>
 #include <string>
 
 namespace mg {
@@ -89,6 +90,65 @@ __device__ __forceinline__ void mt_twist_warp(uint64_t* x, int lane) {
       __syncwarp();
     }
   }
+}
+
+// Text form of a mt19937_64 state as libstdc++'s operator<< / operator>> write and read it:
+// the 312 state words, then the position index, separated by spaces.
+inline int parse_mt_state(const char* text, uint64_t* out313) {
+  std::istringstream ss(text);
+  for (int i = 0; i < MT_N + 1; ++i) {
+    unsigned long long v;
+    if (!(ss >> v)) return -1;
+    out313[i] = v;
+  }
+  return 0;
+}
+
+inline std::string format_mt_state(const uint64_t* s313) {
+  std::ostringstream ss;
+  for (int i = 0; i < MT_N; ++i) ss << (unsigned long long)s313[i] << ' ';
+  ss << (unsigned long long)s313[MT_N];
+  return ss.str();
+}
+
+// next tempered word of a warp-shared state (x: 312 words in shared memory, p: position,
+// uniform across the warp); the warp regenerates the state when it is used up
+__device__ __forceinline__ uint64_t mt_next_warp(uint64_t* x, int& p, int lane) {
+  if (p >= MT_N) {
+    mt_twist_warp(x, lane);
+    p = 0;
+  }
+  const uint64_t y = x[p];
+  p += 1;
+  return mt_temper(y);
+}
+
+// std::uniform_int_distribution<64-bit>(0, range - 1) over mt19937_64 as libstdc++
+// computes it for a range below 2^64: Lemire's method with a 128-bit product, drawing again
+// while the low half is below (2^64 - range) mod range.
+__device__ __forceinline__ uint64_t mt_uniform_int_warp(uint64_t* x, int& p, int lane, uint64_t range) {
+  uint64_t w = mt_next_warp(x, p, lane);
+  uint64_t lo = w * range;
+  uint64_t hi = __umul64hi(w, range);
+  if (lo < range) {
+    const uint64_t threshold = (0ull - range) % range;
+    while (lo < threshold) {
+      w = mt_next_warp(x, p, lane);
+      lo = w * range;
+      hi = __umul64hi(w, range);
+    }
+  }
+  return hi;
+}
+
+// std::generate_canonical<double, 53>(mt19937_64) as libstdc++ computes it: one word,
+// double(word) / 2^64 (exact scaling of the rounded word), and the largest double below 1
+// if that rounds up to 1.
+__device__ __forceinline__ double mt_canonical_warp(uint64_t* x, int& p, int lane) {
+  const uint64_t w = mt_next_warp(x, p, lane);
+  double u = __dmul_rn(__ull2double_rn(w), 5.421010862427522170e-20);
+  if (u >= 1.0) u = 0.99999999999999988898;
+  return u;
 }
 
 // Lemire's nearly-divisionless bounded integer in [0, range) from 64-bit words

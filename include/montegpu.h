@@ -268,6 +268,32 @@ int mg_ce_pool_check(mg_ce_pool* p, const int32_t* slots, int n, double abs_prec
                      double* out);
 int mg_ce_pool_destroy(mg_ce_pool* p);
 
+/* ---- serial replay of the reference's semi-grand canonical dynamics (cluster expansion) ----
+ * Replaces, for an FCC cluster expansion on one asymmetric unit, the loop of
+ * methods/occupation_metropolis.hh:114-150 with propose_semigrand_canonical_event
+ * (events/OccEventProposal.hh:260-336), OccLocation::choose_mol / apply
+ * (events/OccLocation.hh:257-261, OccLocation.cc:216-283) and metropolis_acceptance
+ * (methods/metropolis.hh:26-35), consuming each chain's std::mt19937_64 exactly as the
+ * reference's RandomNumberGenerator does (RandomNumberGenerator.hh:32-41): one warp per
+ * chain, N = L0 L1 L2 steps per pass.  engine_states: the engines' text form (312 words and
+ * the position, as operator<< writes it).  occ[n_chains][N] occupant indices; mu
+ * [n_chains][n_species-1].  mg_ce_replay_run: out (optional) [n_passes][n_chains]
+ * [n_classes+2] = {accepted steps of the pass, change of each integer correlation sum
+ * (classes 1..n_classes-1), rejected steps of the pass, 0}.  mg_ce_replay_candidates: the
+ * occupant lists (OccLocation::m_loc, one candidate per species) in list order, species by
+ * species, with their sizes.  At most 200000 sites. */
+typedef struct mg_ce_replay mg_ce_replay;
+int mg_ce_replay_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chains, const double* temperature,
+                        const double* mu, const int8_t* occ, const char* const* engine_states,
+                        mg_ce_replay** out);
+int mg_ce_replay_run(mg_ce_replay* h, int n_passes, long long* out);
+int mg_ce_replay_get_occ(mg_ce_replay* h, int8_t* occ);
+int mg_ce_replay_engine_state(mg_ce_replay* h, int chain, char* buf, int buf_len);
+int mg_ce_replay_candidates(mg_ce_replay* h, int chain, int32_t* sizes, int32_t* sites);
+int mg_ce_replay_counts(mg_ce_replay* h, unsigned long long* n_accept, unsigned long long* n_reject);
+int mg_ce_replay_last_kernel_ms(const mg_ce_replay* h, float* ms);
+int mg_ce_replay_destroy(mg_ce_replay* h);
+
 /* ---- allocation-free coloured sweep (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc (an embedding framework owns all device
  * memory, allocation is forbidden during a run, or the device is fully reserved): the

@@ -424,6 +424,95 @@ long long orc_ce_sgc_samples(void* h, int* occ, double T, const double* mu, int 
   return nacc;
 }
 
+// The same semi-grand canonical dynamics as orc_ce_sgc_samples from a given engine state
+// (std::mt19937_64 text form, as operator<< writes it), for the serial-replay comparison:
+// per pass the accepted count nacc_out[p], the potential energy per site e_out[p] (E_f
+// tracked by accepted FP64 changes) and x_out[p][i]; at the end the occupant lists
+// (OccLocation::m_loc per species, list order) in loc_out with their sizes in
+// loc_sizes_out[ns], and the engine state in state_out.  Returns the accepted count, or -1.
+long long orc_ce_sgc_run(void* h, int* occ, double T, const double* mu, int n_mu, const char* engine_state,
+                         long n_passes, double* e_out, double* x_out, long long* nacc_out, int* loc_sizes_out,
+                         int* loc_out, char* state_out, long state_len) {
+  auto* S = static_cast<CESupercell*>(h);
+  const int ns = S->basis.n_species;
+  if (n_mu != ns - 1) return -1;
+  std::vector<double> m(mu, mu + n_mu);
+  std::mt19937_64 e;
+  {
+    std::stringstream in(engine_state);
+    in >> e;
+    if (in.fail()) return -1;
+  }
+  RNG rng{&e};
+  const double beta = 1.0 / (KB * T);
+  const long N = S->n();
+  std::vector<std::vector<long>> loc(ns);
+  std::vector<long> mol_loc(N);
+  for (long l = 0; l < N; ++l) {
+    if (occ[l] < 0 || occ[l] >= ns) return -1;
+    mol_loc[l] = (long)loc[occ[l]].size();
+    loc[occ[l]].push_back(l);
+  }
+  std::vector<std::pair<int, int>> swaps;  // OccCandidate.cc:136-152 order for one asymmetric unit
+  for (int a = 0; a < ns; ++a)
+    for (int b = 0; b < ns; ++b)
+      if (a != b) swaps.push_back({a, b});
+  std::vector<double> tsum(swaps.size() + 1);
+  long long nacc = 0;
+  double Ef = S->formation_per_supercell(occ);
+  for (long p = 0; p < n_passes; ++p) {
+    long long pass_acc = 0;
+    for (long t = 0; t < N; ++t) {
+      tsum[0] = 0.0;
+      for (size_t i = 0; i < swaps.size(); ++i) tsum[i + 1] = tsum[i] + (double)loc[swaps[i].first].size();
+      if (tsum.back() == 0.0) return -1;
+      const double r = rng.random_real(tsum.back());
+      size_t k = swaps.size();
+      for (size_t i = 0; i < swaps.size(); ++i)
+        if (r < tsum[i + 1]) {
+          k = i;
+          break;
+        }
+      if (k == swaps.size()) return -1;  // the reference throws here
+      const int a = swaps[k].first, b = swaps[k].second;
+      const long l = loc[a][(size_t)std::uniform_int_distribution<unsigned long>(0, loc[a].size() - 1)(e)];
+      const double dEf = S->delta_formation(occ, l, b);
+      const double dE = dEf - S->mu_dot_Ndx(m, a, b);
+      if (metropolis_acceptance(dE, beta, rng)) {
+        ++nacc;
+        ++pass_acc;
+        Ef += dEf;
+        const long back = loc[a].back();
+        loc[a][mol_loc[l]] = back;
+        mol_loc[back] = mol_loc[l];
+        loc[a].pop_back();
+        mol_loc[l] = (long)loc[b].size();
+        loc[b].push_back(l);
+        occ[l] = b;
+      }
+    }
+    nacc_out[p] = pass_acc;
+    double Esgc = Ef;
+    for (int i = 0; i < ns - 1; ++i) {
+      const double Ni = (double)loc[i + 1].size();
+      Esgc -= m[i] * Ni;
+      x_out[p * (ns - 1) + i] = Ni / (double)N;
+    }
+    e_out[p] = Esgc / (double)N;
+  }
+  long off = 0;
+  for (int s = 0; s < ns; ++s) {
+    loc_sizes_out[s] = (int)loc[s].size();
+    for (long v : loc[s]) loc_out[off++] = (int)v;
+  }
+  std::stringstream ss;
+  ss << e;
+  const std::string st = ss.str();
+  if ((long)st.size() + 1 > state_len) return -1;
+  std::memcpy(state_out, st.c_str(), st.size() + 1);
+  return nacc;
+}
+
 int orc_ce_canonical_sweep(void* h, int* occ, double T, unsigned long long seed, unsigned int chain,
                            const int* color_a, int n_a, const int* color_b, int n_b, const int* order_a,
                            const int* order_b, long pass0, long n_passes, long long* corr_out, long long* nacc_out) {

@@ -46,6 +46,9 @@ def load():
         L.orc_engine_seed.argtypes = [C.c_ulonglong, C.c_char_p, C.c_long]
         L.orc_ce_sgc_samples.restype = C.c_longlong
         L.orc_ce_sgc_samples.argtypes = [C.c_void_p, ip, C.c_double, dp, C.c_int, C.c_ulonglong, C.c_long, dp, dp]
+        L.orc_ce_sgc_run.restype = C.c_longlong
+        L.orc_ce_sgc_run.argtypes = [C.c_void_p, ip, C.c_double, dp, C.c_int, C.c_char_p, C.c_long, dp, dp,
+                                     C.POINTER(C.c_longlong), ip, ip, C.c_char_p, C.c_long]
         L.orc_sgc_proposals.argtypes = [C.c_long, C.c_int, ip, C.c_ulonglong, C.c_long, C.c_int, lp, ip]
         L.orc_ising_run.argtypes = [C.c_long, C.c_long, C.c_double, C.c_int, C.c_double, C.c_double, ip,
                                     C.POINTER(OrcCCParams), C.c_int, C.c_char_p, dp, C.c_long,
@@ -226,6 +229,29 @@ class OracleCE:
                                          n_passes, p(e, C.c_double), p(x, C.c_double))
         assert nacc >= 0
         return e, x, nacc
+
+    def sgc_run(self, occ, T, mu, engine_state: str, n_passes):
+        """The reference's semi-grand canonical dynamics from an engine state: dict with the final
+        occupation, per-pass accepted counts, potential energy and composition per site, the
+        final occupant lists per species and the final engine state."""
+        occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int32).copy())
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64))
+        e = np.zeros(n_passes, dtype=np.float64)
+        x = np.zeros((n_passes, self.n_species - 1), dtype=np.float64)
+        nacc = np.zeros(n_passes, dtype=np.int64)
+        sizes = np.zeros(self.n_species, dtype=np.int32)
+        lists = np.zeros(self.n, dtype=np.int32)
+        st = C.create_string_buffer(16384)
+        r = load().orc_ce_sgc_run(self.h, p(occ, C.c_int), T, p(mu, C.c_double), mu.size, engine_state.encode(),
+                                  n_passes, p(e, C.c_double), p(x, C.c_double), p(nacc, C.c_longlong),
+                                  p(sizes, C.c_int), p(lists, C.c_int), st, len(st))
+        assert r >= 0, r
+        out, off = [], 0
+        for s in sizes:
+            out.append(lists[off:off + s].copy())
+            off += s
+        return {"occ": occ, "n_accept": nacc, "potential_energy": e, "param_composition": x, "lists": out,
+                "engine": st.value.decode()}
 
     def nfold_run(self, occ, T, mu, seed, n_events):
         """The N-fold way on the CPU (binary): final occupation, wall seconds, simulated time."""

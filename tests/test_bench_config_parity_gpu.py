@@ -26,8 +26,8 @@ def _bench_inputs():
     return clex.ClexModel("fcc_binary", eci), eci, occ, T, mu, seeds
 
 
-def _check(b, model, eci, occ0, T, mu, seeds, ids, corr0, out, n_passes, pending):
-    s = clex.accumulate(model, corr0, out, mu, b.n_sites)
+def _check(b, model, mu, ids, corr0, out, pending):
+    s = clex.accumulate(model, corr0, out, mu[ids], b.n_sites)
     got = b.occupation()
     results = pending.get(timeout=1800)
     for k, (occ_ref, corr_ref, nacc_ref) in enumerate(results):
@@ -52,7 +52,7 @@ def test_fcc64_bench_chains_match_oracle(gpu_lib, ctas):
              model.n_classes) for c in ids])
         corr0 = b.corr()
         out = b.run(n_passes)
-        _check(b, model, eci, occ, T, mu, seeds, ids, corr0, out, n_passes, pending)
+        _check(b, model, mu, ids, corr0, out, pending)
     b.close()
 
 
@@ -78,5 +78,5 @@ def test_fcc64_rotated_bench_run_matches_oracle(gpu_lib):
         corr0 = b.corr()
         out = b.run(n_passes)
         assert b.last_launches() > 8, b.last_launches()
-        _check(b, model, eci, occ, T, mu, seeds, ids, corr0, out, n_passes, pending)
+        _check(b, model, mu, ids, corr0, out, pending)
     b.close()

@@ -74,3 +74,42 @@ def test_coloured_statistics_match_reference_dynamics(gpu_lib, kind, T, mu, n_pa
         (mg, pg), (mr, pr) = qg[k], qr[k]
         bound = 2.0 * np.hypot(pg, pr)
         assert np.isfinite(bound) and abs(mg - mr) <= bound, (k, mg, mr, pg, pr)
+
+
+def test_bench_config_statistics_match_reference_dynamics(gpu_lib):
+    """The benchmark's own chains (binary FCC 64^3, its ECIs, occupations and temperatures:
+    543 K for chain 1, 1514 K for chain 5; mu = 0) swept on the GPU against the reference's
+    semi-grand canonical dynamics in the oracle from the same starts: <E>, <x>, C and chi
+    within twice the combined 95 % error bars.  Both dynamics equilibrate within a few passes
+    at these temperatures; the first 30 passes are discarded."""
+    import bench
+    from tests import oracle_lib
+
+    eci, occ, T, mu, seeds = bench.make_inputs(0)
+    n = 64**3
+    model = clex.ClexModel("fcc_binary", eci)
+    chains = [1, 5]
+    n_ref, n_gpu, discard = 160, 1000, 30
+    with oracle_lib.oracle_pool(len(chains)) as pool:
+        pending = oracle_lib.sgc_samples_async(pool, [((64, 64, 64), 2, eci, occ[c], float(T[c]), mu[c], 777 + c,
+                                                       n_ref) for c in chains])
+        b = clex.ChainBatch(model, (64, 64, 64), occ[chains], T[chains], mu[chains], seeds[chains], chain_ids=chains)
+        corr = b.corr()
+        s = clex.accumulate(model, corr, b.run(n_gpu), mu[chains], n)
+        b.close()
+        refs = pending.get(timeout=3600)
+    for k, c in enumerate(chains):
+        e_gpu, x_gpu = s.potential_energy[discard:, k], s.param_composition[discard:, k, :]
+        e_ref, x_ref = refs[k][0][discard:], refs[k][1][discard:]
+        Tc = float(T[c])
+
+        def quantities(e, x):
+            return {"E": _stat(e), "x": _stat(x[:, 0]),
+                    "C": _stat(n * (e - e.mean()) ** 2 / (KB * Tc) ** 2),
+                    "chi": _stat(n * (x[:, 0] - x[:, 0].mean()) ** 2 / (KB * Tc))}
+
+        qg, qr = quantities(e_gpu, x_gpu), quantities(e_ref, x_ref)
+        for q in qg:
+            (mg, pg), (mr, pr) = qg[q], qr[q]
+            bound = 2.0 * np.hypot(pg, pr)
+            assert np.isfinite(bound) and abs(mg - mr) <= bound, (c, q, mg, mr, pg, pr)
