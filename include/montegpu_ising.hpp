@@ -18,6 +18,14 @@
 // run_metropolis_passes() replaces the host loop of basic_occupation_metropolis for this
 // model: the GPU consumes the engine's own draws (random_int(N-1), then random_real(1.0) for
 // uphill steps) and hands the advanced engine back, so the trajectory equals the host loop's.
+//
+// SemiGrandCanonicalCalculator<System, EventGenerator>::run (basic_semigrand_canonical.hh:
+// 322-470) with the sampling-function factories of :476-627: for IsingSystem with the
+// built-in SemiGrandCanonicalEventGenerator the passes run on the GPU as a serial replay,
+// with the completion check evaluated exactly as the reference evaluates it before every step
+// (samples and counts change only at pass boundaries, so a launch ends at the first pass
+// boundary where that check could end the run or run a convergence check); any other system
+// or event generator runs the reference's generic loop (montegpu_methods.hpp) on the host.
 #pragma once
 
 #include <cstdint>
@@ -29,7 +37,10 @@
 #include <string>
 #include <vector>
 
+#include <type_traits>
+
 #include "montegpu.h"
+#include "montegpu_methods.hpp"
 
 namespace montegpu {
 namespace ising_cpp {
@@ -45,26 +56,7 @@ struct ValueMap {
   std::map<std::string, std::vector<double>> vector_values;
 };
 
-template <typename EngineType = std::mt19937_64>
-class RandomNumberGenerator {
- public:
-  explicit RandomNumberGenerator(std::shared_ptr<EngineType> _engine = nullptr) : engine(_engine) {
-    if (!engine) {
-      engine = std::make_shared<EngineType>();
-      std::random_device device;
-      engine->seed(device());
-    }
-  }
-  template <typename IntType>
-  IntType random_int(IntType maximum_value) {
-    return std::uniform_int_distribution<IntType>(0, maximum_value)(*engine);
-  }
-  template <typename RealType>
-  RealType random_real(RealType maximum_value) {
-    return std::uniform_real_distribution<RealType>(0, maximum_value)(*engine);
-  }
-  std::shared_ptr<EngineType> engine;
-};
+using monte::RandomNumberGenerator;
 
 struct OccEvent {
   std::vector<Index> linear_site_index;
@@ -74,6 +66,14 @@ struct OccEvent {
 class IsingConfiguration {
  public:
   IsingConfiguration() : IsingConfiguration(std::vector<int>{0, 0}, 1) {}
+  /// JSON text {"shape": [...], "occupation": [...]} (model.hh:133-138)
+  std::string to_json() const {
+    std::ostringstream ss;
+    ss << "{\"shape\": [" << shape[0] << ", " << shape[1] << "], \"occupation\": [";
+    for (size_t k = 0; k < m_occupation.size(); ++k) ss << (k ? ", " : "") << m_occupation[k];
+    ss << "]}";
+    return ss.str();
+  }
   explicit IsingConfiguration(std::vector<int> _shape, int fill_value = 1) : shape(_shape) {
     if (shape.size() != 2) throw std::runtime_error("IsingConfiguration only supports 2d");
     m_occupation.assign(static_cast<size_t>(shape[0]) * shape[1], fill_value);
@@ -204,6 +204,11 @@ class IsingFormationEnergy {
             s[c.to_linear_site_index(c.within(i - 1, 0), j)] + s[c.to_linear_site_index(c.within(i + 1, 0), j)]);
   }
   bool m_use_nlist = true;
+
+ public:
+  bool uses_nlist() const { return m_use_nlist; }
+
+ private:
   std::vector<std::vector<Index>> m_nlist;
   std::vector<std::vector<Index>> m_flower;
 };
@@ -320,6 +325,8 @@ template <typename EngineType = std::mt19937_64>
 class SemiGrandCanonicalEventGenerator {
  public:
   typedef IsingState state_type;
+  typedef EngineType engine_type;
+  typedef RandomNumberGenerator<EngineType> random_number_generator_type;
   void set_state(state_type* _state) {
     if (_state == nullptr) throw std::runtime_error("Error in SemiGrandCanonicalEventGenerator::set_state: _state==nullptr");
     state = _state;
@@ -376,6 +383,313 @@ inline MetropolisCounts run_metropolis_passes(IsingState& state, SemiGrandCanoni
   std::istringstream is(std::string(buf.data()));
   is >> engine;
   return counts;
+}
+
+typedef monte::methods::BasicOccupationMetropolisData<monte::BasicStatistics> SemiGrandCanonicalData;
+
+/// Semi-grand canonical Metropolis calculator (basic_semigrand_canonical.hh:322-470).
+template <typename SystemType = IsingSystem,
+          typename EventGeneratorType = SemiGrandCanonicalEventGenerator<std::mt19937_64>>
+class SemiGrandCanonicalCalculator {
+ public:
+  typedef SystemType system_type;
+  typedef typename system_type::state_type state_type;
+  typedef typename system_type::formation_energy_f_type formation_energy_f_type;
+  typedef typename system_type::param_composition_f_type param_composition_f_type;
+  typedef SemiGrandCanonicalPotential potential_type;
+  typedef EventGeneratorType event_generator_type;
+  typedef typename event_generator_type::engine_type engine_type;
+  typedef typename event_generator_type::random_number_generator_type random_number_generator_type;
+
+  explicit SemiGrandCanonicalCalculator(std::shared_ptr<system_type> _system)
+      : system(_system ? _system
+                       : throw std::runtime_error("Error constructing SemiGrandCanonicalCalculator: _system==nullptr")),
+        state(nullptr), conditions(nullptr), potential(_system),
+        formation_energy_calculator(&potential.system->formation_energy_calculator),
+        param_composition_calculator(&potential.system->param_composition_calculator) {}
+
+  std::shared_ptr<system_type> system;
+  state_type* state;
+  std::shared_ptr<SemiGrandCanonicalConditions> conditions;
+  potential_type potential;
+  formation_energy_f_type* formation_energy_calculator;
+  param_composition_f_type* param_composition_calculator;
+  std::shared_ptr<SemiGrandCanonicalData> data;
+  /// device time of the GPU passes of the last run (ms; 0 for a host run)
+  double last_kernel_ms = 0.0;
+  /// most passes per GPU launch
+  int max_passes_per_launch = 4096;
+
+  /// Run at the state's conditions until the completion check ends it; `state` is modified in
+  /// place and the engine advanced.  write_status_f(calculator, method_log) is called when a
+  /// status is due and at the end.
+  template <typename WriteStatusF>
+  std::shared_ptr<SemiGrandCanonicalData> run(state_type& state,
+                                              monte::StateSamplingFunctionMap const& sampling_functions,
+                                              monte::jsonStateSamplingFunctionMap const& json_sampling_functions,
+                                              monte::CompletionCheckParams<monte::BasicStatistics> const& completion_check_params,
+                                              event_generator_type event_generator, int sample_period,
+                                              std::optional<monte::MethodLog> method_log,
+                                              std::shared_ptr<engine_type> random_engine, WriteStatusF write_status_f) {
+    this->state = &state;
+    this->conditions = std::make_shared<SemiGrandCanonicalConditions>(
+        SemiGrandCanonicalConditions::from_values(this->state->conditions));
+    const double temperature = this->conditions->temperature;
+    const monte::CountType n_steps_per_pass = this->state->configuration.n_variable_sites;
+    this->potential.set_state(this->state, this->conditions);
+    event_generator.set_state(this->state);
+    this->data = std::make_shared<SemiGrandCanonicalData>(sampling_functions, json_sampling_functions,
+                                                          n_steps_per_pass, completion_check_params);
+    last_kernel_ms = 0.0;
+    if (!random_engine) {
+      random_engine = std::make_shared<engine_type>();
+      std::random_device device;
+      random_engine->seed(device());
+    }
+    if (!method_log.has_value()) {
+      method_log = monte::MethodLog();
+      method_log->logfile_path = "status.json";
+      method_log->log_frequency = 600.0;
+    }
+    if constexpr (std::is_same<system_type, IsingSystem>::value &&
+                  std::is_same<event_generator_type, SemiGrandCanonicalEventGenerator<std::mt19937_64>>::value) {
+      method_log->log.restart_clock();
+      method_log->log.begin_lap();
+      gpu_replay(sample_period, *method_log, *random_engine, write_status_f);
+      write_status_f(*this, *method_log);
+    } else {
+      auto dpotential_f = [this](OccEvent const& e) { return this->potential.occ_delta_per_supercell(e); };
+      auto propose_event_f = [&](random_number_generator_type& rng) -> OccEvent const& {
+        return event_generator.propose(rng);
+      };
+      auto apply_event_f = [&](OccEvent const& e) -> void { event_generator.apply(e); };
+      auto _write_status_f = [&](SemiGrandCanonicalData const&, monte::MethodLog& log) { write_status_f(*this, log); };
+      monte::methods::basic_occupation_metropolis(*this->data, temperature, dpotential_f, propose_event_f,
+                                                  apply_event_f, sample_period, method_log, random_engine,
+                                                  _write_status_f);
+    }
+    return this->data;
+  }
+
+  /// run() writing no status
+  std::shared_ptr<SemiGrandCanonicalData> run(state_type& state,
+                                              monte::StateSamplingFunctionMap const& sampling_functions,
+                                              monte::jsonStateSamplingFunctionMap const& json_sampling_functions,
+                                              monte::CompletionCheckParams<monte::BasicStatistics> const& completion_check_params,
+                                              event_generator_type event_generator, int sample_period = 1,
+                                              std::optional<monte::MethodLog> method_log = std::nullopt,
+                                              std::shared_ptr<engine_type> random_engine = nullptr) {
+    return run(state, sampling_functions, json_sampling_functions, completion_check_params, event_generator,
+               sample_period, method_log, random_engine,
+               [](SemiGrandCanonicalCalculator const&, monte::MethodLog& log) { log.log.begin_lap(); });
+  }
+
+ private:
+  // The main loop of basic_occupation_metropolis.hh:381-422 for the built-in model, as a GPU
+  // serial replay in chunks of whole passes; the completion check is called once per pass
+  // boundary and its N - 1 further calls of the pass are applied with repeat_calls.
+  template <typename WriteStatusF>
+  void gpu_replay(int sample_period, monte::MethodLog& method_log, engine_type& engine, WriteStatusF& write_status_f) {
+    SemiGrandCanonicalData& d = *this->data;
+    IsingConfiguration& cfg = this->state->configuration;
+    const int rows = cfg.shape[0], cols = cfg.shape[1];
+    const monte::CountType N = cfg.n_variable_sites;
+    const double J = this->system->formation_energy_calculator.J;
+    const bool use_nlist = this->system->formation_energy_calculator.uses_nlist();
+    if (this->conditions->exchange_potential.size() != 1)
+      throw std::runtime_error("Error in SemiGrandCanonicalCalculator::run: exchange_potential must have size 1");
+    const double mu = this->conditions->exchange_potential[0];
+    const double T = this->conditions->temperature;
+    if (sample_period < 1) throw std::runtime_error("Error in SemiGrandCanonicalCalculator::run: sample_period < 1");
+    std::ostringstream es;
+    es << engine;
+    const std::string est = es.str();
+    const char* states[1] = {est.c_str()};
+    std::vector<int32_t> occ(cfg.occupation().begin(), cfg.occupation().end());
+    mg_ising_replay* h = nullptr;
+    if (mg_ising_replay_create(rows, cols, 1, use_nlist ? 1 : 0, &J, &T, &mu, occ.data(), states, &h) != MG_OK)
+      throw std::runtime_error(mg_last_error());
+    std::string err;
+    try {
+      main_loop(h, d, N, rows, cols, J, mu, use_nlist, sample_period, method_log, write_status_f);
+    } catch (std::exception const& e) {
+      err = e.what();
+    }
+    // bring the occupation, the engine and the counts back (also after an error)
+    std::vector<char> buf(est.size() + 8192);
+    char* out_states[1] = {buf.data()};
+    unsigned long long acc = 0, rej = 0;
+    const int st = mg_ising_replay_get_state(h, occ.data(), out_states, buf.size(), &acc, &rej);
+    if (st != MG_OK && err.empty()) err = mg_last_error();
+    mg_ising_replay_destroy(h);
+    if (!err.empty()) throw std::runtime_error(err);
+    cfg.set_occupation(std::vector<int>(occ.begin(), occ.end()));
+    std::istringstream is(std::string(buf.data()));
+    is >> engine;
+    d.n_accept = acc;
+    d.n_reject = rej;
+  }
+
+  template <typename WriteStatusF>
+  void main_loop(mg_ising_replay* h, SemiGrandCanonicalData& d, monte::CountType N, int rows, int cols, double J,
+                 double mu, bool use_nlist, int sample_period, monte::MethodLog& method_log,
+                 WriteStatusF& write_status_f) {
+    auto& cc = d.completion_check;
+    bool device_only = d.json_sampling_functions.empty();
+    for (auto const& pair : d.sampling_functions)
+      device_only &= pair.second.device_owner == this && !pair.second.device_quantity.empty();
+    int max_chunk = std::max(1, max_passes_per_launch);
+    if (cc.params().cutoff_params.max_clocktime.has_value()) max_chunk = std::min(max_chunk, sample_period);
+    const int stride = 2 + rows + cols;
+    monte::CountType n_samples_now = 0;
+    auto check = [&]() { return cc.is_complete(d.samplers, d.sample_weight, d.n_pass, method_log.log); };
+    bool complete = check();
+    while (!complete) {
+      cc.repeat_calls(N - 1);
+      // the chunk: up to the first pass boundary at which the check could act
+      int k = 0;
+      monte::CountType ns = n_samples_now;
+      int limit = device_only ? max_chunk
+                              : (int)std::max<monte::CountType>(1, sample_period - (d.n_pass % sample_period));
+      limit = std::min(limit, max_chunk);
+      while (k < limit) {
+        ++k;
+        const monte::CountType p = d.n_pass + k;
+        if (p % sample_period == 0) ++ns;
+        if (cc.could_complete_at(ns, p)) break;
+      }
+      const monte::CountType expected = (d.n_pass + k) / sample_period - d.n_pass / sample_period;
+      std::vector<long long> buf((size_t)std::max<monte::CountType>(expected, 1) * stride);
+      int n_written = 0;
+      if (mg_ising_replay_run(h, k, sample_period, buf.data(), (int)std::max<monte::CountType>(expected, 1),
+                              &n_written) != MG_OK)
+        throw std::runtime_error(mg_last_error());
+      float ms = 0.f;
+      mg_ising_replay_last_kernel_ms(h, &ms);
+      last_kernel_ms += ms;
+      int si = 0;
+      for (int b = 0; b < k; ++b) {
+        d.n_pass += 1;
+        if (d.n_pass % sample_period == 0) {
+          push_sample(h, d, &buf[(size_t)si * stride], N, rows, cols, J, mu, use_nlist, device_only);
+          ++si;
+          ++n_samples_now;
+          if (method_log.log_frequency.has_value() && method_log.log.lap_time() >= method_log.log_frequency.value())
+            write_status_f(*this, method_log);
+        }
+        complete = check();
+        if (complete) {
+          if (b != k - 1) throw std::runtime_error("internal error: completion inside a planned chunk");
+          break;
+        }
+        if (b < k - 1) cc.repeat_calls(N - 1);
+      }
+    }
+  }
+
+  // One sample from the device's integer sums (spin sum, bond sum or row/column dot products)
+  // in the reference's arithmetic order; other sampling functions read the host state, which
+  // is brought back from the device first.
+  void push_sample(mg_ising_replay* h, SemiGrandCanonicalData& d, const long long* row, monte::CountType N, int rows,
+                   int cols, double J, double mu, bool use_nlist, bool device_only) {
+    const long long spin_sum = row[0], bond_sum = row[1];
+    const double Nx = static_cast<double>(N + spin_sum) / 2.0;
+    double ef;
+    if (use_nlist) {
+      ef = static_cast<double>(bond_sum);
+      ef *= -J;
+    } else {
+      ef = 0.0;
+      for (int i = 0; i < rows; ++i) ef += -J * static_cast<double>(row[2 + i]);
+      for (int j = 0; j < cols; ++j) ef += -J * static_cast<double>(row[2 + rows + j]);
+    }
+    if (!device_only) {
+      std::vector<int32_t> occ((size_t)N);
+      if (mg_ising_replay_get_state(h, occ.data(), nullptr, 0, nullptr, nullptr) != MG_OK)
+        throw std::runtime_error(mg_last_error());
+      this->state->configuration.set_occupation(std::vector<int>(occ.begin(), occ.end()));
+    }
+    for (auto const& pair : d.sampling_functions) {
+      auto const& f = pair.second;
+      if (f.device_owner == this && f.device_quantity == "param_composition") {
+        d.samplers.at(f.name)->push_back(std::vector<double>{Nx / static_cast<double>(N)});
+      } else if (f.device_owner == this && f.device_quantity == "formation_energy") {
+        d.samplers.at(f.name)->push_back(std::vector<double>{ef / static_cast<double>(N)});
+      } else if (f.device_owner == this && f.device_quantity == "potential_energy") {
+        d.samplers.at(f.name)->push_back(std::vector<double>{(ef - mu * Nx) / static_cast<double>(N)});
+      } else {
+        d.samplers.at(f.name)->push_back(f());
+      }
+    }
+    for (auto const& pair : d.json_sampling_functions)
+      d.json_samplers.at(pair.second.name).values.push_back(pair.second());
+  }
+};
+
+/// Parametric composition per unit cell (basic_semigrand_canonical.hh:486-517).
+template <typename CalculatorType>
+monte::StateSamplingFunction make_parametric_composition_f(std::shared_ptr<CalculatorType> mc_calculator) {
+  if (mc_calculator == nullptr)
+    throw std::runtime_error("Error in parametric_composition sampling function: mc_calculator == nullptr");
+  std::vector<monte::Index> shape;
+  shape.push_back(mc_calculator->system->param_composition_calculator.n_independent_compositions());
+  CalculatorType* c = mc_calculator.get();
+  monte::StateSamplingFunction f("param_composition", "Parametric composition", shape, [c]() -> std::vector<double> {
+    if (c->param_composition_calculator == nullptr || c->param_composition_calculator->state == nullptr)
+      throw std::runtime_error(
+          "Error in parametric_composition sampling function: "
+          "mc_calculator->param_composition_calculator->state == nullptr");
+    return c->param_composition_calculator->per_unitcell();
+  });
+  f.device_quantity = "param_composition";
+  f.device_owner = c;
+  return f;
+}
+
+/// Formation energy per unit cell (basic_semigrand_canonical.hh:530-556).
+template <typename CalculatorType>
+monte::StateSamplingFunction make_formation_energy_f(std::shared_ptr<CalculatorType> mc_calculator) {
+  if (mc_calculator == nullptr)
+    throw std::runtime_error("Error in formation_energy sampling function: mc_calculator == nullptr");
+  CalculatorType* c = mc_calculator.get();
+  monte::StateSamplingFunction f("formation_energy", "Intensive formation energy", {}, [c]() -> std::vector<double> {
+    if (c->formation_energy_calculator == nullptr || c->formation_energy_calculator->state == nullptr)
+      throw std::runtime_error(
+          "Error in formation_energy sampling function: mc_calculator->formation_energy_calculator->state == nullptr");
+    return {c->formation_energy_calculator->per_unitcell()};
+  });
+  f.device_quantity = "formation_energy";
+  f.device_owner = c;
+  return f;
+}
+
+/// Semi-grand canonical potential energy per unit cell (basic_semigrand_canonical.hh:569-590).
+template <typename CalculatorType>
+monte::StateSamplingFunction make_potential_energy_f(std::shared_ptr<CalculatorType> mc_calculator) {
+  if (mc_calculator == nullptr)
+    throw std::runtime_error("Error in formation_energy sampling function: mc_calculator == nullptr");
+  CalculatorType* c = mc_calculator.get();
+  monte::StateSamplingFunction f("potential_energy", "Intensive potential energy", {}, [c]() -> std::vector<double> {
+    if (c->potential.state == nullptr)
+      throw std::runtime_error("Error in formation_energy sampling function: mc_calculator->potential.state == nullptr");
+    return {c->potential.per_unitcell()};
+  });
+  f.device_quantity = "potential_energy";
+  f.device_owner = c;
+  return f;
+}
+
+/// The configuration as JSON text (basic_semigrand_canonical.hh:606-627).
+template <typename CalculatorType>
+monte::jsonStateSamplingFunction make_configuration_json_f(std::shared_ptr<CalculatorType> mc_calculator) {
+  if (mc_calculator == nullptr)
+    throw std::runtime_error("Error in formation_energy sampling function: mc_calculator == nullptr");
+  CalculatorType* c = mc_calculator.get();
+  return monte::jsonStateSamplingFunction("configuration", "Configuration values", [c]() -> std::string {
+    if (c->potential.state == nullptr)
+      throw std::runtime_error("Error in formation_energy sampling function: mc_calculator->potential.state == nullptr");
+    return c->state->configuration.to_json();
+  });
 }
 
 }  // namespace semigrand_canonical
