@@ -32,6 +32,20 @@ struct ShapeLists {
   std::vector<uint32_t> entries, site;
   int max_words = 0;  // most words (word lists) or sites of one CTA and colour
 };
+// Device copies of a shape's site lists on one device, shared by every batch of that shape
+// and CTA count (uploaded once per process; freed when evicted from the bounded cache and no
+// batch holds them).
+struct DeviceLists {
+  int* cstart = nullptr;
+  uint32_t* entries = nullptr;
+  uint32_t* site = nullptr;
+  int max_words = 0;
+  ~DeviceLists() {
+    cudaFree(cstart);
+    cudaFree(entries);
+    cudaFree(site);
+  }
+};
 
 struct mg_ce_batch {
   const mg_ce_model* model = nullptr;
@@ -48,13 +62,19 @@ struct mg_ce_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
   int last_launches = 0;  // sweep kernels launched by the last run
+  // one device allocation holds the occupations, chain parameters, correlation sums of
+  // mg_ce_batch_corr and the per-pass outputs of runs of up to kOutPasses passes
+  unsigned char* dblock = nullptr;
   int8_t* docc = nullptr;
   mg::CeChainParams* dcp = nullptr;
+  long long* dcorr = nullptr;
   std::vector<mg::CeChainParams> hcp;
+  std::shared_ptr<const DeviceLists> lists;
   int* dcstart = nullptr;
   uint32_t* dentries = nullptr;
   uint32_t* dsite = nullptr;
-  long long* dout = nullptr;
+  long long* dout = nullptr;  // within dblock, or a separate allocation for longer runs
+  bool dout_own = false;
   size_t out_cap = 0;
   // Rotation over two cluster sizes (warp-specialised layout with the CTA count chosen by
   // occupancy).  When n_chains - 1 clusters of S_fast > S CTAs fit on the GPU at once but
@@ -64,15 +84,20 @@ struct mg_ce_batch {
   int S_fast = 0;  // 0: no rotation
   int rotation_mode = 1;  // 0: never; 1: when the plan beats one unrotated launch; 2: whenever a plan exists
   double launch_passes = 0.0;  // fixed cost of one launch in slow-slot passes (0: not yet measured)
+  std::shared_ptr<const DeviceLists> lists_f;
   int* dcstart_f = nullptr;
   uint32_t* dentries_f = nullptr;
   uint32_t* dsite_f = nullptr;
   int max_words = 0, max_words_f = 0;
   double ratio = 1.0;  // time per pass on S_fast CTAs over that on S CTAs (re-measured by rotated calls)
   std::vector<cudaStream_t> stream_fast;  // n_chains - 1 fast lanes, high priority (the batch's
-                                          // stream is the slow lane)
+                                          // stream is the slow lane); created by the first
+                                          // rotated run
   std::vector<cudaEvent_t> rev;            // six per chain (launch_rotated) and a join
 };
+
+// per-pass output rows kept in a batch's own allocation
+constexpr int kOutPasses = 128;
 
 // Pass counts of one rotated call (rotation_plan)
 struct RotationPlan {
@@ -154,6 +179,55 @@ std::shared_ptr<const ShapeLists> shape_lists(int kind, int L0, int L1, int L2, 
   return g_lists[key];
 }
 
+// Device lists per (device, shape, CTA count, list family), uploaded on `st` once per process.
+// The cache is never destroyed (no device frees during process exit); at most
+// kMaxCachedDeviceLists entries are kept, the oldest dropped first (batches still using an
+// entry keep it alive).
+constexpr size_t kMaxCachedDeviceLists = 32;
+typedef std::tuple<int, int, int, int, int, int, int> DevListKey;
+std::map<DevListKey, std::shared_ptr<const DeviceLists>>* g_dev_lists =
+    new std::map<DevListKey, std::shared_ptr<const DeviceLists>>();
+std::deque<DevListKey>* g_dev_lists_order = new std::deque<DevListKey>();
+
+int device_lists(int kind, int L0, int L1, int L2, int S, int layout, const ShapeColouring& col, cudaStream_t st,
+                 std::shared_ptr<const DeviceLists>* out) {
+  int dev = 0;
+  MG_CUDA_TRY(cudaGetDevice(&dev));
+  const DevListKey key = std::make_tuple(dev, kind, L0, L1, L2, S, layout >= 1 ? 1 : 0);
+  {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    const auto it = g_dev_lists->find(key);
+    if (it != g_dev_lists->end()) {
+      *out = it->second;
+      return MG_OK;
+    }
+  }
+  const auto host = shape_lists(kind, L0, L1, L2, S, layout, col);
+  auto d = std::make_shared<DeviceLists>();
+  d->max_words = host->max_words;
+  MG_CUDA_TRY(cudaMalloc(&d->cstart, sizeof(int) * host->cstart.size()));
+  MG_CUDA_TRY(cudaMalloc(&d->entries, sizeof(uint32_t) * host->entries.size()));
+  MG_CUDA_TRY(cudaMalloc(&d->site, sizeof(uint32_t) * host->site.size()));
+  MG_CUDA_TRY(cudaMemcpyAsync(d->cstart, host->cstart.data(), sizeof(int) * host->cstart.size(),
+                              cudaMemcpyHostToDevice, st));
+  MG_CUDA_TRY(cudaMemcpyAsync(d->entries, host->entries.data(), sizeof(uint32_t) * host->entries.size(),
+                              cudaMemcpyHostToDevice, st));
+  MG_CUDA_TRY(cudaMemcpyAsync(d->site, host->site.data(), sizeof(uint32_t) * host->site.size(),
+                              cudaMemcpyHostToDevice, st));
+  MG_CUDA_TRY(cudaStreamSynchronize(st));
+  std::lock_guard<std::mutex> lk(g_shape_mu);
+  auto ins = g_dev_lists->emplace(key, d);
+  if (ins.second) {
+    g_dev_lists_order->push_back(key);
+    if (g_dev_lists_order->size() > kMaxCachedDeviceLists) {
+      g_dev_lists->erase(g_dev_lists_order->front());
+      g_dev_lists_order->pop_front();
+    }
+  }
+  *out = ins.first->second;
+  return MG_OK;
+}
+
 bool make_model(int kind, const double* eci, int n, mg_ce_model* m, std::string& err) {
   m->kind = kind;
   const mg::ClassInfo* info;
@@ -203,17 +277,19 @@ bool make_model(int kind, const double* eci, int n, mg_ce_model* m, std::string&
   return true;
 }
 
+// every code of occ[0, n) in [0, n_species): one pass without early exit (vectorisable)
+bool occupants_in_range(const int8_t* occ, long long n, int n_species) {
+  unsigned bad = 0;
+  const unsigned char* u = reinterpret_cast<const unsigned char*>(occ);
+  for (long long i = 0; i < n; ++i) bad |= (unsigned)(u[i] >= (unsigned)n_species);
+  return bad == 0;
+}
+
 void free_batch(mg_ce_batch* b) {
   if (!b) return;
-  cudaFree(b->docc);
-  cudaFree(b->dcp);
-  cudaFree(b->dcstart);
-  cudaFree(b->dentries);
-  cudaFree(b->dsite);
-  cudaFree(b->dout);
-  cudaFree(b->dcstart_f);
-  cudaFree(b->dentries_f);
-  cudaFree(b->dsite_f);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  cudaFree(b->dblock);
+  if (b->dout_own) cudaFree(b->dout);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
   for (cudaEvent_t e : b->rev) cudaEventDestroy(e);
@@ -235,9 +311,7 @@ constexpr double kWsPhaseFixedWords = 288.0;
 // runs beside them: on GB300 seven 16-CTA clusters leave a group of 12 SMs that holds one
 // 12-CTA cluster (measured: both launches keep their own speed when run together).
 int setup_rotation(mg_ce_batch* b) {
-  cudaFree(b->dcstart_f);
-  cudaFree(b->dentries_f);
-  cudaFree(b->dsite_f);
+  b->lists_f.reset();
   b->dcstart_f = nullptr;
   b->dentries_f = nullptr;
   b->dsite_f = nullptr;
@@ -261,16 +335,26 @@ int setup_rotation(mg_ce_batch* b) {
     if (lists->max_words > mg::host::NW_WS) continue;
     const double r = (lists->max_words + kWsPhaseFixedWords) / (b->max_words + kWsPhaseFixedWords);
     if (((C - 1) / r + 1.0) / C < 1.03) break;
-    MG_CUDA_TRY(cudaMalloc(&b->dcstart_f, sizeof(int) * lists->cstart.size()));
-    MG_CUDA_TRY(cudaMalloc(&b->dentries_f, sizeof(uint32_t) * lists->entries.size()));
-    MG_CUDA_TRY(cudaMalloc(&b->dsite_f, sizeof(uint32_t) * lists->site.size()));
-    MG_CUDA_TRY(cudaMemcpyAsync(b->dcstart_f, lists->cstart.data(), sizeof(int) * lists->cstart.size(),
-                                cudaMemcpyHostToDevice, b->stream));
-    MG_CUDA_TRY(cudaMemcpyAsync(b->dentries_f, lists->entries.data(), sizeof(uint32_t) * lists->entries.size(),
-                                cudaMemcpyHostToDevice, b->stream));
-    MG_CUDA_TRY(cudaMemcpyAsync(b->dsite_f, lists->site.data(), sizeof(uint32_t) * lists->site.size(),
-                                cudaMemcpyHostToDevice, b->stream));
-    MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    b->S_fast = s;
+    b->max_words_f = lists->max_words;
+    b->ratio = r;
+    break;
+  }
+  return MG_OK;
+}
+
+// Device lists, fast-lane streams and events of a rotated run, made by the batch's first
+// rotated run (a batch whose runs are too short to rotate never makes them).
+int ensure_rotation_resources(mg_ce_batch* b) {
+  const int C = b->n_chains;
+  if (!b->lists_f) {
+    const int rc = device_lists(b->model->kind, b->L0, b->L1, b->L2, b->S_fast, 3, *b->col, b->stream, &b->lists_f);
+    if (rc != MG_OK) return rc;
+    b->dcstart_f = b->lists_f->cstart;
+    b->dentries_f = b->lists_f->entries;
+    b->dsite_f = b->lists_f->site;
+  }
+  if (b->stream_fast.size() < (size_t)C - 1) {
     int least = 0, greatest = 0;
     MG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     while (b->stream_fast.size() < (size_t)C - 1) {
@@ -278,15 +362,11 @@ int setup_rotation(mg_ce_batch* b) {
       MG_CUDA_TRY(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, greatest));
       b->stream_fast.push_back(st);
     }
-    while (b->rev.size() < 6 * (size_t)C + 1) {
-      cudaEvent_t e = nullptr;
-      MG_CUDA_TRY(cudaEventCreate(&e));
-      b->rev.push_back(e);
-    }
-    b->S_fast = s;
-    b->max_words_f = lists->max_words;
-    b->ratio = r;
-    break;
+  }
+  while (b->rev.size() < 6 * (size_t)C + 1) {
+    cudaEvent_t e = nullptr;
+    MG_CUDA_TRY(cudaEventCreate(&e));
+    b->rev.push_back(e);
   }
   return MG_OK;
 }
@@ -496,22 +576,13 @@ int setup_layout(mg_ce_batch* b, int layout) {
               "kernel stages");
     return MG_ERR_INVALID;
   }
-  const std::vector<int>& cstart = lists->cstart;
-  const std::vector<uint32_t>& entries = lists->entries;
-  const std::vector<uint32_t>& site = lists->site;
-  cudaFree(b->dcstart);
-  cudaFree(b->dentries);
-  cudaFree(b->dsite);
-  b->dcstart = nullptr;
-  b->dentries = nullptr;
-  b->dsite = nullptr;
-  MG_CUDA_TRY(cudaMalloc(&b->dcstart, sizeof(int) * cstart.size()));
-  MG_CUDA_TRY(cudaMalloc(&b->dentries, sizeof(uint32_t) * entries.size()));
-  MG_CUDA_TRY(cudaMalloc(&b->dsite, sizeof(uint32_t) * site.size()));
-  MG_CUDA_TRY(cudaMemcpyAsync(b->dcstart, cstart.data(), sizeof(int) * cstart.size(), cudaMemcpyHostToDevice, b->stream));
-  MG_CUDA_TRY(cudaMemcpyAsync(b->dentries, entries.data(), sizeof(uint32_t) * entries.size(), cudaMemcpyHostToDevice, b->stream));
-  MG_CUDA_TRY(cudaMemcpyAsync(b->dsite, site.data(), sizeof(uint32_t) * site.size(), cudaMemcpyHostToDevice, b->stream));
-  MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  std::shared_ptr<const DeviceLists> dl;
+  rc = device_lists(m->kind, b->L0, b->L1, b->L2, S, layout, *b->col, b->stream, &dl);
+  if (rc != MG_OK) return rc;
+  b->lists = dl;
+  b->dcstart = dl->cstart;
+  b->dentries = dl->entries;
+  b->dsite = dl->site;
   b->layout = layout;
   b->S = S;
   b->smem = smem;
@@ -591,11 +662,10 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
     set_error("Error in mg_ce_batch_create: supercell too large");
     return MG_ERR_INVALID;
   }
-  for (long long i = 0; i < N * n_chains; ++i)
-    if (occ[i] < 0 || occ[i] >= m->n_species) {
-      set_error("Error in mg_ce_batch_create: occupant index out of range");
-      return MG_ERR_INVALID;
-    }
+  if (!occupants_in_range(occ, N * n_chains, m->n_species)) {
+    set_error("Error in mg_ce_batch_create: occupant index out of range");
+    return MG_ERR_INVALID;
+  }
   for (int c = 0; c < n_chains; ++c)
     if (!(temperature[c] > 0.0)) {
       set_error("Error in mg_ce_batch_create: temperature must be > 0");
@@ -638,8 +708,20 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   MGX(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
   MGX(cudaEventCreate(&b->ev0), "event");
   MGX(cudaEventCreate(&b->ev1), "event");
-  MGX(cudaMalloc(&b->docc, (size_t)N * n_chains), "malloc occ");
-  MGX(cudaMalloc(&b->dcp, sizeof(mg::CeChainParams) * n_chains), "malloc params");
+  {
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t nslot = (size_t)m->n_classes + 2;
+    const size_t o_cp = al((size_t)N * n_chains);
+    const size_t o_corr = o_cp + al(sizeof(mg::CeChainParams) * n_chains);
+    const size_t o_out = o_corr + al(sizeof(long long) * m->n_classes * n_chains);
+    const size_t total = o_out + sizeof(long long) * kOutPasses * n_chains * nslot;
+    MGX(cudaMalloc(&b->dblock, total), "malloc");
+    b->docc = reinterpret_cast<int8_t*>(b->dblock);
+    b->dcp = reinterpret_cast<mg::CeChainParams*>(b->dblock + o_cp);
+    b->dcorr = reinterpret_cast<long long*>(b->dblock + o_corr);
+    b->dout = reinterpret_cast<long long*>(b->dblock + o_out);
+    b->out_cap = (size_t)kOutPasses * n_chains * nslot;
+  }
   MGX(cudaMemcpyAsync(b->docc, occ, (size_t)N * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
   MGX(cudaMemcpyAsync(b->dcp, b->hcp.data(), sizeof(mg::CeChainParams) * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
 #undef MGX
@@ -827,9 +909,11 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   const size_t nslot = (size_t)b->model->n_classes + 2;
   const size_t need = (size_t)n_passes * b->n_chains * nslot;
   if (need > b->out_cap) {
-    cudaFree(b->dout);
+    if (b->dout_own) cudaFree(b->dout);
     b->dout = nullptr;
+    b->dout_own = false;
     MG_CUDA_TRY(cudaMalloc(&b->dout, sizeof(long long) * need));
+    b->dout_own = true;
     b->out_cap = need;
   }
   MG_CUDA_TRY(cudaMemsetAsync(b->dout, 0, sizeof(long long) * need, b->stream));
@@ -839,8 +923,10 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   int rc;
   RotationPlan plan;
   const bool rotated = b->layout == 3 && rotation_plan(b, n_passes, &plan);
-  if (rotated)
-    rc = launch_rotated(b, plan);
+  if (rotated) {
+    rc = ensure_rotation_resources(b);
+    if (rc == MG_OK) rc = launch_rotated(b, plan);
+  }
   else if (b->layout == 3)
     rc = launch_sweep_ws(b->model, L, b->pipe);
   else if (b->layout >= 1)
@@ -931,11 +1017,10 @@ int mg_ce_batch_set_occ(mg_ce_batch* b, const int8_t* occ) {
     set_error("Error in mg_ce_batch_set_occ: invalid argument");
     return MG_ERR_INVALID;
   }
-  for (long long i = 0; i < b->N * b->n_chains; ++i)
-    if (occ[i] < 0 || occ[i] >= b->model->n_species) {
-      set_error("Error in mg_ce_batch_set_occ: occupant index out of range");
-      return MG_ERR_INVALID;
-    }
+  if (!occupants_in_range(occ, b->N * b->n_chains, b->model->n_species)) {
+    set_error("Error in mg_ce_batch_set_occ: occupant index out of range");
+    return MG_ERR_INVALID;
+  }
   MG_CUDA_TRY(cudaMemcpyAsync(b->docc, occ, (size_t)b->N * b->n_chains, cudaMemcpyHostToDevice, b->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
   return MG_OK;
@@ -947,8 +1032,7 @@ int mg_ce_batch_corr(mg_ce_batch* b, long long* out) {
     return MG_ERR_INVALID;
   }
   const int nc = b->model->n_classes;
-  long long* d = nullptr;
-  MG_CUDA_TRY(cudaMalloc(&d, sizeof(long long) * (size_t)nc * b->n_chains));
+  long long* d = b->dcorr;
   cudaError_t e = cudaMemsetAsync(d, 0, sizeof(long long) * (size_t)nc * b->n_chains, b->stream);
   const int nblk = (int)std::min<long long>((b->N + 255) / 256, 1024);
   dim3 grid(nblk, b->n_chains);
@@ -961,7 +1045,6 @@ int mg_ce_batch_corr(mg_ce_batch* b, long long* out) {
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, sizeof(long long) * (size_t)nc * b->n_chains, cudaMemcpyDeviceToHost, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-  cudaFree(d);
   if (e != cudaSuccess) {
     set_error(std::string("CUDA error in mg_ce_batch_corr: ") + cudaGetErrorString(e));
     return MG_ERR_CUDA;
