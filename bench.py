@@ -429,7 +429,8 @@ def run_gpu(args) -> None:
         # the passes of one launch of this run (traffic per launch grows with its passes:
         # the lattice stays in shared memory for the launch, so per pass it is nearly flat)
         traffic = tj["dram_bytes_per_pass"] * args.steps / launches
-        traffic_source = f"{os.path.relpath(tp, ROOT)}: {tj['source']}; scaled to {args.steps / launches:g} passes per launch"
+        traffic_source = (f"{os.path.relpath(tp, ROOT)}: {tj['source']}; scaled to {args.steps / launches:g} "
+                          "passes per launch")
     rotation = batch.rotation()
     extras = {}
     if not args.no_extras:
@@ -553,6 +554,76 @@ def run_canonical(args) -> None:
         print(json.dumps(line), flush=True)
 
 
+ISING_METRIC = "serial-replay Metropolis site-attempts/s (2-D Ising 25x25)"
+
+
+def run_ising(args) -> None:
+    """The plain method at CPU scale: 2-D square Ising, 25x25 periodic, occupation +-1 drawn
+    uniformly from seed 1, J = 0.1 eV, T = 2000 K, mu = 0, 1000 passes, one sample of energy and
+    composition per pass.  A step is one site-attempt.  The GPU path is the bit-exact serial
+    replay (one warp, the reference's mt19937_64 draws) behind the reference's calculator
+    interface (ising_cpp.semigrand_canonical.SemiGrandCanonicalCalculator.run); value: device
+    time of the replay kernels; e2e: the calculator's run end to end (host state in and out);
+    cpu_baseline: the reference's loop restated in the oracle on one host core."""
+    import casmcode_monte_gb300 as monte
+    import casmcode_monte_gb300.ising_cpp as ising
+    import casmcode_monte_gb300.ising_cpp.semigrand_canonical as sgc
+    import casmcode_monte_gb300.sampling as sampling
+
+    rows = cols = 25
+    n_pass = 1000
+    rng = np.random.default_rng(1)
+    occ0 = rng.choice(np.array([-1, 1], dtype=np.int32), size=rows * cols)
+
+    def one_run():
+        calc = sgc.SemiGrandCanonicalCalculator(ising.IsingSystem(ising.IsingFormationEnergy(J=0.1),
+                                                                  ising.IsingParamComposition()))
+        cfg = ising.IsingConfiguration((rows, cols))
+        cfg.set_occupation(occ0)
+        state = ising.IsingState(cfg, monte.ValueMap.from_dict({"temperature": 2000.0, "exchange_potential": [0.0]}))
+        p = sampling.CompletionCheckParams()
+        p.cutoff_params.max_count = n_pass
+        engine = monte.RandomNumberEngine()
+        engine.seed(1)
+        t0 = time.perf_counter()
+        data = calc.run(state, calc.default_sampling_functions(), {}, p, sgc.SemiGrandCanonicalEventGenerator(),
+                        method_log=monte.MethodLog(None, None), random_engine=engine,
+                        write_status_f=lambda c, l: None)
+        return time.perf_counter() - t0, calc.last_kernel_ms, data
+
+    for _ in range(args.warmup):
+        one_run()
+    walls, kms = [], []
+    for _ in range(args.steps):
+        w, k, data = one_run()
+        walls.append(w)
+        kms.append(k)
+    attempts = rows * cols * n_pass
+    kernel_ms = statistics.median(kms)
+    line = {"metric": ISING_METRIC, "value": attempts / (kernel_ms * 1e-3), "unit": "site-attempts/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True,
+            "scaling": "none (one chain)", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "ising25x25_sgc_1000_passes", "J": 0.1, "T": 2000.0, "mu": 0.0, "passes": n_pass,
+                       "step": "one 1000-pass run of the calculator"},
+            "e2e": {"value": attempts / statistics.median(walls), "unit": "site-attempts/s",
+                    "h2d_bytes_per_step": rows * cols * 4 + 6700, "d2h_bytes_per_step": rows * cols * 4 + 6700 + n_pass * 8 * 52},
+            "gpu_launches": None, "n_accept": int(data.n_accept)}
+    if args.cpu_seconds > 0:
+        from tests import oracle_lib
+
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < min(args.cpu_seconds, 5.0) or reps == 0:
+            oracle_lib.ising_run(rows, cols, 0.1, True, 2000.0, 0.0, occ0, oracle_lib.make_cc_params(max_count=n_pass),
+                                 1, oracle_lib.engine_state(1))
+            reps += 1
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": attempts * reps / dt, "unit": "site-attempts/s", "cores": 1, "kind": "port",
+                                "sample": f"{reps} runs of the reference loop (oracle restatement, g++ -O2, samples "
+                                          "and completion checks included)"}
+    print(json.dumps(line), flush=True)
+
+
 NFOLD_METRIC = "rejection-free (N-fold way) events/s (FCC binary CE)"
 
 
@@ -629,9 +700,10 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving workloads")
     ap.add_argument("--batched-chains", type=int, default=4096)
     ap.add_argument("--serving-jobs", type=int, default=2000)
-    ap.add_argument("--workload", default="fcc64_sgc", choices=["fcc64_sgc", "canonical", "nfold"],
+    ap.add_argument("--workload", default="fcc64_sgc", choices=["fcc64_sgc", "canonical", "nfold", "ising"],
                     help="fcc64_sgc: the headline semi-grand canonical pass; canonical: fixed-composition "
-                         "sweeps of 48^3 chains; nfold: rejection-free dynamics of 32^3 chains")
+                         "sweeps of 48^3 chains; nfold: rejection-free dynamics of 32^3 chains; ising: the 25x25 "
+                         "Ising serial replay")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -645,6 +717,8 @@ def main():
         run_canonical(args)
     elif args.workload == "nfold":
         run_nfold(args)
+    elif args.workload == "ising":
+        run_ising(args)
     else:
         run_gpu(args)
 
