@@ -182,12 +182,15 @@ class ChainBatch:
     def n_slots(self) -> int:
         return self.model.n_classes + 2
 
-    def run(self, n_passes: int, want_output: bool = True) -> Optional[np.ndarray]:
-        """Advance every chain by n_passes; returns [n_passes, n_chains, n_classes+2] int64."""
+    def run(self, n_passes: int, want_output: bool = True, out: Optional[np.ndarray] = None) -> Optional[np.ndarray]:
+        """Advance every chain by n_passes; returns [n_passes, n_chains, n_classes+2] int64
+        (written into ``out`` when given, e.g. a pinned host buffer)."""
         if int(n_passes) < 0:
             raise RuntimeError("Error in mg_ce_batch_run: invalid argument")
-        out = None
-        if want_output:
+        if out is not None:
+            if out.dtype != np.int64 or not out.flags.c_contiguous or out.size < n_passes * self.n_chains * self.n_slots:
+                raise ValueError("out must be a C-contiguous int64 array of n_passes * n_chains * (n_classes+2)")
+        elif want_output:
             out = np.zeros((n_passes, self.n_chains, self.n_slots), dtype=np.int64)
         _lib.check(_lib.lib().mg_ce_batch_run(self._h, int(n_passes),
                                               _lib.ptr(out, C.c_longlong) if out is not None else None))
@@ -226,10 +229,14 @@ class ChainBatch:
         mode = 2 if allowed == "always" else (1 if allowed else 0)
         _lib.check(_lib.lib().mg_ce_batch_set_rotation(self._h, mode))
 
-    def occupation(self) -> np.ndarray:
-        occ = np.zeros((self.n_chains, self.n_sites), dtype=np.int8)
-        _lib.check(_lib.lib().mg_ce_batch_get_occ(self._h, _lib.ptr(occ, C.c_int8)))
-        return occ
+    def occupation(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """The chains' occupations [n_chains, N] (into ``out`` when given, e.g. a pinned buffer)."""
+        if out is None:
+            out = np.zeros((self.n_chains, self.n_sites), dtype=np.int8)
+        elif out.dtype != np.int8 or not out.flags.c_contiguous or out.size != self.n_chains * self.n_sites:
+            raise ValueError("out must be a C-contiguous int8 array of n_chains * N")
+        _lib.check(_lib.lib().mg_ce_batch_get_occ(self._h, _lib.ptr(out, C.c_int8)))
+        return out
 
     def set_occupation(self, occ) -> None:
         occ = np.ascontiguousarray(np.asarray(occ, dtype=np.int8).reshape(self.n_chains, self.n_sites))

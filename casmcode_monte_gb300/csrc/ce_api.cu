@@ -1034,15 +1034,7 @@ int mg_ce_batch_corr(mg_ce_batch* b, long long* out) {
   const int nc = b->model->n_classes;
   long long* d = b->dcorr;
   cudaError_t e = cudaMemsetAsync(d, 0, sizeof(long long) * (size_t)nc * b->n_chains, b->stream);
-  const int nblk = (int)std::min<long long>((b->N + 255) / 256, 1024);
-  dim3 grid(nblk, b->n_chains);
-  if (e == cudaSuccess) {
-    if (b->model->kind == 0)
-      mg::ce_corr_kernel<mg::FccBinary><<<grid, 256, 0, b->stream>>>(b->docc, b->L0, b->L1, b->L2, b->n_chains, d);
-    else
-      mg::ce_corr_kernel<mg::FccTernary><<<grid, 256, 0, b->stream>>>(b->docc, b->L0, b->L1, b->L2, b->n_chains, d);
-    e = cudaGetLastError();
-  }
+  if (e == cudaSuccess) e = launch_corr(b->model->kind, b->docc, b->L0, b->L1, b->L2, b->n_chains, d, b->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, sizeof(long long) * (size_t)nc * b->n_chains, cudaMemcpyDeviceToHost, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) {

@@ -443,15 +443,7 @@ int mg_ce_canon_corr(mg_ce_canon* h, long long* out) {
   long long* d = nullptr;
   MG_CUDA_TRY(cudaMalloc(&d, sizeof(long long) * (size_t)nc * h->n_chains));
   cudaError_t e = cudaMemsetAsync(d, 0, sizeof(long long) * (size_t)nc * h->n_chains, h->stream);
-  const int nblk = (int)std::min<long long>((h->N + 255) / 256, 1024);
-  dim3 grid(nblk, h->n_chains);
-  if (e == cudaSuccess) {
-    if (h->model->kind == 0)
-      mg::ce_corr_kernel<mg::FccBinary><<<grid, 256, 0, h->stream>>>(h->docc, h->L0, h->L1, h->L2, h->n_chains, d);
-    else
-      mg::ce_corr_kernel<mg::FccTernary><<<grid, 256, 0, h->stream>>>(h->docc, h->L0, h->L1, h->L2, h->n_chains, d);
-    e = cudaGetLastError();
-  }
+  if (e == cudaSuccess) e = mg::host::launch_corr(h->model->kind, h->docc, h->L0, h->L1, h->L2, h->n_chains, d, h->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(out, d, sizeof(long long) * (size_t)nc * h->n_chains, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);

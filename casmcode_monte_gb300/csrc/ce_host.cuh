@@ -840,6 +840,40 @@ inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe)
   return MG_OK;
 }
 
+// Integer correlation sums of n_chains chains (out[chain][NCLASS], added to; clear it first):
+// the shared-memory tiled recompute (four planes per CTA) where a tile fits, else the
+// grid-stride kernel with periodic global loads.
+template <class B>
+cudaError_t launch_corr(const int8_t* occ, int L0, int L1, int L2, int n_chains, long long* out, cudaStream_t st) {
+  constexpr int H = B::HALO;
+  const int nk = std::min(4, L2);
+  const size_t smem = (size_t)(L0 + 2 * H) * (L1 + 2 * H) * (nk + 2 * H);
+  if (smem <= 200 * 1024) {
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (smem > 48 * 1024 && dev >= 0 && dev < 64 && !attr_set[dev]) {
+      e = cudaFuncSetAttribute(ce_corr_tiled_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      if (e != cudaSuccess) return e;
+      attr_set[dev] = true;
+    }
+    const dim3 grid((unsigned)((L2 + nk - 1) / nk), (unsigned)n_chains);
+    ce_corr_tiled_kernel<B><<<grid, 256, smem, st>>>(occ, L0, L1, L2, nk, out);
+    return cudaGetLastError();
+  }
+  const long long N = (long long)L0 * L1 * L2;
+  const int nblk = (int)std::min<long long>((N + 255) / 256, 1024);
+  ce_corr_kernel<B><<<dim3(nblk, n_chains), 256, 0, st>>>(occ, L0, L1, L2, n_chains, out);
+  return cudaGetLastError();
+}
+
+inline cudaError_t launch_corr(int kind, const int8_t* occ, int L0, int L1, int L2, int n_chains, long long* out,
+                               cudaStream_t st) {
+  return kind == 0 ? launch_corr<FccBinary>(occ, L0, L1, L2, n_chains, out, st)
+                   : launch_corr<FccTernary>(occ, L0, L1, L2, n_chains, out, st);
+}
+
 inline int launch_sweep(const mg_ce_model* m, const SweepLaunch& L) {
   return m->kind == 0 ? launch_sweep_t<FccBinary, NT_BINARY>(m, L) : launch_sweep_t<FccTernary, NT_TERNARY>(m, L);
 }

@@ -60,10 +60,7 @@ size_t nfold_smem(int L0, int L1, int L2, int n_super) {
 
 int corr_recompute(mg_ce_nfold* h, long long* d) {
   MG_CUDA_TRY(cudaMemsetAsync(d, 0, sizeof(long long) * (size_t)h->model->n_classes * h->n_chains, h->stream));
-  const int nblk = (int)std::min<long long>((h->N + 255) / 256, 1024);
-  dim3 grid(nblk, h->n_chains);
-  mg::ce_corr_kernel<mg::FccBinary><<<grid, 256, 0, h->stream>>>(h->docc, h->L0, h->L1, h->L2, h->n_chains, d);
-  MG_CUDA_TRY(cudaGetLastError());
+  MG_CUDA_TRY(mg::host::launch_corr<mg::FccBinary>(h->docc, h->L0, h->L1, h->L2, h->n_chains, d, h->stream));
   return MG_OK;
 }
 

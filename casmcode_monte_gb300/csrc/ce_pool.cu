@@ -470,12 +470,7 @@ int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, co
     long long* st = p->dstate + (size_t)slot * nc;
     MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(long long) * nc, p->stream));
     MG_CUDA_TRY(cudaMemsetAsync(p->dnsamp + slot, 0, sizeof(int), p->stream));
-    const int nblk = (int)std::min<long long>((N + 255) / 256, 1024);
-    if (p->model->kind == 0)
-      mg::ce_corr_kernel<mg::FccBinary><<<dim3(nblk, 1), 256, 0, p->stream>>>(p->darena + off, L0, L1, L2, 1, st);
-    else
-      mg::ce_corr_kernel<mg::FccTernary><<<dim3(nblk, 1), 256, 0, p->stream>>>(p->darena + off, L0, L1, L2, 1, st);
-    MG_CUDA_TRY(cudaGetLastError());
+    MG_CUDA_TRY(mg::host::launch_corr(p->model->kind, p->darena + off, L0, L1, L2, 1, st, p->stream));
   }
   MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
   PoolSlot& s = p->slots[slot];
@@ -720,13 +715,7 @@ int mg_ce_pool_corr(mg_ce_pool* p, int slot, long long* out) {
   const PoolSlot& s = p->slots[slot];
   const int nc = p->model->n_classes;
   MG_CUDA_TRY(cudaMemsetAsync(p->dcorr, 0, sizeof(long long) * nc, p->stream));
-  const int nblk = (int)std::min<long long>((s.N + 255) / 256, 1024);
-  dim3 grid(nblk, 1);
-  if (p->model->kind == 0)
-    mg::ce_corr_kernel<mg::FccBinary><<<grid, 256, 0, p->stream>>>(p->darena + s.offset, s.L0, s.L1, s.L2, 1, p->dcorr);
-  else
-    mg::ce_corr_kernel<mg::FccTernary><<<grid, 256, 0, p->stream>>>(p->darena + s.offset, s.L0, s.L1, s.L2, 1, p->dcorr);
-  MG_CUDA_TRY(cudaGetLastError());
+  MG_CUDA_TRY(mg::host::launch_corr(p->model->kind, p->darena + s.offset, s.L0, s.L1, s.L2, 1, p->dcorr, p->stream));
   MG_CUDA_TRY(cudaMemcpyAsync(out, p->dcorr, sizeof(long long) * nc, cudaMemcpyDeviceToHost, p->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
   return MG_OK;

@@ -1750,6 +1750,47 @@ __global__ void ce_delta_e_kernel(CeWeights<B::NFEAT> w, const int8_t* occ, int 
   out[t] = __dsub_rn(dE, cp[c].dmu64[o * NS + o2]);
 }
 
+// Integer correlation sums of every class, recomputed from the occupation with the chain's
+// planes staged in shared memory: CTA (x, chain) holds planes [x nk, x nk + nk) plus a
+// HALO-plane border in k and a HALO border in i and j (periodic images), as occupant codes,
+// so that every cluster member is a constant offset (out[chain][NCLASS], added atomically).
+template <class B>
+__global__ void __launch_bounds__(256) ce_corr_tiled_kernel(const int8_t* occ, int L0, int L1, int L2, int nk,
+                                                            long long* out) {
+  constexpr int H = B::HALO;
+  constexpr int NC = B::NCLASS;
+  extern __shared__ __align__(16) int8_t s[];
+  const int chain = blockIdx.y;
+  const int k0 = blockIdx.x * nk;
+  const int nkb = min(nk, L2 - k0);
+  const int PX = L0 + 2 * H, PY = L1 + 2 * H, PXY = PX * PY;
+  const int8_t* g = occ + (size_t)chain * L0 * L1 * L2;
+  for (int idx = threadIdx.x; idx < PXY * (nkb + 2 * H); idx += blockDim.x) {
+    const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
+    int i = ip - H, j = jp - H, k = k0 + kp - H;
+    i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+    j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+    k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+    s[idx] = B::code_of_occ(g[i + (long long)L0 * (j + (long long)L1 * k)]);
+  }
+  __syncthreads();
+  long long C[NC];
+#pragma unroll
+  for (int f = 0; f < NC; ++f) C[f] = 0;
+  const int L01 = L0 * L1;
+  for (int site = threadIdx.x; site < L01 * nkb; site += blockDim.x) {
+    const int i = site % L0, j = (site / L0) % L1, kl = site / L01;
+    B::anchored(SmemLoader{s + (i + H) + PX * ((j + H) + PY * (kl + H)), PX, PXY}, C);
+  }
+#pragma unroll
+  for (int f = 0; f < NC; ++f) {
+    long long v = C[f];
+    for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o2);
+    if ((threadIdx.x & 31) == 0 && v)
+      atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)chain * NC + f), (unsigned long long)v);
+  }
+}
+
 template <class B>
 __global__ void ce_corr_kernel(const int8_t* occ, int L0, int L1, int L2, int n_chains, long long* out) {
   // grid: (blocks per chain, chains); out[chain][NCLASS]
