@@ -257,6 +257,102 @@ def _quad_pipelines(bs, offs) -> list:
     return out
 
 
+# Site functions of the ternary Chebyshev basis over the indicators u = [o != 1] and
+# s = [o == 2] of the occupant o in {0, 1, 2}: psi_0 = o - 1 = 2 s - u, psi_1 = 3 u - 2;
+# coefficients of (1, u, s).
+_CHEB_IND = {0: (0, -1, 2), 1: (-2, 3, 0)}
+
+
+def ternary_count_groups(bs):
+    """Monomial counts of the ternary word layout.
+
+    Every product of the other sites' psi values in a feature term expands over the
+    indicators (u, s) of those sites into monomials (products of one indicator per site, at
+    most three sites).  Monomials with the same coefficient in every feature form one
+    group; a group's count is the number of its monomials equal to 1, at most the group
+    size (below 256, so four sites' counts share a word byte by byte).  Returns
+    (groups, coef, const): groups[j] lists the monomials (tuples of (offset, 'u'|'s')),
+    coef[k][j] the coefficient of count j in feature k, const[k] the constant term, so that
+    F[k] = const[k] + sum_j coef[k][j] count[j]."""
+    import itertools as it
+    nf = bs.n_features
+    mono: dict = {}
+    for k, f in enumerate(bs.features):
+        for term in f.terms:
+            choices = []
+            for off, b in term:
+                a, be, g = _CHEB_IND[b]
+                opts = []
+                if a:
+                    opts.append(((), a))
+                if be:
+                    opts.append((((off, "u"),), be))
+                if g:
+                    opts.append((((off, "s"),), g))
+                choices.append(opts)
+            for combo in it.product(*choices):
+                m = tuple(sorted(sum((c[0] for c in combo), ())))
+                c = 1
+                for x in combo:
+                    c *= x[1]
+                mono.setdefault(m, [0] * nf)[k] += c
+    const = mono.pop((), [0] * nf)
+    by_vec: dict = {}
+    for m in sorted(mono):
+        v = tuple(mono[m])
+        if any(v):
+            by_vec.setdefault(v, []).append(m)
+    groups = sorted(by_vec.values(), key=lambda ms: ms[0])
+    assert all(len(g) < 256 for g in groups)
+    coef = [[mono[g[0]][k] for g in groups] for k in range(nf)]
+    return groups, coef, const
+
+
+def _ternary_counts(bs, offs) -> list:
+    """Byte-parallel monomial counts for the ternary word layout: ld(di,dj,dk) returns a
+    word of four sites' occupants (bytes 0, 1, 2); M[j] receives the four sites' counts of
+    group j (ternary_count_groups), one per byte.  Indicators per neighbour word:
+    u = (c ^ 0x01010101) & 0x01010101, s = (c >> 1) & 0x01010101; products are ANDs, pair
+    products sharing a factor are mask(factor) & (sum of the partners)."""
+    groups, coef, const = ternary_count_groups(bs)
+    nj = len(groups)
+    out = [f"constexpr int NCOUNT = {nj};",
+           "// F[k] = tq_const(k) + sum_j tq_coef(k, j) M[j] (M: monomial counts of counts_quad)",
+           "__host__ __device__ constexpr int tq_coef(int k, int j) {",
+           "  constexpr int t[NFEAT][NCOUNT] = {" + ", ".join(
+               "{" + ", ".join(str(x) for x in row) + "}" for row in coef) + "};",
+           "  return t[k][j];",
+           "}",
+           "__host__ __device__ constexpr int tq_const(int k) {",
+           "  constexpr int t[NFEAT] = {" + ", ".join(str(x) for x in const) + "};",
+           "  return t[k];",
+           "}",
+           "// Byte-parallel monomial counts of four sites (one per byte) from words of occupants.",
+           "template <class Loader>",
+           "__device__ __forceinline__ void counts_quad(const Loader& ld, uint32_t (&M)[NCOUNT]) {"]
+    used = sorted({o for g in groups for m in g for o, _ in m})
+    for o in used:
+        v = _var(o)
+        out.append(f"  const uint32_t c_{v} = ld({o[0]}, {o[1]}, {o[2]});")
+        out.append(f"  const uint32_t u_{v} = (c_{v} ^ 0x01010101u) & 0x01010101u;")
+        out.append(f"  const uint32_t s_{v} = (c_{v} >> 1) & 0x01010101u;")
+    masks_all = set()
+    body = []
+    for j, g in enumerate(groups):
+        names = [tuple(f"{ind}_{_var(o)}" for o, ind in m) for m in g]
+        parts = [m[0] for m in names if len(m) == 1]
+        pp, masks = _factor_pairs([m for m in names if len(m) == 2])
+        parts += pp
+        masks_all |= masks
+        parts += [_and(list(m)) for m in names if len(m) >= 3]
+        body.append(f"  M[{j}] = " + _sum_expr(parts) + ";")
+    for v in sorted(masks_all):
+        out.append(f"  const uint32_t m_{v} = {v} * 0xFFu;")
+    out += body
+    out.append("}")
+    return out
+
+
 def generate(kind: str) -> tuple[str, dict]:
     bs = O.make_basis_set(kind)
     basis = bs.basis
@@ -334,6 +430,8 @@ def generate(kind: str) -> tuple[str, dict]:
     if basis.name == "occupation":
         lines += _quad_features(bs, offs)
         lines += _quad_pipelines(bs, offs)
+    else:
+        lines += _ternary_counts(bs, offs)
 
     # anchored correlations
     anc_offs = sorted({o for cls in bs.anchored for t in cls for o, _ in t})
