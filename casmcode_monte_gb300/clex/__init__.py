@@ -159,9 +159,11 @@ class ChainBatch:
         return {"layout": LAYOUTS[lay.value], "ctas_per_chain": S.value, "ms_per_pass": float(ms.value)}
 
     def set_layout(self, layout: str) -> None:
-        """Sweep with one site per byte ("byte"), four sites per word ("word", binary
-        basis with L0 a multiple of 4), four sites per word with the features split around
-        the phase barrier ("word_pipelined") or the same with warp-specialised CTAs
+        """Sweep with one site per byte ("byte"), four sites per word ("word", L0 a multiple
+        of 4 and a colouring that gives sites i and i + L0/4 one colour; byte-parallel
+        features for the binary basis, byte-parallel monomial counts for the ternary one),
+        and, binary basis only, four sites per word with the features split around the phase
+        barrier ("word_pipelined") or the same with warp-specialised CTAs
         ("word_specialised"); trajectories are identical."""
         codes = {v: k for k, v in LAYOUTS.items()}
         if layout not in codes:

@@ -588,7 +588,8 @@ int setup_layout(mg_ce_batch* b, int layout) {
   b->smem = smem;
   b->PZ = (b->L2 + S - 1) / S + 2 * mg::CE_HALO;
   b->threads = layout == 3 ? 2 * mg::host::NW_WS
-                           : (layout >= 1 ? mg::host::NT_QUAD : (m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY));
+                           : (layout >= 1 ? (m->kind == 1 ? mg::host::NT_TQUAD : mg::host::NT_QUAD)
+                                          : (m->kind == 0 ? mg::NT_BINARY : mg::NT_TERNARY));
   b->max_words = lists->max_words;
   return setup_rotation(b);
 }
@@ -693,7 +694,7 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
     delete b;
     return MG_ERR_INVALID;
   }
-  const int layout = !b->col->word ? 0 : (b->pipe >= 0 ? 3 : 1);
+  const int layout = !b->col->word ? 0 : ((m->kind == 0 && b->pipe >= 0) ? 3 : 1);
   b->hcp.resize(n_chains);
   make_chain_params(m, n_chains, temperature, mu, seeds, chain_ids, b->hcp.data());
 
@@ -765,7 +766,8 @@ int mg_ce_color_supercell(int basis_kind, int L0, int L1, int L2, int32_t* color
     set_error("Error in mg_ce_color_supercell: colouring needs more than 64 colours");
     return -MG_ERR_INVALID;
   }
-  if (word_layout) *word_layout = !quad_eligible(basis_kind, L0, L1, L2, color) ? 0 : (pipe >= 0 ? 2 : 1);
+  if (word_layout)
+    *word_layout = !quad_eligible(basis_kind, L0, L1, L2, color) ? 0 : ((basis_kind == 0 && pipe >= 0) ? 2 : 1);
   // (a batch may further use layout 3 when its CTA split stages few enough words)
   return n;
 }
@@ -789,6 +791,11 @@ int mg_ce_batch_set_layout(mg_ce_batch* b, int layout) {
               "and a colouring with colour(i + Q) = colour(i)");
     return MG_ERR_INVALID;
   }
+  if (layout >= 2 && b->model->kind != 0) {
+    set_error("Error in mg_ce_batch_set_layout: the pipelined and warp-specialised word layouts need the binary "
+              "basis");
+    return MG_ERR_INVALID;
+  }
   if (layout >= 2 && b->pipe < 0) {
     set_error("Error in mg_ce_batch_set_layout: the pipelined word layout needs one of the generated pipeline "
               "colourings");
@@ -807,7 +814,7 @@ int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout_out, int*
   const bool word = b->col->word;
   std::vector<int> layouts = {0};
   if (word) layouts.push_back(1);
-  if (word && b->pipe >= 0) {
+  if (word && b->pipe >= 0 && m->kind == 0) {
     layouts.push_back(2);
     layouts.push_back(3);
   }
@@ -856,7 +863,7 @@ int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout_out, int*
   // the occupancy choice of the warp-specialised layout with rotation over two cluster sizes,
   // timed per pass on runs long enough to rotate (at least 4 n_chains passes)
   bool best_rot = false;
-  if (rc == MG_OK && word && b->pipe >= 0 && b->rotation_mode != 0) {
+  if (rc == MG_OK && word && b->pipe >= 0 && m->kind == 0 && b->rotation_mode != 0) {
     b->ctas_requested = 0;
     if (setup_layout(b, 3) == MG_OK && b->S_fast > 0) {
       const int np = std::max(probe_passes, 4 * b->n_chains);
@@ -929,6 +936,8 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   }
   else if (b->layout == 3)
     rc = launch_sweep_ws(b->model, L, b->pipe);
+  else if (b->layout >= 1 && b->model->kind == 1)
+    rc = launch_sweep_tquad(b->model, L);
   else if (b->layout >= 1)
     rc = launch_sweep_quad(b->model, L, b->layout == 2 ? b->pipe : -1);
   else

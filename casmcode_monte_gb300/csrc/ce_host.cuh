@@ -53,9 +53,19 @@ namespace mg {
   }                                                                                      \
   template <int P>                                                                       \
   using Pipe = fcc_binary::Pipe<P>;
+// the ternary basis has byte-parallel monomial counts (word layout)
+#define MG_TQUAD_COUNTS                                                                   \
+  static constexpr int NCOUNT = fcc_ternary::NCOUNT;                                     \
+  __host__ __device__ static constexpr int tq_coef(int k, int j) { return fcc_ternary::tq_coef(k, j); } \
+  __host__ __device__ static constexpr int tq_const(int k) { return fcc_ternary::tq_const(k); } \
+  template <class L>                                                                     \
+  __device__ static __forceinline__ void counts_quad(const L& ld, uint32_t(&M)[NCOUNT]) { \
+    fcc_ternary::counts_quad(ld, M);                                                     \
+  }
 MG_BASIS_ADAPTER(FccBinary, fcc_binary, MG_QUAD_FEATURES)
-MG_BASIS_ADAPTER(FccTernary, fcc_ternary, )
+MG_BASIS_ADAPTER(FccTernary, fcc_ternary, MG_TQUAD_COUNTS)
 #undef MG_QUAD_FEATURES
+#undef MG_TQUAD_COUNTS
 #undef MG_BASIS_ADAPTER
 
 constexpr int NT_BINARY = 512;
@@ -144,7 +154,7 @@ inline const int* offsets(int kind, int* n) {
 inline int color_supercell(int L0, int L1, int L2, int kind, int32_t* col, int* pipe = nullptr) {
   int noff = 0;
   const int* off = offsets(kind, &noff);
-  const bool want_quad = kind == 0 && L0 % 4 == 0;
+  const bool want_quad = (kind == 0 || kind == 1) && L0 % 4 == 0;  // both bases have word layouts
   if (pipe) *pipe = -1;
   auto fill_linear = [&](long long a, long long b, long long c, int m) {
     for (int k = 0; k < L2; ++k)
@@ -327,6 +337,8 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
 // ---- word layout (four sites per 32-bit word, binary basis)
 
 constexpr int NT_QUAD = 384;
+// threads of the ternary word-layout kernel
+constexpr int NT_TQUAD = 256;
 // threads per role of the warp-specialised kernel: 11 warps, one word per thread (FCC
 // 64^3 in 12 row slabs proposes at most 344 words per CTA and colour)
 constexpr int NW_WS = 352;
@@ -399,10 +411,11 @@ inline size_t ws_smem(int L0, int L1, int L2, int S, int n_colors = CE_MAX_COLOR
          sizeof(int) * (n_colors + 1);
 }
 
-// The word layout applies to the binary basis when L0 = 4Q with Q >= 4 and the colouring
-// gives the four sites i0 + tQ of every row one colour.
+// The word layout applies when L0 = 4Q with Q >= 4 and the colouring gives the four sites
+// i0 + tQ of every row one colour (binary: byte-parallel features; ternary: byte-parallel
+// monomial counts).
 inline bool quad_eligible(int kind, int L0, int L1, int L2, const int32_t* col) {
-  if (kind != 0 || L0 % 4 != 0 || L0 / 4 < 4) return false;
+  if ((kind != 0 && kind != 1) || L0 % 4 != 0 || L0 / 4 < 4) return false;
   const int Q = L0 / 4;
   const long long rows = (long long)L1 * L2;
   for (long long r = 0; r < rows; ++r) {
@@ -589,6 +602,8 @@ int max_active_clusters_k(Kern kern, int NT, int S, size_t smem, int* out) {
 // layout 0: one site per byte (ce_sweep_kernel); layout 1: four sites per word
 // (ce_sweep_quad_kernel, binary basis); layout 2: the same with pipelined features
 inline int max_active_chains(int kind, int S, size_t smem, int* out, int layout = 0) {
+  if (layout == 1 && kind == 1)
+    return max_active_clusters_k(ce_sweep_tquad_kernel<FccTernary, NT_TQUAD>, NT_TQUAD, S, smem, out);
   if (layout == 1)
     return max_active_clusters_k(ce_sweep_quad_kernel<FccBinary, NT_QUAD, -1>, NT_QUAD, S, smem, out);
   if (layout == 2)
@@ -756,6 +771,74 @@ inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L, int pip
     cfg.numAttrs = 1;
   }
   MG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, A));
+  MG_CUDA_TRY(cudaGetLastError());
+  return MG_OK;
+}
+
+// Weights of the ternary word layout from the model's quantised feature weights:
+// W[b][j] = sum over features k of basis b of wq[k] tq_coef(k, j), gc[b] = sum wq[k] tq_const(k)
+// (modulo 2^32, as the kernel's int32 sums).
+inline void fill_tquad_weights(const mg_ce_model* m, TernQuadWeights<FccTernary::NCOUNT>& tw) {
+  long long W[2][FccTernary::NCOUNT] = {}, gc[2] = {};
+  for (int k = 0; k < FccTernary::NFEAT; ++k) {
+    const int b = FccTernary::feat_b(k);
+    gc[b] += (long long)m->wq[k] * FccTernary::tq_const(k);
+    for (int j = 0; j < FccTernary::NCOUNT; ++j) W[b][j] += (long long)m->wq[k] * FccTernary::tq_coef(k, j);
+  }
+  for (int b = 0; b < 2; ++b) {
+    tw.gc[b] = (int)(uint32_t)(unsigned long long)gc[b];
+    for (int j = 0; j < FccTernary::NCOUNT; ++j) tw.W[b][j] = (int)(uint32_t)(unsigned long long)W[b][j];
+  }
+}
+
+// word-layout sweep of the ternary basis
+inline int launch_sweep_tquad(const mg_ce_model* m, const SweepLaunch& L) {
+  using B = FccTernary;
+  CeTQuadArgs<B::NFEAT, B::NCOUNT> TA;
+  CeQuadArgs<B::NFEAT>& A = TA.q;
+  A.g.L0 = L.L0;
+  A.g.L1 = L.L1;
+  A.g.L2 = L.L2;
+  A.g.Q = L.L0 / 4;
+  A.g.S = L.S;
+  A.g.planes = word_slab_kind(L.L1, L.L2, L.S);
+  A.g.window_planes = row_window_planes(L.L1, L.L2, L.S, B::HALO, A.g.planes);
+  A.g.max_rows = row_slab_max_rows(L.L1, L.L2, L.S, A.g.planes);
+  A.g.RS = quad_row_stride(L.L0 / 4);
+  A.g.RY = L.L1 + 2 * CE_HALO;
+  A.g.n_colors = L.n_colors;
+  A.g.color_start = L.cstart;
+  A.g.entries = L.entries;
+  A.g.site_l = L.site;
+  fill_weights(m, A.w);
+  fill_tquad_weights(m, TA.tw);
+  A.cp = L.cp;
+  A.occ = L.occ;
+  A.pass0 = L.pass0;
+  A.n_passes = L.n_passes;
+  A.n_chains = L.n_chains;
+  A.precision = L.precision;
+  A.out = L.out;
+  A.n_map = 0;
+  const size_t smem = quad_smem(L.L0, L.L1, L.L2, L.S);
+  auto kern = ce_sweep_tquad_kernel<B, NT_TQUAD>;
+  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);
+  cfg.blockDim = dim3(NT_TQUAD, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = L.stream;
+  cudaLaunchAttribute attr[1];
+  if (L.S > 1) {
+    if (L.S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)L.S;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  MG_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, TA));
   MG_CUDA_TRY(cudaGetLastError());
   return MG_OK;
 }

@@ -171,7 +171,8 @@ int shape_plan(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan** out) {
   };
   sp.layout = 0;
   sp.cls = -1;
-  if (quad_eligible(p->model->kind, L0, L1, L2, sp.color.data())) {
+  // the pool's word-layout kernels are the binary basis's
+  if (p->model->kind == 0 && quad_eligible(p->model->kind, L0, L1, L2, sp.color.data())) {
     sp.cls = fit(1);
     if (sp.cls >= 0) sp.layout = 1;
   }

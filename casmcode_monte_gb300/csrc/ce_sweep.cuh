@@ -854,6 +854,255 @@ struct QuadSweeper {
   }
 };
 
+// ---- word layout of the ternary Chebyshev basis
+//
+// The same four-sites-per-word lattice (bytes hold occupants 0, 1, 2) and row slabs as the
+// binary word layout.  A site's local features are linear in byte-parallel monomial counts
+// of the indicators u = [o != 1] and s = [o == 2] of its neighbours (B::counts_quad; F[k] =
+// tq_const(k) + sum_j tq_coef(k, j) M[j], exact integers), so the four sites' energy sums
+// G_b = sum over features of basis b of wq[k] F[k] come from the counts with the weights
+// gc[b] + sum_j W[b][j] M[j] (int32, exact modulo 2^32 and equal to the per-site sums).
+// Random numbers are those of the per-site (byte) layout: Philox block with counter
+// (site, pass, chain, tag) per site, word 0 for the acceptance and bit 31 of word 1 for the
+// target occupant; decisions use the same FP32 rule and FP64 re-decision, so trajectories
+// equal the byte layout's.
+template <int NJ>
+struct TernQuadWeights {
+  int W[2][NJ];
+  int gc[2];
+};
+
+// FP64 re-decision of one site of a word (MetropolisRule::exact) with its features from the
+// counts: returns bit 0 the decision and bit 1 whether FP32 mode flipped it.  Kept out of
+// line: it is taken for few proposals and would otherwise enlarge the update's registers.
+template <class B>
+__device__ __noinline__ int tern_exact(const MetropolisRule<B>& rule, int o, int o2, int dpsi0, int dpsi1,
+                                       const uint32_t* M, int shift, uint32_t x0, bool acc32) {
+  struct Fi {
+    const uint32_t* M;
+    int shift;
+    __device__ __forceinline__ int operator()(int k) const {
+      int v = B::tq_const(k);
+#pragma unroll
+      for (int j = 0; j < B::NCOUNT; ++j)
+        if (B::tq_coef(k, j) != 0) v += B::tq_coef(k, j) * (int)((M[j] >> shift) & 0xFFu);
+      return v;
+    }
+  };
+  int cnt[CeSlots<B::NCLASS>::N] = {};
+  const int dpsi[2] = {dpsi0, dpsi1};
+  const bool a = rule.exact(o, o2, dpsi, Fi{M, shift}, x0, acc32, cnt);
+  return (a ? 1 : 0) | (cnt[B::NCLASS + 1] ? 2 : 0);
+}
+
+template <class B>
+struct TernQuadSweeper {
+  static constexpr int NF = B::NFEAT;
+  static constexpr int NC = B::NCLASS;
+  static constexpr int NSLOT = CeSlots<NC>::N;
+  static constexpr int NJ = B::NCOUNT;
+  static_assert(B::NSPECIES == 3 && B::NFUNC == 2, "ternary word layout needs the three-species basis");
+  uint32_t* s;
+  uint32_t* s_prev;
+  uint32_t* s_next;
+  int RS, RSY;
+  int Q, dJ, dKp, dKn;
+  MetropolisRule<B> rule;
+  const TernQuadWeights<NJ>* tw;
+
+  __device__ __forceinline__ WordLoader loader(uint32_t ent) const {
+    return WordLoader{s + (int)(ent & 0xFFFFFFu), RS, RSY};
+  }
+
+  // one word: counts, the four sites' decisions (Philox block per site), write-back of the
+  // accepted changes and their correlation changes
+  __device__ __forceinline__ void update(uint32_t ent, uint32_t site0, uint32_t pass, uint32_t chain_id,
+                                         uint32_t key0, uint32_t key1, int (&acc)[NSLOT]) const {
+    const int pw = (int)(ent & 0xFFFFFFu);
+    const uint32_t v = s[pw];
+    uint32_t M[NJ];
+    B::counts_quad(loader(ent), M);
+    uint32_t nv = v, sg0 = 0u, sg1 = 0u;
+    int n_acc = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const U32x4 x = philox4x32_10(U32x4{site0 + (uint32_t)(t * Q), pass, chain_id, SWEEP_TAG}, key0, key1);
+      const int o = (int)((v >> (8 * t)) & 0xFFu);
+      const int o2 = (o + 1 + (int)(x.y >> 31)) % 3;
+      const int dpsi[2] = {B::psi(0, o2) - B::psi(0, o), B::psi(1, o2) - B::psi(1, o)};
+      int G0 = tw->gc[0], G1 = tw->gc[1];
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const int m = (int)((M[j] >> (8 * t)) & 0xFFu);
+        G0 += tw->W[0][j] * m;
+        G1 += tw->W[1][j] * m;
+      }
+      bool amb;
+      bool a = rule.fast(o, o2, dpsi[0] * G0 + dpsi[1] * G1, x.x, amb);
+      if (amb) {
+        // rare: the FP64 decision out of line, from a copy of the counts
+        uint32_t Mc[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) Mc[j] = M[j];
+        const int r = tern_exact<B>(rule, o, o2, dpsi[0], dpsi[1], Mc, 8 * t, x.x, a);
+        a = (r & 1) != 0;
+        acc[NC] += 1;
+        acc[NC + 1] += (r >> 1) & 1;
+      }
+      if (a) {
+        nv = (nv & ~(0xFFu << (8 * t))) | ((uint32_t)o2 << (8 * t));
+        sg0 |= (uint32_t)(dpsi[0] & 0xFF) << (8 * t);
+        sg1 |= (uint32_t)(dpsi[1] & 0xFF) << (8 * t);
+        ++n_acc;
+      }
+    }
+    if (n_acc) {
+      const uint32_t flags = ent >> 24;
+      uint32_t vi = nv;
+      int oi = 0;
+      if (flags & 1u) {
+        oi = Q;
+        vi = __funnelshift_r(nv, nv, 8);
+      } else if (flags & 2u) {
+        oi = -Q;
+        vi = __funnelshift_l(nv, nv, 8);
+      }
+      const int oj = (flags & 4u) ? dJ : ((flags & 8u) ? -dJ : 0);
+      auto put = [&](uint32_t* r) {
+        r[0] = nv;
+        if (oi) r[oi] = vi;
+        if (oj) r[oj] = nv;
+        if (oi && oj) r[oi + oj] = vi;
+      };
+      put(s + pw);
+      if (flags & 16u) put(s_prev + pw + dKp);
+      if (flags & 32u) put(s_next + pw - dKn);
+      // correlation changes: sum over the accepted sites of dpsi_b * F[k] =
+      // tq_const(k) sum dpsi_b + sum_j tq_coef(k, j) (signed byte dot product of M[j], dpsi_b)
+      acc[0] += n_acc;
+      const int c0 = __dp4a((int)0x01010101, (int)sg0, 0), c1 = __dp4a((int)0x01010101, (int)sg1, 0);
+#pragma unroll
+      for (int k = 0; k < NF; ++k)
+        if (B::tq_const(k) != 0) acc[B::feat_class(k)] += B::tq_const(k) * (B::feat_b(k) == 0 ? c0 : c1);
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const int d0 = __dp4a((int)M[j], (int)sg0, 0), d1 = __dp4a((int)M[j], (int)sg1, 0);
+#pragma unroll
+        for (int k = 0; k < NF; ++k)
+          if (B::tq_coef(k, j) != 0) acc[B::feat_class(k)] += B::tq_coef(k, j) * (B::feat_b(k) == 0 ? d0 : d1);
+      }
+    }
+  }
+};
+
+template <int NFEAT, int NJ>
+struct CeTQuadArgs {
+  CeQuadArgs<NFEAT> q;
+  TernQuadWeights<NJ> tw;
+};
+
+// Word-layout sweep of the ternary basis (one or S CTAs per chain in a cluster, row slabs);
+// the structure of ce_sweep_quad_kernel without the pipelined prefetch.
+template <class B, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    ce_sweep_tquad_kernel(const __grid_constant__ CeTQuadArgs<B::NFEAT, B::NCOUNT> TA) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  const CeQuadArgs<B::NFEAT>& A = TA.q;
+  extern __shared__ __align__(16) uint32_t sq[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+
+  const QuadGeometry& g = A.g;
+  const int S = g.S;
+  const int chain = blockIdx.x / S;
+  int rank = 0;
+  cg::cluster_group cluster = cg::this_cluster();
+  if (S > 1) rank = (int)cluster.block_rank();
+  auto barrier = [&]() {
+    if (S > 1)
+      cluster.sync();
+    else
+      __syncthreads();
+  };
+
+  const int Q = g.Q, RS = g.RS, RY = g.RY, RSY = RS * RY;
+  const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+  const RowSlab sl = row_slab(L1, L2, S, rank, g.planes);
+  const int rprev = (rank + S - 1) % S;
+  const long long N = (long long)L0 * L1 * L2;
+  int8_t* gocc = A.occ + (size_t)chain * N;
+
+  load_word_window<B::HALO>(sq, gocc, L0, L1, L2, Q, RS, RY, sl.kb, sl.nk, threadIdx.x, NT);
+  if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+  const CeChainParams* cpg = A.cp + chain;
+  load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+  const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+  const int* cstart = g.color_start + rank * (g.n_colors + 1);
+
+  TernQuadSweeper<B> sw;
+  sw.s = sq;
+  sw.s_prev = sq;
+  sw.s_next = sq;
+  if (S > 1) {
+    sw.s_prev = cluster.map_shared_rank(sq, (unsigned)rprev);
+    sw.s_next = cluster.map_shared_rank(sq, (unsigned)((rank + 1) % S));
+  }
+  sw.RS = RS;
+  sw.RSY = RSY;
+  sw.Q = Q;
+  sw.dJ = L1 * RS;
+  sw.dKp = sl.dkp * RSY;
+  sw.dKn = sl.dkn * RSY;
+  sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
+                              A.precision};
+  sw.tw = &TA.tw;
+  const int lane = threadIdx.x & 31;
+  int acc[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+  barrier();
+
+#pragma unroll 1
+  for (int pass = 0; pass < A.n_passes; ++pass) {
+    const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
+#pragma unroll 1
+    for (int c = 0; c < g.n_colors; ++c) {
+#pragma unroll 1
+      for (int e = cstart[c] + threadIdx.x; e < cstart[c + 1]; e += NT)
+        sw.update(__ldg(g.entries + e), __ldg(g.site_l + e), pass_g, chain_id, key0, key1, acc);
+      barrier();
+      if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+        int* buf = acc_sm[(pass - 1) & 1];
+        const int v = buf[threadIdx.x];
+        buf[threadIdx.x] = 0;
+        if (v)
+          atomicAdd(reinterpret_cast<unsigned long long*>(
+                        A.out + ((size_t)(pass - 1) * A.n_chains + chain) * NSLOT + threadIdx.x),
+                    (unsigned long long)(long long)v);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) {
+      const int v = warp_sum(acc[q]);
+      if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+      acc[q] = 0;
+    }
+  }
+  barrier();
+  if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+    const int pl = A.n_passes - 1;
+    int* buf = acc_sm[pl & 1];
+    const int v = buf[threadIdx.x];
+    if (v)
+      atomicAdd(reinterpret_cast<unsigned long long*>(A.out + ((size_t)pl * A.n_chains + chain) * NSLOT + threadIdx.x),
+                (unsigned long long)(long long)v);
+  }
+  store_word_rows<B::HALO>(sq, gocc, L0, L1, Q, RS, RY, sl, threadIdx.x, NT);
+  barrier();
+}
+
 // Philox block of the first word of a thread in one colour phase: its four sites take
 // words 0..3 of the block with counter (site of byte 0, pass, chain, tag)
 struct QuadPrefetch {

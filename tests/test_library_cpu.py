@@ -146,7 +146,8 @@ def test_statistics_edge_cases():
                                            ("fcc_binary", (16, 16, 8), "word_pipelined"),
                                            ("fcc_binary", (16, 8, 16), "word_pipelined"),
                                            ("fcc_binary", (20, 12, 10), "word"),
-                                           ("fcc_binary", (8, 8, 8), "byte"), ("fcc_ternary", (16, 16, 16), "byte"),
+                                           ("fcc_binary", (8, 8, 8), "byte"), ("fcc_ternary", (16, 16, 16), "word"),
+                                           ("fcc_ternary", (12, 12, 12), "byte"),
                                            ("fcc_binary", (13, 11, 7), "byte")])
 def test_colouring_is_proper_host(kind, L, layout):
     """The sweep's colouring (host entry point, no device): no neighbour offset of the

@@ -41,7 +41,9 @@ def test_layout_selection(gpu_lib):
     tern = clex.ClexModel("fcc_ternary", clex.make_eci("fcc_ternary", 1))
     occt = clex.random_occupation(3, 16**3, np.random.default_rng(1))[None, :]
     bt = clex.ChainBatch(tern, (16, 16, 16), occt, [900.0], np.zeros((1, 2)), [5])
-    assert bt.layout == "byte"
+    assert bt.layout == "word"  # the ternary basis has a word layout (no pipelined form)
+    with pytest.raises(RuntimeError):
+        bt.set_layout("word_pipelined")
 
 
 WORD_SHAPES = [((16, 16, 16), 1), ((16, 16, 16), 2), ((16, 16, 8), 3), ((32, 16, 16), 8), ((20, 12, 10), 5),
