@@ -312,8 +312,13 @@ def _ternary_counts(bs, offs) -> list:
     """Byte-parallel monomial counts for the ternary word layout: ld(di,dj,dk) returns a
     word of four sites' occupants (bytes 0, 1, 2); M[j] receives the four sites' counts of
     group j (ternary_count_groups), one per byte.  Indicators per neighbour word:
-    u = (c ^ 0x01010101) & 0x01010101, s = (c >> 1) & 0x01010101; products are ANDs, pair
-    products sharing a factor are mask(factor) & (sum of the partners)."""
+    u = (c ^ 0x01010101) & 0x01010101, s = (c >> 1) & 0x01010101; products are ANDs.
+
+    The neighbours are visited in order of distance, and every monomial is added when its
+    last neighbour (in that order) arrives, so that a neighbour's indicators are live only
+    until its last monomial (at most about 15 neighbours at a time instead of all 54);
+    monomials completed by the same neighbour indicator x in one group are summed as
+    mask(x) & (sum of the rest), mask(x) = x * 0xFF (0x00 or 0xFF per byte)."""
     groups, coef, const = ternary_count_groups(bs)
     nj = len(groups)
     out = [f"constexpr int NCOUNT = {nj};",
@@ -330,25 +335,43 @@ def _ternary_counts(bs, offs) -> list:
            "// Byte-parallel monomial counts of four sites (one per byte) from words of occupants.",
            "template <class Loader>",
            "__device__ __forceinline__ void counts_quad(const Loader& ld, uint32_t (&M)[NCOUNT]) {"]
-    used = sorted({o for g in groups for m in g for o, _ in m})
-    for o in used:
+    used = sorted({o for g in groups for m in g for o, _ in m}, key=lambda o: (sum(x * x for x in o), o))
+    pos = {o: i for i, o in enumerate(used)}
+    # monomials completed at each neighbour: by group, keyed by the arriving indicator
+    due: dict = {}
+    for j, g in enumerate(groups):
+        for m in g:
+            last = max(m, key=lambda f: pos[f[0]])
+            rest = tuple(f for f in m if f != last)
+            due.setdefault(pos[last[0]], {}).setdefault((j, last[1]), []).append(rest)
+    started = [False] * nj
+    for i, o in enumerate(used):
         v = _var(o)
         out.append(f"  const uint32_t c_{v} = ld({o[0]}, {o[1]}, {o[2]});")
         out.append(f"  const uint32_t u_{v} = (c_{v} ^ 0x01010101u) & 0x01010101u;")
         out.append(f"  const uint32_t s_{v} = (c_{v} >> 1) & 0x01010101u;")
-    masks_all = set()
-    body = []
-    for j, g in enumerate(groups):
-        names = [tuple(f"{ind}_{_var(o)}" for o, ind in m) for m in g]
-        parts = [m[0] for m in names if len(m) == 1]
-        pp, masks = _factor_pairs([m for m in names if len(m) == 2])
-        parts += pp
-        masks_all |= masks
-        parts += [_and(list(m)) for m in names if len(m) >= 3]
-        body.append(f"  M[{j}] = " + _sum_expr(parts) + ";")
-    for v in sorted(masks_all):
-        out.append(f"  const uint32_t m_{v} = {v} * 0xFFu;")
-    out += body
+        masked = set()
+        for (j, ind), rests in sorted(due.get(i, {}).items()):
+            x = f"{ind}_{v}"
+            parts = []
+            singles = [r for r in rests if len(r) == 0]
+            if singles:
+                parts.append(x if len(singles) == 1 else f"{len(singles)}u * {x}")
+            others = [_and([f"{ind2}_{_var(o2)}" for o2, ind2 in r]) for r in rests if len(r) > 0]
+            if len(others) == 1:
+                parts.append(f"({x} & {others[0]})")
+            elif others:
+                if x not in masked:
+                    out.append(f"  const uint32_t m_{x} = {x} * 0xFFu;")
+                    masked.add(x)
+                parts.append(f"(m_{x} & ({' + '.join(others)}))")
+            expr = " + ".join(parts)
+            if started[j]:
+                out.append(f"  M[{j}] += {expr};")
+            else:
+                out.append(f"  M[{j}] = {expr};")
+                started[j] = True
+    assert all(started)
     out.append("}")
     return out
 

@@ -338,7 +338,7 @@ inline void build_site_lists(int L0, int L1, int L2, int S, const int32_t* col, 
 
 constexpr int NT_QUAD = 384;
 // threads of the ternary word-layout kernel
-constexpr int NT_TQUAD = 256;
+constexpr int NT_TQUAD = 384;
 // threads per role of the warp-specialised kernel: 11 warps, one word per thread (FCC
 // 64^3 in 12 row slabs proposes at most 344 words per CTA and colour)
 constexpr int NW_WS = 352;
