@@ -171,8 +171,7 @@ int shape_plan(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan** out) {
   };
   sp.layout = 0;
   sp.cls = -1;
-  // the pool's word-layout kernels are the binary basis's
-  if (p->model->kind == 0 && quad_eligible(p->model->kind, L0, L1, L2, sp.color.data())) {
+  if (quad_eligible(p->model->kind, L0, L1, L2, sp.color.data())) {
     sp.cls = fit(1);
     if (sp.cls >= 0) sp.layout = 1;
   }
@@ -230,9 +229,24 @@ int geometry(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan& sp, int* ou
   return MG_OK;
 }
 
+// the word-layout pool kernel of basis B (binary: byte-parallel features; ternary: monomial
+// counts, whose launch carries the count weights too)
+template <class B, bool CLUSTER>
+const void* pool_word_kernel(int* nt) {
+  if constexpr (B::NSPECIES == 3) {
+    *nt = NT_TQUAD;
+    return (const void*)mg::ce_pool_tquad_kernel<B, NT_TQUAD, CLUSTER>;
+  } else {
+    *nt = NT_QUAD;
+    return (const void*)mg::ce_pool_quad_kernel<B, NT_QUAD, CLUSTER>;
+  }
+}
+
 template <class B, int NT>
 int launch_pool(mg_ce_pool* p, int cls, int layout, int item0, int n_items, int n_passes, size_t smem) {
-  mg::CePoolArgs<B::NFEAT> A;
+  mg::CeTPoolArgs<B::NFEAT, mg::FccTernary::NCOUNT> TA;  // the binary kernels read TA.p only
+  mg::CePoolArgs<B::NFEAT>& A = TA.p;
+  if constexpr (B::NSPECIES == 3) mg::host::fill_tquad_weights(p->model, TA.tw);
   A.geoms = p->dgeoms;
   A.items = p->ditems + item0;
   A.n_items = n_items;
@@ -247,8 +261,8 @@ int launch_pool(mg_ce_pool* p, int cls, int layout, int item0, int n_items, int 
   cudaStream_t st = p->cls_stream[2 * cls + layout];
   if (S == 1) {
     const void* kern = (const void*)mg::ce_pool_kernel<B, NT>;
-    if (layout == 1) kern = (const void*)mg::ce_pool_quad_kernel<mg::FccBinary, NT_QUAD, false>;
-    const int nt = layout == 1 ? NT_QUAD : NT;
+    int nt = NT;
+    if (layout == 1) kern = pool_word_kernel<B, false>(&nt);
     MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0, dev = 0, sms = 0;
     MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
@@ -259,14 +273,14 @@ int launch_pool(mg_ce_pool* p, int cls, int layout, int item0, int n_items, int 
       return MG_ERR_INVALID;
     }
     const int grid = std::max(1, std::min(n_items, per_sm * sms));
-    void* args[] = {(void*)&A};
+    void* args[] = {layout == 1 && B::NSPECIES == 3 ? (void*)&TA : (void*)&A};
     MG_CUDA_TRY(cudaLaunchKernel(kern, dim3(grid), dim3(nt), args, smem, st));
     MG_CUDA_TRY(cudaGetLastError());
     return MG_OK;
   }
   const void* kern = (const void*)mg::ce_pool_cluster_kernel<B, NT>;
-  if (layout == 1) kern = (const void*)mg::ce_pool_quad_kernel<mg::FccBinary, NT_QUAD, true>;
-  const int nt = layout == 1 ? NT_QUAD : NT;
+  int nt = NT;
+  if (layout == 1) kern = pool_word_kernel<B, true>(&nt);
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
@@ -288,7 +302,7 @@ int launch_pool(mg_ce_pool* p, int cls, int layout, int item0, int n_items, int 
     return MG_ERR_INVALID;
   }
   cfg.gridDim = dim3((unsigned)(S * std::max(1, std::min(n_items, n_cl))), 1, 1);
-  void* args[] = {(void*)&A};
+  void* args[] = {layout == 1 && B::NSPECIES == 3 ? (void*)&TA : (void*)&A};
   MG_CUDA_TRY(cudaLaunchKernelExC(&cfg, kern, args));
   MG_CUDA_TRY(cudaGetLastError());
   return MG_OK;

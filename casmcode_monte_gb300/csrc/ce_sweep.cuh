@@ -1950,6 +1950,122 @@ __global__ void __launch_bounds__(NT, 1) ce_pool_quad_kernel(const __grid_consta
   }
 }
 
+// Persistent pool kernel of the ternary word layout: the work queue and phases of
+// ce_pool_quad_kernel with the ternary sweeper (per-site Philox blocks, monomial counts).
+template <int NFEAT, int NJ>
+struct CeTPoolArgs {
+  CePoolArgs<NFEAT> p;
+  TernQuadWeights<NJ> tw;
+};
+
+template <class B, int NT, bool CLUSTER>
+__global__ void __launch_bounds__(NT, 1)
+    ce_pool_tquad_kernel(const __grid_constant__ CeTPoolArgs<B::NFEAT, B::NCOUNT> TA) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  const CePoolArgs<B::NFEAT>& A = TA.p;
+  extern __shared__ __align__(16) uint32_t sq[];
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+  __shared__ int item_sm;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int S = CLUSTER ? (int)cluster.num_blocks() : 1;
+  const int rank = CLUSTER ? (int)cluster.block_rank() : 0;
+  const int lane = threadIdx.x & 31;
+  auto sync_all = [&]() {
+    if (CLUSTER)
+      cluster.sync();
+    else
+      __syncthreads();
+  };
+
+#pragma unroll 1
+  while (true) {
+    if (rank == 0 && threadIdx.x == 0) {
+      const int it = atomicAdd(A.next_item, 1);
+      if (CLUSTER) {
+        for (int r = 0; r < S; ++r) *cluster.map_shared_rank(&item_sm, (unsigned)r) = it;
+      } else {
+        item_sm = it;
+      }
+    }
+    sync_all();
+    const int it = item_sm;
+    if (it >= A.n_items) break;
+    const PoolItem item = A.items[it];
+    const PoolGeometry g = A.geoms[item.geom];
+    const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+    const int Q = L0 / 4, RS = (Q + 2 * B::HALO) | 1, RY = L1 + 2 * B::HALO, RSY = RS * RY;
+    const RowSlab sl = row_slab(L1, L2, S, rank, g.planes);
+    const int rprev = (rank + S - 1) % S;
+    int8_t* gocc = A.occ + item.occ_offset;
+    load_word_window<B::HALO>(sq, gocc, L0, L1, L2, Q, RS, RY, sl.kb, sl.nk, threadIdx.x, NT);
+    if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+    const CeChainParams* cpg = A.cp + item.param;
+    load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+    const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+    const int* cstart = g.color_start + rank * (g.n_colors + 1);
+    TernQuadSweeper<B> sw;
+    sw.s = sq;
+    sw.s_prev = sq;
+    sw.s_next = sq;
+    if (CLUSTER) {
+      sw.s_prev = cluster.map_shared_rank(sq, (unsigned)rprev);
+      sw.s_next = cluster.map_shared_rank(sq, (unsigned)((rank + 1) % S));
+    }
+    sw.RS = RS;
+    sw.RSY = RSY;
+    sw.Q = Q;
+    sw.dJ = L1 * RS;
+    sw.dKp = sl.dkp * RSY;
+    sw.dKn = sl.dkn * RSY;
+    sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
+                                A.precision};
+    sw.tw = &TA.tw;
+    int acc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+    long long* out = A.out + item.out_offset;
+    sync_all();
+#pragma unroll 1
+    for (int pass = 0; pass < A.n_passes; ++pass) {
+      const uint32_t pass_g = (uint32_t)(item.pass0 + pass);
+#pragma unroll 1
+      for (int c = 0; c < g.n_colors; ++c) {
+#pragma unroll 1
+        for (int e = cstart[c] + threadIdx.x; e < cstart[c + 1]; e += NT)
+          sw.update(__ldg(g.entries + e), __ldg(g.site_l + e), pass_g, chain_id, key0, key1, acc);
+        sync_all();
+        if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+          int* buf = acc_sm[(pass - 1) & 1];
+          const int v = buf[threadIdx.x];
+          buf[threadIdx.x] = 0;
+          if (v)
+            atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)(pass - 1) * NSLOT + threadIdx.x),
+                      (unsigned long long)(long long)v);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q) {
+        const int v = warp_sum(acc[q]);
+        if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+        acc[q] = 0;
+      }
+    }
+    sync_all();
+    if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+      const int pl = A.n_passes - 1;
+      const int v = acc_sm[pl & 1][threadIdx.x];
+      if (v)
+        atomicAdd(reinterpret_cast<unsigned long long*>(out + (size_t)pl * NSLOT + threadIdx.x),
+                  (unsigned long long)(long long)v);
+    }
+    store_word_rows<B::HALO>(sq, gocc, L0, L1, Q, RS, RY, sl, threadIdx.x, NT);
+    sync_all();
+  }
+}
+
 // ---- global-memory evaluation (per-proposal dE and full correlation sums)
 
 struct GlobalLoader {

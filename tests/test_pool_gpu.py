@@ -126,3 +126,27 @@ def test_pool_device_series_and_check_match_host(gpu_lib):
                 st = sampling.BasicStatisticsCalculator()(ser[eq.N_samples_for_equilibration:])
                 assert res[i, 3] == st.mean and res[i, 4] == st.calculated_precision
                 assert bool(res[i, 5]) == (st.calculated_precision < prec)
+
+
+def test_pool_ternary_word_layout_matches_oracle(gpu_lib):
+    """Ternary chains whose L0 is a multiple of four take the pool's ternary word-layout
+    kernels (one CTA, and a cluster for the largest), the others the byte layout; every
+    trajectory equals the oracle's coloured sweep."""
+    model = clex.ClexModel("fcc_ternary", clex.make_eci("fcc_ternary", 8))
+    shapes = [(16, 16, 16), (32, 16, 16), (24, 12, 12), (48, 48, 48), (12, 12, 12)]
+    chains = _chains(model, shapes, seed=7)
+    pool = clex.ChainPool(model, arena_bytes=1 << 21, max_chains=8)
+    slots = [pool.add(L, occ, T, mu, seed, cid) for (L, occ, T, mu, seed, cid) in chains]
+    corr0 = [pool.corr(s) for s in slots]
+    n_passes = 4
+    out = pool.run(slots, n_passes)
+    for i, ((L, occ, T, mu, seed, cid), s) in enumerate(zip(chains, slots)):
+        col, nc = pool.colors(s)
+        orc = OracleCE(L, 3, model.eci)
+        occ_ref, corr_ref, nacc_ref = orc.colored_sweep(occ, T, mu, seed, cid, col, nc, 0, n_passes,
+                                                        model.n_classes)
+        assert np.array_equal(pool.occupation(s), occ_ref.astype(np.int8)), (i, L)
+        d = out[i, :, : model.n_classes].copy()
+        d[:, 0] = 0
+        assert np.array_equal(corr0[i][None, :] + np.cumsum(d, axis=0), corr_ref), (i, L)
+        assert np.array_equal(out[i, :, 0], nacc_ref), (i, L)
