@@ -14,6 +14,10 @@ value   device throughput of the sweep: attempts / sum over runs of the CUDA-eve
 e2e     the same job through the public C-ABI with host buffers: create the batch
         (H2D of occupations and parameters), run the passes returning per-pass samples to
         the host (D2H), read the final occupations (D2H); wall clock.
+full_config
+        the same chains as one job of the configuration's 2000 passes (--config-passes):
+        device time of one run call (long runs rotate) and the same job end to end from
+        pinned host buffers.
 batched the batched-chains workload (4096 binary FCC chains, L uniform in {8,12,16,24,32,48},
         T in [300,2000] K, mu in [-0.3,0.3] eV, 500 passes, one persistent launch per CTA
         class and layout) as converged-or-finished jobs/s, beside the same jobs one launch per
@@ -339,6 +343,60 @@ def run_serving_extra(rank: int, world: int, dist_mod, n_jobs: int = 2000, rate:
             "speedup_vs_plain": (conv / wall) / max(plain_rate, 1e-12)}
 
 
+def run_full_config_extra(rank: int, world: int, dist_mod, model, occ, T, mu, seeds, passes: int = 2000,
+                          peak: float = 6800.0) -> dict:
+    """The workload as the configuration names it: the same 8 chains of 64^3, ``passes`` passes
+    as one job.  Device time: one run call on a fresh batch (the library's own choice of
+    launches; long runs rotate the chains over two cluster sizes), L2 flushed before it.  End to
+    end: the same job from pinned host buffers (create the batch, initial correlations, the
+    passes with per-pass outputs, final occupations), median of three; max over ranks."""
+    import torch
+
+    from casmcode_monte_gb300 import clex
+
+    attempts = N_CHAINS * L**3 * passes
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    b = clex.ChainBatch(model, (L, L, L), occ, T, mu, seeds)
+    flush_l2(flush)
+    torch.cuda.synchronize()
+    b.run(passes, want_output=False)
+    torch.cuda.synchronize()
+    dev_ms = max_over_ranks(b.last_kernel_ms(), dist_mod, "cuda")
+    launches = b.last_launches()
+    b.close()
+    del flush
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype={np.dtype(np.int8): torch.int8, np.dtype(np.int64): torch.int64}[a.dtype],
+                        pin_memory=True)
+        t.numpy()[...] = a
+        return t
+
+    occ_h = pinned(occ)
+    out_h = pinned(np.zeros((passes, N_CHAINS, model.n_classes + 2), dtype=np.int64))
+    final_h = pinned(np.zeros_like(occ))
+    walls = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b = clex.ChainBatch(model, (L, L, L), occ_h.numpy(), T, mu, seeds)
+        b.corr()
+        b.run(passes, out=out_h.numpy())
+        b.occupation(out=final_h.numpy())
+        torch.cuda.synchronize()
+        walls.append((time.perf_counter() - t0) * 1e3)
+        b.close()
+    e2e_ms = max_over_ranks(statistics.median(walls), dist_mod, "cuda")
+    value = job_throughput(attempts, world, dev_ms)
+    achieved = BYTES_PER_ATTEMPT * attempts / (dev_ms * 1e-3) / 1e9
+    return {"workload": f"{WORKLOAD}, {passes} passes as one job", "passes": passes,
+            "value": value, "unit": "site-attempts/s", "ms": dev_ms, "gpu_launches": launches,
+            "roofline_frac": achieved / peak, "achieved_gbs": achieved,
+            "e2e": {"value": job_throughput(attempts, world, e2e_ms), "unit": "site-attempts/s", "ms": e2e_ms,
+                    "h2d_bytes": int(occ.nbytes + T.nbytes + mu.nbytes + seeds.nbytes),
+                    "d2h_bytes": int(out_h.numel() * 8 + occ.nbytes)}}
+
+
 def run_gpu(args) -> None:
     import torch
 
@@ -450,6 +508,8 @@ def run_gpu(args) -> None:
     rotation = batch.rotation()
     extras = {}
     if not args.no_extras:
+        extras["full_config"] = run_full_config_extra(rank, world, dist, model, occ, T, mu, seeds,
+                                                      passes=args.config_passes, peak=peak)
         extras["batched"] = run_batched_extra(rank, world, dist, n_chains=args.batched_chains)
         extras["serving"] = run_serving_extra(rank, world, dist, n_jobs=args.serving_jobs)
     if rank == 0:
@@ -717,6 +777,8 @@ def main():
     ap.add_argument("--ref-steps-per-sample", type=float, default=2e6)
     ap.add_argument("--nfold-size", type=int, default=32, help="supercell edge of the nfold workload")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and serving workloads")
+    ap.add_argument("--config-passes", type=int, default=2000,
+                    help="passes of the full-configuration job reported beside the headline")
     ap.add_argument("--batched-chains", type=int, default=4096)
     ap.add_argument("--serving-jobs", type=int, default=2000)
     ap.add_argument("--workload", default="fcc64_sgc", choices=["fcc64_sgc", "canonical", "nfold", "ising"],
