@@ -93,6 +93,8 @@ SIGNATURES = {
     "mg_ce_pool_create": (C.c_int, [vp, C.c_longlong, C.c_int, C.c_int, vpp]),
     "mg_ce_pool_add": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_double, c_double_p, C.c_uint64, C.c_uint32,
                                  c_int8_p, c_int_p]),
+    "mg_ce_pool_add_many": (C.c_int, [vp, C.c_int, c_int32_p, c_double_p, c_double_p, c_uint64_p, c_uint32_p,
+                                      c_int8_p, c_int32_p]),
     "mg_ce_pool_remove": (C.c_int, [vp, C.c_int]),
     "mg_ce_pool_prepare": (C.c_int, [vp, C.c_int, C.c_int, C.c_int]),
     "mg_ce_pool_info": (C.c_int, [vp, c_ll_p, c_ll_p, c_int_p, c_int_p]),

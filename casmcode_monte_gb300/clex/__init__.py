@@ -558,6 +558,33 @@ class ChainPool:
         self.shapes[slot.value] = (L0, L1, L2)
         return slot.value
 
+    def add_many(self, shapes, occs, temperatures, mu, seeds, chain_ids) -> list:
+        """Admit n chains in one call (all or none): ``shapes`` n triples, ``occs`` n
+        occupations, ``temperatures``/``seeds``/``chain_ids`` length n, ``mu`` [n, n_species-1].
+        Returns the slots, the ones n calls of ``add`` would give."""
+        n = len(shapes)
+        dims = np.ascontiguousarray(np.asarray(shapes, dtype=np.int32).reshape(n, 3))
+        occ = np.ascontiguousarray(np.concatenate([np.asarray(o, dtype=np.int8).reshape(-1) for o in occs])
+                                   if n else np.zeros(0, dtype=np.int8))
+        if occ.size != int(np.prod(dims.astype(np.int64), axis=1).sum()):
+            raise ValueError("occupation sizes do not match the shapes")
+        T = np.ascontiguousarray(np.asarray(temperatures, dtype=np.float64).reshape(n))
+        mu = np.ascontiguousarray(np.asarray(mu, dtype=np.float64).reshape(n, self.model.n_species - 1))
+        sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(n))
+        ids = np.ascontiguousarray(np.asarray(chain_ids, dtype=np.uint32).reshape(n))
+        slots = np.zeros(n, dtype=np.int32)
+        rc = _lib.lib().mg_ce_pool_add_many(self._h, n, _lib.ptr(dims, C.c_int32), _lib.ptr(T, C.c_double),
+                                            _lib.ptr(mu, C.c_double), _lib.ptr(sd, C.c_uint64),
+                                            _lib.ptr(ids, C.c_uint32), _lib.ptr(occ, C.c_int8),
+                                            _lib.ptr(slots, C.c_int32))
+        if rc == 5:
+            raise PoolFull(_lib.lib().mg_last_error().decode())
+        _lib.check(rc)
+        out = [int(s) for s in slots]
+        for s, d in zip(out, dims):
+            self.shapes[s] = tuple(int(x) for x in d)
+        return out
+
     def prepare(self, shape) -> None:
         """Build and cache the geometry (colouring, site lists) of a supercell shape."""
         L0, L1, L2 = (int(x) for x in shape)

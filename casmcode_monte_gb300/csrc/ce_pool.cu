@@ -429,77 +429,184 @@ int mg_ce_pool_prepare(mg_ce_pool* p, int L0, int L1, int L2) {
   return geometry(p, L0, L1, L2, *sp, &gi);
 }
 
+namespace {
+
+// the argument checks of one chain (dimensions, temperature, occupant codes)
+int check_chain(const mg_ce_pool* p, const char* fn, int L0, int L1, int L2, double temperature,
+                const int8_t* occ) {
+  if (L0 < 4 || L1 < 4 || L2 < 4) {
+    set_error(std::string("Error in ") + fn + ": supercell dimensions must be >= 4");
+    return MG_ERR_INVALID;
+  }
+  if (!(temperature > 0.0)) {
+    set_error(std::string("Error in ") + fn + ": temperature must be > 0");
+    return MG_ERR_INVALID;
+  }
+  const long long N = (long long)L0 * L1 * L2;
+  const int ns = p->model->n_species;
+  int bad = 0;
+  for (long long i = 0; i < N; ++i) bad |= (occ[i] < 0) | (occ[i] >= ns);
+  if (bad) {
+    set_error(std::string("Error in ") + fn + ": occupant index out of range");
+    return MG_ERR_INVALID;
+  }
+  return MG_OK;
+}
+
+struct Reserved {
+  int slot = -1, geom = -1;
+  long long off = 0, N = 0;
+  const ShapePlan* sp = nullptr;
+};
+
+// a free slot (searched from *hint on), arena space and the shape's geometry; the slot is
+// marked used so that the next reservation skips it; on failure nothing is held
+int reserve_chain(mg_ce_pool* p, const char* fn, int L0, int L1, int L2, int* hint, Reserved* r) {
+  const int rc0 = shape_plan(p, L0, L1, L2, &r->sp);
+  if (rc0 != MG_OK) return rc0;
+  int slot = -1;
+  for (int i = *hint; i < (int)p->slots.size(); ++i)
+    if (!p->slots[i].used) {
+      slot = i;
+      break;
+    }
+  if (slot < 0) {
+    set_error(std::string("Error in ") + fn + ": no free chain slot");
+    return MG_ERR_FULL;
+  }
+  r->N = (long long)L0 * L1 * L2;
+  if (!arena_alloc(p, r->N, &r->off)) {
+    set_error(std::string("Error in ") + fn + ": occupation does not fit in the arena");
+    return MG_ERR_FULL;
+  }
+  const int rc = geometry(p, L0, L1, L2, *r->sp, &r->geom);
+  if (rc != MG_OK) {
+    arena_free(p, r->off, r->N);
+    return rc;
+  }
+  r->slot = slot;
+  p->slots[slot].used = true;
+  *hint = slot + 1;
+  return MG_OK;
+}
+
+void release_chain(mg_ce_pool* p, const Reserved& r) {
+  arena_free(p, r.off, r.N);
+  p->slots[r.slot] = PoolSlot();
+}
+
+// the copies and series set-up of reserved chains (occupations from one host array, the
+// chains' occupations back to back), merged where both sides are contiguous, then one
+// stream synchronisation; fills the slot records
+int admit_chains(mg_ce_pool* p, const Reserved* r, const int32_t* dims, int n, const int8_t* occ,
+                 const mg::CeChainParams* cp) {
+  long long src = 0;
+  for (int i = 0; i < n;) {
+    long long len = r[i].N, s0 = src, d0 = r[i].off;
+    src += r[i].N;
+    int j = i + 1;
+    while (j < n && r[j].off == d0 + len && (r[j - 1].N & 15) == 0) {
+      len += r[j].N;
+      src += r[j].N;
+      ++j;
+    }
+    MG_CUDA_TRY(cudaMemcpyAsync(p->darena + d0, occ + s0, (size_t)len, cudaMemcpyHostToDevice, p->stream));
+    i = j;
+  }
+  for (int i = 0; i < n;) {
+    int j = i + 1;
+    while (j < n && r[j].slot == r[j - 1].slot + 1) ++j;
+    MG_CUDA_TRY(cudaMemcpyAsync(p->dcp + r[i].slot, cp + i, sizeof(mg::CeChainParams) * (j - i),
+                                cudaMemcpyHostToDevice, p->stream));
+    i = j;
+  }
+  if (p->max_samples > 0) {
+    // each series starts from the integer correlation sums of the initial occupation
+    const int nc = p->model->n_classes;
+    for (int i = 0; i < n; ++i) {
+      long long* st = p->dstate + (size_t)r[i].slot * nc;
+      MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(long long) * nc, p->stream));
+      MG_CUDA_TRY(cudaMemsetAsync(p->dnsamp + r[i].slot, 0, sizeof(int), p->stream));
+      MG_CUDA_TRY(mg::host::launch_corr(p->model->kind, p->darena + r[i].off, dims[3 * i], dims[3 * i + 1],
+                                        dims[3 * i + 2], 1, st, p->stream));
+    }
+  }
+  MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  for (int i = 0; i < n; ++i) {
+    PoolSlot& s = p->slots[r[i].slot];
+    s.used = true;
+    s.L0 = dims[3 * i];
+    s.L1 = dims[3 * i + 1];
+    s.L2 = dims[3 * i + 2];
+    s.cls = r[i].sp->cls;
+    s.layout = r[i].sp->layout;
+    s.N = r[i].N;
+    s.offset = r[i].off;
+    s.pass = 0;
+    s.geom = r[i].geom;
+  }
+  return MG_OK;
+}
+
+}  // namespace
+
 int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, const double* mu,
                    uint64_t seed, uint32_t chain_id, const int8_t* occ, int* slot_out) {
   if (!p || !occ || !slot_out || (p->model->n_species > 1 && !mu)) {
     set_error("Error in mg_ce_pool_add: invalid argument");
     return MG_ERR_INVALID;
   }
-  if (L0 < 4 || L1 < 4 || L2 < 4) {
-    set_error("Error in mg_ce_pool_add: supercell dimensions must be >= 4");
-    return MG_ERR_INVALID;
-  }
-  if (!(temperature > 0.0)) {
-    set_error("Error in mg_ce_pool_add: temperature must be > 0");
-    return MG_ERR_INVALID;
-  }
-  const long long N = (long long)L0 * L1 * L2;
-  for (long long i = 0; i < N; ++i)
-    if (occ[i] < 0 || occ[i] >= p->model->n_species) {
-      set_error("Error in mg_ce_pool_add: occupant index out of range");
-      return MG_ERR_INVALID;
-    }
-  const ShapePlan* sp = nullptr;
-  {
-    const int rc0 = shape_plan(p, L0, L1, L2, &sp);
-    if (rc0 != MG_OK) return rc0;
-  }
-  int slot = -1;
-  for (int i = 0; i < (int)p->slots.size(); ++i)
-    if (!p->slots[i].used) {
-      slot = i;
-      break;
-    }
-  if (slot < 0) {
-    set_error("Error in mg_ce_pool_add: no free chain slot");
-    return MG_ERR_FULL;
-  }
-  long long off = 0;
-  if (!arena_alloc(p, N, &off)) {
-    set_error("Error in mg_ce_pool_add: occupation does not fit in the arena");
-    return MG_ERR_FULL;
-  }
-  int gi = -1;
-  int rc = geometry(p, L0, L1, L2, *sp, &gi);
-  if (rc != MG_OK) {
-    arena_free(p, off, N);
-    return rc;
-  }
+  const char* fn = "mg_ce_pool_add";
+  int rc = check_chain(p, fn, L0, L1, L2, temperature, occ);
+  if (rc != MG_OK) return rc;
+  Reserved r;
+  int hint = 0;
+  rc = reserve_chain(p, fn, L0, L1, L2, &hint, &r);
+  if (rc != MG_OK) return rc;
   mg::CeChainParams cp;
   make_chain_params(p->model, 1, &temperature, mu, &seed, &chain_id, &cp);
-  MG_CUDA_TRY(cudaMemcpyAsync(p->darena + off, occ, N, cudaMemcpyHostToDevice, p->stream));
-  MG_CUDA_TRY(cudaMemcpyAsync(p->dcp + slot, &cp, sizeof(cp), cudaMemcpyHostToDevice, p->stream));
-  if (p->max_samples > 0) {
-    // the series starts from the integer correlation sums of the initial occupation
-    const int nc = p->model->n_classes;
-    long long* st = p->dstate + (size_t)slot * nc;
-    MG_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(long long) * nc, p->stream));
-    MG_CUDA_TRY(cudaMemsetAsync(p->dnsamp + slot, 0, sizeof(int), p->stream));
-    MG_CUDA_TRY(mg::host::launch_corr(p->model->kind, p->darena + off, L0, L1, L2, 1, st, p->stream));
+  const int32_t dims[3] = {L0, L1, L2};
+  rc = admit_chains(p, &r, dims, 1, occ, &cp);
+  if (rc != MG_OK) {
+    release_chain(p, r);
+    return rc;
   }
-  MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
-  PoolSlot& s = p->slots[slot];
-  s.used = true;
-  s.L0 = L0;
-  s.L1 = L1;
-  s.L2 = L2;
-  s.cls = sp->cls;
-  s.layout = sp->layout;
-  s.N = N;
-  s.offset = off;
-  s.pass = 0;
-  s.geom = gi;
-  *slot_out = slot;
+  *slot_out = r.slot;
+  return MG_OK;
+}
+
+int mg_ce_pool_add_many(mg_ce_pool* p, int n, const int32_t* dims, const double* temperature, const double* mu,
+                        const uint64_t* seeds, const uint32_t* chain_ids, const int8_t* occ, int32_t* slots_out) {
+  if (!p || n < 0 || (n > 0 && (!dims || !temperature || !seeds || !chain_ids || !occ || !slots_out ||
+                                (p->model->n_species > 1 && !mu)))) {
+    set_error("Error in mg_ce_pool_add_many: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  if (n == 0) return MG_OK;
+  const char* fn = "mg_ce_pool_add_many";
+  long long off = 0;
+  for (int i = 0; i < n; ++i) {
+    const int rc = check_chain(p, fn, dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], temperature[i], occ + off);
+    if (rc != MG_OK) return rc;
+    off += (long long)dims[3 * i] * dims[3 * i + 1] * dims[3 * i + 2];
+  }
+  std::vector<Reserved> r((size_t)n);
+  int hint = 0;
+  for (int i = 0; i < n; ++i) {
+    const int rc = reserve_chain(p, fn, dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], &hint, &r[i]);
+    if (rc != MG_OK) {
+      for (int k = 0; k < i; ++k) release_chain(p, r[k]);
+      return rc;
+    }
+  }
+  std::vector<mg::CeChainParams> cp((size_t)n);
+  make_chain_params(p->model, n, temperature, mu, seeds, chain_ids, cp.data());
+  const int rc = admit_chains(p, r.data(), dims, n, occ, cp.data());
+  if (rc != MG_OK) {
+    for (int k = 0; k < n; ++k) release_chain(p, r[k]);
+    return rc;
+  }
+  for (int i = 0; i < n; ++i) slots_out[i] = r[i].slot;
   return MG_OK;
 }
 

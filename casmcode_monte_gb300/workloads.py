@@ -55,7 +55,8 @@ def run_batched(n_chains: int = 4096, n_passes: int = 500, plain_sample: int = 6
     total_sites = sum(j["L"] ** 3 for j in jobs)
     pool = clex.ChainPool(model, arena_bytes=total_sites + 16 * n_chains, max_chains=n_chains, precision=precision)
     t0 = time.perf_counter()
-    slots = [pool.add((j["L"],) * 3, j["occ"], j["T"], j["mu"], j["seed"], j["id"]) for j in jobs]
+    slots = pool.add_many([(j["L"],) * 3 for j in jobs], [j["occ"] for j in jobs], [j["T"] for j in jobs],
+                          np.stack([j["mu"] for j in jobs]), [j["seed"] for j in jobs], [j["id"] for j in jobs])
     t_admit = time.perf_counter() - t0
     torch.cuda.synchronize()
     t1 = time.perf_counter()

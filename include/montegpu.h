@@ -243,6 +243,15 @@ int mg_ce_pool_create(const mg_ce_model* m, long long arena_bytes, int max_chain
                       mg_ce_pool** out);
 int mg_ce_pool_add(mg_ce_pool* p, int L0, int L1, int L2, double temperature, const double* mu,
                    uint64_t seed, uint32_t chain_id, const int8_t* occ, int* slot);
+/* admission of n chains in one call: dims [n][3], temperature [n], mu [n][n_species-1],
+ * seeds [n], chain_ids [n], occ the n occupations back to back; slots [n] out.  Every
+ * chain is checked first, then all are admitted or none (MG_ERR_FULL / MG_ERR_INVALID
+ * leave the pool as it was); the same chains one mg_ce_pool_add each give the same slots
+ * and trajectories.  The host-to-device copies are merged where the chains' arena spaces
+ * are contiguous, with one stream synchronisation for the call. */
+int mg_ce_pool_add_many(mg_ce_pool* p, int n, const int32_t* dims, const double* temperature,
+                        const double* mu, const uint64_t* seeds, const uint32_t* chain_ids,
+                        const int8_t* occ, int32_t* slots);
 int mg_ce_pool_remove(mg_ce_pool* p, int slot);
 /* build (and cache) the colouring and site lists of a supercell shape ahead of its first
  * chain; a geometry depends only on the shape, so servers prepare the shapes they expect */

@@ -150,3 +150,57 @@ def test_pool_ternary_word_layout_matches_oracle(gpu_lib):
         d[:, 0] = 0
         assert np.array_equal(corr0[i][None, :] + np.cumsum(d, axis=0), corr_ref), (i, L)
         assert np.array_equal(out[i, :, 0], nacc_ref), (i, L)
+
+
+@pytest.mark.parametrize("kind", ["fcc_binary", "fcc_ternary"])
+def test_pool_add_many_equals_single_adds(gpu_lib, kind):
+    """Bulk admission gives the slots, trajectories, outputs and device series of one add per
+    chain, with a freed slot and a non-multiple-of-16 arena gap in the way."""
+    model = clex.ClexModel(kind, clex.make_eci(kind, 6))
+    shapes = [(8, 8, 8), (5, 7, 9), (16, 8, 12), (12, 12, 12), (8, 8, 8), (16, 16, 16)]
+    chains = _chains(model, shapes, seed=11)
+    filler = np.zeros(6 * 9 * 7, dtype=np.int8)
+    pools, slots, outs = [], [], []
+    for bulk in (False, True):
+        pool = clex.ChainPool(model, arena_bytes=1 << 20, max_chains=12)
+        pool.enable_series(8)
+        f = [pool.add((6, 9, 7), filler, 900.0, np.zeros(model.n_species - 1), 9, 90 + k) for k in range(3)]
+        pool.remove(f[1])
+        if bulk:
+            s = pool.add_many([c[0] for c in chains], [c[1] for c in chains], [c[2] for c in chains],
+                              np.stack([c[3] for c in chains]), [c[4] for c in chains], [c[5] for c in chains])
+        else:
+            s = [pool.add(*c) for c in chains]
+        pools.append(pool)
+        slots.append(s)
+        outs.append(pool.run(s, 4))
+    assert slots[0] == slots[1] and slots[0][0] == 1
+    assert np.array_equal(outs[0], outs[1])
+    for x in slots[0]:
+        assert np.array_equal(pools[0].occupation(x), pools[1].occupation(x))
+        assert np.array_equal(pools[0].series(x), pools[1].series(x))
+    assert pools[0].info() == pools[1].info()
+    for p in pools:
+        p.close()
+
+
+def test_pool_add_many_all_or_none(gpu_lib):
+    model = clex.ClexModel("fcc_binary", clex.make_eci("fcc_binary", 2))
+    pool = clex.ChainPool(model, arena_bytes=3 * 4096, max_chains=8)
+    occ = np.zeros(16 * 16 * 16, dtype=np.int8)
+    before = pool.info()
+    # the fourth chain does not fit: nothing is admitted
+    with pytest.raises(clex.PoolFull):
+        pool.add_many([(16, 16, 16)] * 4, [occ] * 4, [1000.0] * 4, np.zeros((4, 1)), [1, 2, 3, 4], [0, 1, 2, 3])
+    assert pool.info() == before
+    # an occupant code out of range in the last chain: nothing is admitted
+    bad = occ.copy()
+    bad[7] = 2
+    with pytest.raises(RuntimeError, match="occupant index out of range"):
+        pool.add_many([(16, 16, 16)] * 2, [occ, bad], [1000.0] * 2, np.zeros((2, 1)), [1, 2], [0, 1])
+    assert pool.info() == before
+    s = pool.add_many([(16, 16, 16)] * 3, [occ] * 3, [1000.0] * 3, np.zeros((3, 1)), [1, 2, 3], [0, 1, 2])
+    assert s == [0, 1, 2] and pool.info()["arena_free_bytes"] == 0
+    assert pool.add_many([], [], [], np.zeros((0, 1)), [], []) == []
+    pool.run(s, 2)
+    pool.close()
