@@ -274,7 +274,7 @@ def run_batched_extra(rank: int, world: int, dist_mod, n_chains: int = 4096, n_p
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     kernel_ms = pool.last_kernel_ms()
-    launches = pool.last_launches() if hasattr(pool, "last_launches") else None
+    launches = pool.last_launches()
     pool.close()
     rng = np.random.default_rng(1)
     sample = [mine[int(i)] for i in rng.choice(len(mine), size=min(plain_sample, len(mine)), replace=False)]

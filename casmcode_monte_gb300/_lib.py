@@ -100,6 +100,7 @@ SIGNATURES = {
     "mg_ce_pool_info": (C.c_int, [vp, c_ll_p, c_ll_p, c_int_p, c_int_p]),
     "mg_ce_pool_run": (C.c_int, [vp, c_int32_p, C.c_int, C.c_int, c_ll_p]),
     "mg_ce_pool_last_kernel_ms": (C.c_int, [vp, c_float_p]),
+    "mg_ce_pool_last_launches": (C.c_int, [vp, c_int_p]),
     "mg_ce_pool_get_occ": (C.c_int, [vp, C.c_int, c_int8_p]),
     "mg_ce_pool_colors": (C.c_int, [vp, C.c_int, c_int32_p]),
     "mg_ce_pool_corr": (C.c_int, [vp, C.c_int, c_ll_p]),

@@ -614,6 +614,13 @@ class ChainPool:
         _lib.check(_lib.lib().mg_ce_pool_last_kernel_ms(self._h, C.byref(ms)))
         return float(ms.value)
 
+    def last_launches(self) -> int:
+        """Kernels the last run launched (one per CTA class and layout with chains, plus the
+        series kernel when series are on)."""
+        n = C.c_int()
+        _lib.check(_lib.lib().mg_ce_pool_last_launches(self._h, C.byref(n)))
+        return int(n.value)
+
     def occupation(self, slot: int) -> np.ndarray:
         n = int(np.prod(self.shapes[slot]))
         occ = np.zeros(n, dtype=np.int8)

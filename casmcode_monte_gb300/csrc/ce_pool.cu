@@ -72,6 +72,7 @@ struct mg_ce_pool {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t cls_done[kGroups] = {};
   float last_ms = 0.f;
+  int last_launches = 0;  // kernels launched by the last run
   // device-resident sample series (potential energy per site after every pass)
   int max_samples = 0;
   long long* dstate = nullptr;  // [slot][n_classes] integer correlation sums
@@ -690,11 +691,13 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
   MG_CUDA_TRY(cudaMemsetAsync(p->dcounter, 0, sizeof(int) * kGroups, p->stream));
   MG_CUDA_TRY(cudaMemsetAsync(p->dout, 0, sizeof(long long) * need, p->stream));
   MG_CUDA_TRY(cudaEventRecord(p->ev0, p->stream));
+  p->last_launches = 0;
   // one launch per CTA class, each on its own stream after the set-up copies; the
   // largest class first so that its long chains start while the others fill in
   for (int c = kGroups - 1; c >= 0; --c) {
     const int cnt = first[c + 1] - first[c];
     if (cnt <= 0) continue;
+    ++p->last_launches;
     MG_CUDA_TRY(cudaStreamWaitEvent(p->cls_stream[c], p->ev0, 0));
     const int cls = c / 2, layout = c % 2;
     int rc = p->model->kind == 0
@@ -720,6 +723,7 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
           p->ditems, n, p->dgeoms, p->dcp, p->dout, n_passes, p->dstate, p->dseries, p->dnsamp, p->max_samples, wc);
     }
     MG_CUDA_TRY(cudaGetLastError());
+    ++p->last_launches;
   }
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, p->dout, sizeof(long long) * need, cudaMemcpyDeviceToHost, p->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(p->stream));
@@ -804,6 +808,15 @@ int mg_ce_pool_last_kernel_ms(const mg_ce_pool* p, float* ms) {
     return MG_ERR_INVALID;
   }
   *ms = p->last_ms;
+  return MG_OK;
+}
+
+int mg_ce_pool_last_launches(const mg_ce_pool* p, int* n) {
+  if (!p || !n) {
+    set_error("Error in mg_ce_pool_last_launches: invalid argument");
+    return MG_ERR_INVALID;
+  }
+  *n = p->last_launches;
   return MG_OK;
 }
 

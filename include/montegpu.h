@@ -110,8 +110,9 @@ int mg_ce_batch_info(const mg_ce_batch* b, int* ctas_per_chain, int* n_colors, i
                      size_t* smem_bytes);
 int mg_ce_batch_colors(const mg_ce_batch* b, int32_t* color /* [N] */);
 /* Shared-memory layout of the sweep: 0 = one site per byte (any basis and shape);
- * 1 = four sites per 32-bit word (binary basis, L0 = 4Q with Q >= 4, colour(i+Q) =
- * colour(i)); 2 = layout 1 with the feature sums split around the phase barrier (the
+ * 1 = four sites per 32-bit word (either basis, L0 = 4Q with Q >= 4, colour(i+Q) =
+ * colour(i); the ternary basis sums its energies from byte-parallel monomial counts);
+ * 2 = layout 1 with the feature sums split around the phase barrier (binary basis; the
  * colourings generated for it: L0 a multiple of 16, L1/L2 multiples of 16/8); 3 = layout 2
  * with warp-specialised CTAs (one role prepares the next colour while the other decides the
  * current one; at most 384 words per CTA and colour).  The best one that applies is
@@ -260,6 +261,9 @@ int mg_ce_pool_info(const mg_ce_pool* p, long long* arena_free_bytes, long long*
                     int* n_used, int* max_chains);
 int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, long long* out);
 int mg_ce_pool_last_kernel_ms(const mg_ce_pool* p, float* ms);
+/* kernels the last mg_ce_pool_run launched (one per CTA class and layout with chains, plus
+ * the series kernel when series are on) */
+int mg_ce_pool_last_launches(const mg_ce_pool* p, int* n);
 int mg_ce_pool_get_occ(mg_ce_pool* p, int slot, int8_t* occ);
 /* colouring of the slot's supercell [N]; returns the number of colours (>0) or an error */
 int mg_ce_pool_colors(const mg_ce_pool* p, int slot, int32_t* color);

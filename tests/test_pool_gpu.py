@@ -174,6 +174,7 @@ def test_pool_add_many_equals_single_adds(gpu_lib, kind):
         pools.append(pool)
         slots.append(s)
         outs.append(pool.run(s, 4))
+        assert pool.last_launches() >= 2  # at least one sweep kernel and the series kernel
     assert slots[0] == slots[1] and slots[0][0] == 1
     assert np.array_equal(outs[0], outs[1])
     for x in slots[0]:
