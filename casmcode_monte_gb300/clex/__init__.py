@@ -94,7 +94,7 @@ class ClexModel:
         return np.stack([nB, nC], axis=-1).astype(np.float64)
 
 
-LAYOUTS = {0: "byte", 1: "word", 2: "word_pipelined", 3: "word_specialised"}
+LAYOUTS = {0: "byte", 1: "word", 2: "word_pipelined", 3: "word_specialised", 4: "grid"}
 
 
 def color_supercell(kind: str, shape) -> tuple[np.ndarray, int, str]:
@@ -164,7 +164,9 @@ class ChainBatch:
         features for the binary basis, byte-parallel monomial counts for the ternary one),
         and, binary basis only, four sites per word with the features split around the phase
         barrier ("word_pipelined") or the same with warp-specialised CTAs
-        ("word_specialised"); trajectories are identical."""
+        ("word_specialised"); ternary basis only, the word layout swept by CTAs on every SM
+        ("grid": each chain's lattice in global memory, a grid barrier between colours);
+        trajectories are identical."""
         codes = {v: k for k, v in LAYOUTS.items()}
         if layout not in codes:
             raise ValueError(f"layout must be one of {sorted(codes)}")

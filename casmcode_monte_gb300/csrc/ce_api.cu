@@ -52,7 +52,8 @@ struct mg_ce_batch {
   int L0 = 0, L1 = 0, L2 = 0, n_chains = 0, precision = 0;
   long long N = 0;
   int S = 1, PX = 0, PY = 0, PZ = 0, n_colors = 0, threads = 0;
-  int layout = 0;  // 0: one site per byte; 1: four sites per word (binary); 2: 1 pipelined; 3: 2 warp-specialised
+  int layout = 0;  // 0: one site per byte; 1: four sites per word; 2: 1 pipelined; 3: 2 warp-specialised;
+                   // 4: word layout swept by the whole grid (ternary)
   int pipe = -1;           // pipeline colouring id of the colouring, or -1
   int ctas_requested = 0;  // 0: chosen by occupancy
   size_t smem = 0;
@@ -94,6 +95,12 @@ struct mg_ce_batch {
                                           // stream is the slow lane); created by the first
                                           // rotated run
   std::vector<cudaEvent_t> rev;            // six per chain (launch_rotated) and a join
+  // grid sweep (layout 4, ternary basis): one allocation holding the barrier words
+  // (count[n_chains], gen[n_chains], status, abort) and the chains' windows
+  unsigned char* dgrid = nullptr;
+  size_t dgrid_bytes = 0, dgrid_bar_bytes = 0;
+  mg::GridBarrier gb{};
+  uint32_t* dwin = nullptr;
 };
 
 // per-pass output rows kept in a batch's own allocation
@@ -289,6 +296,7 @@ void free_batch(mg_ce_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
   cudaFree(b->dblock);
+  cudaFree(b->dgrid);
   if (b->dout_own) cudaFree(b->dout);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
@@ -557,10 +565,66 @@ void update_ratio(mg_ce_batch* b, const RotationPlan& p) {
   }
 }
 
+// Grid sweep (layout 4): the one-slab word lists, G CTAs per chain (requested, else the
+// resident CTAs shared evenly between the chains: one cooperative launch holds them all),
+// the chains' windows and the barrier words.
+int setup_grid(mg_ce_batch* b) {
+  const mg_ce_model* m = b->model;
+  if (m->kind != 1 || !b->col->word) {
+    set_error("Error in mg_ce_batch_set_layout: the grid sweep needs the ternary basis and the word layout");
+    return MG_ERR_INVALID;
+  }
+  int total = 0;
+  int rc = mg::host::tgrid_resident_ctas(&total);
+  if (rc != MG_OK) return rc;
+  const int G = b->ctas_requested > 0 ? b->ctas_requested : total / b->n_chains;
+  if (G < 1 || (long long)G * b->n_chains > total) {
+    set_error("Error in mg_ce_batch_set_layout: the grid sweep needs all n_chains x ctas_per_chain CTAs resident "
+              "at once (" + std::to_string(total) + " on this device)");
+    return MG_ERR_INVALID;
+  }
+  const long long ww = mg::host::tgrid_window_words(b->L0, b->L1, b->L2);
+  if (ww >= (1LL << 24)) {
+    set_error("Error in mg_ce_batch_set_layout: supercell too large for 24-bit window offsets");
+    return MG_ERR_INVALID;
+  }
+  std::shared_ptr<const DeviceLists> dl;
+  rc = device_lists(m->kind, b->L0, b->L1, b->L2, 1, 1, *b->col, b->stream, &dl);
+  if (rc != MG_OK) return rc;
+  const size_t bar = ((sizeof(unsigned) * 2 * b->n_chains + 2 * sizeof(int)) + 255) & ~(size_t)255;
+  const size_t need = bar + sizeof(uint32_t) * (size_t)ww * b->n_chains;
+  if (b->dgrid_bytes < need) {
+    MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    cudaFree(b->dgrid);
+    b->dgrid = nullptr;
+    b->dgrid_bytes = 0;
+    MG_CUDA_TRY(cudaMalloc(&b->dgrid, need));
+    b->dgrid_bytes = need;
+  }
+  b->dgrid_bar_bytes = bar;
+  b->gb.count = reinterpret_cast<unsigned*>(b->dgrid);
+  b->gb.gen = b->gb.count + b->n_chains;
+  b->gb.status = reinterpret_cast<int*>(b->gb.gen + b->n_chains);
+  b->gb.abort = b->gb.status + 1;
+  b->dwin = reinterpret_cast<uint32_t*>(b->dgrid + bar);
+  b->lists = dl;
+  b->dcstart = dl->cstart;
+  b->dentries = dl->entries;
+  b->dsite = dl->site;
+  b->layout = 4;
+  b->S = G;
+  b->smem = 0;
+  b->PZ = b->L2 + 2 * mg::CE_HALO;
+  b->threads = mg::host::NT_TQUAD;
+  b->max_words = 0;
+  return setup_rotation(b);
+}
+
 // CTA count, shared-memory size and site (or word) lists of the batch's layout, uploaded
 // to the device (replacing earlier lists).
 int setup_layout(mg_ce_batch* b, int layout) {
   const mg_ce_model* m = b->model;
+  if (layout == 4) return setup_grid(b);
   int S = 0;
   int rc = choose_ctas(m->kind, b->L0, b->L1, b->L2, b->n_chains, b->ctas_requested, &S, layout);
   if (rc != MG_OK) return rc;
@@ -694,7 +758,10 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
     delete b;
     return MG_ERR_INVALID;
   }
-  const int layout = !b->col->word ? 0 : ((m->kind == 0 && b->pipe >= 0) ? 3 : 1);
+  // (ternary word layout with more CTAs per chain requested than a cluster holds: the grid sweep)
+  const int layout = !b->col->word ? 0
+                     : (m->kind == 1 && ctas_per_chain > 16) ? 4
+                                                             : ((m->kind == 0 && b->pipe >= 0) ? 3 : 1);
   b->hcp.resize(n_chains);
   make_chain_params(m, n_chains, temperature, mu, seeds, chain_ids, b->hcp.data());
 
@@ -729,10 +796,13 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   // the best layout that applies; a layout can still be refused for this CTA count (shared
   // memory, staged words), then the next one is tried
   int rc = MG_ERR_INVALID;
-  for (int lay = layout; lay >= 0 && rc == MG_ERR_INVALID; --lay) {
-    if (lay == 1 && layout >= 2) continue;  // a pipeline colouring: layout 2 is always at least as fast
-    rc = setup_layout(b, lay);
-  }
+  if (layout == 4)
+    rc = setup_layout(b, 4);
+  else
+    for (int lay = layout; lay >= 0 && rc == MG_ERR_INVALID; --lay) {
+      if (lay == 1 && layout >= 2) continue;  // a pipeline colouring: layout 2 is always at least as fast
+      rc = setup_layout(b, lay);
+    }
   if (rc != MG_OK) {
     free_batch(b);
     return rc;
@@ -782,10 +852,11 @@ int mg_ce_batch_layout(const mg_ce_batch* b, int* layout) {
 }
 
 int mg_ce_batch_set_layout(mg_ce_batch* b, int layout) {
-  if (!b || layout < 0 || layout > 3) {
+  if (!b || layout < 0 || layout > 4) {
     set_error("Error in mg_ce_batch_set_layout: invalid argument");
     return MG_ERR_INVALID;
   }
+  if (layout == 4) return layout == b->layout ? MG_OK : setup_layout(b, 4);
   if (layout >= 1 && !b->col->word) {
     set_error("Error in mg_ce_batch_set_layout: the word layout needs the binary basis, L0 = 4Q with Q >= 4 "
               "and a colouring with colour(i + Q) = colour(i)");
@@ -860,6 +931,30 @@ int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout_out, int*
       }
     }
   }
+  // ternary: the grid sweep with the resident CTAs shared between the chains
+  bool best_grid = false;
+  if (rc == MG_OK && word && m->kind == 1) {
+    b->ctas_requested = 0;
+    if (setup_layout(b, 4) == MG_OK) {
+      rc = mg_ce_batch_run(b, probe_passes, nullptr);
+      if (rc == MG_OK) rc = mg_ce_batch_run(b, probe_passes, nullptr);
+      if (rc == MG_OK) {
+        const float ms = b->last_ms;
+        b->pass = pass_keep;
+        e = cudaMemcpyAsync(b->docc, saved, occ_bytes, cudaMemcpyDeviceToDevice, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e != cudaSuccess) {
+          rc = MG_ERR_CUDA;
+          set_error(std::string("CUDA error in mg_ce_batch_autotune: ") + cudaGetErrorString(e));
+        } else if (ms < best) {
+          best = ms;
+          best_layout = 4;
+          best_S = b->S;
+          best_grid = true;
+        }
+      }
+    }
+  }
   // the occupancy choice of the warp-specialised layout with rotation over two cluster sizes,
   // timed per pass on runs long enough to rotate (at least 4 n_chains passes)
   bool best_rot = false;
@@ -887,7 +982,7 @@ int mg_ce_batch_autotune(mg_ce_batch* b, int probe_passes, int* layout_out, int*
     }
   }
   cudaFree(saved);
-  b->ctas_requested = best_rot ? 0 : best_S;
+  b->ctas_requested = (best_rot || best_grid) ? 0 : best_S;
   const int rc2 = setup_layout(b, best_layout);
   if (rc != MG_OK) return rc;
   if (rc2 != MG_OK) return rc2;
@@ -936,6 +1031,8 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   }
   else if (b->layout == 3)
     rc = launch_sweep_ws(b->model, L, b->pipe);
+  else if (b->layout == 4)
+    rc = launch_sweep_tgrid(b->model, L, b->S, b->dwin, b->gb, b->dgrid, b->dgrid_bar_bytes);
   else if (b->layout >= 1 && b->model->kind == 1)
     rc = launch_sweep_tquad(b->model, L);
   else if (b->layout >= 1)
@@ -947,6 +1044,15 @@ int mg_ce_batch_run(mg_ce_batch* b, int n_passes, long long* out) {
   if (out) MG_CUDA_TRY(cudaMemcpyAsync(out, b->dout, sizeof(long long) * need, cudaMemcpyDeviceToHost, b->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
   MG_CUDA_TRY(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+  if (b->layout == 4) {
+    int status = 0;
+    MG_CUDA_TRY(cudaMemcpy(&status, b->gb.status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status != 0) {
+      set_error("Error in mg_ce_batch_run: a grid barrier wait of the sweep ran out; the passes were abandoned "
+                "and the occupations left as they were");
+      return MG_ERR_DEVICE;
+    }
+  }
   b->last_launches = 1;
   if (rotated) {
     b->last_launches = b->n_chains;

@@ -843,6 +843,68 @@ inline int launch_sweep_tquad(const mg_ce_model* m, const SweepLaunch& L) {
   return MG_OK;
 }
 
+// Words of one chain's window in the grid sweep: the one-slab (S = 1) word window
+inline long long tgrid_window_words(int L0, int L1, int L2) {
+  return (long long)quad_row_stride(L0 / 4) * (L1 + 2 * CE_HALO) * (L2 + 2 * CE_HALO);
+}
+
+// CTAs of the grid sweep that can be resident at once on this device (one cooperative
+// launch holds n_chains * G of them)
+inline int tgrid_resident_ctas(int* out) {
+  int dev = 0, sms = 0, per_sm = 0;
+  MG_CUDA_TRY(cudaGetDevice(&dev));
+  MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ce_sweep_tgrid_kernel<FccTernary, NT_TQUAD>,
+                                                            NT_TQUAD, 0));
+  *out = sms * per_sm;
+  return MG_OK;
+}
+
+// Grid sweep of ternary chains (G CTAs per chain, cooperative launch; lists of the S = 1
+// word layout in L.cstart/entries/site; win: n_chains windows of tgrid_window_words words;
+// gb: barrier words, zeroed here before the launch)
+inline int launch_sweep_tgrid(const mg_ce_model* m, const SweepLaunch& L, int G, uint32_t* win,
+                              const GridBarrier& gb, void* gb_block, size_t gb_bytes) {
+  using B = FccTernary;
+  CeTGridArgs<B::NFEAT, B::NCOUNT> GA;
+  CeQuadArgs<B::NFEAT>& A = GA.t.q;
+  A.g.L0 = L.L0;
+  A.g.L1 = L.L1;
+  A.g.L2 = L.L2;
+  A.g.Q = L.L0 / 4;
+  A.g.S = 1;
+  A.g.planes = word_slab_kind(L.L1, L.L2, 1);
+  A.g.window_planes = row_window_planes(L.L1, L.L2, 1, B::HALO, A.g.planes);
+  A.g.max_rows = row_slab_max_rows(L.L1, L.L2, 1, A.g.planes);
+  A.g.RS = quad_row_stride(L.L0 / 4);
+  A.g.RY = L.L1 + 2 * CE_HALO;
+  A.g.n_colors = L.n_colors;
+  A.g.color_start = L.cstart;
+  A.g.entries = L.entries;
+  A.g.site_l = L.site;
+  fill_weights(m, A.w);
+  fill_tquad_weights(m, GA.t.tw);
+  A.cp = L.cp;
+  A.occ = L.occ;
+  A.pass0 = L.pass0;
+  A.n_passes = L.n_passes;
+  A.n_chains = L.n_chains;
+  A.precision = L.precision;
+  A.out = L.out;
+  A.n_map = 0;
+  GA.win = win;
+  GA.win_words = tgrid_window_words(L.L0, L.L1, L.L2);
+  GA.G = G;
+  GA.gb = gb;
+  MG_CUDA_TRY(cudaMemsetAsync(gb_block, 0, gb_bytes, L.stream));
+  void* args[] = {&GA};
+  MG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)ce_sweep_tgrid_kernel<B, NT_TQUAD>,
+                                          dim3((unsigned)(L.n_chains * G), 1, 1), dim3(NT_TQUAD, 1, 1), args, 0,
+                                          L.stream));
+  MG_CUDA_TRY(cudaGetLastError());
+  return MG_OK;
+}
+
 // warp-specialised kernel (pipeline colouring `pipe`, at most NW_WS words per CTA and colour)
 inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe) {
   using B = FccBinary;

@@ -715,13 +715,20 @@ struct CeQuadArgs {
   int map_pass[CE_MAX_MAP];
 };
 
-struct WordLoader {
+// neighbour words of a word at p (window strides RS, RSY); CG: the window is in global
+// memory, written by other SMs between phases, so loads bypass L1 (ld.global.cg)
+template <bool CG>
+struct WordLoaderT {
   const uint32_t* p;
   int RS, RSY;
   __device__ __forceinline__ uint32_t operator()(int di, int dj, int dk) const {
-    return p[di + dj * RS + dk * RSY];
+    if constexpr (CG)
+      return __ldcg(p + di + dj * RS + dk * RSY);
+    else
+      return p[di + dj * RS + dk * RSY];
   }
 };
+using WordLoader = WordLoaderT<false>;
 
 // F[k] of one byte lane, as an int (FP64 re-decisions)
 template <int NF>
@@ -895,7 +902,10 @@ __device__ __noinline__ int tern_exact(const MetropolisRule<B>& rule, int o, int
   return (a ? 1 : 0) | (cnt[B::NCLASS + 1] ? 2 : 0);
 }
 
-template <class B>
+// GMEM: the window is one chain's lattice in global memory shared by the CTAs of a grid
+// sweep (ce_sweep_tgrid_kernel): its words are read with ld.global.cg and written with
+// st.global.cg, so no SM keeps a stale copy in L1 across the grid barriers
+template <class B, bool GMEM = false>
 struct TernQuadSweeper {
   static constexpr int NF = B::NFEAT;
   static constexpr int NC = B::NCLASS;
@@ -910,8 +920,8 @@ struct TernQuadSweeper {
   MetropolisRule<B> rule;
   const TernQuadWeights<NJ>* tw;
 
-  __device__ __forceinline__ WordLoader loader(uint32_t ent) const {
-    return WordLoader{s + (int)(ent & 0xFFFFFFu), RS, RSY};
+  __device__ __forceinline__ WordLoaderT<GMEM> loader(uint32_t ent) const {
+    return WordLoaderT<GMEM>{s + (int)(ent & 0xFFFFFFu), RS, RSY};
   }
 
   // one word: counts, the four sites' decisions (Philox block per site), write-back of the
@@ -919,7 +929,11 @@ struct TernQuadSweeper {
   __device__ __forceinline__ void update(uint32_t ent, uint32_t site0, uint32_t pass, uint32_t chain_id,
                                          uint32_t key0, uint32_t key1, int (&acc)[NSLOT]) const {
     const int pw = (int)(ent & 0xFFFFFFu);
-    const uint32_t v = s[pw];
+    uint32_t v;
+    if constexpr (GMEM)
+      v = __ldcg(s + pw);
+    else
+      v = s[pw];
     uint32_t M[NJ];
     B::counts_quad(loader(ent), M);
     uint32_t nv = v, sg0 = 0u, sg1 = 0u;
@@ -968,11 +982,17 @@ struct TernQuadSweeper {
         vi = __funnelshift_l(nv, nv, 8);
       }
       const int oj = (flags & 4u) ? dJ : ((flags & 8u) ? -dJ : 0);
+      auto st = [&](uint32_t* r, uint32_t x) {
+        if constexpr (GMEM)
+          __stcg(r, x);
+        else
+          *r = x;
+      };
       auto put = [&](uint32_t* r) {
-        r[0] = nv;
-        if (oi) r[oi] = vi;
-        if (oj) r[oj] = nv;
-        if (oi && oj) r[oi + oj] = vi;
+        st(r, nv);
+        if (oi) st(r + oi, vi);
+        if (oj) st(r + oj, nv);
+        if (oi && oj) st(r + oi + oj, vi);
       };
       put(s + pw);
       if (flags & 16u) put(s_prev + pw + dKp);
@@ -1101,6 +1121,171 @@ __global__ void __launch_bounds__(NT, 1)
   }
   store_word_rows<B::HALO>(sq, gocc, L0, L1, Q, RS, RY, sl, threadIdx.x, NT);
   barrier();
+}
+
+// Barrier of the CTAs of one chain in a cooperative launch (every CTA resident): one
+// arrival counter and one generation word per chain in global memory; the last CTA to
+// arrive resets the counter and advances the generation.  Waits are bounded: a CTA that
+// polls kGridSpinLimit times without the generation moving records status 3 and sets the
+// abort word, and every waiting CTA leaves at its next poll; the kernel then returns
+// without writing the occupations back.
+constexpr unsigned kGridSpinLimit = 1u << 22;  // polls of >= 64 ns each: well over a second
+
+struct GridBarrier {
+  unsigned* count;  // [n_chains]
+  unsigned* gen;    // [n_chains]
+  int* status;      // 0, or 3: a barrier wait ran out
+  int* abort;       // non-zero: leave the sweep
+};
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// all CTAs of `chain` (n_ctas of them) reach this point; returns false after an abort
+__device__ __forceinline__ bool grid_chain_sync(const GridBarrier& gb, int chain, unsigned n_ctas, int* s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int stop = 0;
+    const unsigned g0 = ld_acquire_gpu(gb.gen + chain);
+    __threadfence();
+    if (atomicAdd(gb.count + chain, 1u) + 1u == n_ctas) {
+      atomicExch(gb.count + chain, 0u);
+      __threadfence();
+      atomicAdd(gb.gen + chain, 1u);
+    } else {
+      unsigned polls = 0;
+      while (ld_acquire_gpu(gb.gen + chain) == g0) {
+        if (*(volatile int*)gb.abort) {
+          stop = 1;
+          break;
+        }
+        if (++polls > kGridSpinLimit) {
+          atomicExch(gb.status, 3);
+          atomicExch(gb.abort, 1);
+          stop = 1;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    *s_flag = stop | *(volatile int*)gb.abort;
+  }
+  __syncthreads();
+  return *s_flag == 0;
+}
+
+template <int NFEAT, int NJ>
+struct CeTGridArgs {
+  CeTQuadArgs<NFEAT, NJ> t;  // geometry of the one-slab (S = 1) word window and lists
+  uint32_t* win;             // [n_chains][win_words] the chains' windows in global memory
+  long long win_words;
+  int G;                     // CTAs per chain
+  GridBarrier gb;
+};
+
+// Grid sweep of the ternary word layout for chains too large for one cluster to sweep
+// quickly (a single 96^3 chain holds 16 of 152 SMs in a 16-CTA cluster): each chain's whole
+// padded window (the S = 1 window of ce_sweep_tquad_kernel) lives in global memory and L2,
+// G CTAs share each colour's word list (word e of the colour to thread e mod G*NT), and a
+// grid barrier per chain separates the colours.  Same words, neighbours, random numbers and
+// decisions as the cluster kernels, so the trajectories are identical.
+template <class B, int NT>
+__global__ void __launch_bounds__(NT, 1)
+    ce_sweep_tgrid_kernel(const __grid_constant__ CeTGridArgs<B::NFEAT, B::NCOUNT> GA) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  const CeQuadArgs<B::NFEAT>& A = GA.t.q;
+  __shared__ int acc_sm[2][NSLOT];
+  __shared__ float dmu32_sm[NS * NS];
+  __shared__ double dmu64_sm[NS * NS];
+  __shared__ int s_flag;
+
+  const QuadGeometry& g = A.g;
+  const int G = GA.G;
+  const int chain = blockIdx.x / G, part = blockIdx.x % G;
+  const int Q = g.Q, RS = g.RS, RY = g.RY, RSY = RS * RY;
+  const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+  const long long N = (long long)L0 * L1 * L2;
+  int8_t* gocc = A.occ + (size_t)chain * N;
+  uint32_t* win = GA.win + (size_t)chain * GA.win_words;
+  const int gtid = part * NT + threadIdx.x, gthreads = G * NT;
+
+  load_word_window<B::HALO>(win, gocc, L0, L1, L2, Q, RS, RY, 0, L2, gtid, gthreads);
+  if (threadIdx.x < 2 * NSLOT) (&acc_sm[0][0])[threadIdx.x] = 0;
+  const CeChainParams* cpg = A.cp + chain;
+  load_dmu<NS>(cpg, dmu32_sm, dmu64_sm);
+  const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+  const int* cstart = g.color_start;
+
+  TernQuadSweeper<B, true> sw;
+  sw.s = win;
+  sw.s_prev = win;
+  sw.s_next = win;
+  sw.RS = RS;
+  sw.RSY = RSY;
+  sw.Q = Q;
+  sw.dJ = L1 * RS;
+  sw.dKp = L2 * RSY;  // the one slab's halo images: L2 planes up and down
+  sw.dKn = L2 * RSY;
+  sw.rule = MetropolisRule<B>{dmu32_sm, dmu64_sm, &A.w, cpg->beta, cpg->beta_log2e, cpg->dtol, cpg->eps,
+                              A.precision};
+  sw.tw = &GA.t.tw;
+  const int lane = threadIdx.x & 31;
+  int acc[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+  bool ok = grid_chain_sync(GA.gb, chain, (unsigned)G, &s_flag);
+
+#pragma unroll 1
+  for (int pass = 0; ok && pass < A.n_passes; ++pass) {
+    const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
+#pragma unroll 1
+    for (int c = 0; c < g.n_colors; ++c) {
+#pragma unroll 1
+      for (int e = cstart[c] + gtid; e < cstart[c + 1]; e += gthreads)
+        sw.update(__ldg(g.entries + e), __ldg(g.site_l + e), pass_g, chain_id, key0, key1, acc);
+      ok = grid_chain_sync(GA.gb, chain, (unsigned)G, &s_flag);
+      if (!ok) break;
+      if (c == 0 && pass > 0 && threadIdx.x < NSLOT) {
+        int* buf = acc_sm[(pass - 1) & 1];
+        const int v = buf[threadIdx.x];
+        buf[threadIdx.x] = 0;
+        if (v)
+          atomicAdd(reinterpret_cast<unsigned long long*>(
+                        A.out + ((size_t)(pass - 1) * A.n_chains + chain) * NSLOT + threadIdx.x),
+                    (unsigned long long)(long long)v);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) {
+      const int v = warp_sum(acc[q]);
+      if (lane == 0 && v) atomicAdd(&acc_sm[pass & 1][q], v);
+      acc[q] = 0;
+    }
+  }
+  if (!ok) return;
+  __syncthreads();
+  if (A.n_passes > 0 && threadIdx.x < NSLOT) {
+    const int pl = A.n_passes - 1;
+    const int v = acc_sm[pl & 1][threadIdx.x];
+    if (v)
+      atomicAdd(reinterpret_cast<unsigned long long*>(A.out + ((size_t)pl * A.n_chains + chain) * NSLOT + threadIdx.x),
+                (unsigned long long)(long long)v);
+  }
+  // the owned rows back to the occupation array (words read past L1: other SMs wrote them)
+  for (long long idx = gtid; idx < (long long)Q * L1 * L2; idx += gthreads) {
+    const int w = (int)(idx % Q);
+    const long long R = idx / Q;
+    const int j = (int)(R % L1), k = (int)(R / L1);
+    const uint32_t word = __ldcg(win + (w + B::HALO) + (size_t)RS * ((j + B::HALO) + (size_t)RY * (k + B::HALO)));
+    int8_t* row = gocc + (long long)L0 * (j + (long long)L1 * k);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) row[w + t * Q] = (int8_t)((word >> (8 * t)) & 0xFFu);
+  }
 }
 
 // Philox block of the first word of a thread in one colour phase: its four sites take

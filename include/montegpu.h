@@ -100,7 +100,8 @@ typedef struct mg_ce_batch mg_ce_batch;
  * mu[n_chains][n_species-1] exchange potentials conjugate to x_i = n(species i+1)/N,
  * seeds[n_chains] (Philox keys), chain_ids (Philox counter word, NULL = 0..n-1).
  * precision 0: FP64 acceptance decisions; 1: FP32 decisions (disagreements counted).
- * ctas_per_chain 0 = choose automatically. */
+ * ctas_per_chain 0 = choose automatically; above 16 (more than one cluster holds) the
+ * ternary word layout is swept by that many CTAs per chain on the whole grid (layout 4). */
 int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chains,
                        const double* temperature, const double* mu, const uint64_t* seeds,
                        const uint32_t* chain_ids, const int8_t* occ, int precision,
@@ -115,7 +116,10 @@ int mg_ce_batch_colors(const mg_ce_batch* b, int32_t* color /* [N] */);
  * 2 = layout 1 with the feature sums split around the phase barrier (binary basis; the
  * colourings generated for it: L0 a multiple of 16, L1/L2 multiples of 16/8); 3 = layout 2
  * with warp-specialised CTAs (one role prepares the next colour while the other decides the
- * current one; at most 384 words per CTA and colour).  The best one that applies is
+ * current one; at most 384 words per CTA and colour); 4 = layout 1 of the ternary basis
+ * swept by ctas_per_chain CTAs per chain on the whole grid (one cooperative launch, each
+ * chain's word window in global memory, a grid barrier per chain between colours; default
+ * CTA count: the resident CTAs shared between the chains).  The best one that applies is
  * chosen automatically.  All give identical trajectories; set_layout rebuilds the site
  * lists (MG_ERR_INVALID where the layout does not apply). */
 int mg_ce_batch_layout(const mg_ce_batch* b, int* layout);
