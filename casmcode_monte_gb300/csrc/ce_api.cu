@@ -106,6 +106,9 @@ struct mg_ce_batch {
 // per-pass output rows kept in a batch's own allocation
 constexpr int kOutPasses = 128;
 
+// words of one colour per CTA above which a ternary chain is swept by the whole grid
+constexpr int kGridWordsPerCta = 1024;
+
 // Pass counts of one rotated call (rotation_plan)
 struct RotationPlan {
   std::vector<int> a, g, b;  // chain c: passes on a fast cluster, in the slow slot, fast again
@@ -803,6 +806,14 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
       if (lay == 1 && layout >= 2) continue;  // a pipeline colouring: layout 2 is always at least as fast
       rc = setup_layout(b, lay);
     }
+  // Large ternary chains: when the word window of a 16-CTA cluster does not fit in shared
+  // memory (the batch fell back to the byte layout) or a CTA of the cluster layout holds more
+  // than kGridWordsPerCta words of one colour, the grid sweep (every resident CTA) is faster
+  // (GB300: 128^3 on the byte layout 1261 -> 209 us per pass; 96^3, 864 words per CTA and
+  // colour, stays on the cluster: 232 against 253 us)
+  if (rc == MG_OK && m->kind == 1 && b->col->word && ctas_per_chain == 0 &&
+      (b->layout == 0 || (b->layout == 1 && b->max_words > kGridWordsPerCta)))
+    (void)setup_layout(b, 4);  // refused (too many chains to be resident): stays where it is
   if (rc != MG_OK) {
     free_batch(b);
     return rc;

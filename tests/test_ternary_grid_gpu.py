@@ -115,3 +115,19 @@ def test_grid_layout_refusals(gpu_lib):
     assert g.layout == "word"
     g.run(1)
     g.close()
+
+
+def test_large_ternary_chain_chooses_grid(gpu_lib):
+    """A ternary 128^3 chain: its word window does not fit in the shared memory of a 16-CTA
+    cluster, so the batch chooses the grid sweep by itself; a batch held on a 16-CTA cluster
+    (the byte layout) gives the same outputs and occupations."""
+    L = (128, 128, 128)
+    model, occ, T, mu, seeds = _setup(L, 1, seed=12)
+    g = clex.ChainBatch(model, L, occ, T, mu, seeds)
+    assert g.layout == "grid" and g.ctas_per_chain > 16
+    w = clex.ChainBatch(model, L, occ, T, mu, seeds, ctas_per_chain=16)
+    assert w.layout in ("word", "byte")
+    assert np.array_equal(g.run(2), w.run(2))
+    assert np.array_equal(g.occupation(), w.occupation())
+    g.close()
+    w.close()
