@@ -33,6 +33,7 @@ SIGNATURES = {
     "mg_version": (C.c_int, []),
     "mg_device_count": (C.c_int, [c_int_p]),
     "mg_device_sm_count": (C.c_int, [c_int_p]),
+    "mg_release_cached_memory": (C.c_int, []),
     "mg_engine_create": (C.c_int, [C.c_int, vpp]),
     "mg_engine_destroy": (C.c_int, [vp]),
     "mg_engine_seed": (C.c_int, [vp, C.c_uint64]),

@@ -109,6 +109,12 @@ def color_supercell(kind: str, shape) -> tuple[np.ndarray, int, str]:
     return col, n, LAYOUTS[word.value]
 
 
+def release_cached_memory() -> None:
+    """Free the device blocks that closed batches left in the library's cache (later
+    batches of a shape seen before reuse them instead of allocating)."""
+    _lib.check(_lib.lib().mg_release_cached_memory())
+
+
 class ChainBatch:
     """Chains of one L0 x L1 x L2 supercell resident on the GPU (handle to mg_ce_batch).
 

@@ -66,6 +66,8 @@ struct mg_ce_batch {
   // one device allocation holds the occupations, chain parameters, correlation sums of
   // mg_ce_batch_corr and the per-pass outputs of runs of up to kOutPasses passes
   unsigned char* dblock = nullptr;
+  size_t dblock_bytes = 0;      // size of the (possibly cached, larger) block
+  unsigned int* dbad = nullptr;  // occupant codes out of range found by the creation check
   int8_t* docc = nullptr;
   mg::CeChainParams* dcp = nullptr;
   long long* dcorr = nullptr;
@@ -298,7 +300,7 @@ bool occupants_in_range(const int8_t* occ, long long n, int n_species) {
 void free_batch(mg_ce_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
-  cudaFree(b->dblock);
+  mg::host::cached_free(b->dblock, b->dblock_bytes);
   cudaFree(b->dgrid);
   if (b->dout_own) cudaFree(b->dout);
   if (b->ev0) cudaEventDestroy(b->ev0);
@@ -665,6 +667,8 @@ int setup_layout(mg_ce_batch* b, int layout) {
 
 extern "C" {
 
+int mg_release_cached_memory(void) { return mg::host::release_cached_blocks(); }
+
 int mg_ce_model_create(int basis_kind, const double* eci, int n_eci, mg_ce_model** out) {
   if (!out || !eci) {
     set_error("Error in mg_ce_model_create: invalid argument");
@@ -730,10 +734,6 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
     set_error("Error in mg_ce_batch_create: supercell too large");
     return MG_ERR_INVALID;
   }
-  if (!occupants_in_range(occ, N * n_chains, m->n_species)) {
-    set_error("Error in mg_ce_batch_create: occupant index out of range");
-    return MG_ERR_INVALID;
-  }
   for (int c = 0; c < n_chains; ++c)
     if (!(temperature[c] > 0.0)) {
       set_error("Error in mg_ce_batch_create: temperature must be > 0");
@@ -784,9 +784,11 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
     const size_t nslot = (size_t)m->n_classes + 2;
     const size_t o_cp = al((size_t)N * n_chains);
     const size_t o_corr = o_cp + al(sizeof(mg::CeChainParams) * n_chains);
-    const size_t o_out = o_corr + al(sizeof(long long) * m->n_classes * n_chains);
+    const size_t o_bad = o_corr + al(sizeof(long long) * m->n_classes * n_chains);
+    const size_t o_out = o_bad + al(sizeof(unsigned int));
     const size_t total = o_out + sizeof(long long) * kOutPasses * n_chains * nslot;
-    MGX(cudaMalloc(&b->dblock, total), "malloc");
+    MGX(mg::host::cached_malloc(reinterpret_cast<void**>(&b->dblock), total, &b->dblock_bytes), "malloc");
+    b->dbad = reinterpret_cast<unsigned int*>(b->dblock + o_bad);
     b->docc = reinterpret_cast<int8_t*>(b->dblock);
     b->dcp = reinterpret_cast<mg::CeChainParams*>(b->dblock + o_cp);
     b->dcorr = reinterpret_cast<long long*>(b->dblock + o_corr);
@@ -795,6 +797,22 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   }
   MGX(cudaMemcpyAsync(b->docc, occ, (size_t)N * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
   MGX(cudaMemcpyAsync(b->dcp, b->hcp.data(), sizeof(mg::CeChainParams) * n_chains, cudaMemcpyHostToDevice, b->stream), "copy");
+  {
+    // occupant codes checked on the device after the copy
+    const long long n_occ = N * n_chains;
+    const int blocks = (int)std::min<long long>((n_occ + 255) / 256, 1216);
+    unsigned int h_bad = 0;
+    MGX(cudaMemsetAsync(b->dbad, 0, sizeof(unsigned int), b->stream), "memset");
+    mg::host::occ_out_of_range_kernel<<<blocks, 256, 0, b->stream>>>(b->docc, n_occ, m->n_species, b->dbad);
+    MGX(cudaGetLastError(), "occupant check");
+    MGX(cudaMemcpyAsync(&h_bad, b->dbad, sizeof(unsigned int), cudaMemcpyDeviceToHost, b->stream), "copy");
+    MGX(cudaStreamSynchronize(b->stream), "occupant check");
+    if (h_bad != 0) {
+      set_error("Error in mg_ce_batch_create: occupant index out of range");
+      free_batch(b);
+      return MG_ERR_INVALID;
+    }
+  }
 #undef MGX
   // the best layout that applies; a layout can still be refused for this CTA count (shared
   // memory, staged words), then the next one is tried

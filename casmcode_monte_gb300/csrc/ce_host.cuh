@@ -104,6 +104,103 @@ struct mg_ce_model {
 namespace mg {
 namespace host {
 
+// Codes outside [0, n_species) in occ[0, n), counted into *bad (reads only): the device-side
+// admission check of occupations already copied to the device (a host scan of a few MB costs
+// more than the copy).
+static __global__ void occ_out_of_range_kernel(const int8_t* __restrict__ occ, long long n, int n_species,
+                                        unsigned int* __restrict__ bad) {
+  unsigned int count = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int o = occ[i];
+    count += (o < 0 || o >= n_species) ? 1u : 0u;
+  }
+  count = __reduce_add_sync(0xffffffffu, count);
+  if ((threadIdx.x & 31) == 0 && count) atomicAdd(bad, count);
+}
+
+// Process-wide cache of device blocks released by chain batches, per device: a batch of a
+// shape seen before takes a released block of at least its size (and at most twice it plus
+// 1 MB) instead of cudaMalloc, and its release keeps the block instead of cudaFree (which
+// also waits for the whole device).  At most kCacheBlocks blocks and kCacheBytes bytes are
+// kept; mg_release_cached_memory frees them.  Callers release a block only after the work
+// that used it has finished.
+constexpr size_t kCacheBlocks = 8;
+constexpr size_t kCacheBytes = size_t(1) << 30;
+
+struct BlockCache {
+  std::mutex mu;
+  struct Entry {
+    int dev;
+    void* p;
+    size_t bytes;
+  };
+  std::vector<Entry> blocks;
+  size_t total = 0;
+};
+
+inline BlockCache& block_cache() {
+  static BlockCache* c = new BlockCache();  // never destroyed: batches may outlive static destruction
+  return *c;
+}
+
+inline cudaError_t cached_malloc(void** p, size_t bytes, size_t* got) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    BlockCache& c = block_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    int best = -1;
+    for (int i = 0; i < (int)c.blocks.size(); ++i) {
+      const auto& b = c.blocks[i];
+      if (b.dev == dev && b.bytes >= bytes && b.bytes <= 2 * bytes + (size_t(1) << 20) &&
+          (best < 0 || b.bytes < c.blocks[best].bytes))
+        best = i;
+    }
+    if (best >= 0) {
+      *p = c.blocks[best].p;
+      *got = c.blocks[best].bytes;
+      c.total -= c.blocks[best].bytes;
+      c.blocks.erase(c.blocks.begin() + best);
+      return cudaSuccess;
+    }
+  }
+  *got = bytes;
+  return cudaMalloc(p, bytes);
+}
+
+inline void cached_free(void* p, size_t bytes) {
+  if (!p) return;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) {
+    BlockCache& c = block_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (c.blocks.size() < kCacheBlocks && c.total + bytes <= kCacheBytes) {
+      c.blocks.push_back({dev, p, bytes});
+      c.total += bytes;
+      return;
+    }
+  }
+  cudaFree(p);
+}
+
+inline int release_cached_blocks() {
+  BlockCache& c = block_cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  cudaError_t first = cudaSuccess;
+  for (auto& b : c.blocks) {
+    const cudaError_t e = cudaFree(b.p);
+    if (first == cudaSuccess) first = e;
+  }
+  c.blocks.clear();
+  c.total = 0;
+  if (first != cudaSuccess) {
+    set_error(std::string("CUDA error in mg_release_cached_memory: ") + cudaGetErrorString(first));
+    return MG_ERR_CUDA;
+  }
+  return MG_OK;
+}
+
 inline int dpsi_max(int kind, int b) {
   if (kind == 0) return 1;
   return b == 0 ? 2 : 3;

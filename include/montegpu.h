@@ -45,6 +45,10 @@ const char* mg_last_error(void); /* thread-local message of the last failure */
 int mg_version(void);            /* 100 * major + minor */
 int mg_device_count(int* n);
 int mg_device_sm_count(int* n);
+/* free the device blocks that destroyed chain batches left in the library's cache (a batch
+ * created later for a shape seen before reuses such a block instead of allocating; at most
+ * 8 blocks and 1 GiB are kept per process) */
+int mg_release_cached_memory(void);
 
 /* ---- mt19937_64 engine (RandomNumberEngine; monte.cpp:469-513) ---- */
 typedef struct mg_engine mg_engine;
@@ -119,7 +123,11 @@ int mg_ce_batch_colors(const mg_ce_batch* b, int32_t* color /* [N] */);
  * current one; at most 384 words per CTA and colour); 4 = layout 1 of the ternary basis
  * swept by ctas_per_chain CTAs per chain on the whole grid (one cooperative launch, each
  * chain's word window in global memory, a grid barrier per chain between colours; default
- * CTA count: the resident CTAs shared between the chains).  The best one that applies is
+ * CTA count: the resident CTAs shared between the chains; chosen by itself for ternary chains
+ * whose word window does not fit a 16-CTA cluster or would give a CTA more than 1024 words of
+ * one colour).  The grid sweep expects the device to itself while it runs: if other work
+ * holds SMs long enough for a barrier wait to run out (over a second), the run is abandoned
+ * with MG_ERR_DEVICE and the occupations are left as they were.  The best one that applies is
  * chosen automatically.  All give identical trajectories; set_layout rebuilds the site
  * lists (MG_ERR_INVALID where the layout does not apply). */
 int mg_ce_batch_layout(const mg_ce_batch* b, int* layout);

@@ -56,3 +56,57 @@ def test_zero_passes_and_invalid_arguments(gpu_lib):
         clex.ChainBatch(model, (8, 8, 8), bad, [1000.0], np.zeros((1, 1)), [5])
     with pytest.raises(RuntimeError, match=">= 4"):
         clex.ChainBatch(model, (3, 8, 8), occ[:, :192], [1000.0], np.zeros((1, 1)), [5])
+
+
+@pytest.mark.parametrize("bad_value", [2, -1, 127])
+def test_batch_occupant_check_on_device(gpu_lib, bad_value):
+    """The creation check runs on the device after the copy: a bad code in the last chain's
+    last site (and a negative one) is refused, and a batch created afterwards works."""
+    model = _model()
+    rng = np.random.default_rng(8)
+    occ = np.stack([clex.random_occupation(2, 16**3, rng) for _ in range(3)])
+    bad = occ.copy()
+    bad[2, -1] = bad_value
+    with pytest.raises(RuntimeError, match="occupant index out of range"):
+        clex.ChainBatch(model, (16, 16, 16), bad, [900.0] * 3, np.zeros((3, 1)), [1, 2, 3])
+    b = clex.ChainBatch(model, (16, 16, 16), occ, [900.0] * 3, np.zeros((3, 1)), [1, 2, 3])
+    b.run(2)
+    b.close()
+
+
+def test_batch_block_cache_reuse(gpu_lib):
+    """Closed batches leave their device block in the library's cache: a batch of the same shape
+    created next takes it (device free memory unchanged), starts from its own inputs whatever the
+    block held, and gives the trajectory of a batch on fresh memory; release_cached_memory frees
+    the cached blocks."""
+    import torch
+
+    model = _model()
+    rng = np.random.default_rng(9)
+    L = (64, 64, 64)
+    occ = np.stack([clex.random_occupation(2, 64**3, rng) for _ in range(8)])
+    T, mu, seeds = np.linspace(400, 1600, 8), np.zeros((8, 1)), np.arange(1, 9, dtype=np.uint64)
+    clex.release_cached_memory()
+    torch.cuda.synchronize()
+    a = clex.ChainBatch(model, L, occ, T, mu, seeds)
+    ref = a.run(6)
+    ref_occ = a.occupation()
+    a.close()
+    other = np.stack([clex.random_occupation(2, 64**3, rng) for _ in range(8)])
+    for _ in range(3):
+        x = clex.ChainBatch(model, L, other, T, mu, seeds)  # fills the block with other data
+        x.run(3)
+        x.close()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    b = clex.ChainBatch(model, L, occ, T, mu, seeds)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert np.array_equal(b.run(6), ref)
+    assert np.array_equal(b.occupation(), ref_occ)
+    b.close()
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    clex.release_cached_memory()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] >= free1 + (2 << 20)  # the 8 x 64^3 block (2.2 MB)
