@@ -1088,13 +1088,22 @@ inline int launch_sweep_ws(const mg_ce_model* m, const SweepLaunch& L, int pipe)
 template <class B>
 cudaError_t launch_corr(const int8_t* occ, int L0, int L1, int L2, int n_chains, long long* out, cudaStream_t st) {
   constexpr int H = B::HALO;
-  const int nk = std::min(4, L2);
+  static int sm_count[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && sm_count[dev] == 0) {
+    e = cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+  }
+  const int sms = (dev >= 0 && dev < 64) ? sm_count[dev] : 152;
+  // planes per CTA: up to 4, fewer while that leaves under four CTAs per SM (the CTAs are
+  // latency-bound: more of them beat the extra halo planes each one loads)
+  int nk = std::min(4, L2);
+  while (nk > 1 && (long long)((L2 + nk - 1) / nk) * n_chains < 4LL * sms) --nk;
   const size_t smem = (size_t)(L0 + 2 * H) * (L1 + 2 * H) * (nk + 2 * H);
   if (smem <= 200 * 1024) {
     static bool attr_set[64] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
     if (smem > 48 * 1024 && dev >= 0 && dev < 64 && !attr_set[dev]) {
       e = cudaFuncSetAttribute(ce_corr_tiled_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
       if (e != cudaSuccess) return e;
