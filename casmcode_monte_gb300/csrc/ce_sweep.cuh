@@ -2315,22 +2315,31 @@ __global__ void __launch_bounds__(256) ce_corr_tiled_kernel(const int8_t* occ, i
   const int nkb = min(nk, L2 - k0);
   const int PX = L0 + 2 * H, PY = L1 + 2 * H, PXY = PX * PY;
   const int8_t* g = occ + (size_t)chain * L0 * L1 * L2;
-  for (int idx = threadIdx.x; idx < PXY * (nkb + 2 * H); idx += blockDim.x) {
-    const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
-    int i = ip - H, j = jp - H, k = k0 + kp - H;
-    i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+  // one padded row (PX bytes) per warp and step: row r = jp + PY kp of the window, its
+  // lattice row and periodic images found once per row
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+  for (int r = warp; r < PY * (nkb + 2 * H); r += n_warps) {
+    const int jp = r % PY, kp = r / PY;
+    int j = jp - H, k = k0 + kp - H;
     j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
     k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
-    s[idx] = B::code_of_occ(g[i + (long long)L0 * (j + (long long)L1 * k)]);
+    const int8_t* grow = g + (long long)L0 * (j + (long long)L1 * k);
+    int8_t* srow = s + (size_t)r * PX;
+    for (int ip = lane; ip < PX; ip += 32) {
+      int i = ip - H;
+      i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+      srow[ip] = B::code_of_occ(grow[i]);
+    }
   }
   __syncthreads();
   long long C[NC];
 #pragma unroll
   for (int f = 0; f < NC; ++f) C[f] = 0;
-  const int L01 = L0 * L1;
-  for (int site = threadIdx.x; site < L01 * nkb; site += blockDim.x) {
-    const int i = site % L0, j = (site / L0) % L1, kl = site / L01;
-    B::anchored(SmemLoader{s + (i + H) + PX * ((j + H) + PY * (kl + H)), PX, PXY}, C);
+  // the owned sites row by row (row rr = j + L1 kl)
+  for (int rr = warp; rr < L1 * nkb; rr += n_warps) {
+    const int j = rr % L1, kl = rr / L1;
+    const int8_t* srow = s + H + PX * ((j + H) + PY * (kl + H));
+    for (int i = lane; i < L0; i += 32) B::anchored(SmemLoader{srow + i, PX, PXY}, C);
   }
 #pragma unroll
   for (int f = 0; f < NC; ++f) {
