@@ -2315,20 +2315,47 @@ __global__ void __launch_bounds__(256) ce_corr_tiled_kernel(const int8_t* occ, i
   const int nkb = min(nk, L2 - k0);
   const int PX = L0 + 2 * H, PY = L1 + 2 * H, PXY = PX * PY;
   const int8_t* g = occ + (size_t)chain * L0 * L1 * L2;
-  // one padded row (PX bytes) per warp and step: row r = jp + PY kp of the window, its
-  // lattice row and periodic images found once per row
+  // padded rows (PX bytes; row r = jp + PY kp of the window) by warps, four rows per step
+  // so that four independent loads are in flight per lane; each row's lattice row and
+  // periodic images found once.  Rows of 4-byte aligned length are read in 32-bit words
+  // (the interior) plus the 2H halo bytes.
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
-  for (int r = warp; r < PY * (nkb + 2 * H); r += n_warps) {
-    const int jp = r % PY, kp = r / PY;
-    int j = jp - H, k = k0 + kp - H;
-    j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
-    k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
-    const int8_t* grow = g + (long long)L0 * (j + (long long)L1 * k);
-    int8_t* srow = s + (size_t)r * PX;
-    for (int ip = lane; ip < PX; ip += 32) {
+  const int R = PY * (nkb + 2 * H);
+  const bool vec = (L0 & 3) == 0 && (reinterpret_cast<uintptr_t>(g) & 3u) == 0;
+  const int n_items = vec ? L0 / 4 + 2 * H : PX;  // per row: words + halo bytes, or bytes
+  for (int r0 = 4 * warp; r0 < R; r0 += 4 * n_warps) {
+    const int8_t* grow[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int r = min(r0 + u, R - 1);
+      const int jp = r % PY, kp = r / PY;
+      int j = jp - H, k = k0 + kp - H;
+      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+      grow[u] = g + (long long)L0 * (j + (long long)L1 * k);
+    }
+    for (int t = lane; t < n_items; t += 32) {
+      // item t: a word of the interior (vec, t < L0/4), else one byte at padded position ip
+      const bool word = vec && t < L0 / 4;
+      int ip = t;
+      if (vec && !word) ip = (t - L0 / 4 < H) ? t - L0 / 4 : L0 + (t - L0 / 4);
       int i = ip - H;
       i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
-      srow[ip] = B::code_of_occ(grow[i]);
+      uint32_t w[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        w[u] = word ? __ldg(reinterpret_cast<const uint32_t*>(grow[u]) + t) : (uint32_t)(uint8_t)__ldg(grow[u] + i);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (r0 + u >= R) break;
+        int8_t* srow = s + (size_t)(r0 + u) * PX;
+        if (word) {
+#pragma unroll
+          for (int b = 0; b < 4; ++b) srow[H + 4 * t + b] = B::code_of_occ((int8_t)((w[u] >> (8 * b)) & 0xFFu));
+        } else {
+          srow[ip] = B::code_of_occ((int8_t)w[u]);
+        }
+      }
     }
   }
   __syncthreads();
