@@ -234,6 +234,23 @@ inline void fill_weights(const mg_ce_model* m, CeWeights<NF>& w) {
     w.w64[k] = m->w64[k];
   }
   w.qscale = (float)std::ldexp(1.0, -m->qshift);
+  // ternary: energy-sum weights of the monomial counts (int32 modulo 2^32, like the sums)
+  for (int b = 0; b < 2; ++b) {
+    w.cgc[b] = 0;
+    for (int j = 0; j < kMaxCounts; ++j) w.cw[b][j] = 0;
+  }
+  if (m->kind == 1 && NF == FccTernary::NFEAT) {
+    long long W[2][FccTernary::NCOUNT] = {}, gc[2] = {};
+    for (int k = 0; k < FccTernary::NFEAT; ++k) {
+      const int b = FccTernary::feat_b(k);
+      gc[b] += (long long)m->wq[k] * FccTernary::tq_const(k);
+      for (int j = 0; j < FccTernary::NCOUNT; ++j) W[b][j] += (long long)m->wq[k] * FccTernary::tq_coef(k, j);
+    }
+    for (int b = 0; b < 2; ++b) {
+      w.cgc[b] = (int)(uint32_t)(unsigned long long)gc[b];
+      for (int j = 0; j < FccTernary::NCOUNT; ++j) w.cw[b][j] = (int)(uint32_t)(unsigned long long)W[b][j];
+    }
+  }
 }
 
 inline const int* offsets(int kind, int* n) {

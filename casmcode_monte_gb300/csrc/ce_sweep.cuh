@@ -64,11 +64,18 @@ struct CeWeightsClass {
 // Energy weights: FP64 for the exact decision; quantised integers wq[k] = round(w[k] * 2^s)
 // for the fast path, whose change of energy sum_b dpsi_b * sum_k wq[k] F[k] is an exact
 // int32 (s chosen so it cannot overflow) scaled by qscale = 2^-s.
+// Ternary basis: the same quantised energy sums from monomial counts of the neighbours'
+// indicators (the word layouts' counts_quad): sum_k wq[k] F_k of basis b = cgc[b] +
+// sum_j cw[b][j] M_j (int32, exact modulo 2^32).  Unused for the binary basis.
+constexpr int kMaxCounts = 32;
+
 template <int NFEAT>
 struct CeWeights {
   int wq[NFEAT];
   float qscale;
   double w64[NFEAT];
+  int cw[2][kMaxCounts];
+  int cgc[2];
 };
 
 struct CeGeometry {
@@ -215,6 +222,21 @@ struct MetropolisRule {
   }
 };
 
+template <class B>
+__device__ __noinline__ int tern_exact(const MetropolisRule<B>& rule, int o, int o2, int dpsi0, int dpsi1,
+                                       const uint32_t* M, int shift, uint32_t x0, bool acc32);
+
+// Neighbour occupants of a byte-layout site as words with the occupant in byte 0 (input of
+// counts_quad, whose counts then hold this site's in byte 0; bytes 1-3 are not read)
+template <class B>
+struct CodeWordLoader {
+  const int8_t* p;
+  int PX, PXY;
+  __device__ __forceinline__ uint32_t operator()(int di, int dj, int dk) const {
+    return (uint32_t)B::occ_of_code(p[di + dj * PX + dk * PXY]);
+  }
+};
+
 // Per-CTA context of the site update: shared-memory lattice and its periodic copies,
 // chain constants and the FP32/FP64 decision rule.  Shared by the cluster sweep kernel
 // and the persistent pool kernel.
@@ -262,6 +284,56 @@ struct SiteSweeper {
       acc[0] += 1;
 #pragma unroll
       for (int k = 0; k < NF; ++k) acc[B::feat_class(k)] += dpsi[B::feat_b(k)] * F[k];
+    }
+  }
+
+  // Ternary basis: the whole update of one site from its monomial counts (about a third of
+  // the instructions of the 52 feature sums): the same proposal (x1), energy sums (equal to
+  // sum_k wq[k] F_k), FP32 rule and FP64 re-decision as decide(), so the trajectory is
+  // unchanged; the correlation changes dpsi_b F_k with F_k = tq_const(k) + sum_j
+  // tq_coef(k, j) M_j.
+  __device__ __forceinline__ void update_counts(uint32_t ent, uint32_t x0, uint32_t x1, int (&acc)[NSLOT]) const {
+    constexpr int NJ = B::NCOUNT;
+    static_assert(NJ <= kMaxCounts, "count weights");
+    const int8_t* p = s + (int)(ent & 0xFFFFFFu);
+    const int o = B::occ_of_code(*p);
+    uint32_t M[NJ];
+    B::counts_quad(CodeWordLoader<B>{p, PX, PXY}, M);
+    const int o2 = (o + 1 + (int)(x1 >> 31)) % 3;
+    const int dpsi0 = B::psi(0, o2) - B::psi(0, o), dpsi1 = B::psi(1, o2) - B::psi(1, o);
+    int G0 = w->cgc[0], G1 = w->cgc[1];
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      const int m = (int)(M[j] & 0xFFu);
+      G0 += w->cw[0][j] * m;
+      G1 += w->cw[1][j] * m;
+    }
+    const MetropolisRule<B> rule{dmu32, dmu64, w, beta, beta_log2e, dtol, eps, precision};
+    bool amb;
+    bool a = rule.fast(o, o2, dpsi0 * G0 + dpsi1 * G1, x0, amb);
+    if (amb) {
+      uint32_t Mc[NJ];
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) Mc[j] = M[j];
+      const int r = tern_exact<B>(rule, o, o2, dpsi0, dpsi1, Mc, 0, x0, a);
+      a = (r & 1) != 0;
+      acc[NC] += 1;
+      acc[NC + 1] += (r >> 1) & 1;
+    }
+    if (a) {
+      store(ent, B::code_of_occ(o2));
+      acc[0] += 1;
+#pragma unroll
+      for (int k = 0; k < NF; ++k)
+        if (B::tq_const(k) != 0) acc[B::feat_class(k)] += B::tq_const(k) * (B::feat_b(k) == 0 ? dpsi0 : dpsi1);
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const int m = (int)(M[j] & 0xFFu);
+        const int d0 = dpsi0 * m, d1 = dpsi1 * m;
+#pragma unroll
+        for (int k = 0; k < NF; ++k)
+          if (B::tq_coef(k, j) != 0) acc[B::feat_class(k)] += B::tq_coef(k, j) * (B::feat_b(k) == 0 ? d0 : d1);
+      }
     }
   }
 
@@ -333,19 +405,27 @@ __device__ __forceinline__ void sweep_phase(const SiteSweeper<B>& sw, const Phas
 #pragma unroll
   for (int q = 0; q < PRE; ++q)
     if (e0 + q * NT < e_end) {
-      int o;
-      int F[B::NFEAT];
-      sw.gather(pf.ent[q], o, F);
-      sw.decide(pf.ent[q], pf.x0[q], pf.x1[q], o, F, acc);
+      if constexpr (B::NSPECIES == 3) {
+        sw.update_counts(pf.ent[q], pf.x0[q], pf.x1[q], acc);
+      } else {
+        int o;
+        int F[B::NFEAT];
+        sw.gather(pf.ent[q], o, F);
+        sw.decide(pf.ent[q], pf.x0[q], pf.x1[q], o, F, acc);
+      }
     }
 #pragma unroll 1
   for (int e = e0 + PRE * NT; e < e_end; e += NT) {
     const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
     const uint32_t ent = __ldg(entries + e);
-    int o;
-    int F[B::NFEAT];
-    sw.gather(ent, o, F);
-    sw.decide(ent, philox_word(x, ent >> 30), x.y, o, F, acc);
+    if constexpr (B::NSPECIES == 3) {
+      sw.update_counts(ent, philox_word(x, ent >> 30), x.y, acc);
+    } else {
+      int o;
+      int F[B::NFEAT];
+      sw.gather(ent, o, F);
+      sw.decide(ent, philox_word(x, ent >> 30), x.y, o, F, acc);
+    }
   }
 }
 
