@@ -815,7 +815,11 @@ int launch_sweep_t(const mg_ce_model* m, const SweepLaunch& L) {
   A.precision = L.precision;
   A.out = L.out;
   const size_t smem = slab_smem(L.L0, L.L1, L.L2, L.S);
-  auto kern = ce_sweep_kernel<B, NT>;
+  // ternary: four sites per thread and step when a CTA has more than 1.5 sites per thread
+  // and colour on average
+  auto kern = ce_sweep_kernel<B, NT, kSitesOne>;
+  if (B::NSPECIES == 3 && 2 * ((long long)L.L0 * L.L1 * L.L2) > 3LL * NT * L.S * L.n_colors)
+    kern = ce_sweep_kernel<B, NT, kSitesFour>;
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(L.n_chains * L.S), 1, 1);

@@ -226,14 +226,26 @@ template <class B>
 __device__ __noinline__ int tern_exact(const MetropolisRule<B>& rule, int o, int o2, int dpsi0, int dpsi1,
                                        const uint32_t* M, int shift, uint32_t x0, bool acc32);
 
-// Neighbour occupants of a byte-layout site as words with the occupant in byte 0 (input of
-// counts_quad, whose counts then hold this site's in byte 0; bytes 1-3 are not read)
+// word `w` (0..3) of a Philox block
+__device__ __forceinline__ uint32_t philox_word(const U32x4& x, uint32_t w) {
+  return w == 0u ? x.x : (w == 1u ? x.y : (w == 2u ? x.z : x.w));
+}
+
+// Neighbours of four byte-layout sites (any four of one colour) packed into words, byte t
+// from site t, as occupants 0..2 (codes o - 1 = 0xFF, 0x00, 0x01 plus one per byte, without
+// carries between bytes): the input of counts_quad for four sites at once
 template <class B>
-struct CodeWordLoader {
-  const int8_t* p;
+struct GatherWordLoader {
+  const int8_t* s;
+  int i0, i1, i2, i3;  // padded indices of the four sites
   int PX, PXY;
   __device__ __forceinline__ uint32_t operator()(int di, int dj, int dk) const {
-    return (uint32_t)B::occ_of_code(p[di + dj * PX + dk * PXY]);
+    const int off = di + dj * PX + dk * PXY;
+    const uint32_t a = (uint8_t)s[i0 + off], b = (uint8_t)s[i1 + off], c = (uint8_t)s[i2 + off],
+                   d = (uint8_t)s[i3 + off];
+    const uint32_t w = __byte_perm(__byte_perm(a, b, 0x0040), __byte_perm(c, d, 0x0040), 0x5410);
+    static_assert(B::code_of_occ(0) == -1 && B::code_of_occ(2) == 1, "ternary codes are o - 1");
+    return ((w & 0x7F7F7F7Fu) + 0x01010101u) ^ (w & 0x80808080u);
   }
 };
 
@@ -287,49 +299,76 @@ struct SiteSweeper {
     }
   }
 
-  // Ternary basis: the whole update of one site from its monomial counts (about a third of
-  // the instructions of the 52 feature sums): the same proposal (x1), energy sums (equal to
-  // sum_k wq[k] F_k), FP32 rule and FP64 re-decision as decide(), so the trajectory is
-  // unchanged; the correlation changes dpsi_b F_k with F_k = tq_const(k) + sum_j
-  // tq_coef(k, j) M_j.
-  __device__ __forceinline__ void update_counts(uint32_t ent, uint32_t x0, uint32_t x1, int (&acc)[NSLOT]) const {
+  // Ternary basis, four sites of one colour at once (entries ent[t], Philox counter words
+  // sl[t]; sites t >= n are absent and only repeat site 0's loads): the counts of the four
+  // sites byte-parallel from gathered neighbour words, then per site the proposal, energy
+  // sums (equal to sum_k wq[k] F_k), FP32 rule and FP64 re-decision of decide(), so every
+  // decision and the trajectory are those of the one-site update; the correlation changes of
+  // the accepted sites as byte dot products of the counts with the packed dpsi.
+  // (entries and counter words of site t at index e[t] of `entries` / `site_l`; read
+  // again after the counts rather than held through them)
+  __device__ __forceinline__ void update_gathered(const uint32_t* entries, const uint32_t* site_l, const int (&e)[4],
+                                                  int n, uint32_t pass, uint32_t chain_id, uint32_t key0,
+                                                  uint32_t key1, int (&acc)[NSLOT]) const {
     constexpr int NJ = B::NCOUNT;
     static_assert(NJ <= kMaxCounts, "count weights");
-    const int8_t* p = s + (int)(ent & 0xFFFFFFu);
-    const int o = B::occ_of_code(*p);
+    uint32_t v;
     uint32_t M[NJ];
-    B::counts_quad(CodeWordLoader<B>{p, PX, PXY}, M);
-    const int o2 = (o + 1 + (int)(x1 >> 31)) % 3;
-    const int dpsi0 = B::psi(0, o2) - B::psi(0, o), dpsi1 = B::psi(1, o2) - B::psi(1, o);
-    int G0 = w->cgc[0], G1 = w->cgc[1];
-#pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-      const int m = (int)(M[j] & 0xFFu);
-      G0 += w->cw[0][j] * m;
-      G1 += w->cw[1][j] * m;
+    {
+      const int i0 = (int)(__ldg(entries + e[0]) & 0xFFFFFFu);
+      const int i1 = n > 1 ? (int)(__ldg(entries + e[1]) & 0xFFFFFFu) : i0;
+      const int i2 = n > 2 ? (int)(__ldg(entries + e[2]) & 0xFFFFFFu) : i0;
+      const int i3 = n > 3 ? (int)(__ldg(entries + e[3]) & 0xFFFFFFu) : i0;
+      const GatherWordLoader<B> ld{s, i0, i1, i2, i3, PX, PXY};
+      v = ld(0, 0, 0);
+      B::counts_quad(ld, M);
     }
     const MetropolisRule<B> rule{dmu32, dmu64, w, beta, beta_log2e, dtol, eps, precision};
-    bool amb;
-    bool a = rule.fast(o, o2, dpsi0 * G0 + dpsi1 * G1, x0, amb);
-    if (amb) {
-      uint32_t Mc[NJ];
+    uint32_t sg0 = 0u, sg1 = 0u;
+    int n_acc = 0;
 #pragma unroll
-      for (int j = 0; j < NJ; ++j) Mc[j] = M[j];
-      const int r = tern_exact<B>(rule, o, o2, dpsi0, dpsi1, Mc, 0, x0, a);
-      a = (r & 1) != 0;
-      acc[NC] += 1;
-      acc[NC + 1] += (r >> 1) & 1;
-    }
-    if (a) {
-      store(ent, B::code_of_occ(o2));
-      acc[0] += 1;
-#pragma unroll
-      for (int k = 0; k < NF; ++k)
-        if (B::tq_const(k) != 0) acc[B::feat_class(k)] += B::tq_const(k) * (B::feat_b(k) == 0 ? dpsi0 : dpsi1);
+    for (int t = 0; t < 4; ++t) {
+      if (t >= n) break;
+      const uint32_t ent = __ldg(entries + e[t]);
+      const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e[t]), pass, chain_id, SWEEP_TAG}, key0, key1);
+      const uint32_t x0 = philox_word(x, ent >> 30);
+      const int o = (int)((v >> (8 * t)) & 0xFFu);
+      const int o2 = (o + 1 + (int)(x.y >> 31)) % 3;
+      const int dpsi0 = B::psi(0, o2) - B::psi(0, o), dpsi1 = B::psi(1, o2) - B::psi(1, o);
+      int G0 = w->cgc[0], G1 = w->cgc[1];
 #pragma unroll
       for (int j = 0; j < NJ; ++j) {
-        const int m = (int)(M[j] & 0xFFu);
-        const int d0 = dpsi0 * m, d1 = dpsi1 * m;
+        const int m = (int)((M[j] >> (8 * t)) & 0xFFu);
+        G0 += w->cw[0][j] * m;
+        G1 += w->cw[1][j] * m;
+      }
+      bool amb;
+      bool a = rule.fast(o, o2, dpsi0 * G0 + dpsi1 * G1, x0, amb);
+      if (amb) {
+        uint32_t Mc[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) Mc[j] = M[j];
+        const int r = tern_exact<B>(rule, o, o2, dpsi0, dpsi1, Mc, 8 * t, x0, a);
+        a = (r & 1) != 0;
+        acc[NC] += 1;
+        acc[NC + 1] += (r >> 1) & 1;
+      }
+      if (a) {
+        store(ent, B::code_of_occ(o2));
+        sg0 |= (uint32_t)(dpsi0 & 0xFF) << (8 * t);
+        sg1 |= (uint32_t)(dpsi1 & 0xFF) << (8 * t);
+        ++n_acc;
+      }
+    }
+    if (n_acc) {
+      acc[0] += n_acc;
+      const int c0 = __dp4a((int)0x01010101, (int)sg0, 0), c1 = __dp4a((int)0x01010101, (int)sg1, 0);
+#pragma unroll
+      for (int k = 0; k < NF; ++k)
+        if (B::tq_const(k) != 0) acc[B::feat_class(k)] += B::tq_const(k) * (B::feat_b(k) == 0 ? c0 : c1);
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const int d0 = __dp4a((int)M[j], (int)sg0, 0), d1 = __dp4a((int)M[j], (int)sg1, 0);
 #pragma unroll
         for (int k = 0; k < NF; ++k)
           if (B::tq_coef(k, j) != 0) acc[B::feat_class(k)] += B::tq_coef(k, j) * (B::feat_b(k) == 0 ? d0 : d1);
@@ -365,11 +404,6 @@ struct SiteSweeper {
   }
 };
 
-// word `w` (0..3) of a Philox block
-__device__ __forceinline__ uint32_t philox_word(const U32x4& x, uint32_t w) {
-  return w == 0u ? x.x : (w == 1u ? x.y : (w == 2u ? x.z : x.w));
-}
-
 // Philox words of the first PRE sites of a thread in one colour phase, drawn ahead of
 // the phase (they depend on (site, pass, chain) only, not on the lattice).  The list
 // holds each site's counter word and, in the entry's top two bits, the word it takes.
@@ -395,37 +429,57 @@ struct PhasePrefetch {
   }
 };
 
+// Site grouping of the ternary byte-layout sweep: one site per thread and step, four, or
+// chosen per phase (four when the phase has more than 1.5 sites per thread).  The host picks
+// one or four per launch of a chain batch from its sites per CTA and colour (the two paths
+// compiled together spill more registers); the pool kernels, whose chains differ in shape,
+// choose per phase.
+constexpr int kSitesOne = 1, kSitesFour = 2, kSitesPerPhase = 0;
+
 // One colour phase of one CTA: the prefetched sites, then any further sites inline.
-template <class B, int NT, int PRE>
+template <class B, int NT, int PRE, int GROUP = kSitesPerPhase>
 __device__ __forceinline__ void sweep_phase(const SiteSweeper<B>& sw, const PhasePrefetch<PRE>& pf,
                                             const int* cstart, int c, const uint32_t* entries,
                                             const uint32_t* site_l, uint32_t pass, uint32_t chain_id,
                                             uint32_t key0, uint32_t key1, int (&acc)[SiteSweeper<B>::NSLOT]) {
   const int e0 = cstart[c] + threadIdx.x, e_end = cstart[c + 1];
+  // ternary basis, four sites per thread and step (entries q, q + T, q + 2T, q + 3T of the
+  // phase's list, T = ceil(n / 4), so the lanes of a warp still read consecutive entries);
+  // with few sites per thread one site per thread and step is faster (its dependent chain is
+  // shorter): GB300, 8 ternary chains of 64^3 (3.6 sites per thread and colour) 259 -> 167 us
+  // per pass with four, 8 of 30^3 (0.4 per thread) 58 us with one against 109 with four
+  if (B::NSPECIES == 3 && GROUP != kSitesOne &&
+      (GROUP == kSitesFour || 2 * (e_end - cstart[c]) > 3 * NT)) {
+    const int base = cstart[c], n_e = e_end - base, T = (n_e + 3) >> 2;
+#pragma unroll 1
+    for (int q = threadIdx.x; q < T; q += NT) {
+      int e[4];
+      int n = 0;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        e[t] = base + q + t * T;
+        if (q + t * T < n_e) n = t + 1;
+      }
+      if constexpr (B::NSPECIES == 3) sw.update_gathered(entries, site_l, e, n, pass, chain_id, key0, key1, acc);
+    }
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < PRE; ++q)
     if (e0 + q * NT < e_end) {
-      if constexpr (B::NSPECIES == 3) {
-        sw.update_counts(pf.ent[q], pf.x0[q], pf.x1[q], acc);
-      } else {
-        int o;
-        int F[B::NFEAT];
-        sw.gather(pf.ent[q], o, F);
-        sw.decide(pf.ent[q], pf.x0[q], pf.x1[q], o, F, acc);
-      }
+      int o;
+      int F[B::NFEAT];
+      sw.gather(pf.ent[q], o, F);
+      sw.decide(pf.ent[q], pf.x0[q], pf.x1[q], o, F, acc);
     }
 #pragma unroll 1
   for (int e = e0 + PRE * NT; e < e_end; e += NT) {
     const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
     const uint32_t ent = __ldg(entries + e);
-    if constexpr (B::NSPECIES == 3) {
-      sw.update_counts(ent, philox_word(x, ent >> 30), x.y, acc);
-    } else {
-      int o;
-      int F[B::NFEAT];
-      sw.gather(ent, o, F);
-      sw.decide(ent, philox_word(x, ent >> 30), x.y, o, F, acc);
-    }
+    int o;
+    int F[B::NFEAT];
+    sw.gather(ent, o, F);
+    sw.decide(ent, philox_word(x, ent >> 30), x.y, o, F, acc);
   }
 }
 
@@ -437,7 +491,7 @@ __device__ __forceinline__ void load_dmu(const CeChainParams* cp, float* dmu32, 
   }
 }
 
-template <class B, int NT>
+template <class B, int NT, int GROUP = kSitesOne>
 __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__ CeSweepArgs<B::NFEAT> A) {
   constexpr int NS = B::NSPECIES;
   constexpr int NSLOT = CeSlots<B::NCLASS>::N;
@@ -525,7 +579,7 @@ __global__ void __launch_bounds__(NT, 1) ce_sweep_kernel(const __grid_constant__
     const uint32_t pass_g = (uint32_t)(A.pass0 + pass);
 #pragma unroll 1
     for (int c = 0; c < g.n_colors; ++c) {
-      sweep_phase<B, NT, PRE>(sw, pf, cstart, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
+      sweep_phase<B, NT, PRE, GROUP>(sw, pf, cstart, c, g.entries, g.site_l, pass_g, chain_id, key0, key1, acc);
       const bool last = (c + 1 == g.n_colors);
       if (S > 1) {
         // arrive, draw the next phase's random numbers while others finish, then wait
