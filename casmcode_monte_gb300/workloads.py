@@ -17,6 +17,12 @@
     initial occupations, all swept in one launch of the persistent pool kernel; compared
     with running the same jobs one launch per job (ChainBatch, one chain) on a sample.
 
+``python -m casmcode_monte_gb300.workloads sweep --kind fcc_ternary --L 64 --chains 8 --passes 20``
+    one chain batch of L^3 chains (seeded occupations, T spread over 600..1500 K, mu = 0)
+    on the layout the library chooses or ``--layout byte|word|grid``: 3 warm-up passes,
+    then three runs of --passes passes with L2 flushed before each; µs per pass and
+    site-attempts/s of the median run (device time of the run).
+
 Each prints one JSON line.  Inputs are seeded synthetic data of the configurations' shapes.
 """
 from __future__ import annotations
@@ -196,9 +202,42 @@ def run_serving(n_jobs: int = 20000, rate: float = 200.0, plain_sample: int = 10
             "mean_passes": float(np.mean([j.n_pass for j in st.jobs])) if st.jobs else 0.0}
 
 
+def run_sweep(kind: str = "fcc_ternary", L: int = 64, n_chains: int = 8, n_passes: int = 20,
+              layout: str = "auto", seed: int = 4) -> dict:
+    import torch
+
+    model = clex.ClexModel(kind, clex.make_eci(kind, seed))
+    rng = np.random.default_rng(1)
+    occ = np.stack([clex.random_occupation(model.n_species, L**3, rng) for _ in range(n_chains)])
+    T = np.linspace(600.0, 1500.0, n_chains)
+    mu = np.zeros((n_chains, model.n_species - 1))
+    seeds = np.arange(1, n_chains + 1, dtype=np.uint64)
+    b = clex.ChainBatch(model, (L, L, L), occ, T, mu, seeds)
+    if layout != "auto":
+        b.set_layout(layout)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    b.run(3, want_output=False)
+    ms = []
+    for _ in range(3):
+        flush.add_(1)  # 256 MB written: L2 flushed
+        torch.cuda.synchronize()
+        b.run(n_passes, want_output=False)
+        ms.append(b.last_kernel_ms())
+    m = float(np.median(ms))
+    r = {"workload": f"sweep_{kind}_{L}^3_x{n_chains}", "layout": b.layout, "ctas_per_chain": b.ctas_per_chain,
+         "threads": b.threads, "colors": b.n_colors, "passes": n_passes, "ms": ms,
+         "us_per_pass": 1e3 * m / n_passes, "site_attempts_per_s": n_chains * L**3 * n_passes / (m * 1e-3)}
+    b.close()
+    return r
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("workload", choices=["batched", "precision", "serving"])
+    ap.add_argument("workload", choices=["batched", "precision", "serving", "sweep"])
+    ap.add_argument("--kind", default="fcc_ternary", choices=["fcc_binary", "fcc_ternary"])
+    ap.add_argument("--L", type=int, default=64)
+    ap.add_argument("--layout", default="auto", choices=["auto", "byte", "word", "word_pipelined",
+                                                         "word_specialised", "grid"])
     ap.add_argument("--jobs", type=int, default=20000)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--chains", type=int, default=4096)
@@ -212,6 +251,8 @@ def main(argv=None):
         r = run_precision(n_passes=a.passes if a.passes != 500 else 5000)
     elif a.workload == "serving":
         r = run_serving(a.jobs, a.rate, a.plain_sample, precision="fp32" if a.precision == "fp64" else a.precision)
+    elif a.workload == "sweep":
+        r = run_sweep(a.kind, a.L, a.chains if a.chains != 4096 else 8, a.passes if a.passes != 500 else 20, a.layout)
     print(json.dumps(r), flush=True)
 
 
