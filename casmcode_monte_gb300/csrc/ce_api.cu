@@ -67,6 +67,7 @@ struct mg_ce_batch {
   // mg_ce_batch_corr and the per-pass outputs of runs of up to kOutPasses passes
   unsigned char* dblock = nullptr;
   size_t dblock_bytes = 0;      // size of the (possibly cached, larger) block
+  int dev = 0;                   // device current at creation (owner of the block)
   unsigned int* dbad = nullptr;  // occupant codes out of range found by the creation check
   int8_t* docc = nullptr;
   mg::CeChainParams* dcp = nullptr;
@@ -300,7 +301,7 @@ bool occupants_in_range(const int8_t* occ, long long n, int n_species) {
 void free_batch(mg_ce_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
-  mg::host::cached_free(b->dblock, b->dblock_bytes);
+  mg::host::cached_free(b->dblock, b->dblock_bytes, b->dev);
   cudaFree(b->dgrid);
   if (b->dout_own) cudaFree(b->dout);
   if (b->ev0) cudaEventDestroy(b->ev0);
@@ -776,6 +777,7 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   cudaError_t e;
 #define MGX(expr, what) \
   if ((e = (expr)) != cudaSuccess) return fail(e, what)
+  MGX(cudaGetDevice(&b->dev), "device");
   MGX(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
   MGX(cudaEventCreate(&b->ev0), "event");
   MGX(cudaEventCreate(&b->ev1), "event");

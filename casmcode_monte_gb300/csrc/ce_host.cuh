@@ -169,10 +169,10 @@ inline cudaError_t cached_malloc(void** p, size_t bytes, size_t* got) {
   return cudaMalloc(p, bytes);
 }
 
-inline void cached_free(void* p, size_t bytes) {
+// (dev: the device the block was allocated on, which need not be the current one)
+inline void cached_free(void* p, size_t bytes, int dev) {
   if (!p) return;
-  int dev = 0;
-  if (cudaGetDevice(&dev) == cudaSuccess) {
+  {
     BlockCache& c = block_cache();
     std::lock_guard<std::mutex> lk(c.mu);
     if (c.blocks.size() < kCacheBlocks && c.total + bytes <= kCacheBytes) {
