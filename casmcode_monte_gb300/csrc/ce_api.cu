@@ -287,6 +287,7 @@ bool make_model(int kind, const double* eci, int n, mg_ce_model* m, std::string&
     m->w32.push_back((float)w);
   }
   mg::host::quantise_weights(m);
+  mg::host::set_count_weights(m);
   return true;
 }
 

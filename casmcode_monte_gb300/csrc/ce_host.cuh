@@ -99,6 +99,10 @@ struct mg_ce_model {
   std::vector<int32_t> wq;
   int qshift = 0;
   double qerr = 0.0, qmax = 0.0;
+  // ternary basis: weights of the monomial counts in the quantised energy sums,
+  // sum_k wq[k] F_k = cgc[b] + sum_j cw[b][j] M_j (int32 modulo 2^32), set with wq
+  int32_t cw[2][mg::kMaxCounts] = {};
+  int32_t cgc[2] = {};
 };
 
 namespace mg {
@@ -234,22 +238,27 @@ inline void fill_weights(const mg_ce_model* m, CeWeights<NF>& w) {
     w.w64[k] = m->w64[k];
   }
   w.qscale = (float)std::ldexp(1.0, -m->qshift);
-  // ternary: energy-sum weights of the monomial counts (int32 modulo 2^32, like the sums)
+  std::memcpy(w.cw, m->cw, sizeof(w.cw));
+  std::memcpy(w.cgc, m->cgc, sizeof(w.cgc));
+}
+
+// The count weights of a ternary model (once, when its quantised weights are set: the
+// constexpr coefficient tables are cheap in device code, not in a host loop per launch)
+inline void set_count_weights(mg_ce_model* m) {
   for (int b = 0; b < 2; ++b) {
-    w.cgc[b] = 0;
-    for (int j = 0; j < kMaxCounts; ++j) w.cw[b][j] = 0;
+    m->cgc[b] = 0;
+    for (int j = 0; j < kMaxCounts; ++j) m->cw[b][j] = 0;
   }
-  if (m->kind == 1 && NF == FccTernary::NFEAT) {
-    long long W[2][FccTernary::NCOUNT] = {}, gc[2] = {};
-    for (int k = 0; k < FccTernary::NFEAT; ++k) {
-      const int b = FccTernary::feat_b(k);
-      gc[b] += (long long)m->wq[k] * FccTernary::tq_const(k);
-      for (int j = 0; j < FccTernary::NCOUNT; ++j) W[b][j] += (long long)m->wq[k] * FccTernary::tq_coef(k, j);
-    }
-    for (int b = 0; b < 2; ++b) {
-      w.cgc[b] = (int)(uint32_t)(unsigned long long)gc[b];
-      for (int j = 0; j < FccTernary::NCOUNT; ++j) w.cw[b][j] = (int)(uint32_t)(unsigned long long)W[b][j];
-    }
+  if (m->kind != 1) return;
+  long long W[2][FccTernary::NCOUNT] = {}, gc[2] = {};
+  for (int k = 0; k < FccTernary::NFEAT; ++k) {
+    const int b = FccTernary::feat_b(k);
+    gc[b] += (long long)m->wq[k] * FccTernary::tq_const(k);
+    for (int j = 0; j < FccTernary::NCOUNT; ++j) W[b][j] += (long long)m->wq[k] * FccTernary::tq_coef(k, j);
+  }
+  for (int b = 0; b < 2; ++b) {
+    m->cgc[b] = (int32_t)(uint32_t)(unsigned long long)gc[b];
+    for (int j = 0; j < FccTernary::NCOUNT; ++j) m->cw[b][j] = (int32_t)(uint32_t)(unsigned long long)W[b][j];
   }
 }
 
@@ -897,15 +906,9 @@ inline int launch_sweep_quad(const mg_ce_model* m, const SweepLaunch& L, int pip
 // W[b][j] = sum over features k of basis b of wq[k] tq_coef(k, j), gc[b] = sum wq[k] tq_const(k)
 // (modulo 2^32, as the kernel's int32 sums).
 inline void fill_tquad_weights(const mg_ce_model* m, TernQuadWeights<FccTernary::NCOUNT>& tw) {
-  long long W[2][FccTernary::NCOUNT] = {}, gc[2] = {};
-  for (int k = 0; k < FccTernary::NFEAT; ++k) {
-    const int b = FccTernary::feat_b(k);
-    gc[b] += (long long)m->wq[k] * FccTernary::tq_const(k);
-    for (int j = 0; j < FccTernary::NCOUNT; ++j) W[b][j] += (long long)m->wq[k] * FccTernary::tq_coef(k, j);
-  }
   for (int b = 0; b < 2; ++b) {
-    tw.gc[b] = (int)(uint32_t)(unsigned long long)gc[b];
-    for (int j = 0; j < FccTernary::NCOUNT; ++j) tw.W[b][j] = (int)(uint32_t)(unsigned long long)W[b][j];
+    tw.gc[b] = m->cgc[b];
+    for (int j = 0; j < FccTernary::NCOUNT; ++j) tw.W[b][j] = m->cw[b][j];
   }
 }
 

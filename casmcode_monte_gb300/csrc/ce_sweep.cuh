@@ -462,24 +462,24 @@ __device__ __forceinline__ void sweep_phase(const SiteSweeper<B>& sw, const Phas
       }
       if constexpr (B::NSPECIES == 3) sw.update_gathered(entries, site_l, e, n, pass, chain_id, key0, key1, acc);
     }
-    return;
-  }
+  } else if constexpr (B::NSPECIES != 3 || GROUP != kSitesFour) {
 #pragma unroll
-  for (int q = 0; q < PRE; ++q)
-    if (e0 + q * NT < e_end) {
+    for (int q = 0; q < PRE; ++q)
+      if (e0 + q * NT < e_end) {
+        int o;
+        int F[B::NFEAT];
+        sw.gather(pf.ent[q], o, F);
+        sw.decide(pf.ent[q], pf.x0[q], pf.x1[q], o, F, acc);
+      }
+#pragma unroll 1
+    for (int e = e0 + PRE * NT; e < e_end; e += NT) {
+      const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
+      const uint32_t ent = __ldg(entries + e);
       int o;
       int F[B::NFEAT];
-      sw.gather(pf.ent[q], o, F);
-      sw.decide(pf.ent[q], pf.x0[q], pf.x1[q], o, F, acc);
+      sw.gather(ent, o, F);
+      sw.decide(ent, philox_word(x, ent >> 30), x.y, o, F, acc);
     }
-#pragma unroll 1
-  for (int e = e0 + PRE * NT; e < e_end; e += NT) {
-    const U32x4 x = philox4x32_10(U32x4{__ldg(site_l + e), pass, chain_id, SWEEP_TAG}, key0, key1);
-    const uint32_t ent = __ldg(entries + e);
-    int o;
-    int F[B::NFEAT];
-    sw.gather(ent, o, F);
-    sw.decide(ent, philox_word(x, ent >> 30), x.y, o, F, acc);
   }
 }
 
