@@ -832,9 +832,14 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   // than kGridWordsPerCta words of one colour, the grid sweep (every resident CTA) is faster
   // (GB300: 128^3 on the byte layout 1261 -> 209 us per pass; 96^3, 864 words per CTA and
   // colour, stays on the cluster: 232 against 253 us)
+  // (and only when the grid gives each chain more CTAs than its cluster: 152 chains of 48^3
+  // hold one CTA each either way, and their one-CTA word layout is twice as fast)
   if (rc == MG_OK && m->kind == 1 && b->col->word && ctas_per_chain == 0 &&
-      (b->layout == 0 || (b->layout == 1 && b->max_words > kGridWordsPerCta)))
-    (void)setup_layout(b, 4);  // refused (too many chains to be resident): stays where it is
+      (b->layout == 0 || (b->layout == 1 && b->max_words > kGridWordsPerCta))) {
+    int resident = 0;
+    if (mg::host::tgrid_resident_ctas(&resident) == MG_OK && resident / n_chains > b->S)
+      (void)setup_layout(b, 4);  // refused (too many chains to be resident): stays where it is
+  }
   if (rc != MG_OK) {
     free_batch(b);
     return rc;

@@ -131,3 +131,13 @@ def test_large_ternary_chain_chooses_grid(gpu_lib):
     assert np.array_equal(g.occupation(), w.occupation())
     g.close()
     w.close()
+
+
+def test_many_large_ternary_chains_stay_on_one_cta_each(gpu_lib):
+    """152 chains of 48^3 (1728 words per CTA and colour on one CTA each) would get one CTA each
+    from the grid sweep too: the batch keeps the one-CTA word layout."""
+    L = (48, 48, 48)
+    model, occ, T, mu, seeds = _setup(L, 152, seed=3)
+    b = clex.ChainBatch(model, L, occ, T, mu, seeds)
+    assert b.layout == "word" and b.ctas_per_chain == 1
+    b.close()
