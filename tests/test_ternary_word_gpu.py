@@ -83,3 +83,14 @@ def test_ternary_word_full_size_tracks_correlations(gpu_lib):
     assert np.array_equal(w.corr(), s.int_corr[-1])
     w.close()
     b.close()
+
+
+def test_sweep_probe_reports_layout_and_rate(gpu_lib):
+    """The sweep probe of the workloads module (used for the ternary ncu captures) runs a
+    small batch on the layout asked for and reports a positive rate."""
+    from casmcode_monte_gb300 import workloads
+
+    for layout in ("auto", "byte", "grid"):
+        r = workloads.run_sweep("fcc_ternary", L=16, n_chains=2, n_passes=2, layout=layout)
+        assert r["layout"] == ("word" if layout == "auto" else layout)
+        assert r["site_attempts_per_s"] > 0 and len(r["ms"]) == 3
