@@ -25,8 +25,19 @@ constexpr int kMaxGeoms = 1024;
 // CTA classes: chains are swept by 1, 2, 4, 8 or 16 CTAs (the smallest whose slab fits)
 constexpr int kClasses = 5;
 constexpr int kClassS[kClasses] = {1, 2, 4, 8, 16};
-// launch groups: (CTA class, layout) with layout 0 = one site per byte, 1 = four per word
-constexpr int kGroups = 2 * kClasses;
+// launch groups: (CTA class, layout) with layout 0 = one site per byte, 1 = four per word,
+// and the small byte-layout chains of class 1 whose padded lattice fits kWarpWindow bytes,
+// swept one chain per warp (ce_pool_warp_kernel)
+constexpr int kWarpGroup = 2 * kClasses;
+constexpr int kGroups = 2 * kClasses + 1;
+constexpr int kWarpWindow = 6144;
+constexpr int kWarpsBinary = 16, kWarpsTernary = 12;
+
+// bytes of a chain's padded byte-layout lattice, rounded to 16
+inline int warp_window(int L0, int L1, int L2) {
+  const long long w = (long long)(L0 + 2 * mg::CE_HALO) * (L1 + 2 * mg::CE_HALO) * (L2 + 2 * mg::CE_HALO);
+  return (int)std::min<long long>((w + 15) & ~15LL, 1LL << 30);
+}
 
 struct PoolGeom {
   int L0 = 0, L1 = 0, L2 = 0, S = 1, layout = 0, n_colors = 0;
@@ -241,6 +252,40 @@ const void* pool_word_kernel(int* nt) {
     *nt = NT_QUAD;
     return (const void*)mg::ce_pool_quad_kernel<B, NT_QUAD, CLUSTER>;
   }
+}
+
+// the warp-per-chain kernel over the small byte-layout chains (win: the largest padded
+// lattice of them, bytes)
+template <class B>
+int launch_pool_warp(mg_ce_pool* p, int item0, int n_items, int n_passes, int win) {
+  constexpr int NW = B::NSPECIES == 3 ? kWarpsTernary : kWarpsBinary;
+  mg::CePoolArgs<B::NFEAT> A;
+  A.geoms = p->dgeoms;
+  A.items = p->ditems + item0;
+  A.n_items = n_items;
+  A.next_item = p->dcounter + kWarpGroup;
+  mg::host::fill_weights(p->model, A.w);
+  A.cp = p->dcp;
+  A.occ = p->darena;
+  A.n_passes = n_passes;
+  A.precision = p->precision;
+  A.out = p->dout;
+  const void* kern = (const void*)mg::ce_pool_warp_kernel<B, NW>;
+  const size_t smem = (size_t)NW * win;
+  MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0, dev = 0, sms = 0;
+  MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * NW, smem));
+  MG_CUDA_TRY(cudaGetDevice(&dev));
+  MG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  if (per_sm < 1) {
+    set_error("Error in mg_ce_pool_run: the warp kernel does not fit on an SM");
+    return MG_ERR_INVALID;
+  }
+  const int grid = std::max(1, std::min((n_items + NW - 1) / NW, per_sm * sms));
+  void* args[] = {(void*)&A, (void*)&win};
+  MG_CUDA_TRY(cudaLaunchKernel(kern, dim3(grid), dim3(32 * NW), args, smem, p->cls_stream[kWarpGroup]));
+  MG_CUDA_TRY(cudaGetLastError());
+  return MG_OK;
 }
 
 template <class B, int NT>
@@ -662,7 +707,10 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
   }
   // grouped by launch group (CTA class, layout), largest chains first within a group
   // (LPT work queue)
-  auto group = [&](const PoolSlot& x) { return 2 * x.cls + x.layout; };
+  auto group = [&](const PoolSlot& x) {
+    if (x.cls == 0 && x.layout == 0 && warp_window(x.L0, x.L1, x.L2) <= kWarpWindow) return kWarpGroup;
+    return 2 * x.cls + x.layout;
+  };
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     const PoolSlot &x = p->slots[slots[a]], &y = p->slots[slots[b]];
     if (group(x) != group(y)) return group(x) < group(y);
@@ -677,7 +725,9 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
     const PoolSlot& s = p->slots[slots[i]];
     items[t] = mg::PoolItem{s.geom, slots[i], s.offset, (long long)i * n_passes * nslot, s.pass};
     first[group(s)] = t;
-    smem[group(s)] = std::max(smem[group(s)], layout_smem(s.layout, s.L0, s.L1, s.L2, kClassS[s.cls]));
+    smem[group(s)] = std::max(smem[group(s)], group(s) == kWarpGroup
+                                                  ? (size_t)warp_window(s.L0, s.L1, s.L2)
+                                                  : layout_smem(s.layout, s.L0, s.L1, s.L2, kClassS[s.cls]));
   }
   for (int c = kGroups - 1; c >= 0; --c) first[c] = std::min(first[c], first[c + 1]);
   const size_t need = (size_t)n * n_passes * nslot;
@@ -700,9 +750,14 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
     ++p->last_launches;
     MG_CUDA_TRY(cudaStreamWaitEvent(p->cls_stream[c], p->ev0, 0));
     const int cls = c / 2, layout = c % 2;
-    int rc = p->model->kind == 0
-                 ? launch_pool<mg::FccBinary, mg::NT_BINARY>(p, cls, layout, first[c], cnt, n_passes, smem[c])
-                 : launch_pool<mg::FccTernary, mg::NT_TERNARY>(p, cls, layout, first[c], cnt, n_passes, smem[c]);
+    int rc;
+    if (c == kWarpGroup)
+      rc = p->model->kind == 0 ? launch_pool_warp<mg::FccBinary>(p, first[c], cnt, n_passes, (int)smem[c])
+                               : launch_pool_warp<mg::FccTernary>(p, first[c], cnt, n_passes, (int)smem[c]);
+    else
+      rc = p->model->kind == 0
+               ? launch_pool<mg::FccBinary, mg::NT_BINARY>(p, cls, layout, first[c], cnt, n_passes, smem[c])
+               : launch_pool<mg::FccTernary, mg::NT_TERNARY>(p, cls, layout, first[c], cnt, n_passes, smem[c]);
     if (rc != MG_OK) return rc;
     MG_CUDA_TRY(cudaEventRecord(p->cls_done[c], p->cls_stream[c]));
     MG_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->cls_done[c], 0));

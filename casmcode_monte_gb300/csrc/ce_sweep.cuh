@@ -2029,6 +2029,103 @@ __global__ void __launch_bounds__(NT, 1) ce_pool_kernel(const __grid_constant__ 
   }
 }
 
+// Persistent pool kernel for small byte-layout chains, one warp per chain: every warp of
+// the CTA takes chains from the work queue on its own and sweeps each in its own window of
+// win_bytes bytes of shared memory (padded lattice, periodic borders), the lanes sharing a
+// colour's sites and __syncwarp between colours.  A chain of 8^3 sites has 32 sites per
+// colour: a CTA per chain would leave all but one warp idle behind CTA barriers.  The site
+// update and the per-pass outputs are those of ce_pool_kernel.
+template <class B, int NW>
+__global__ void __launch_bounds__(32 * NW, 1)
+    ce_pool_warp_kernel(const __grid_constant__ CePoolArgs<B::NFEAT> A, int win_bytes) {
+  constexpr int NS = B::NSPECIES;
+  constexpr int NSLOT = CeSlots<B::NCLASS>::N;
+  extern __shared__ __align__(16) int8_t s_all[];
+  __shared__ float dmu32_sm[NW][NS * NS];
+  __shared__ double dmu64_sm[NW][NS * NS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int8_t* s = s_all + (size_t)warp * win_bytes;
+
+#pragma unroll 1
+  while (true) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(A.next_item, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= A.n_items) break;
+    const PoolItem item = A.items[it];
+    const PoolGeometry g = A.geoms[item.geom];
+    const int L0 = g.L0, L1 = g.L1, L2 = g.L2;
+    const int PX = L0 + 2 * B::HALO, PY = L1 + 2 * B::HALO, PXY = PX * PY;
+    int8_t* gocc = A.occ + item.occ_offset;
+    for (int idx = lane; idx < PXY * (L2 + 2 * B::HALO); idx += 32) {
+      const int ip = idx % PX, jp = (idx / PX) % PY, kp = idx / PXY;
+      int i = ip - B::HALO, j = jp - B::HALO, k = kp - B::HALO;
+      i = (i < 0) ? i + L0 : (i >= L0 ? i - L0 : i);
+      j = (j < 0) ? j + L1 : (j >= L1 ? j - L1 : j);
+      k = (k < 0) ? k + L2 : (k >= L2 ? k - L2 : k);
+      s[idx] = B::code_of_occ(gocc[i + (long long)L0 * (j + (long long)L1 * k)]);
+    }
+    const CeChainParams* cpg = A.cp + item.param;
+    if (lane < NS * NS) {
+      dmu32_sm[warp][lane] = cpg->dmu32[lane];
+      dmu64_sm[warp][lane] = cpg->dmu64[lane];
+    }
+    const uint32_t key0 = cpg->key0, key1 = cpg->key1, chain_id = cpg->chain_id;
+    SiteSweeper<B> sw;
+    sw.s = s;
+    sw.s_prev = s;
+    sw.s_next = s;
+    sw.PX = PX;
+    sw.PXY = PXY;
+    sw.dI = L0;
+    sw.dJ = L1 * PX;
+    sw.dKp = L2 * PXY;
+    sw.dKn = L2 * PXY;
+    sw.dmu32 = dmu32_sm[warp];
+    sw.dmu64 = dmu64_sm[warp];
+    sw.w = &A.w;
+    sw.beta = cpg->beta;
+    sw.beta_log2e = cpg->beta_log2e;
+    sw.dtol = cpg->dtol;
+    sw.eps = cpg->eps;
+    sw.precision = A.precision;
+    int acc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) acc[q] = 0;
+    long long* out = A.out + item.out_offset;
+    __syncwarp();
+#pragma unroll 1
+    for (int pass = 0; pass < A.n_passes; ++pass) {
+      const uint32_t pass_g = (uint32_t)(item.pass0 + pass);
+#pragma unroll 1
+      for (int c = 0; c < g.n_colors; ++c) {
+#pragma unroll 1
+        for (int e = g.color_start[c] + lane; e < g.color_start[c + 1]; e += 32) {
+          const U32x4 x = philox4x32_10(U32x4{__ldg(g.site_l + e), pass_g, chain_id, SWEEP_TAG}, key0, key1);
+          const uint32_t ent = __ldg(g.entries + e);
+          int o;
+          int F[B::NFEAT];
+          sw.gather(ent, o, F);
+          sw.decide(ent, philox_word(x, ent >> 30), x.y, o, F, acc);
+        }
+        __syncwarp();
+      }
+#pragma unroll
+      for (int q = 0; q < NSLOT; ++q) {
+        const int v = warp_sum(acc[q]);
+        if (lane == 0) out[(size_t)pass * NSLOT + q] = v;
+        acc[q] = 0;
+      }
+    }
+    for (int idx = lane; idx < L0 * L1 * L2; idx += 32) {
+      const int i = idx % L0, j = (idx / L0) % L1, k = idx / (L0 * L1);
+      const int pidx = (i + B::HALO) + PX * ((j + B::HALO) + PY * (k + B::HALO));
+      gocc[i + (long long)L0 * (j + (long long)L1 * k)] = (int8_t)B::occ_of_code(s[pidx]);
+    }
+    __syncwarp();
+  }
+}
+
 // Persistent pool kernel for chains too large for one CTA: each thread-block cluster of
 // S CTAs takes chains from the work queue (rank 0 draws the item and writes it into every
 // CTA's shared memory) and sweeps them as the batch kernel does (slabs, halo copies
