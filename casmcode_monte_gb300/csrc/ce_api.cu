@@ -831,9 +831,9 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
   // memory (the batch fell back to the byte layout) or a CTA of the cluster layout holds more
   // than kGridWordsPerCta words of one colour, the grid sweep (every resident CTA) is faster
   // (GB300: 128^3 on the byte layout 1261 -> 209 us per pass; 96^3, 864 words per CTA and
-  // colour, stays on the cluster: 232 against 253 us)
-  // (and only when the grid gives each chain more CTAs than its cluster: 152 chains of 48^3
-  // hold one CTA each either way, and their one-CTA word layout is twice as fast)
+  // colour, stays on the cluster: 232 against 253 us) -- provided the grid gives each chain
+  // more CTAs than its cluster (152 chains of 48^3 hold one CTA each either way, and their
+  // one-CTA word layout is twice as fast as the grid sweep)
   if (rc == MG_OK && m->kind == 1 && b->col->word && ctas_per_chain == 0 &&
       (b->layout == 0 || (b->layout == 1 && b->max_words > kGridWordsPerCta))) {
     int resident = 0;
