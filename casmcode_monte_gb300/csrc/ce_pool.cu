@@ -29,8 +29,13 @@ constexpr int kClassS[kClasses] = {1, 2, 4, 8, 16};
 // and the small byte-layout chains of class 1 whose padded lattice fits kWarpWindow bytes,
 // swept one chain per warp (ce_pool_warp_kernel)
 constexpr int kWarpGroup = 2 * kClasses;
-constexpr int kGroups = 2 * kClasses + 1;
+// one-CTA word-layout chains of the binary basis whose lattice fits kSmallWindow bytes
+// launch apart from the larger ones (a launch's shared memory is its largest chain's) with
+// a kernel built for two CTAs per SM (80 registers), so that two such chains share an SM
+constexpr int kSmallWordGroup = 2 * kClasses + 1;
+constexpr int kGroups = 2 * kClasses + 2;
 constexpr int kWarpWindow = 6144;
+constexpr size_t kSmallWindow = 100 * 1024;
 constexpr int kWarpsBinary = 16, kWarpsTernary = 12;
 
 // bytes of a chain's padded byte-layout lattice, rounded to 16
@@ -244,12 +249,13 @@ int geometry(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan& sp, int* ou
 // the word-layout pool kernel of basis B (binary: byte-parallel features; ternary: monomial
 // counts, whose launch carries the count weights too)
 template <class B, bool CLUSTER>
-const void* pool_word_kernel(int* nt) {
+const void* pool_word_kernel(int* nt, bool two_per_sm = false) {
   if constexpr (B::NSPECIES == 3) {
     *nt = NT_TQUAD;
     return (const void*)mg::ce_pool_tquad_kernel<B, NT_TQUAD, CLUSTER>;
   } else {
     *nt = NT_QUAD;
+    if (two_per_sm && !CLUSTER) return (const void*)mg::ce_pool_quad_kernel<B, NT_QUAD, false, 2>;
     return (const void*)mg::ce_pool_quad_kernel<B, NT_QUAD, CLUSTER>;
   }
 }
@@ -289,14 +295,14 @@ int launch_pool_warp(mg_ce_pool* p, int item0, int n_items, int n_passes, int wi
 }
 
 template <class B, int NT>
-int launch_pool(mg_ce_pool* p, int cls, int layout, int item0, int n_items, int n_passes, size_t smem) {
+int launch_pool(mg_ce_pool* p, int grp, int cls, int layout, int item0, int n_items, int n_passes, size_t smem) {
   mg::CeTPoolArgs<B::NFEAT, mg::FccTernary::NCOUNT> TA;  // the binary kernels read TA.p only
   mg::CePoolArgs<B::NFEAT>& A = TA.p;
   if constexpr (B::NSPECIES == 3) mg::host::fill_tquad_weights(p->model, TA.tw);
   A.geoms = p->dgeoms;
   A.items = p->ditems + item0;
   A.n_items = n_items;
-  A.next_item = p->dcounter + 2 * cls + layout;
+  A.next_item = p->dcounter + grp;
   mg::host::fill_weights(p->model, A.w);
   A.cp = p->dcp;
   A.occ = p->darena;
@@ -304,11 +310,11 @@ int launch_pool(mg_ce_pool* p, int cls, int layout, int item0, int n_items, int 
   A.precision = p->precision;
   A.out = p->dout;
   const int S = kClassS[cls];
-  cudaStream_t st = p->cls_stream[2 * cls + layout];
+  cudaStream_t st = p->cls_stream[grp];
   if (S == 1) {
     const void* kern = (const void*)mg::ce_pool_kernel<B, NT>;
     int nt = NT;
-    if (layout == 1) kern = pool_word_kernel<B, false>(&nt);
+    if (layout == 1) kern = pool_word_kernel<B, false>(&nt, grp == kSmallWordGroup);
     MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0, dev = 0, sms = 0;
     MG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, smem));
@@ -709,6 +715,8 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
   // (LPT work queue)
   auto group = [&](const PoolSlot& x) {
     if (x.cls == 0 && x.layout == 0 && warp_window(x.L0, x.L1, x.L2) <= kWarpWindow) return kWarpGroup;
+    if (p->model->kind == 0 && x.cls == 0 && x.layout == 1 && layout_smem(1, x.L0, x.L1, x.L2, 1) <= kSmallWindow)
+      return kSmallWordGroup;
     return 2 * x.cls + x.layout;
   };
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
@@ -742,22 +750,29 @@ int mg_ce_pool_run(mg_ce_pool* p, const int32_t* slots, int n, int n_passes, lon
   MG_CUDA_TRY(cudaMemsetAsync(p->dout, 0, sizeof(long long) * need, p->stream));
   MG_CUDA_TRY(cudaEventRecord(p->ev0, p->stream));
   p->last_launches = 0;
-  // one launch per CTA class, each on its own stream after the set-up copies; the
-  // largest class first so that its long chains start while the others fill in
-  for (int c = kGroups - 1; c >= 0; --c) {
+  // one launch per group, each on its own stream after the set-up copies; the largest
+  // class first so that its long chains start while the others fill in, the small-chain
+  // groups last
+  int launch_order[kGroups];
+  for (int i = 0; i < 2 * kClasses; ++i) launch_order[i] = 2 * kClasses - 1 - i;
+  launch_order[2 * kClasses] = kSmallWordGroup;
+  launch_order[2 * kClasses + 1] = kWarpGroup;
+  static_assert(kGroups == 2 * kClasses + 2, "the launch order covers every group");
+  for (int oi = 0; oi < kGroups; ++oi) {
+    const int c = launch_order[oi];
     const int cnt = first[c + 1] - first[c];
     if (cnt <= 0) continue;
     ++p->last_launches;
     MG_CUDA_TRY(cudaStreamWaitEvent(p->cls_stream[c], p->ev0, 0));
-    const int cls = c / 2, layout = c % 2;
+    const int cls = c == kSmallWordGroup ? 0 : c / 2, layout = c == kSmallWordGroup ? 1 : c % 2;
     int rc;
     if (c == kWarpGroup)
       rc = p->model->kind == 0 ? launch_pool_warp<mg::FccBinary>(p, first[c], cnt, n_passes, (int)smem[c])
                                : launch_pool_warp<mg::FccTernary>(p, first[c], cnt, n_passes, (int)smem[c]);
     else
       rc = p->model->kind == 0
-               ? launch_pool<mg::FccBinary, mg::NT_BINARY>(p, cls, layout, first[c], cnt, n_passes, smem[c])
-               : launch_pool<mg::FccTernary, mg::NT_TERNARY>(p, cls, layout, first[c], cnt, n_passes, smem[c]);
+               ? launch_pool<mg::FccBinary, mg::NT_BINARY>(p, c, cls, layout, first[c], cnt, n_passes, smem[c])
+               : launch_pool<mg::FccTernary, mg::NT_TERNARY>(p, c, cls, layout, first[c], cnt, n_passes, smem[c]);
     if (rc != MG_OK) return rc;
     MG_CUDA_TRY(cudaEventRecord(p->cls_done[c], p->cls_stream[c]));
     MG_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->cls_done[c], 0));

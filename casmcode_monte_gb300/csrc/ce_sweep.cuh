@@ -2251,8 +2251,8 @@ __global__ void __launch_bounds__(NT, 1) ce_pool_cluster_kernel(const __grid_con
 // (CLUSTER = false, one CTA per chain) or ce_pool_cluster_kernel (CLUSTER = true, S CTAs
 // per chain), with the lattice held four sites per word (see ce_sweep_quad_kernel).
 // Per-pass outputs are accumulated with atomics (the host zeroes them).
-template <class B, int NT, bool CLUSTER>
-__global__ void __launch_bounds__(NT, 1) ce_pool_quad_kernel(const __grid_constant__ CePoolArgs<B::NFEAT> A) {
+template <class B, int NT, bool CLUSTER, int MINB = 1>
+__global__ void __launch_bounds__(NT, MINB) ce_pool_quad_kernel(const __grid_constant__ CePoolArgs<B::NFEAT> A) {
   constexpr int NS = B::NSPECIES;
   constexpr int NSLOT = CeSlots<B::NCLASS>::N;
   extern __shared__ __align__(16) uint32_t sq[];
