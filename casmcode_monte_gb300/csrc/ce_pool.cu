@@ -36,6 +36,7 @@ constexpr int kSmallWordGroup = 2 * kClasses + 1;
 constexpr int kGroups = 2 * kClasses + 2;
 constexpr int kWarpWindow = 6144;
 constexpr size_t kSmallWindow = 100 * 1024;
+constexpr size_t kTwoPerSm = 110 * 1024;  // two CTAs' shared memory per SM (227 KB opt-in)
 constexpr int kWarpsBinary = 16, kWarpsTernary = 12;
 
 // bytes of a chain's padded byte-layout lattice, rounded to 16
@@ -191,6 +192,11 @@ int shape_plan(mg_ce_pool* p, int L0, int L1, int L2, const ShapePlan** out) {
   if (quad_eligible(p->model->kind, L0, L1, L2, sp.color.data())) {
     sp.cls = fit(1);
     if (sp.cls >= 0) sp.layout = 1;
+    // binary word chains too large for two one-CTA lattices per SM: a 2-CTA cluster whose
+    // halves fit two per SM (kTwoPerSm) keeps twice the warps of one CTA per SM
+    if (sp.cls == 0 && p->model->kind == 0 && layout_smem(1, L0, L1, L2, 1) > kSmallWindow && slabs_ok(1, L1, L2, 2) &&
+        layout_smem(1, L0, L1, L2, 2) <= kTwoPerSm)
+      sp.cls = 1;
   }
   if (sp.cls < 0) sp.cls = fit(0);
   if (sp.cls < 0) {
@@ -255,7 +261,7 @@ const void* pool_word_kernel(int* nt, bool two_per_sm = false) {
     return (const void*)mg::ce_pool_tquad_kernel<B, NT_TQUAD, CLUSTER>;
   } else {
     *nt = NT_QUAD;
-    if (two_per_sm && !CLUSTER) return (const void*)mg::ce_pool_quad_kernel<B, NT_QUAD, false, 2>;
+    if (two_per_sm) return (const void*)mg::ce_pool_quad_kernel<B, NT_QUAD, CLUSTER, 2>;
     return (const void*)mg::ce_pool_quad_kernel<B, NT_QUAD, CLUSTER>;
   }
 }
@@ -332,7 +338,7 @@ int launch_pool(mg_ce_pool* p, int grp, int cls, int layout, int item0, int n_it
   }
   const void* kern = (const void*)mg::ce_pool_cluster_kernel<B, NT>;
   int nt = NT;
-  if (layout == 1) kern = pool_word_kernel<B, true>(&nt);
+  if (layout == 1) kern = pool_word_kernel<B, true>(&nt, smem <= kTwoPerSm);
   MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (S > 8) MG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};

@@ -78,7 +78,8 @@ def test_pool_admission_by_footprint(gpu_lib):
 
 
 @pytest.mark.parametrize("kind,L", [("fcc_binary", (64, 64, 64)), ("fcc_binary", (72, 72, 72)),
-                                    ("fcc_ternary", (64, 64, 60))])
+                                    ("fcc_ternary", (64, 64, 60)), ("fcc_binary", (48, 48, 48)),
+                                    ("fcc_binary", (32, 32, 32))])
 def test_pool_large_chains_match_batch(gpu_lib, kind, L):
     """Chains too large for one CTA run in the pool's cluster classes; same trajectory as the
     (oracle-validated) batch path."""
