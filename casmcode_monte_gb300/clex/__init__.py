@@ -607,12 +607,18 @@ class ChainPool:
         _lib.check(_lib.lib().mg_ce_pool_info(self._h, C.byref(fb), C.byref(ab), C.byref(nu), C.byref(mc)))
         return {"arena_free_bytes": fb.value, "arena_bytes": ab.value, "n_used": nu.value, "max_chains": mc.value}
 
-    def run(self, slots, n_passes: int, want_output: bool = True) -> Optional[np.ndarray]:
-        """Sweep the chains in ``slots``; returns [len(slots), n_passes, n_classes+2] int64."""
+    def run(self, slots, n_passes: int, want_output: bool = True,
+            out: Optional[np.ndarray] = None) -> Optional[np.ndarray]:
+        """Sweep the chains in ``slots``; returns [len(slots), n_passes, n_classes+2] int64
+        (written into ``out`` when given, e.g. a pinned host buffer)."""
         if int(n_passes) < 0:
             raise RuntimeError("Error in mg_ce_pool_run: invalid argument")
         sl = np.ascontiguousarray(np.asarray(slots, dtype=np.int32).reshape(-1))
-        out = np.zeros((sl.size, n_passes, self.n_slots), dtype=np.int64) if want_output else None
+        if out is not None:
+            if out.dtype != np.int64 or not out.flags.c_contiguous or out.size < sl.size * n_passes * self.n_slots:
+                raise ValueError("out must be a C-contiguous int64 array of len(slots) * n_passes * (n_classes+2)")
+        elif want_output:
+            out = np.zeros((sl.size, n_passes, self.n_slots), dtype=np.int64)
         _lib.check(_lib.lib().mg_ce_pool_run(self._h, _lib.ptr(sl, C.c_int32), sl.size, int(n_passes),
                                              _lib.ptr(out, C.c_longlong) if out is not None else None))
         return out
