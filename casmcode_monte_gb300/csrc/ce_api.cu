@@ -72,6 +72,7 @@ struct mg_ce_batch {
   int8_t* docc = nullptr;
   mg::CeChainParams* dcp = nullptr;
   long long* dcorr = nullptr;
+  long long corr_pass = -1;  // pass count at which dcorr holds the current sums (-1: none)
   std::vector<mg::CeChainParams> hcp;
   std::shared_ptr<const DeviceLists> lists;
   int* dcstart = nullptr;
@@ -305,10 +306,9 @@ void free_batch(mg_ce_batch* b) {
   mg::host::cached_free(b->dblock, b->dblock_bytes, b->dev);
   cudaFree(b->dgrid);
   if (b->dout_own) cudaFree(b->dout);
-  if (b->ev0) cudaEventDestroy(b->ev0);
-  if (b->ev1) cudaEventDestroy(b->ev1);
+
   for (cudaEvent_t e : b->rev) cudaEventDestroy(e);
-  if (b->stream) cudaStreamDestroy(b->stream);
+  mg::host::release_stream_set(mg::host::StreamSet{b->dev, b->stream, b->ev0, b->ev1});
   for (cudaStream_t s : b->stream_fast) cudaStreamDestroy(s);
   delete b;
 }
@@ -779,9 +779,14 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
 #define MGX(expr, what) \
   if ((e = (expr)) != cudaSuccess) return fail(e, what)
   MGX(cudaGetDevice(&b->dev), "device");
-  MGX(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
-  MGX(cudaEventCreate(&b->ev0), "event");
-  MGX(cudaEventCreate(&b->ev1), "event");
+  {
+    mg::host::StreamSet ss;
+    e = mg::host::acquire_stream_set(b->dev, &ss);
+    b->stream = ss.stream;
+    b->ev0 = ss.ev0;
+    b->ev1 = ss.ev1;
+    MGX(e, "stream");
+  }
   {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t nslot = (size_t)m->n_classes + 2;
@@ -815,6 +820,11 @@ int mg_ce_batch_create(const mg_ce_model* m, int L0, int L1, int L2, int n_chain
       free_batch(b);
       return MG_ERR_INVALID;
     }
+    // the initial correlation sums, which nearly every caller asks for next, computed while
+    // the call returns (mg_ce_batch_corr then only copies them back)
+    MGX(cudaMemsetAsync(b->dcorr, 0, sizeof(long long) * (size_t)m->n_classes * n_chains, b->stream), "memset");
+    MGX(launch_corr(m->kind, b->docc, L0, L1, L2, n_chains, b->dcorr, b->stream), "correlations");
+    b->corr_pass = 0;
   }
 #undef MGX
   // the best layout that applies; a layout can still be refused for this CTA count (shared
@@ -1173,6 +1183,7 @@ int mg_ce_batch_set_occ(mg_ce_batch* b, const int8_t* occ) {
     set_error("Error in mg_ce_batch_set_occ: occupant index out of range");
     return MG_ERR_INVALID;
   }
+  b->corr_pass = -1;
   MG_CUDA_TRY(cudaMemcpyAsync(b->docc, occ, (size_t)b->N * b->n_chains, cudaMemcpyHostToDevice, b->stream));
   MG_CUDA_TRY(cudaStreamSynchronize(b->stream));
   return MG_OK;
@@ -1185,14 +1196,18 @@ int mg_ce_batch_corr(mg_ce_batch* b, long long* out) {
   }
   const int nc = b->model->n_classes;
   long long* d = b->dcorr;
-  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(long long) * (size_t)nc * b->n_chains, b->stream);
-  if (e == cudaSuccess) e = launch_corr(b->model->kind, b->docc, b->L0, b->L1, b->L2, b->n_chains, d, b->stream);
+  cudaError_t e = cudaSuccess;
+  if (b->corr_pass != b->pass) {
+    e = cudaMemsetAsync(d, 0, sizeof(long long) * (size_t)nc * b->n_chains, b->stream);
+    if (e == cudaSuccess) e = launch_corr(b->model->kind, b->docc, b->L0, b->L1, b->L2, b->n_chains, d, b->stream);
+  }
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, sizeof(long long) * (size_t)nc * b->n_chains, cudaMemcpyDeviceToHost, b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) {
     set_error(std::string("CUDA error in mg_ce_batch_corr: ") + cudaGetErrorString(e));
     return MG_ERR_CUDA;
   }
+  b->corr_pass = b->pass;
   return MG_OK;
 }
 

@@ -188,7 +188,70 @@ inline void cached_free(void* p, size_t bytes, int dev) {
   cudaFree(p);
 }
 
+// Streams of closed batches (a non-blocking stream and two timing events each), kept per
+// device like the blocks: creating them costs more than a small job's copies
+struct StreamSet {
+  int dev;
+  cudaStream_t stream;
+  cudaEvent_t ev0, ev1;
+};
+
+struct StreamCache {
+  std::mutex mu;
+  std::vector<StreamSet> sets;
+};
+
+inline StreamCache& stream_cache() {
+  static StreamCache* c = new StreamCache();  // never destroyed, like the block cache
+  return *c;
+}
+
+inline cudaError_t acquire_stream_set(int dev, StreamSet* out) {
+  {
+    StreamCache& c = stream_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    for (size_t i = 0; i < c.sets.size(); ++i)
+      if (c.sets[i].dev == dev) {
+        *out = c.sets[i];
+        c.sets.erase(c.sets.begin() + (long)i);
+        return cudaSuccess;
+      }
+  }
+  out->dev = dev;
+  out->stream = nullptr;
+  out->ev0 = out->ev1 = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&out->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&out->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&out->ev1);
+  return e;
+}
+
+// (the stream has no work left: its batch synchronised it)
+inline void release_stream_set(const StreamSet& s) {
+  {
+    StreamCache& c = stream_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (s.stream && s.ev0 && s.ev1 && c.sets.size() < kCacheBlocks) {
+      c.sets.push_back(s);
+      return;
+    }
+  }
+  if (s.ev0) cudaEventDestroy(s.ev0);
+  if (s.ev1) cudaEventDestroy(s.ev1);
+  if (s.stream) cudaStreamDestroy(s.stream);
+}
+
 inline int release_cached_blocks() {
+  {
+    StreamCache& sc = stream_cache();
+    std::lock_guard<std::mutex> lk(sc.mu);
+    for (auto& t : sc.sets) {
+      cudaEventDestroy(t.ev0);
+      cudaEventDestroy(t.ev1);
+      cudaStreamDestroy(t.stream);
+    }
+    sc.sets.clear();
+  }
   BlockCache& c = block_cache();
   std::lock_guard<std::mutex> lk(c.mu);
   cudaError_t first = cudaSuccess;
