@@ -110,3 +110,29 @@ def test_batch_block_cache_reuse(gpu_lib):
     clex.release_cached_memory()
     torch.cuda.synchronize()
     assert torch.cuda.mem_get_info()[0] >= free1 + (2 << 20)  # the 8 x 64^3 block (2.2 MB)
+
+
+def test_batch_corr_follows_occupation_changes(gpu_lib):
+    """The initial correlation sums are computed when the batch is created; corr() must still
+    follow every change of the occupations: after set_occupation (no pass run) and after runs
+    it equals the sums of a fresh batch created on the same occupations."""
+    model = _model()
+    rng = np.random.default_rng(12)
+    L = (16, 16, 16)
+    occ = np.stack([clex.random_occupation(2, 16**3, rng) for _ in range(2)])
+    other = np.stack([clex.random_occupation(2, 16**3, rng) for _ in range(2)])
+    T, mu, seeds = [700.0, 1300.0], np.zeros((2, 1)), [5, 6]
+
+    def fresh(o):
+        f = clex.ChainBatch(model, L, o, T, mu, seeds)
+        c = f.corr()
+        f.close()
+        return c
+
+    b = clex.ChainBatch(model, L, occ, T, mu, seeds)
+    assert np.array_equal(b.corr(), fresh(occ))
+    b.set_occupation(other)
+    assert np.array_equal(b.corr(), fresh(other))
+    b.run(3)
+    assert np.array_equal(b.corr(), fresh(b.occupation()))
+    b.close()
