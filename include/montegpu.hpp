@@ -5,7 +5,9 @@
 #ifndef MONTEGPU_HPP
 #define MONTEGPU_HPP
 
+#include <array>
 #include <cstdint>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -254,6 +256,87 @@ class CeNfold {
   long long n_sites_;
   int n_slots_, n_classes_;
 };
+
+/* Many chains of any supercell shapes in one HBM arena, swept by persistent kernels
+ * (mg_ce_pool_*): the batched and served form of the per-chain run.  add / add_many throw
+ * std::runtime_error on invalid input and return -1 / an empty vector when the arena or the
+ * slots are full (MG_ERR_FULL: wait for running jobs and retry). */
+class CePool {
+ public:
+  CePool(const CeModel& m, long long arena_bytes, int max_chains, bool fp32_decisions = false)
+      : n_slots_(m.n_classes() + 2), n_classes_(m.n_classes()), n_species_(m.n_species()) {
+    mg_ce_pool* p = nullptr;
+    check(mg_ce_pool_create(m.get(), arena_bytes, max_chains, fp32_decisions ? 1 : 0, &p));
+    h_ = H(p);
+  }
+  int add(int L0, int L1, int L2, double temperature, const std::vector<double>& mu, uint64_t seed,
+          uint32_t chain_id, const std::vector<int8_t>& occ) {
+    int slot = -1;
+    const int rc = mg_ce_pool_add(h_.get(), L0, L1, L2, temperature, mu.data(), seed, chain_id, occ.data(), &slot);
+    if (rc == MG_ERR_FULL) return -1;
+    check(rc);
+    shapes_[slot] = {L0, L1, L2};
+    return slot;
+  }
+  /* n chains at once, all or none: dims [n][3], mu [n][n_species-1], occupations back to back */
+  std::vector<int32_t> add_many(const std::vector<int32_t>& dims, const std::vector<double>& temperature,
+                                const std::vector<double>& mu, const std::vector<uint64_t>& seeds,
+                                const std::vector<uint32_t>& chain_ids, const std::vector<int8_t>& occ) {
+    const int n = (int)temperature.size();
+    if (dims.size() != 3 * (size_t)n || seeds.size() != (size_t)n || chain_ids.size() != (size_t)n ||
+        mu.size() != (size_t)n * (n_species_ - 1))
+      throw std::runtime_error("Error in CePool::add_many: argument sizes do not match");
+    std::vector<int32_t> slots((size_t)n);
+    const int rc = mg_ce_pool_add_many(h_.get(), n, dims.data(), temperature.data(), mu.data(), seeds.data(),
+                                       chain_ids.data(), occ.data(), slots.data());
+    if (rc == MG_ERR_FULL) return {};
+    check(rc);
+    for (int i = 0; i < n; ++i) shapes_[slots[i]] = {dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]};
+    return slots;
+  }
+  void remove(int slot) {
+    check(mg_ce_pool_remove(h_.get(), slot));
+    shapes_.erase(slot);
+  }
+  /* per-pass outputs [slot][n_passes][n_classes + 2] in the order of `slots` */
+  std::vector<long long> run(const std::vector<int32_t>& slots, int n_passes) {
+    std::vector<long long> out(slots.size() * (size_t)n_passes * n_slots_);
+    check(mg_ce_pool_run(h_.get(), slots.data(), (int)slots.size(), n_passes, out.data()));
+    return out;
+  }
+  std::vector<int8_t> occupation(int slot) {
+    const auto it = shapes_.find(slot);
+    if (it == shapes_.end()) throw std::runtime_error("Error in CePool::occupation: invalid slot");
+    std::vector<int8_t> occ((size_t)it->second[0] * it->second[1] * it->second[2]);
+    check(mg_ce_pool_get_occ(h_.get(), slot, occ.data()));
+    return occ;
+  }
+  std::vector<long long> corr(int slot) {
+    std::vector<long long> c((size_t)n_classes_);
+    check(mg_ce_pool_corr(h_.get(), slot, c.data()));
+    return c;
+  }
+  float last_kernel_ms() const {
+    float ms = 0.f;
+    check(mg_ce_pool_last_kernel_ms(h_.get(), &ms));
+    return ms;
+  }
+  int last_launches() const {
+    int n = 0;
+    check(mg_ce_pool_last_launches(h_.get(), &n));
+    return n;
+  }
+  mg_ce_pool* get() const { return h_.get(); }
+
+ private:
+  using H = Handle<mg_ce_pool, mg_ce_pool_destroy>;
+  H h_;
+  int n_slots_, n_classes_, n_species_;
+  std::map<int, std::array<int, 3>> shapes_;
+};
+
+/* free the device blocks and streams that destroyed batches left in the library's cache */
+inline void release_cached_memory() { check(mg_release_cached_memory()); }
 
 /* The sweep's colouring of a supercell (host only): colours per site, number of
  * colours, layout (0 byte, 1 word, 2 pipelined word). */

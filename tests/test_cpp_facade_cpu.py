@@ -40,6 +40,21 @@ int main() {
   for (auto& v : obs) v = std::uniform_real_distribution<double>(0.0, 1.0)(g);
   auto st = montegpu::basic_statistics(obs);
   std::printf("mean %.17g precision %.17g\n", st.first, st.second);
+  // the chain pool: without a device its creation throws the library's message; with one,
+  // add_many checks its argument sizes on the host before any device work
+  try {
+    montegpu::CeModel m(0, std::vector<double>(10, 0.01));
+    montegpu::CePool pool(m, 1 << 20, 4);
+    try {
+      pool.add_many({8, 8, 8}, {1000.0, 900.0}, {0.0}, {1}, {0}, std::vector<int8_t>(512, 0));
+      std::printf("pool: no exception\n");
+      return 1;
+    } catch (const std::runtime_error& err) {
+      std::printf("pool: %s\n", err.what());
+    }
+  } catch (const std::runtime_error& err) {
+    std::printf("pool: %s\n", err.what());
+  }
   return 0;
 }
 '''
@@ -59,6 +74,8 @@ def test_cpp_facade(tmp_path):
     assert lines[0] == "colours 16 layout 2"
     assert lines[1].startswith("caught: Error in mg_ce_color_supercell")
     mean, prec = (float(x) for x in lines[2].split()[1::2])
+    assert lines[3].startswith("pool: Error in CePool::add_many: argument sizes do not match") or \
+        lines[3].startswith("pool: CUDA error") or lines[3].startswith("pool: Error in mg_ce_pool_create"), lines[3]
     import casmcode_monte_gb300 as monte
     from casmcode_monte_gb300.sampling import BasicStatisticsCalculator
 
